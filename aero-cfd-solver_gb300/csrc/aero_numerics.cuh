@@ -1,0 +1,442 @@
+// aero_numerics.cuh -- per-face and per-cell arithmetic of the 2D Euler path, written for
+// the device (sm_103a) and templated on the bulk type T (float or double).
+//
+// The operation order and branch structure follow the reference functions cited per
+// function (paths relative to the AeroCFD project root) so that, apart from FMA
+// contraction, the device produces the reference's numbers. In 2D the reference carries
+// a fifth component (rho*w, w) that is identically zero: every term it contributes is an
+// exact +0, so the device works on four components (rho, rho*u, rho*v, rho*E) /
+// (rho, u, v, p) and writes 0 for the fifth.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace aero {
+
+template <class T>
+struct Kn {
+  static constexpr T rho_floor = T(1.0e-8);
+  static constexpr T p_floor = T(1.0e-8);
+  static constexpr T wave_floor = T(1.0e-8);
+  static constexpr T low_mach_min = T(1.0e-4);
+  static constexpr T all_speed_floor = T(1.0e-6);
+  static constexpr T smooth_eps = T(1.0e-6);
+  static constexpr T vol_floor = T(1.0e-12);
+};
+
+// std::max / std::min / std::clamp semantics (NaN handling included).
+template <class T>
+__host__ __device__ __forceinline__ T smax(T a, T b) {
+  return (a < b) ? b : a;
+}
+template <class T>
+__host__ __device__ __forceinline__ T smin(T a, T b) {
+  return (b < a) ? b : a;
+}
+template <class T>
+__host__ __device__ __forceinline__ T sclamp(T v, T lo, T hi) {
+  return (v < lo) ? lo : ((hi < v) ? hi : v);
+}
+template <class T>
+__host__ __device__ __forceinline__ T sabs(T x) {
+  return fabs(x);
+}
+template <>
+__host__ __device__ __forceinline__ float sabs<float>(float x) {
+  return fabsf(x);
+}
+template <class T>
+__host__ __device__ __forceinline__ T ssqrt(T x) {
+  return sqrt(x);
+}
+template <>
+__host__ __device__ __forceinline__ float ssqrt<float>(float x) {
+  return sqrtf(x);
+}
+template <class T>
+__host__ __device__ __forceinline__ bool sfinite(T x) {
+  return isfinite(x);
+}
+
+template <class T>
+struct Prim {
+  T r, u, v, p;
+};
+template <class T>
+struct Cons {
+  T r, ru, rv, rE;
+};
+template <class T>
+struct Flux {
+  T m, fx, fy, e;
+};
+
+// euler_flux.cpp:101-113
+template <class T>
+__device__ __forceinline__ Cons<T> prim_to_cons(const Prim<T>& w, T gamma) {
+  Cons<T> c;
+  c.r = smax(w.r, Kn<T>::rho_floor);
+  c.ru = c.r * w.u;
+  c.rv = c.r * w.v;
+  const T ke = T(0.5) * c.r * (w.u * w.u + w.v * w.v);
+  const T p = smax(w.p, Kn<T>::p_floor);
+  c.rE = p / (gamma - T(1)) + ke;
+  return c;
+}
+
+// euler_flux.cpp:115-127
+template <class T>
+__device__ __forceinline__ Prim<T> cons_to_prim(const Cons<T>& c, T gamma) {
+  Prim<T> w;
+  w.r = smax(c.r, Kn<T>::rho_floor);
+  const T inv = T(1) / w.r;
+  w.u = c.ru * inv;
+  w.v = c.rv * inv;
+  const T ke = T(0.5) * w.r * (w.u * w.u + w.v * w.v);
+  w.p = smax((gamma - T(1)) * (c.rE - ke), Kn<T>::p_floor);
+  return w;
+}
+
+// euler_flux.cpp:129-144
+template <class T>
+__device__ __forceinline__ void enforce_physical(Cons<T>* s, T gamma) {
+  s->r = smax(s->r, Kn<T>::rho_floor);
+  const T inv = T(1) / s->r;
+  const T u = s->ru * inv, v = s->rv * inv;
+  const T ke = T(0.5) * s->r * (u * u + v * v);
+  const T pf = Kn<T>::p_floor / (gamma - T(1));
+  s->rE = smax(s->rE, ke + pf);
+  const T p = (gamma - T(1)) * (s->rE - ke);
+  if (p < Kn<T>::p_floor) s->rE = ke + pf;
+}
+
+// euler_flux.cpp:150-152
+template <class T>
+__device__ __forceinline__ T sound_speed(const Prim<T>& w, T gamma) {
+  return ssqrt(smax(gamma * w.p / smax(w.r, Kn<T>::rho_floor), T(0)));
+}
+
+template <class T>
+__device__ __forceinline__ T vmag(const Prim<T>& w) {
+  return ssqrt(w.u * w.u + w.v * w.v);
+}
+
+// preconditioning.cpp:17-22
+template <class T>
+__device__ __forceinline__ T local_mach(const Prim<T>& w, T gamma) {
+  return vmag(w) / smax(sound_speed(w, gamma), Kn<T>::wave_floor);
+}
+
+// euler_flux.cpp:28-39
+template <class T>
+__device__ __forceinline__ Flux<T> physical_flux(const Cons<T>& c, const Prim<T>& w, T nx, T ny) {
+  const T un = w.u * nx + w.v * ny;
+  return {c.r * un, c.ru * un + nx * w.p, c.rv * un + ny * w.p, (c.rE + w.p) * un};
+}
+
+// euler_flux.cpp:45-51
+template <class T>
+__device__ __forceinline__ T with_sign_floor(T x) {
+  if (sabs(x) >= Kn<T>::wave_floor) return x;
+  return (x >= T(0)) ? Kn<T>::wave_floor : -Kn<T>::wave_floor;
+}
+
+template <class T>
+struct Speeds {
+  T lm, lp, sr;
+};
+
+// euler_flux.cpp:58-74; the radius is also boundary_conditions.cpp:14-25.
+template <class T>
+__device__ __forceinline__ Speeds<T> precond_speeds(T un, T a, T acoustic_scale) {
+  const T beta = sclamp(acoustic_scale, Kn<T>::low_mach_min, T(1));
+  const T b2 = beta * beta;
+  const T omb2 = T(1) - b2;
+  const T ut = T(0.5) * (T(1) + b2) * un;
+  const T disc = omb2 * omb2 * un * un + T(4) * b2 * a * a;
+  const T ct = T(0.5) * ssqrt(smax(disc, T(0)));
+  Speeds<T> s;
+  s.lm = ut - ct;
+  s.lp = ut + ct;
+  // std::max({|un|, |lm|, |lp|, floor}) keeps the first of equal maxima
+  T m = sabs(un);
+  m = smax(m, sabs(s.lm));
+  m = smax(m, sabs(s.lp));
+  s.sr = smax(m, Kn<T>::wave_floor);
+  return s;
+}
+
+// Settings of one residual evaluation that do not change within a launch
+// (residual_assembly.hpp:12-31, preconditioning.hpp:9-15).
+template <class T>
+struct FaceParams {
+  T gamma;
+  Cons<T> farfield;
+  int limiter;  // 0 minmod, 1 venkat
+  int precond;
+  int low_mach_fix;
+  int precond_farfield_bc;
+  int as_fix;
+  T mach_cutoff;
+  T pc_mach_ref, pc_mach_min, pc_beta_min, pc_beta_max;
+  T stab_floor;
+  T as_cutoff, as_fmin, as_ramp;
+};
+
+// euler_flux.cpp:154-175 (prims already converted by the caller)
+template <class T>
+__device__ __forceinline__ T low_mach_dissipation_scale(const Prim<T>& pl, const Prim<T>& pr,
+                                                        T gamma, T cutoff, T mach_ref) {
+  if (cutoff <= T(0)) return T(1);
+  const T al = smax(sound_speed(pl, gamma), Kn<T>::wave_floor);
+  const T ar = smax(sound_speed(pr, gamma), Kn<T>::wave_floor);
+  const T ml = vmag(pl) / al;
+  const T mr = vmag(pr) / ar;
+  const T fm = T(0.5) * (ml + mr);
+  const T mstar = smax(fm, smax(mach_ref, Kn<T>::wave_floor));
+  const T ratio = mstar / smax(cutoff, Kn<T>::wave_floor);
+  return sclamp(ratio, Kn<T>::low_mach_min, T(1));
+}
+
+// euler_flux.cpp:81-98 + 177-201
+template <class T>
+__device__ __forceinline__ T all_speed_pressure_scale(const Prim<T>& pl, const Prim<T>& pr, T nx,
+                                                      T ny, const FaceParams<T>& fp) {
+  const T unl = pl.u * nx + pl.v * ny, unr = pr.u * nx + pr.v * ny;
+  const T al = smax(sound_speed(pl, fp.gamma), Kn<T>::wave_floor);
+  const T ar = smax(sound_speed(pr, fp.gamma), Kn<T>::wave_floor);
+  const T mach = smax(T(0.5) * (vmag(pl) / al + vmag(pr) / ar), Kn<T>::all_speed_floor);
+  T mn = smax(T(0.5) * (sabs(unl) / al + sabs(unr) / ar), Kn<T>::all_speed_floor);
+  mn = smin(mn, mach);
+  mn = smax(mn, Kn<T>::all_speed_floor);
+  const T cut = smax(fp.as_cutoff, Kn<T>::all_speed_floor);
+  const T tfloor = sclamp(fp.as_fmin, Kn<T>::all_speed_floor, T(1));
+  const T tn = sclamp(mn / cut, tfloor, T(1));
+  const T ratio = sclamp(mach / cut, T(0), T(1));
+  const T gate = ratio * ratio;
+  const T tc = (T(1) - gate) * tn + gate;
+  const T w = sclamp(fp.as_ramp, T(0), T(1));
+  const T te = (T(1) - w) + w * tc;
+  return sclamp(te, tfloor, T(1));
+}
+
+// euler_flux.cpp:203-239. ul/ur conservative, pl/pr = cons_to_prim(ul/ur).
+template <class T>
+__device__ __forceinline__ Flux<T> rusanov(const Cons<T>& ul, const Cons<T>& ur, const Prim<T>& pl,
+                                           const Prim<T>& pr, T nx, T ny, T gamma, T as,
+                                           T* mws) {
+  const T unl = pl.u * nx + pl.v * ny, unr = pr.u * nx + pr.v * ny;
+  const T al = sound_speed(pl, gamma), ar = sound_speed(pr, gamma);
+  const T smax_phys = smax(sabs(unl) + al, sabs(unr) + ar);
+  const T sdiss = smax(precond_speeds(unl, al, as).sr, precond_speeds(unr, ar, as).sr);
+  *mws = smax(smax_phys, Kn<T>::wave_floor);
+  const Flux<T> fl = physical_flux(ul, pl, nx, ny), fr = physical_flux(ur, pr, nx, ny);
+  const T hs = T(0.5) * sdiss;
+  return {T(0.5) * (fl.m + fr.m) - hs * (ur.r - ul.r), T(0.5) * (fl.fx + fr.fx) - hs * (ur.ru - ul.ru),
+          T(0.5) * (fl.fy + fr.fy) - hs * (ur.rv - ul.rv), T(0.5) * (fl.e + fr.e) - hs * (ur.rE - ul.rE)};
+}
+
+template <class T>
+__device__ __forceinline__ bool finite4(T a, T b, T c, T d) {
+  return sfinite(a) && sfinite(b) && sfinite(c) && sfinite(d);
+}
+
+// euler_flux.cpp:241-364. LM selects the all-speed pressure correction; with LM false the
+// pressure scale is the constant 1 the reference uses when the fix is off.
+template <class T, bool LM>
+__device__ __forceinline__ Flux<T> hllc(const Cons<T>& ul, const Cons<T>& ur, T nx, T ny,
+                                        const FaceParams<T>& fp, T as, T* mws, bool* fallback) {
+  const T gamma = fp.gamma;
+  const Prim<T> pl = cons_to_prim(ul, gamma), pr = cons_to_prim(ur, gamma);
+  const T unl = pl.u * nx + pl.v * ny, unr = pr.u * nx + pr.v * ny;
+  const T al = sound_speed(pl, gamma), ar = sound_speed(pr, gamma);
+  T ps = T(1);
+  if (LM) {
+    if (fp.as_fix) ps = all_speed_pressure_scale(pl, pr, nx, ny, fp);
+  }
+  const T pavg = T(0.5) * (pl.p + pr.p);
+  const T plc = pavg + ps * (pl.p - pavg);
+  const T prc = pavg + ps * (pr.p - pavg);
+  const Speeds<T> spl = precond_speeds(unl, al, as);
+  const Speeds<T> spr = precond_speeds(unr, ar, as);
+  const T s_l = smin(spl.lm, spr.lm);
+  const T s_r = smax(spl.lp, spr.lp);
+  const T slp = smin(unl - al, unr - ar);
+  const T srp = smax(unl + al, unr + ar);
+  *mws = smax(smax(sabs(slp), sabs(srp)), Kn<T>::wave_floor);
+  *fallback = false;
+
+  bool diffusive = sabs(s_r - s_l) < Kn<T>::wave_floor;
+  Flux<T> f;
+  if (!diffusive) {
+    const Flux<T> fl = physical_flux(ul, pl, nx, ny);
+    const Flux<T> fr = physical_flux(ur, pr, nx, ny);
+    if (s_l >= T(0)) return fl;
+    if (s_r <= T(0)) return fr;
+    const T rl = smax(pl.r, Kn<T>::rho_floor);
+    const T rr = smax(pr.r, Kn<T>::rho_floor);
+    const T denom = rl * (s_l - unl) - rr * (s_r - unr);
+    diffusive = sabs(denom) < Kn<T>::wave_floor;
+    if (!diffusive) {
+      const T s_m = (prc - plc + rl * unl * (s_l - unl) - rr * unr * (s_r - unr)) / denom;
+      // star states (euler_flux.cpp:313-334) on the side the contact selects; the other
+      // side only enters the finiteness/positivity test, so both are formed.
+      Cons<T> stl = ul, str = ur;
+      {
+        const T skun = s_l - unl, sksm = s_l - s_m;
+        if (!(sabs(skun) < Kn<T>::wave_floor || sabs(sksm) < Kn<T>::wave_floor)) {
+          const T rs = rl * skun / sksm;
+          const T sh = s_m - unl;
+          stl.r = rs;
+          stl.ru = rs * (pl.u + sh * nx);
+          stl.rv = rs * (pl.v + sh * ny);
+          const T et = ul.rE / rl;
+          const T pt = plc / with_sign_floor(rl * skun);
+          stl.rE = rs * (et + sh * (s_m + pt));
+        }
+      }
+      {
+        const T skun = s_r - unr, sksm = s_r - s_m;
+        if (!(sabs(skun) < Kn<T>::wave_floor || sabs(sksm) < Kn<T>::wave_floor)) {
+          const T rs = rr * skun / sksm;
+          const T sh = s_m - unr;
+          str.r = rs;
+          str.ru = rs * (pr.u + sh * nx);
+          str.rv = rs * (pr.v + sh * ny);
+          const T et = ur.rE / rr;
+          const T pt = prc / with_sign_floor(rr * skun);
+          str.rE = rs * (et + sh * (s_m + pt));
+        }
+      }
+      // the w component of both star states is rho_star*(0 + shift*0), always finite
+      diffusive = !finite4(stl.r, stl.ru, stl.rv, stl.rE) || !finite4(str.r, str.ru, str.rv, str.rE) ||
+                  stl.r <= T(0) || str.r <= T(0);
+      if (!diffusive) {
+        if (s_m >= T(0)) {
+          f = {fl.m + s_l * (stl.r - ul.r), fl.fx + s_l * (stl.ru - ul.ru), fl.fy + s_l * (stl.rv - ul.rv),
+               fl.e + s_l * (stl.rE - ul.rE)};
+        } else {
+          f = {fr.m + s_r * (str.r - ur.r), fr.fx + s_r * (str.ru - ur.ru), fr.fy + s_r * (str.rv - ur.rv),
+               fr.e + s_r * (str.rE - ur.rE)};
+        }
+        diffusive = !finite4(f.m, f.fx, f.fy, f.e);
+      }
+    }
+  }
+  if (diffusive) {
+    *fallback = true;
+    f = rusanov(ul, ur, pl, pr, nx, ny, gamma, as, mws);
+  }
+  return f;
+}
+
+// preconditioning.cpp:9-15 + 24-32 on a primitive state
+template <class T>
+__device__ __forceinline__ T cell_beta(const Prim<T>& w, const FaceParams<T>& fp) {
+  const T m = local_mach(w, fp.gamma);
+  T target = m;
+  target = smax(target, fp.pc_mach_ref);
+  target = smax(target, fp.pc_mach_min);
+  target = smax(target, Kn<T>::wave_floor);
+  const T bmin = smax(fp.pc_beta_min, Kn<T>::low_mach_min);
+  const T bmax = smax(bmin, fp.pc_beta_max);
+  return sclamp(target, bmin, bmax);
+}
+
+// residual_assembly.cpp:16-20
+template <class T>
+__device__ __forceinline__ T smooth_max(T a, T b) {
+  const T d = a - b;
+  return T(0.5) * (a + b + ssqrt(d * d + Kn<T>::smooth_eps * Kn<T>::smooth_eps));
+}
+
+// preconditioning.cpp:34-49 (face beta) and residual_assembly.cpp:31-51 (acoustic scale),
+// from the two conservative face states. Without LM the scale is exactly 1.
+template <class T, bool LM>
+__device__ __forceinline__ T face_acoustic_scale(const Cons<T>& l, const Cons<T>& r,
+                                                 const FaceParams<T>& fp) {
+  if (!LM) return T(1);
+  const Prim<T> pl = cons_to_prim(l, fp.gamma), pr = cons_to_prim(r, fp.gamma);
+  T s = T(1);
+  if (fp.precond) {
+    const Prim<T> avg{T(0.5) * (pl.r + pr.r), T(0.5) * (pl.u + pr.u), T(0.5) * (pl.v + pr.v),
+                      T(0.5) * (pl.p + pr.p)};
+    s = sclamp(cell_beta(avg, fp), Kn<T>::low_mach_min, T(1));
+  }
+  if (fp.low_mach_fix) {
+    s = smin(s, low_mach_dissipation_scale(pl, pr, fp.gamma, fp.mach_cutoff, fp.pc_mach_ref));
+  }
+  s = sclamp(s, Kn<T>::low_mach_min, T(1));
+  const T fm = T(0.5) * (local_mach(pl, fp.gamma) + local_mach(pr, fp.gamma));
+  const T fl = sclamp(fp.stab_floor, T(0), T(1));
+  const T stab = sclamp(smooth_max(fm, fl), Kn<T>::low_mach_min, T(1));
+  return smax(s, stab);
+}
+
+// boundary_conditions.cpp:27-78
+template <class T>
+__device__ __forceinline__ Cons<T> precond_farfield_state(const Cons<T>& in, T nx, T ny,
+                                                          const FaceParams<T>& fp, T as) {
+  const T gamma = fp.gamma;
+  const Prim<T> pi = cons_to_prim(in, gamma), pf = cons_to_prim(fp.farfield, gamma);
+  const T uni = pi.u * nx + pi.v * ny, unf = pf.u * nx + pf.v * ny;
+  const T ai = smax(sound_speed(pi, gamma), Kn<T>::rho_floor);
+  const T af = smax(sound_speed(pf, gamma), Kn<T>::rho_floor);
+  const T rho_ref = smax(T(0.5) * (pi.r + pf.r), Kn<T>::rho_floor);
+  const T a_ref = smax(T(0.5) * (ai + af), Kn<T>::rho_floor);
+  const T a_t = smax(sclamp(as, Kn<T>::low_mach_min, T(1)) * a_ref, Kn<T>::all_speed_floor);
+  if (sabs(uni) >= a_t) return (uni >= T(0)) ? in : fp.farfield;
+  const T rp = uni + pi.p / (rho_ref * a_t);
+  const T rm = unf - pf.p / (rho_ref * a_t);
+  const T unb = T(0.5) * (rp + rm);
+  const T pb = smax(T(0.5) * rho_ref * a_t * (rp - rm), Kn<T>::rho_floor);
+  const bool inflow = unb < T(0);
+  const T tu = inflow ? (pf.u - unf * nx) : (pi.u - uni * nx);
+  const T tv = inflow ? (pf.v - unf * ny) : (pi.v - uni * ny);
+  const T rb = inflow ? pf.r : pi.r;
+  const T pb0 = inflow ? pf.p : pi.p;
+  const T ab = inflow ? af : ai;
+  Prim<T> b;
+  b.r = smax(rb + (pb - pb0) / smax(ab * ab, Kn<T>::rho_floor), Kn<T>::rho_floor);
+  b.u = unb * nx + tu;
+  b.v = unb * ny + tv;
+  b.p = pb;
+  return prim_to_cons(b, gamma);
+}
+
+// euler_flux.cpp:366-395
+template <class T, int FLUX, bool LM>
+__device__ __forceinline__ Flux<T> face_flux(const Cons<T>& l, const Cons<T>& r, T nx, T ny,
+                                             const FaceParams<T>& fp, T as, T* mws, bool* fallback) {
+  if (FLUX == 1) return hllc<T, LM>(l, r, nx, ny, fp, as, mws, fallback);
+  *fallback = false;
+  const Prim<T> pl = cons_to_prim(l, fp.gamma), pr = cons_to_prim(r, fp.gamma);
+  return rusanov(l, r, pl, pr, nx, ny, fp.gamma, as, mws);
+}
+
+// reconstruction.cpp:121-146
+template <class T>
+__device__ __forceinline__ T limit(int lim, T a, T b) {
+  if (a * b <= T(0)) return T(0);
+  if (lim == 1) {
+    const T eps2 = T(1.0e-12) * (T(1) + a * a + b * b);
+    const T num = (b * b + T(2) * a * b + eps2) * a;
+    const T den = a * a + T(2) * b * b + a * b + eps2;
+    if (sabs(den) <= T(1.0e-20)) return T(0);
+    const T x = num / den;
+    if (!sfinite(x)) return T(0);
+    if (a > T(0)) return sclamp(x, T(0), a);
+    return sclamp(x, a, T(0));
+  }
+  return (sabs(a) < sabs(b)) ? a : b;
+}
+
+// residual_assembly.cpp:53-58 (w is 0, always finite)
+template <class T>
+__device__ __forceinline__ bool valid_prim(const Prim<T>& w) {
+  return sfinite(w.r) && sfinite(w.u) && sfinite(w.v) && sfinite(w.p) && w.r > Kn<T>::rho_floor &&
+         w.p > Kn<T>::p_floor;
+}
+
+}  // namespace aero

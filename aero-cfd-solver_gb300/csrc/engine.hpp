@@ -1,0 +1,50 @@
+// engine.hpp -- precision-independent interface of the device solver behind the C ABI.
+#pragma once
+
+#include "../../include/aero_gb300.h"
+#include "mesh_prep.hpp"
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+namespace aero {
+
+// Case settings resolved on the host (euler_solver.cpp:340-357, 120-140, 493-566), in double.
+struct Resolved {
+  double gamma;
+  double cons_inf[4];  // rho, rho*u, rho*v, rho*E of the freestream
+  double p_inf, rho_inf, v_inf, a_inf, q_inf, pressure_ref;
+  double pc_mach_ref, pc_mach_min, pc_beta_min, pc_beta_max;
+  double stab_start, stab_target;
+  double as_fmin;
+  double st_fmin_high, st_fmin_mid, st_fmin_low;
+  double pj_target, pj_spike, cfl_drop, cfl_restore, cfl_min_scale;
+  double cos_a, sin_a;
+  int lm;  // any low-Mach feature on
+};
+
+class Engine {
+ public:
+  virtual ~Engine() = default;
+  virtual bool init(std::string* err) = 0;
+  virtual void set_state(const double* u_orig) = 0;
+  virtual void get_state(double* u_orig) = 0;
+  virtual void get_primitive(double* rho, double* u, double* v, double* p) = 0;
+  virtual void residual(const double* u_orig, int second, double stab, int as_fix, double as_fmin,
+                        double as_ramp, double* res, double* sr, double* grad) = 0;
+  virtual int run(int n, aero_iter_record* recs, int* n_done) = 0;
+  virtual void reset_run() = 0;
+  virtual void last_residual(double* res, double* sr) = 0;
+  virtual int time_iterations(int n, int use_graph, int flush_l2, double* ms) = 0;
+  virtual int profile_kernels(int n, int flush_l2, double* ms, int* launches) = 0;
+  virtual void info(long long* out, int n) = 0;
+  virtual cudaError_t last_cuda_error() = 0;
+};
+
+Engine* make_engine_f32(const HostSlots& hs, const aero_case_desc& cfg, const Resolved& rs,
+                        cudaStream_t stream);
+Engine* make_engine_f64(const HostSlots& hs, const aero_case_desc& cfg, const Resolved& rs,
+                        cudaStream_t stream);
+
+}  // namespace aero

@@ -1,0 +1,656 @@
+// engine_impl.cuh -- device solver for one bulk precision T (float or double). Included by
+// engine_f32.cu and engine_f64.cu, which instantiate it.
+#pragma once
+
+#include "aero_kernels.cuh"
+#include "engine.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace aero {
+
+#define AERO_CK(expr)                       \
+  do {                                      \
+    cudaError_t e_ = (expr);                \
+    if (e_ != cudaSuccess && err_ == cudaSuccess) err_ = e_; \
+  } while (0)
+
+template <class T>
+class EngineT final : public Engine {
+  using V4 = typename Vec<T>::v4;
+  using V2 = typename Vec<T>::v2;
+
+ public:
+  EngineT(const HostSlots& hs, const aero_case_desc& cfg, const Resolved& rs, cudaStream_t st)
+      : hs_(hs), cfg_(cfg), rs_(rs), st_(st) {}
+
+  ~EngineT() override {
+    for (auto& g : graph_) {
+      if (g) cudaGraphExecDestroy(g);
+    }
+    for (void* p : allocs_) cudaFree(p);
+    if (flush_) cudaFree(flush_);
+    if (pin_state_) cudaFreeHost(pin_state_);
+  }
+
+  bool init(std::string* err) override {
+    n_ = hs_.n;
+    d_ = hs_.d;
+    block_ = cfg_.block_size > 0 ? cfg_.block_size : 128;
+    if (block_ != 64 && block_ != 128 && block_ != 256) {
+      *err = "block_size must be 64, 128 or 256";
+      return false;
+    }
+    nblocks_ = (n_ + block_ - 1) / block_;
+    const size_t ns = static_cast<size_t>(n_) * d_;
+
+    // slot table
+    link_ = upload(hs_.link);
+    std::vector<double2> nrm(ns);
+    for (size_t i = 0; i < ns; ++i) nrm[i] = make_double2(hs_.nx[i], hs_.ny[i]);
+    nrm_ = upload(nrm);
+    area_ = upload(hs_.area);
+    std::vector<V2> doff(ns), noff(ns);
+    for (size_t i = 0; i < ns; ++i) {
+      if (hs_.link[i] < 0) {
+        doff[i].x = doff[i].y = T(0);
+        noff[i].x = noff[i].y = T(0);
+        continue;
+      }
+      const int o = hs_.own_old[i], b = hs_.nbr_old[i];
+      doff[i].x = T(hs_.fcx[i]) - T(hs_.ccx[o]);
+      doff[i].y = T(hs_.fcy[i]) - T(hs_.ccy[o]);
+      noff[i].x = T(hs_.fcx[i]) - T(hs_.ccx[b]);
+      noff[i].y = T(hs_.fcy[i]) - T(hs_.ccy[b]);
+    }
+    doff_ = upload(doff);
+    noff_ = upload(noff);
+    vol_ = upload(hs_.vol);
+    wall_adj_ = upload(hs_.wall_adj);
+    const int nw = static_cast<int>(hs_.wall_cell.size());
+    ws_.cell = upload(hs_.wall_cell.empty() ? std::vector<int>{0} : hs_.wall_cell);
+    ws_.nx = upload(nonempty(hs_.wnx));
+    ws_.ny = upload(nonempty(hs_.wny));
+    ws_.area = upload(nonempty(hs_.warea));
+    ws_.x = upload(nonempty(hs_.wx));
+    ws_.y = upload(nonempty(hs_.wy));
+
+    // state
+    W_ = alloc<V4>(n_);
+    gx_ = alloc<V4>(n_);
+    gy_ = alloc<V4>(n_);
+    R_ = alloc<V4>(n_);
+    SR_ = alloc<T>(n_);
+    Un_ = alloc<d4>(n_);
+    Us_ = alloc<d4>(n_);
+    part_.norms = alloc<double>(3 * nblocks_);
+    part_.dp = alloc<double>(2 * nblocks_);
+    part_.pjump = alloc<double>(4 * nblocks_);
+    part_.srmax = alloc<double>(nblocks_ * (block_ / 32));
+    ctrl_ = alloc<Ctrl>(1);
+    ctrl_eval_ = alloc<Ctrl>(1);
+    rec_cap_ = 1024;
+    recs_ = alloc<Record>(rec_cap_);
+    if (err_ != cudaSuccess) {
+      *err = std::string("device allocation/upload failed: ") + cudaGetErrorString(err_);
+      return false;
+    }
+
+    dm_.n = n_;
+    dm_.d = d_;
+    dm_.link = link_;
+    dm_.nrm = nrm_;
+    dm_.area = area_;
+    dm_.doff = doff_;
+    dm_.noff = noff_;
+    dm_.vol = vol_;
+
+    fp_.gamma = T(rs_.gamma);
+    fp_.farfield = Cons<T>{T(rs_.cons_inf[0]), T(rs_.cons_inf[1]), T(rs_.cons_inf[2]), T(rs_.cons_inf[3])};
+    fp_.limiter = cfg_.limiter;
+    fp_.precond = cfg_.precond_on;
+    fp_.low_mach_fix = cfg_.low_mach_fix;
+    fp_.precond_farfield_bc = cfg_.precond_farfield_bc;
+    fp_.as_fix = 0;
+    fp_.mach_cutoff = T(cfg_.mach_cutoff);
+    fp_.pc_mach_ref = T(rs_.pc_mach_ref);
+    fp_.pc_mach_min = T(rs_.pc_mach_min);
+    fp_.pc_beta_min = T(rs_.pc_beta_min);
+    fp_.pc_beta_max = T(rs_.pc_beta_max);
+    fp_.stab_floor = T(0);
+    fp_.as_cutoff = T(cfg_.all_speed_mach_cutoff);
+    fp_.as_fmin = T(rs_.as_fmin);
+    fp_.as_ramp = T(1);
+
+    pc_.enabled = cfg_.precond_on;
+    pc_.gamma = rs_.gamma;
+    pc_.mach_ref = double(fp_.pc_mach_ref);
+    pc_.mach_min = double(fp_.pc_mach_min);
+    pc_.beta_min = double(fp_.pc_beta_min);
+    pc_.beta_max = double(fp_.pc_beta_max);
+
+    CtrlConfig& c = cc_;
+    std::memset(&c, 0, sizeof(c));
+    c.n_cells = n_;
+    c.n_wall = nw;
+    c.rk_stages = cfg_.rk_stages;
+    c.local_dt = cfg_.local_time_stepping;
+    c.cfl_ramp = cfg_.cfl_ramp_iters;
+    c.stab_ramp = std::max(cfg_.stab_ramp_iters, 0);
+    c.as_ramp_start = std::max(cfg_.all_speed_ramp_start_iter, 0);
+    c.as_ramp_iters = std::max(cfg_.all_speed_ramp_iters, 0);
+    c.startup_first_order = cfg_.startup_first_order_iters;
+    c.min_iterations = cfg_.min_iterations;
+    c.window = std::min(std::max(cfg_.force_stability_window, 1), kMaxForceWindow);
+    c.staged = cfg_.all_speed_staged_controller;
+    c.st_a_min = std::max(cfg_.all_speed_stage_a_min_iters, 0);
+    c.st_a_max = std::max(cfg_.all_speed_stage_a_max_iters, 0);
+    c.pj_hold = std::max(cfg_.all_speed_pjump_hold_iters, 1);
+    c.freeze_iters = std::max(cfg_.all_speed_freeze_iters, 0);
+    c.as_fix_cfg = cfg_.all_speed_flux_fix;
+    c.n_blocks = nblocks_;
+    pjump_on_ = cfg_.all_speed_staged_controller || cfg_.diagnostics;
+    sym_on_ = cfg_.aoa0_symmetry_enforce && cfg_.aoa0_symmetry_enforce_interval > 0 &&
+              !(std::fabs(cfg_.aoa_deg) > 1.0e-12);
+    c.pjump_blocks = pjump_on_ ? nblocks_ : 0;
+    c.cfl_start = cfg_.cfl_start;
+    c.cfl_max = cfg_.cfl_max;
+    c.stab_start = rs_.stab_start;
+    c.stab_target = rs_.stab_target;
+    c.as_fmin = rs_.as_fmin;
+    c.residual_target = cfg_.residual_reduction_target;
+    c.stab_tol = cfg_.force_stability_tol;
+    c.drift_tol = cfg_.force_mean_drift_tol > 0.0 ? cfg_.force_mean_drift_tol : cfg_.force_stability_tol;
+    c.st_fmin_high = rs_.st_fmin_high;
+    c.st_fmin_mid = rs_.st_fmin_mid;
+    c.st_fmin_low = rs_.st_fmin_low;
+    c.pj_target = rs_.pj_target;
+    c.pj_spike = rs_.pj_spike;
+    c.cfl_drop = rs_.cfl_drop;
+    c.cfl_restore = rs_.cfl_restore;
+    c.cfl_min_scale = rs_.cfl_min_scale;
+    c.p_inf = rs_.p_inf;
+    c.q_inf = rs_.q_inf;
+    c.chord = std::max(cfg_.chord, 1.0e-8);
+    c.s_ref = c.chord * 1.0;
+    c.cos_a = rs_.cos_a;
+    c.sin_a = rs_.sin_a;
+    c.x_ref = cfg_.x_ref;
+    c.y_ref = cfg_.y_ref;
+    c.pressure_ref = rs_.pressure_ref;
+    c.gamma = rs_.gamma;
+
+    // freestream initial state
+    std::vector<d4> u0(static_cast<size_t>(n_), d4{rs_.cons_inf[0], rs_.cons_inf[1], rs_.cons_inf[2], rs_.cons_inf[3]});
+    AERO_CK(cudaMemcpyAsync(Un_, u0.data(), sizeof(d4) * n_, cudaMemcpyHostToDevice, st_));
+    w_valid_ = false;
+    reset_run();
+    AERO_CK(cudaStreamSynchronize(st_));
+    if (err_ != cudaSuccess) {
+      *err = std::string("initialisation failed: ") + cudaGetErrorString(err_);
+      return false;
+    }
+    return true;
+  }
+
+  cudaError_t last_cuda_error() override {
+    const cudaError_t e = err_;
+    err_ = cudaSuccess;
+    return e;
+  }
+
+  void reset_run() override {
+    Ctrl h;
+    std::memset(&h, 0, sizeof(h));
+    h.iter = 0;
+    h.cfl_scale = 1.0;
+    h.prev_l2 = -1.0;
+    h.initial_l2 = -1.0;
+    h.stage = cfg_.all_speed_staged_controller ? 1 : 0;
+    h.stage_b_fmin = rs_.st_fmin_high;
+    apply_schedule(cc_, &h);
+    host_ctrl_ = h;
+    AERO_CK(cudaMemcpyAsync(ctrl_, &host_ctrl_, sizeof(Ctrl), cudaMemcpyHostToDevice, st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+  }
+
+  // State transfers go through a page-locked staging buffer in the device order.
+  void set_state(const double* u) override {
+    d4* h = pinned_state();
+    for (int cn = 0; cn < n_; ++cn) {
+      const double* s = u + 5 * static_cast<size_t>(hs_.perm[cn]);
+      h[cn] = d4{s[0], s[1], s[2], s[4]};
+    }
+    AERO_CK(cudaMemcpyAsync(Un_, h, sizeof(d4) * n_, cudaMemcpyHostToDevice, st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+    w_valid_ = false;
+  }
+
+  void get_state(double* u) override {
+    d4* h = pinned_state();
+    AERO_CK(cudaMemcpyAsync(h, Un_, sizeof(d4) * n_, cudaMemcpyDeviceToHost, st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+    for (int cn = 0; cn < n_; ++cn) {
+      double* s = u + 5 * static_cast<size_t>(hs_.perm[cn]);
+      s[0] = h[cn].x;
+      s[1] = h[cn].y;
+      s[2] = h[cn].z;
+      s[3] = 0.0;
+      s[4] = h[cn].w;
+    }
+  }
+
+  void get_primitive(double* rho, double* u, double* v, double* p) override {
+    std::vector<d4> h(static_cast<size_t>(n_));
+    AERO_CK(cudaMemcpyAsync(h.data(), Un_, sizeof(d4) * n_, cudaMemcpyDeviceToHost, st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+    for (int cn = 0; cn < n_; ++cn) {
+      const int co = hs_.perm[cn];
+      // host restatement of cons_to_prim (euler_flux.cpp:115-127) in double
+      const double r = std::max(h[cn].x, 1.0e-8);
+      const double inv = 1.0 / r;
+      const double uu = h[cn].y * inv, vv = h[cn].z * inv;
+      const double ke = 0.5 * r * (uu * uu + vv * vv);
+      rho[co] = r;
+      u[co] = uu;
+      v[co] = vv;
+      p[co] = std::max((rs_.gamma - 1.0) * (h[cn].w - ke), 1.0e-8);
+    }
+  }
+
+  void residual(const double* u, int second, double stab, int as_fix, double as_fmin, double as_ramp,
+                double* res, double* sr, double* grad) override {
+    std::vector<d4> h(static_cast<size_t>(n_));
+    for (int cn = 0; cn < n_; ++cn) {
+      const double* s = u + 5 * static_cast<size_t>(hs_.perm[cn]);
+      h[cn] = d4{s[0], s[1], s[2], s[4]};
+    }
+    AERO_CK(cudaMemcpyAsync(Us_, h.data(), sizeof(d4) * n_, cudaMemcpyHostToDevice, st_));
+    Ctrl ce;
+    std::memset(&ce, 0, sizeof(ce));
+    ce.stab_floor = stab;
+    ce.as_fix = as_fix;
+    ce.as_fmin = as_fmin;
+    ce.as_ramp = as_ramp;
+    AERO_CK(cudaMemcpyAsync(ctrl_eval_, &ce, sizeof(Ctrl), cudaMemcpyHostToDevice, st_));
+    k_refresh_prim<T><<<nblocks_, block_, 0, st_>>>(n_, Us_, W_, rs_.gamma);
+    if (second) k_gradient<T><<<nblocks_, block_, 0, st_>>>(dm_, W_, gx_, gy_, ctrl_eval_);
+    launch_residual(second != 0, false, ctrl_eval_, 0);
+    AERO_CK(cudaGetLastError());
+    w_valid_ = false;
+    download_residual(res, sr);
+    if (grad) {
+      std::vector<V4> hx(static_cast<size_t>(n_)), hy(static_cast<size_t>(n_));
+      if (second) {
+        AERO_CK(cudaMemcpyAsync(hx.data(), gx_, sizeof(V4) * n_, cudaMemcpyDeviceToHost, st_));
+        AERO_CK(cudaMemcpyAsync(hy.data(), gy_, sizeof(V4) * n_, cudaMemcpyDeviceToHost, st_));
+      }
+      AERO_CK(cudaStreamSynchronize(st_));
+      for (int cn = 0; cn < n_; ++cn) {
+        double* g = grad + 10 * static_cast<size_t>(hs_.perm[cn]);
+        if (!second) {
+          for (int k = 0; k < 10; ++k) g[k] = 0.0;
+          continue;
+        }
+        const V4 a = hx[cn], b = hy[cn];
+        g[0] = a.x; g[1] = b.x;  // rho
+        g[2] = a.y; g[3] = b.y;  // u
+        g[4] = a.z; g[5] = b.z;  // v
+        g[6] = 0.0; g[7] = 0.0;  // w
+        g[8] = a.w; g[9] = b.w;  // p
+      }
+    }
+  }
+
+  void last_residual(double* res, double* sr) override { download_residual(res, sr); }
+
+  int run(int n, aero_iter_record* recs, int* n_done) override {
+    static_assert(sizeof(Record) == sizeof(aero_iter_record), "record layout");
+    int executed = 0;
+    if (!w_valid_) refresh();
+    AERO_CK(cudaMemcpyAsync(&host_ctrl_, ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+    int status = AERO_OK;
+    while (executed < n && !host_ctrl_.done && err_ == cudaSuccess) {
+      const int chunk = std::min(n - executed, rec_cap_);
+      const int it0 = host_ctrl_.iter;
+      host_rec_base_ = it0;
+      AERO_CK(cudaMemcpyAsync(&ctrl_->rec_base, &host_rec_base_, sizeof(int), cudaMemcpyHostToDevice, st_));
+      for (int j = 0; j < chunk; ++j) launch_iteration_graph(second_at(it0 + j));
+      AERO_CK(cudaMemcpyAsync(&host_ctrl_, ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, st_));
+      AERO_CK(cudaStreamSynchronize(st_));
+      const int k = host_ctrl_.iter - it0;
+      if (recs && k > 0) {
+        AERO_CK(cudaMemcpyAsync(recs + executed, recs_, sizeof(Record) * k, cudaMemcpyDeviceToHost, st_));
+        AERO_CK(cudaStreamSynchronize(st_));
+      }
+      executed += k;
+      if (k < chunk && !host_ctrl_.done) break;  // should not happen
+    }
+    if (host_ctrl_.nonfinite) status = AERO_ERR_NONFINITE;
+    if (err_ != cudaSuccess) status = AERO_ERR_CUDA;
+    if (n_done) *n_done = executed;
+    return status;
+  }
+
+  // Device time of n iterations between CUDA events on the context's stream. With
+  // flush_l2, a buffer larger than L2 is overwritten before every iteration and only the
+  // iterations themselves are timed (one event pair per iteration, times summed).
+  int time_iterations(int n, int use_graph, int flush_l2, double* ms) override {
+    const int it0 = begin_untracked();
+    if (use_graph) {
+      ensure_graph(second_at(it0));
+      ensure_graph(second_at(it0 + n - 1));
+    }
+    if (flush_l2 && !ensure_flush_buffer()) return AERO_ERR_NOMEM;
+    const int npairs = flush_l2 ? n : 1;
+    std::vector<cudaEvent_t> ev(2 * static_cast<size_t>(npairs));
+    for (auto& e : ev) AERO_CK(cudaEventCreate(&e));
+    if (!flush_l2) AERO_CK(cudaEventRecord(ev[0], st_));
+    for (int j = 0; j < n; ++j) {
+      if (flush_l2) {
+        AERO_CK(cudaMemsetAsync(flush_, j & 0xff, flush_bytes_, st_));
+        AERO_CK(cudaEventRecord(ev[2 * j], st_));
+      }
+      if (use_graph) {
+        launch_iteration_graph(second_at(it0 + j));
+      } else {
+        launch_iteration(second_at(it0 + j));
+      }
+      if (flush_l2) AERO_CK(cudaEventRecord(ev[2 * j + 1], st_));
+    }
+    if (!flush_l2) AERO_CK(cudaEventRecord(ev[1], st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+    double total = 0.0;
+    for (int k = 0; k < npairs; ++k) {
+      float f = 0.0f;
+      AERO_CK(cudaEventElapsedTime(&f, ev[2 * k], ev[2 * k + 1]));
+      total += f;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    *ms = total;
+    return end_untracked();
+  }
+
+  // Per kernel class: summed device time (ms) and launches over n iterations, each kernel
+  // bracketed by its own events. Classes: 0 gradient, 1 residual, 2 update, 3 global-dt
+  // reduction, 4 symmetry + pressure-jump, 5 controller.
+  int profile_kernels(int n, int flush_l2, double* ms, int* launches) override {
+    const int it0 = begin_untracked();
+    if (flush_l2 && !ensure_flush_buffer()) return AERO_ERR_NOMEM;
+    for (int k = 0; k < 6; ++k) {
+      ms[k] = 0.0;
+      launches[k] = 0;
+    }
+    cudaEvent_t e0, e1;
+    AERO_CK(cudaEventCreate(&e0));
+    AERO_CK(cudaEventCreate(&e1));
+    for (int j = 0; j < n; ++j) {
+      if (flush_l2) AERO_CK(cudaMemsetAsync(flush_, j & 0xff, flush_bytes_, st_));
+      launch_iteration(second_at(it0 + j), [&](int cls, auto&& launch) {
+        AERO_CK(cudaEventRecord(e0, st_));
+        launch();
+        AERO_CK(cudaEventRecord(e1, st_));
+        AERO_CK(cudaEventSynchronize(e1));
+        float f = 0.0f;
+        AERO_CK(cudaEventElapsedTime(&f, e0, e1));
+        ms[cls] += f;
+        ++launches[cls];
+      });
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return end_untracked();
+  }
+
+  void info(long long* out, int n) override {
+    long long v[8] = {n_, hs_.nf, d_, launches_per_iteration(true), static_cast<long long>(bytes_),
+                      sizeof(T) == 4 ? AERO_PRECISION_FP32 : AERO_PRECISION_FP64, block_, nblocks_};
+    for (int i = 0; i < n && i < 8; ++i) out[i] = v[i];
+  }
+
+ private:
+  template <class U>
+  static std::vector<U> nonempty(const std::vector<U>& v) {
+    return v.empty() ? std::vector<U>(1, U()) : v;
+  }
+  template <class U>
+  U* alloc(size_t count) {
+    void* p = nullptr;
+    const size_t b = std::max<size_t>(count, 1) * sizeof(U);
+    const cudaError_t e = cudaMalloc(&p, b);
+    if (e != cudaSuccess) {
+      if (err_ == cudaSuccess) err_ = e;
+      return nullptr;
+    }
+    AERO_CK(cudaMemsetAsync(p, 0, b, st_));
+    allocs_.push_back(p);
+    bytes_ += b;
+    return static_cast<U*>(p);
+  }
+  template <class U>
+  U* upload(const std::vector<U>& v) {
+    U* p = alloc<U>(v.size());
+    if (p) AERO_CK(cudaMemcpyAsync(p, v.data(), sizeof(U) * v.size(), cudaMemcpyHostToDevice, st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+    return p;
+  }
+
+  bool second_at(int it) const { return it >= std::max(cfg_.startup_first_order_iters, 0); }
+
+  long long launches_per_iteration(bool second) const {
+    const int per_stage = (second ? 1 : 0) + 1 + (cfg_.local_time_stepping ? 0 : 1) + 1;
+    return static_cast<long long>(per_stage) * cfg_.rk_stages + (pjump_on_ ? 1 : 0) + (sym_on_ ? 1 : 0) + 1;
+  }
+
+  void refresh() {
+    k_refresh_prim<T><<<nblocks_, block_, 0, st_>>>(n_, Un_, W_, rs_.gamma);
+    AERO_CK(cudaGetLastError());
+    w_valid_ = true;
+  }
+
+  void download_residual(double* res, double* sr) {
+    std::vector<V4> hr(static_cast<size_t>(n_));
+    std::vector<T> hs(static_cast<size_t>(n_));
+    AERO_CK(cudaMemcpyAsync(hr.data(), R_, sizeof(V4) * n_, cudaMemcpyDeviceToHost, st_));
+    AERO_CK(cudaMemcpyAsync(hs.data(), SR_, sizeof(T) * n_, cudaMemcpyDeviceToHost, st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+    for (int cn = 0; cn < n_; ++cn) {
+      const int co = hs_.perm[cn];
+      double* r = res + 5 * static_cast<size_t>(co);
+      r[0] = hr[cn].x;
+      r[1] = hr[cn].y;
+      r[2] = hr[cn].z;
+      r[3] = 0.0;
+      r[4] = hr[cn].w;
+      if (sr) sr[co] = hs[cn];
+    }
+  }
+
+  template <int FLUX, bool SECOND, bool LM, bool NORMS>
+  void residual_t(Ctrl* ctrl, int global_dt) {
+    k_residual<T, FLUX, SECOND, LM, NORMS>
+        <<<nblocks_, block_, 0, st_>>>(dm_, fp_, W_, gx_, gy_, R_, SR_, part_, ctrl, global_dt);
+  }
+  template <int FLUX, bool SECOND, bool LM>
+  void residual_n(bool norms, Ctrl* ctrl, int global_dt) {
+    if (norms) {
+      residual_t<FLUX, SECOND, LM, true>(ctrl, global_dt);
+    } else {
+      residual_t<FLUX, SECOND, LM, false>(ctrl, global_dt);
+    }
+  }
+  template <int FLUX, bool SECOND>
+  void residual_l(bool norms, Ctrl* ctrl, int global_dt) {
+    if (rs_.lm) {
+      residual_n<FLUX, SECOND, true>(norms, ctrl, global_dt);
+    } else {
+      residual_n<FLUX, SECOND, false>(norms, ctrl, global_dt);
+    }
+  }
+  void launch_residual(bool second, bool norms, Ctrl* ctrl, int global_dt) {
+    if (cfg_.flux == AERO_FLUX_HLLC) {
+      if (second) residual_l<1, true>(norms, ctrl, global_dt);
+      else residual_l<1, false>(norms, ctrl, global_dt);
+    } else {
+      if (second) residual_l<0, true>(norms, ctrl, global_dt);
+      else residual_l<0, false>(norms, ctrl, global_dt);
+    }
+  }
+
+  template <bool PRECOND, bool LAST>
+  void update_t(int stage, int global_dt) {
+    k_update<T, PRECOND, LAST><<<nblocks_, block_, 0, st_>>>(n_, stage, pc_, R_, SR_, W_, Un_, Us_, wall_adj_,
+                                                             rs_.p_inf, part_, ctrl_, global_dt);
+  }
+
+  struct Direct {
+    template <class L>
+    void operator()(int, L&& launch) const {
+      launch();
+    }
+  };
+
+  void launch_iteration(bool second) { launch_iteration(second, Direct{}); }
+
+  // The launches of one iteration; `wrap(kernel_class, launch)` issues each one.
+  template <class Wrap>
+  void launch_iteration(bool second, Wrap&& wrap) {
+    const int global_dt = cfg_.local_time_stepping ? 0 : 1;
+    const int ns = cfg_.rk_stages;
+    for (int stage = 0; stage < ns; ++stage) {
+      const bool last = stage == ns - 1;
+      if (second) wrap(0, [&] { k_gradient<T><<<nblocks_, block_, 0, st_>>>(dm_, W_, gx_, gy_, ctrl_); });
+      wrap(1, [&] { launch_residual(second, last, ctrl_, global_dt); });
+      if (global_dt) {
+        wrap(3, [&] { k_srmax<<<1, 1024, 0, st_>>>(part_.srmax, nblocks_ * (block_ / 32), ctrl_); });
+      }
+      wrap(2, [&] {
+        if (cfg_.precond_on) {
+          if (last) update_t<true, true>(stage, global_dt);
+          else update_t<true, false>(stage, global_dt);
+        } else {
+          if (last) update_t<false, true>(stage, global_dt);
+          else update_t<false, false>(stage, global_dt);
+        }
+      });
+    }
+    if (sym_on_) {
+      wrap(4, [&] {
+        k_symmetry<T><<<nblocks_, block_, 0, st_>>>(n_, cfg_.aoa0_symmetry_enforce_interval, rs_.gamma, Un_,
+                                                     W_, wall_adj_, rs_.p_inf, part_, ctrl_);
+      });
+    }
+    if (pjump_on_) {
+      wrap(4, [&] { k_pjump<T><<<nblocks_, block_, 0, st_>>>(dm_, Un_, wall_adj_, rs_.gamma, part_, ctrl_); });
+    }
+    wrap(5, [&] { k_control<<<1, 1024, 0, st_>>>(cc_, ws_, Un_, part_, ctrl_, recs_, rec_cap_); });
+    AERO_CK(cudaGetLastError());
+  }
+
+  // Start/end of a run whose records are not kept (timing, profiling).
+  int begin_untracked() {
+    if (!w_valid_) refresh();
+    AERO_CK(cudaMemcpyAsync(&host_ctrl_, ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+    host_rec_base_ = -(1 << 30);
+    AERO_CK(cudaMemcpyAsync(&ctrl_->rec_base, &host_rec_base_, sizeof(int), cudaMemcpyHostToDevice, st_));
+    return host_ctrl_.iter;
+  }
+  int end_untracked() {
+    AERO_CK(cudaMemcpyAsync(&host_ctrl_, ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+    if (err_ != cudaSuccess) return AERO_ERR_CUDA;
+    return host_ctrl_.nonfinite ? AERO_ERR_NONFINITE : AERO_OK;
+  }
+
+  d4* pinned_state() {
+    if (pin_state_ == nullptr) {
+      if (cudaMallocHost(reinterpret_cast<void**>(&pin_state_), sizeof(d4) * static_cast<size_t>(n_)) !=
+          cudaSuccess) {
+        cudaGetLastError();
+        pin_state_ = nullptr;
+        pin_fallback_.resize(static_cast<size_t>(n_));
+        return pin_fallback_.data();
+      }
+    }
+    return pin_state_;
+  }
+
+  bool ensure_flush_buffer() {
+    if (flush_) return true;
+    flush_bytes_ = size_t(256) << 20;  // twice the 129 MB L2
+    if (cudaMalloc(&flush_, flush_bytes_) != cudaSuccess) {
+      cudaGetLastError();
+      flush_ = nullptr;
+      return false;
+    }
+    return true;
+  }
+
+  void ensure_graph(bool second) {
+    const int i = second ? 1 : 0;
+    if (graph_[i]) return;
+    cudaGraph_t g = nullptr;
+    AERO_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+    launch_iteration(second);
+    AERO_CK(cudaStreamEndCapture(st_, &g));
+    if (g) {
+      AERO_CK(cudaGraphInstantiate(&graph_[i], g, 0));
+      cudaGraphDestroy(g);
+    }
+  }
+
+  void launch_iteration_graph(bool second) {
+    ensure_graph(second);
+    const int i = second ? 1 : 0;
+    if (graph_[i]) {
+      AERO_CK(cudaGraphLaunch(graph_[i], st_));
+    } else {
+      launch_iteration(second);
+    }
+  }
+
+  HostSlots hs_;
+  aero_case_desc cfg_;
+  Resolved rs_;
+  cudaStream_t st_;
+  cudaError_t err_ = cudaSuccess;
+  std::vector<void*> allocs_;
+  size_t bytes_ = 0;
+  int n_ = 0, d_ = 0, block_ = 128, nblocks_ = 0, rec_cap_ = 0;
+  bool pjump_on_ = false, sym_on_ = false, w_valid_ = false;
+  int* link_ = nullptr;
+  double2* nrm_ = nullptr;
+  double* area_ = nullptr;
+  V2* doff_ = nullptr;
+  V2* noff_ = nullptr;
+  double* vol_ = nullptr;
+  unsigned char* wall_adj_ = nullptr;
+  WallSet ws_{};
+  V4 *W_ = nullptr, *gx_ = nullptr, *gy_ = nullptr, *R_ = nullptr;
+  T* SR_ = nullptr;
+  d4 *Un_ = nullptr, *Us_ = nullptr;
+  Partials part_{};
+  Ctrl* ctrl_ = nullptr;
+  Ctrl* ctrl_eval_ = nullptr;
+  Record* recs_ = nullptr;
+  Ctrl host_ctrl_{};
+  int host_rec_base_ = 0;
+  DevMesh<T> dm_{};
+  FaceParams<T> fp_{};
+  PrecondD pc_{};
+  CtrlConfig cc_{};
+  cudaGraphExec_t graph_[2] = {nullptr, nullptr};
+  void* flush_ = nullptr;
+  size_t flush_bytes_ = 0;
+  d4* pin_state_ = nullptr;
+  std::vector<d4> pin_fallback_;
+};
+
+#undef AERO_CK
+
+}  // namespace aero

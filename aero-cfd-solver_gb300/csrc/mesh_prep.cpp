@@ -1,0 +1,242 @@
+// mesh_prep.cpp -- see mesh_prep.hpp.
+#include "mesh_prep.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <numeric>
+#include <queue>
+
+namespace aero {
+namespace {
+
+constexpr int kPadLink = -0x7fffffff;
+constexpr int kMaxFacesPerCell = 32;
+
+// Interleave the low 16 bits of x and y (x in even bit positions).
+uint32_t morton2(uint32_t x, uint32_t y) {
+  auto spread = [](uint32_t v) {
+    v &= 0xffffu;
+    v = (v | (v << 8)) & 0x00ff00ffu;
+    v = (v | (v << 4)) & 0x0f0f0f0fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+  };
+  return spread(x) | (spread(y) << 1);
+}
+
+std::vector<int> morton_order(const aero_mesh_desc& m) {
+  const int n = m.num_cells;
+  double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
+  for (int c = 0; c < n; ++c) {
+    x0 = std::min(x0, m.cell_center[3 * c]);
+    x1 = std::max(x1, m.cell_center[3 * c]);
+    y0 = std::min(y0, m.cell_center[3 * c + 1]);
+    y1 = std::max(y1, m.cell_center[3 * c + 1]);
+  }
+  const double sx = (x1 > x0) ? 65535.0 / (x1 - x0) : 0.0;
+  const double sy = (y1 > y0) ? 65535.0 / (y1 - y0) : 0.0;
+  std::vector<uint64_t> key(static_cast<size_t>(n));
+  for (int c = 0; c < n; ++c) {
+    const auto qx = static_cast<uint32_t>(std::lround((m.cell_center[3 * c] - x0) * sx));
+    const auto qy = static_cast<uint32_t>(std::lround((m.cell_center[3 * c + 1] - y0) * sy));
+    key[c] = (static_cast<uint64_t>(morton2(qx, qy)) << 32) | static_cast<uint32_t>(c);
+  }
+  std::sort(key.begin(), key.end());
+  std::vector<int> perm(static_cast<size_t>(n));
+  for (int i = 0; i < n; ++i) perm[i] = static_cast<int>(key[i] & 0xffffffffu);
+  return perm;
+}
+
+// Reverse Cuthill-McKee on the cell adjacency graph; each connected component starts from
+// a minimum-degree cell, neighbours are visited in increasing degree.
+std::vector<int> rcm_order(const aero_mesh_desc& m) {
+  const int n = m.num_cells;
+  std::vector<int> deg(static_cast<size_t>(n), 0);
+  for (int f = 0; f < m.num_faces; ++f) {
+    if (m.face_neighbor[f] >= 0) {
+      ++deg[m.face_owner[f]];
+      ++deg[m.face_neighbor[f]];
+    }
+  }
+  std::vector<int> start(static_cast<size_t>(n) + 1, 0);
+  for (int c = 0; c < n; ++c) start[c + 1] = start[c] + deg[c];
+  std::vector<int> adj(static_cast<size_t>(start[n]));
+  std::vector<int> fill(start.begin(), start.end() - 1);
+  for (int f = 0; f < m.num_faces; ++f) {
+    const int o = m.face_owner[f], b = m.face_neighbor[f];
+    if (b >= 0) {
+      adj[fill[o]++] = b;
+      adj[fill[b]++] = o;
+    }
+  }
+  std::vector<int> order;
+  order.reserve(static_cast<size_t>(n));
+  std::vector<char> seen(static_cast<size_t>(n), 0);
+  std::vector<int> by_degree(static_cast<size_t>(n));
+  std::iota(by_degree.begin(), by_degree.end(), 0);
+  std::stable_sort(by_degree.begin(), by_degree.end(), [&](int a, int b) { return deg[a] < deg[b]; });
+  std::vector<int> nb;
+  for (int seed : by_degree) {
+    if (seen[seed]) continue;
+    std::queue<int> q;
+    q.push(seed);
+    seen[seed] = 1;
+    while (!q.empty()) {
+      const int c = q.front();
+      q.pop();
+      order.push_back(c);
+      nb.assign(adj.begin() + start[c], adj.begin() + start[c + 1]);
+      std::stable_sort(nb.begin(), nb.end(), [&](int a, int b) { return deg[a] < deg[b]; });
+      for (int x : nb) {
+        if (!seen[x]) {
+          seen[x] = 1;
+          q.push(x);
+        }
+      }
+    }
+  }
+  std::reverse(order.begin(), order.end());
+  return order;
+}
+
+}  // namespace
+
+bool build_slots(const aero_mesh_desc& m, int ordering, HostSlots* out, std::string* err) {
+  const int n = m.num_cells, nf = m.num_faces;
+  if (n <= 0 || nf <= 0) {
+    *err = "mesh must contain cells and faces";
+    return false;
+  }
+  if (!m.face_owner || !m.face_neighbor || !m.face_bc || !m.face_normal || !m.face_center ||
+      !m.face_area || !m.cell_volume || !m.cell_center || (m.num_wall_faces > 0 && !m.wall_faces) ||
+      m.num_wall_faces < 0) {
+    *err = "mesh descriptor has a null array";
+    return false;
+  }
+  std::vector<int> count(static_cast<size_t>(n), 0);
+  int nint = 0;
+  for (int f = 0; f < nf; ++f) {
+    const int o = m.face_owner[f], b = m.face_neighbor[f];
+    if (o < 0 || o >= n || b >= n || b < -1 || b == o) {
+      *err = "face " + std::to_string(f) + " has an invalid owner/neighbour";
+      return false;
+    }
+    if (b >= 0) {
+      ++nint;
+      ++count[b];
+    } else if (m.face_bc[f] != AERO_BC_FARFIELD && m.face_bc[f] != AERO_BC_WALL) {
+      *err = "boundary face " + std::to_string(f) + " has no far-field/wall type";
+      return false;
+    }
+    ++count[o];
+    const double a = m.face_area[f];
+    if (!std::isfinite(a) || !std::isfinite(m.face_normal[3 * f]) || !std::isfinite(m.face_normal[3 * f + 1])) {
+      *err = "face " + std::to_string(f) + " has non-finite geometry";
+      return false;
+    }
+  }
+  int d = 0;
+  for (int c = 0; c < n; ++c) {
+    d = std::max(d, count[c]);
+    if (!std::isfinite(m.cell_volume[c])) {
+      *err = "cell " + std::to_string(c) + " has a non-finite volume";
+      return false;
+    }
+  }
+  if (d > kMaxFacesPerCell) {
+    *err = "a cell has more than 32 faces";
+    return false;
+  }
+  for (int i = 0; i < m.num_wall_faces; ++i) {
+    const int f = m.wall_faces[i];
+    if (f < 0 || f >= nf || m.face_neighbor[f] >= 0) {
+      *err = "wall face list contains an interior or out-of-range face";
+      return false;
+    }
+  }
+
+  HostSlots& s = *out;
+  s = HostSlots();
+  s.n = n;
+  s.d = d;
+  s.nf = nf;
+  s.interior_faces = nint;
+  s.boundary_faces = nf - nint;
+  if (ordering == AERO_ORDER_MORTON) {
+    s.perm = morton_order(m);
+  } else if (ordering == AERO_ORDER_RCM) {
+    s.perm = rcm_order(m);
+  } else {
+    s.perm.resize(static_cast<size_t>(n));
+    std::iota(s.perm.begin(), s.perm.end(), 0);
+  }
+  s.iperm.assign(static_cast<size_t>(n), -1);
+  for (int i = 0; i < n; ++i) s.iperm[s.perm[i]] = i;
+
+  // per original cell, its faces in ascending face order (CSR)
+  std::vector<int> cstart(static_cast<size_t>(n) + 1, 0);
+  for (int c = 0; c < n; ++c) cstart[c + 1] = cstart[c] + count[c];
+  std::vector<int> cface(static_cast<size_t>(cstart[n]));
+  std::vector<int> fill(cstart.begin(), cstart.end() - 1);
+  for (int f = 0; f < nf; ++f) {
+    cface[fill[m.face_owner[f]]++] = f;
+    if (m.face_neighbor[f] >= 0) cface[fill[m.face_neighbor[f]]++] = f;
+  }
+
+  const size_t total = static_cast<size_t>(d) * n;
+  s.link.assign(total, kPadLink);
+  s.nx.assign(total, 0.0);
+  s.ny.assign(total, 0.0);
+  s.area.assign(total, 0.0);
+  s.fcx.assign(total, 0.0);
+  s.fcy.assign(total, 0.0);
+  s.own_old.assign(total, 0);
+  s.nbr_old.assign(total, 0);
+  s.vol.resize(static_cast<size_t>(n));
+  s.wall_adj.assign(static_cast<size_t>(n), 0);
+  s.ccx.resize(static_cast<size_t>(n));
+  s.ccy.resize(static_cast<size_t>(n));
+  for (int c = 0; c < n; ++c) {
+    s.ccx[c] = m.cell_center[3 * c];
+    s.ccy[c] = m.cell_center[3 * c + 1];
+  }
+  for (int cn = 0; cn < n; ++cn) {
+    const int co = s.perm[cn];
+    s.vol[cn] = m.cell_volume[co];
+    int k = 0;
+    for (int j = cstart[co]; j < cstart[co + 1]; ++j, ++k) {
+      const int f = cface[j];
+      const size_t slot = static_cast<size_t>(k) * n + cn;
+      const int o = m.face_owner[f], b = m.face_neighbor[f];
+      if (b >= 0) {
+        const int other = (o == co) ? b : o;
+        const int side = (o == co) ? 0 : 1;
+        s.link[slot] = (s.iperm[other] << 1) | side;
+      } else {
+        s.link[slot] = (m.face_bc[f] == AERO_BC_WALL) ? -2 : -1;
+        if (m.face_bc[f] == AERO_BC_WALL) s.wall_adj[cn] = 1;
+      }
+      s.nx[slot] = m.face_normal[3 * f];
+      s.ny[slot] = m.face_normal[3 * f + 1];
+      s.area[slot] = m.face_area[f];
+      s.fcx[slot] = m.face_center[3 * f];
+      s.fcy[slot] = m.face_center[3 * f + 1];
+      s.own_old[slot] = o;
+      s.nbr_old[slot] = b >= 0 ? b : o;
+    }
+  }
+  for (int i = 0; i < m.num_wall_faces; ++i) {
+    const int f = m.wall_faces[i];
+    s.wall_cell.push_back(s.iperm[m.face_owner[f]]);
+    s.wnx.push_back(m.face_normal[3 * f]);
+    s.wny.push_back(m.face_normal[3 * f + 1]);
+    s.warea.push_back(m.face_area[f]);
+    s.wx.push_back(m.face_center[3 * f]);
+    s.wy.push_back(m.face_center[3 * f + 1]);
+  }
+  return true;
+}
+
+}  // namespace aero

@@ -1,1 +1,271 @@
-"""Python side of the GB300 Euler residual-and-update path (ctypes over libaero_gb300.so)."""
+"""Python side of the GB300 Euler residual-and-update path: ctypes over libaero_gb300.so.
+
+The library is the product; this module only binds it. There is no CPU fallback: every
+solver call goes to the CUDA path, and Solver() raises when no sm_103 device is usable.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import capi
+from .capi import CaseDesc, IterRecord, Mesh, MeshDesc, make_case  # noqa: F401
+
+_lib = None
+_ip = C.POINTER(C.c_int)
+_dp = C.POINTER(C.c_double)
+_llp = C.POINTER(C.c_longlong)
+
+
+class OgridSpec(C.Structure):
+    _fields_ = [
+        ("n_circ", C.c_int), ("n_radial", C.c_int), ("cell_type", C.c_int), ("permute", C.c_int),
+        ("chord", C.c_double), ("thickness", C.c_double), ("wall_spacing", C.c_double),
+        ("farfield_radius", C.c_double), ("jitter", C.c_double), ("seed", C.c_ulonglong),
+    ]
+
+
+class MeshSizes(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("num_cells", "num_faces", "num_points", "num_wall_faces",
+                                       "num_farfield_faces", "conn_length")]
+
+
+class AeroError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"aero error {code}: {msg}")
+        self.code = code
+
+
+def library_path() -> Path:
+    return capi.LIB_PATH
+
+
+def load(build_if_missing: bool = False):
+    """Load libaero_gb300.so (built in-tree by aero-cfd-solver_gb300/build.py)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = capi.LIB_PATH
+    if not path.exists():
+        if not build_if_missing:
+            raise FileNotFoundError(f"{path} is missing: run aero-cfd-solver_gb300/build.py")
+        import importlib.util
+
+        spec = importlib.util.spec_from_file_location("aero_build", capi.PKG_ROOT / "build.py")
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    lib = C.CDLL(str(path))
+    sig = {
+        "aero_abi_version": (C.c_int, []),
+        "aero_version": (C.c_char_p, []),
+        "aero_cuda_available": (C.c_int, []),
+        "aero_case_defaults": (None, [C.POINTER(CaseDesc)]),
+        "aero_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(CaseDesc), C.POINTER(C.c_void_p)]),
+        "aero_destroy": (None, [C.c_void_p]),
+        "aero_last_error": (C.c_char_p, [C.c_void_p]),
+        "aero_set_state": (C.c_int, [C.c_void_p, _dp]),
+        "aero_get_state": (C.c_int, [C.c_void_p, _dp]),
+        "aero_get_primitive": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp]),
+        "aero_residual": (C.c_int, [C.c_void_p, _dp, C.c_int, C.c_double, C.c_int, C.c_double,
+                                    C.c_double, _dp, _dp, _dp]),
+        "aero_run": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(IterRecord), _ip]),
+        "aero_reset_run": (C.c_int, [C.c_void_p]),
+        "aero_get_last_residual": (C.c_int, [C.c_void_p, _dp, _dp]),
+        "aero_time_iterations": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp]),
+        "aero_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip]),
+        "aero_select_device": (C.c_int, [C.c_int]),
+        "aero_get_info": (C.c_int, [C.c_void_p, _llp, C.c_int]),
+        "aero_mesh_ogrid_reference": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double,
+                                                C.c_double, C.POINTER(C.c_void_p)]),
+        "aero_mesh_ogrid_synthetic": (C.c_int, [C.POINTER(OgridSpec), C.POINTER(C.c_void_p)]),
+        "aero_mesh_free": (None, [C.c_void_p]),
+        "aero_mesh_last_error": (C.c_char_p, []),
+        "aero_mesh_get_sizes": (C.c_int, [C.c_void_p, C.POINTER(MeshSizes)]),
+        "aero_mesh_describe": (C.c_int, [C.c_void_p, C.POINTER(MeshDesc)]),
+        "aero_mesh_get_aux": (C.c_int, [C.c_void_p, _dp, _ip, _ip, _ip, C.POINTER(C.c_ubyte), _ip]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def cuda_available() -> bool:
+    return bool(load().aero_cuda_available())
+
+
+def select_device(device: int) -> None:
+    rc = load().aero_select_device(device)
+    if rc != 0:
+        raise AeroError(rc, load().aero_last_error(None).decode())
+
+
+# --------------------------------------------------------------------------------------
+# meshes
+# --------------------------------------------------------------------------------------
+def _mesh_from_handle(h) -> Mesh:
+    lib = load()
+    sz = MeshSizes()
+    lib.aero_mesh_get_sizes(h, C.byref(sz))
+    d = MeshDesc()
+    lib.aero_mesh_describe(h, C.byref(d))
+    nf, nc = sz.num_faces, sz.num_cells
+
+    def arr(ptr, n, dtype):
+        return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+
+    points = np.empty(3 * sz.num_points, np.float64)
+    fv = np.empty(2 * nf, np.int32)
+    conn = np.empty(sz.conn_length, np.int32)
+    offs = np.empty(nc, np.int32)
+    types = np.empty(nc, np.uint8)
+    ff = np.empty(max(sz.num_farfield_faces, 1), np.int32)
+    lib.aero_mesh_get_aux(h, points.ctypes.data_as(_dp), fv.ctypes.data_as(_ip), conn.ctypes.data_as(_ip),
+                          offs.ctypes.data_as(_ip), types.ctypes.data_as(C.POINTER(C.c_ubyte)),
+                          ff.ctypes.data_as(_ip))
+    m = Mesh(arr(d.face_owner, nf, np.int32), arr(d.face_neighbor, nf, np.int32), arr(d.face_bc, nf, np.int32),
+             arr(d.face_normal, 3 * nf, np.float64), arr(d.face_center, 3 * nf, np.float64),
+             arr(d.face_area, nf, np.float64), arr(d.cell_volume, nc, np.float64),
+             arr(d.cell_center, 3 * nc, np.float64),
+             arr(d.wall_faces, sz.num_wall_faces, np.int32) if sz.num_wall_faces else np.zeros(0, np.int32),
+             points=points, face_vertices=fv, cell_conn=conn, cell_offsets=offs,
+             farfield_faces=ff[: sz.num_farfield_faces])
+    m.cell_types = types
+    lib.aero_mesh_free(h)
+    return m
+
+
+def ogrid_reference(naca: str = "0012", n_circ: int = 160, n_radial: int = 48,
+                    farfield_radius: float = 15.0, radial_stretch: float = 1.4, chord: float = 1.0) -> Mesh:
+    """The reference's triangulated O-grid (make_airfoil_ogrid_mesh, airfoil_mesh.cpp:459)."""
+    lib = load()
+    h = C.c_void_p()
+    rc = lib.aero_mesh_ogrid_reference(naca.encode(), n_circ, n_radial, farfield_radius, radial_stretch,
+                                       chord, C.byref(h))
+    if rc != 0:
+        raise AeroError(rc, lib.aero_mesh_last_error().decode())
+    return _mesh_from_handle(h)
+
+
+def ogrid_synthetic(n_circ: int, n_radial: int, cell_type: int = 3, permute: bool = True,
+                    chord: float = 1.0, thickness: float = 0.12, wall_spacing: float = 0.005,
+                    farfield_radius: float = 20.0, jitter: float = 0.1, seed: int = 0) -> Mesh:
+    """Benchmark O-grid: NACA 00xx closed TE, cosine clustering, first wall spacing, geometric
+    growth, quads (cell_type 4) or seeded-diagonal triangles (3), jitter, permutations."""
+    lib = load()
+    spec = OgridSpec(n_circ, n_radial, cell_type, int(permute), chord, thickness, wall_spacing,
+                     farfield_radius, jitter, seed)
+    h = C.c_void_p()
+    rc = lib.aero_mesh_ogrid_synthetic(C.byref(spec), C.byref(h))
+    if rc != 0:
+        raise AeroError(rc, lib.aero_mesh_last_error().decode())
+    return _mesh_from_handle(h)
+
+
+# --------------------------------------------------------------------------------------
+# solver
+# --------------------------------------------------------------------------------------
+class Solver:
+    """One device context (aero_create) on a mesh and a case."""
+
+    def __init__(self, mesh: Mesh, case: CaseDesc):
+        self.lib = load()
+        self.mesh = mesh
+        self.case = case
+        self._mdesc = mesh.desc()
+        h = C.c_void_p()
+        rc = self.lib.aero_create(C.byref(self._mdesc), C.byref(case), C.byref(h))
+        if rc != 0:
+            raise AeroError(rc, self.lib.aero_last_error(None).decode())
+        self.h = h
+        self.n = mesh.num_cells
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.aero_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise AeroError(rc, self.lib.aero_last_error(self.h).decode())
+
+    def set_state(self, u: np.ndarray):
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        assert u.size == 5 * self.n
+        self._check(self.lib.aero_set_state(self.h, u.ctypes.data_as(_dp)))
+
+    def get_state(self) -> np.ndarray:
+        u = np.empty(5 * self.n, np.float64)
+        self._check(self.lib.aero_get_state(self.h, u.ctypes.data_as(_dp)))
+        return u.reshape(self.n, 5)
+
+    def get_primitive(self):
+        out = [np.empty(self.n, np.float64) for _ in range(4)]
+        self._check(self.lib.aero_get_primitive(self.h, *[a.ctypes.data_as(_dp) for a in out]))
+        return out
+
+    def residual(self, u, second_order=True, stab=0.0, as_fix=False, as_fmin=0.05, as_ramp=1.0):
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        r = np.empty(5 * self.n, np.float64)
+        s = np.empty(self.n, np.float64)
+        g = np.empty(10 * self.n, np.float64)
+        self._check(self.lib.aero_residual(self.h, u.ctypes.data_as(_dp), int(second_order), float(stab),
+                                           int(as_fix), float(as_fmin), float(as_ramp), r.ctypes.data_as(_dp),
+                                           s.ctypes.data_as(_dp), g.ctypes.data_as(_dp)))
+        return r.reshape(self.n, 5), s, g.reshape(self.n, 5, 2)
+
+    def run(self, n: int, raise_on_nonfinite: bool = True):
+        recs = (IterRecord * max(n, 1))()
+        done = C.c_int(0)
+        rc = self.lib.aero_run(self.h, n, recs, C.byref(done))
+        out = capi.records_to_array(recs, done.value)
+        if rc == capi.AERO_ERR_NONFINITE and not raise_on_nonfinite:
+            return rc, out
+        self._check(rc)
+        return rc, out
+
+    def reset_run(self):
+        self._check(self.lib.aero_reset_run(self.h))
+
+    def last_residual(self):
+        r = np.empty(5 * self.n, np.float64)
+        s = np.empty(self.n, np.float64)
+        self._check(self.lib.aero_get_last_residual(self.h, r.ctypes.data_as(_dp), s.ctypes.data_as(_dp)))
+        return r.reshape(self.n, 5), s
+
+    def time_iterations(self, n: int, use_graph: bool = True, flush_l2: bool = False) -> float:
+        """Device milliseconds of n iterations (CUDA events on the context's stream)."""
+        ms = C.c_double(0.0)
+        self._check(self.lib.aero_time_iterations(self.h, n, int(use_graph), int(flush_l2), C.byref(ms)))
+        return ms.value
+
+    KERNEL_CLASSES = ("gradient", "residual", "update", "global_dt", "symmetry_pjump", "control")
+
+    def profile_kernels(self, n: int, flush_l2: bool = False) -> dict:
+        """Summed device ms and launch counts per kernel class over n iterations."""
+        ms = (C.c_double * 6)()
+        launches = (C.c_int * 6)()
+        self._check(self.lib.aero_profile_kernels(self.h, n, int(flush_l2), ms, launches))
+        return {k: (ms[i], launches[i]) for i, k in enumerate(self.KERNEL_CLASSES)}
+
+    def info(self) -> dict:
+        v = (C.c_longlong * 8)()
+        self._check(self.lib.aero_get_info(self.h, v, 8))
+        keys = ("cells", "faces", "slots_per_cell", "launches_per_iteration", "device_bytes", "precision",
+                "block_size", "blocks")
+        return dict(zip(keys, list(v)))

@@ -96,6 +96,7 @@ _CASE_FIELDS = [
     ("precision", C.c_int),
     ("ordering", C.c_int),
     ("block_size", C.c_int),
+    ("diagnostics", C.c_int),
 ]
 
 
@@ -155,7 +156,7 @@ CASE_DEFAULTS = dict(
     all_speed_cfl_drop_factor=_F(0.8), all_speed_cfl_restore_factor=_F(1.02),
     all_speed_cfl_min_scale=_F(0.1),
     aoa0_symmetry_enforce=0, aoa0_symmetry_enforce_interval=0,
-    precision=PRECISION_FP64, ordering=ORDER_MORTON, block_size=0,
+    precision=PRECISION_FP64, ordering=ORDER_MORTON, block_size=0, diagnostics=0,
 )
 
 

@@ -1,0 +1,405 @@
+#!/usr/bin/env python
+"""Throughput of the 2D unstructured Euler residual-and-update path on GB300.
+
+Workload (one "step" = one SSP-RK3 pseudo-time iteration over the whole mesh, including
+the per-iteration residual norms, forces and controller): NACA 0012, 512x128 O-grid split
+into 131,072 triangles with a seeded diagonal, interior nodes jittered by up to 10% of the
+local spacing, cells and faces permuted by the seed; M=0.8, alpha=1.25 deg, HLLC + MUSCL
+with the venkat limiter, characteristic far field, local time stepping at CFL 0.8.
+Synthetic data generated on the host from a fixed seed.
+
+Metric: Mcell-iter/s = cells x iterations / device seconds, FP32-bulk (headline) and FP64
+plain; |dCL| between them after a common number of iterations.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+Multi-GPU (torchrun): every rank runs an independent replica (a single case does not
+shard); value is the sum over ranks of cells x K divided by the slowest rank's time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+sys.path.insert(0, str(REPO / "aero-cfd-solver_gb300" / "python"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mcell-iter/s FP64 plain vs FP32 batched, |dCL|<1e-4; adjoint/primal time"
+WORKLOAD = dict(n_circ=512, n_radial=128, cell_type=3, permute=True, jitter=0.1, seed=2,
+                wall_spacing=0.005, farfield_radius=20.0)
+CASE = dict(mach=0.8, aoa_deg=1.25, flux=1, limiter=1, precond_farfield_bc=1, cfl_start=0.2, cfl_max=0.8,
+            cfl_ramp_iters=120, startup_first_order_iters=25, iterations=5000, min_iterations=5000,
+            residual_reduction_target=0.0)
+STARTUP = 25  # first-order start-up iterations run untimed before warm-up
+
+# DRAM traffic per launch of the residual kernel from ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum), keyed by (precision, n_cells); see profiles/.
+NCU_TRAFFIC = {}
+
+
+def algorithmic_bytes(kernel: str, n: int, slots: int, precision: str) -> float:
+    """Compulsory bytes of one launch: every array element the kernel reads or writes,
+    once (neighbour re-reads excluded). s = bulk real size."""
+    s = 4 if precision == "fp32" else 8
+    slot_geo = 4 + 16 + 8  # link, double2 normal, double area
+    if kernel == "residual":
+        return n * (4 * s + 8 * s + slots * (slot_geo + 4 * s) + 4 * s + s)
+    if kernel == "gradient":
+        return n * (4 * s + slots * slot_geo + 8 + 8 * s)
+    if kernel == "update":  # average over the three RK stages (stage 0 reads U_n only)
+        per = [4 * s + s + 32 + 32 + 4 * s, 4 * s + s + 64 + 32 + 4 * s, 4 * s + s + 64 + 1 + 32 + 4 * s]
+        return n * sum(per) / 3.0
+    raise KeyError(kernel)
+
+
+def measured_peak():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = Path(tempfile.mkstemp(suffix=".csv")[1])
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None:
+            return None
+        rows = []
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as td
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        td.init_process_group(backend=backend)
+        dist = td
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def reduce_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_mesh(args):
+    import aero_gb300
+
+    w = dict(WORKLOAD)
+    if args.mesh:
+        w["n_circ"], w["n_radial"] = args.mesh
+    return aero_gb300.ogrid_synthetic(**w)
+
+
+# ------------------------------------------------------------------------------------------
+# CPU arms (the oracle port of the reference, bit-identical to it in float mode)
+# ------------------------------------------------------------------------------------------
+def _cpu_worker(mesh_arrays, case_kw, warmup, steps, barrier_, out_q, state=None):
+    sys.path.insert(0, str(REPO))
+    sys.path.insert(0, str(REPO / "aero-cfd-solver_gb300" / "python"))
+    from aero_gb300 import capi
+    from oracle import oracle_py as op
+
+    mesh = capi.Mesh(**mesh_arrays)
+    case = capi.make_case(**case_kw)
+    sol = op.OracleSolver(op.MODE_FLOAT, mesh, case)
+    if state is not None:
+        sol.set_state(state)
+    sol.run(warmup)
+    if barrier_ is not None:
+        barrier_.wait()
+    t0 = time.perf_counter()
+    sol.run(steps)
+    out_q.put(time.perf_counter() - t0)
+
+
+def _mesh_arrays(mesh):
+    return dict(owner=mesh.owner, neighbor=mesh.neighbor, bc=mesh.bc, normal=mesh.normal, center=mesh.center,
+                area=mesh.area, volume=mesh.volume, cell_center=mesh.cell_center, wall_faces=mesh.wall_faces)
+
+
+def cpu_sample(mesh, state, target_s=12.0, max_iters=40):
+    """Single-core oracle port on a bounded sample: second-order iterations from the
+    device state after start-up, until about target_s seconds of CPU work."""
+    from aero_gb300 import capi
+    from oracle import oracle_py as op
+
+    op.build()
+    kw = dict(CASE, startup_first_order_iters=0)
+    sol = op.OracleSolver(op.MODE_FLOAT, mesh, capi.make_case(**kw))
+    sol.set_state(state)
+    t0 = time.perf_counter()
+    sol.run(1)
+    one = time.perf_counter() - t0
+    n = int(max(1, min(max_iters, target_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    sol.run(n)
+    dt = time.perf_counter() - t0
+    return {"value": mesh.num_cells * n / dt / 1e6, "unit": "Mcell-iter/s", "cores": 1, "kind": "port",
+            "sample": f"{n} second-order iterations of the oracle float port (bit-identical to the "
+                      f"reference CPU path) on the {mesh.num_cells}-cell workload mesh, 1 thread"}
+
+
+def run_reference_arm(args):
+    world, rank, local, dist = dist_setup(args)
+    if rank != 0:
+        return
+    import multiprocessing as mp
+
+    from oracle import oracle_py as op
+
+    op.build()
+    mesh = make_mesh(args)
+    procs_n = max(1, os.cpu_count() or 1)
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    bar = ctx.Barrier(procs_n)
+    kw = dict(CASE, startup_first_order_iters=0)
+    arrays = _mesh_arrays(mesh)
+    procs = [ctx.Process(target=_cpu_worker, args=(arrays, kw, args.warmup, args.steps, bar, q)) for _ in range(procs_n)]
+    t0 = time.perf_counter()
+    for p in procs:
+        p.start()
+    times = [q.get() for _ in procs]
+    for p in procs:
+        p.join()
+    wall = max(times)
+    value = procs_n * mesh.num_cells * args.steps / wall / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mcell-iter/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "NACA0012 512x128 O-grid, 131072 triangles, jitter 10%, permuted; M=0.8, "
+                               "alpha=1.25, HLLC+MUSCL venkat, RK3 local dt, CFL 0.8",
+                   "cells": mesh.num_cells, "replicas": procs_n},
+        "cpu_baseline": {"value": value, "unit": "Mcell-iter/s", "cores": procs_n, "kind": "port",
+                         "sample": f"{args.steps} second-order iterations per process after {args.warmup} "
+                                   f"warm-up, {procs_n} independent single-thread replicas of the oracle float "
+                                   f"port (bit-identical to the reference CPU path); the reference's sources "
+                                   f"are not on this host, so its own binary cannot be built here"},
+        "e2e": {"value": value, "unit": "Mcell-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "elapsed_s": time.perf_counter() - t0,
+    }
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------
+def run_gpu_arm(args):
+    import aero_gb300
+    from aero_gb300 import capi
+
+    world, rank, local, dist = dist_setup(args)
+    aero_gb300.load()
+    aero_gb300.select_device(local)
+    mesh = make_mesh(args)
+    n = mesh.num_cells
+    precisions = ["fp32", "fp64"] if args.precision == "both" else [args.precision]
+    results = {}
+    peak, peak_kind = measured_peak()
+    for prec in precisions:
+        pcode = capi.PRECISION_FP32 if prec == "fp32" else capi.PRECISION_FP64
+        case = capi.make_case(**CASE, precision=pcode)
+        with aero_gb300.Solver(mesh, case) as s:
+            info = s.info()
+            s.run(STARTUP)
+            s.time_iterations(args.warmup, use_graph=True, flush_l2=True)
+            barrier(dist)
+            sampler = ClockSampler(local) if prec == "fp32" and not args.no_clocks else None
+            if sampler:
+                sampler.__enter__()
+            ms = s.time_iterations(args.steps, use_graph=True, flush_l2=not args.no_flush)
+            if sampler:
+                sampler.__exit__(None, None, None)
+            barrier(dist)
+            ms_max = reduce_max(dist, ms)
+            warm_ms = s.time_iterations(args.steps, use_graph=True, flush_l2=False)
+            prof = s.profile_kernels(max(2, min(args.steps, 10)), flush_l2=not args.no_flush)
+            state = s.get_state() if prec == "fp32" else None
+            finite = bool(np.all(np.isfinite(s.get_state())))
+        value = world * n * args.steps / (ms_max / 1e3) / 1e6
+        res_ms, res_n = prof["residual"]
+        avg_res = res_ms / max(res_n, 1)
+        bytes_res = algorithmic_bytes("residual", n, info["slots_per_cell"], prec)
+        achieved = bytes_res / (avg_res / 1e3) / 1e9
+        total_prof = sum(v[0] for v in prof.values())
+        results[prec] = dict(value=value, ms=ms_max, warm_ms=warm_ms, info=info, prof=prof, state=state,
+                             finite=finite, achieved=achieved, avg_res_ms=avg_res, bytes_res=bytes_res,
+                             share=res_ms / total_prof if total_prof else None, clocks=sampler.summary() if sampler else None)
+    head = results[precisions[0]]
+
+    # |dCL| between FP32 and FP64 after a common number of iterations from freestream
+    dcl = None
+    if args.precision == "both" and args.dcl_iters > 0:
+        cls = {}
+        for prec, pcode in (("fp32", capi.PRECISION_FP32), ("fp64", capi.PRECISION_FP64)):
+            with aero_gb300.Solver(mesh, capi.make_case(**CASE, precision=pcode)) as s:
+                _, rec = s.run(args.dcl_iters)
+                cls[prec] = (rec["cl"][-1], rec["cd"][-1], rec["residual_l2"][-1] / rec["residual_l2"][0])
+        dcl = dict(iters=args.dcl_iters, abs_dcl=abs(cls["fp32"][0] - cls["fp64"][0]),
+                   abs_dcd=abs(cls["fp32"][1] - cls["fp64"][1]), cl_fp64=cls["fp64"][0], cd_fp64=cls["fp64"][1],
+                   l2_ratio_fp64=cls["fp64"][2])
+
+    # end to end through the C ABI with host buffers: upload the state, run K iterations
+    # with every iteration's record copied to the host, download the state
+    e2e = None
+    if head["state"] is not None or precisions[0] == "fp64":
+        pcode = capi.PRECISION_FP32 if precisions[0] == "fp32" else capi.PRECISION_FP64
+        with aero_gb300.Solver(mesh, capi.make_case(**CASE, precision=pcode)) as s:
+            u0 = s.get_state() if head["state"] is None else head["state"]
+            s.run(STARTUP)
+            barrier(dist)
+            t0 = time.perf_counter()
+            s.set_state(u0)
+            _, rec = s.run(args.steps)
+            u1 = s.get_state()
+            dt = time.perf_counter() - t0
+            barrier(dist)
+        dt = reduce_max(dist, dt)
+        rec_bytes = len(rec) * rec.dtype.itemsize
+        e2e = {"value": world * n * args.steps / dt / 1e6, "unit": "Mcell-iter/s",
+               "h2d_bytes_per_step": int(u0.nbytes / args.steps),
+               "d2h_bytes_per_step": int((rec_bytes + u1.nbytes) / args.steps)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu and head["state"] is not None:
+        cpu = cpu_sample(mesh, head["state"])
+
+    if rank != 0:
+        return
+    r32 = results.get("fp32")
+    r64 = results.get("fp64")
+    line = {
+        "metric": METRIC, "value": head["value"], "unit": "Mcell-iter/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if precisions[0] == "fp32" else "f64", "data": "synthetic",
+        "config": {
+            "workload": "NACA0012 512x128 O-grid, 131072 triangles, jitter 10%, permuted; M=0.8, alpha=1.25, "
+                        "HLLC+MUSCL venkat, RK3 local dt, CFL 0.8" if not args.mesh else
+                        f"NACA0012 {args.mesh[0]}x{args.mesh[1]} O-grid (small profiling case)",
+            "cells": n, "faces": int(head["info"]["faces"]), "precision_headline": precisions[0],
+            "l2": "flushed before every timed iteration (256 MiB write)" if not args.no_flush else "not flushed",
+            "parallelism": f"replicas x{world}", "timing": "CUDA events on the library stream, CUDA graph per iteration",
+            "fp32_mcell_iter_s": r32["value"] if r32 else None,
+            "fp64_mcell_iter_s": r64["value"] if r64 else None,
+            "fp32_over_fp64": (r32["value"] / r64["value"]) if (r32 and r64) else None,
+            "fp32_l2_warm_mcell_iter_s": world * n * args.steps / (r32["warm_ms"] / 1e3) / 1e6 if r32 else None,
+            "fp64_l2_warm_mcell_iter_s": world * n * args.steps / (r64["warm_ms"] / 1e3) / 1e6 if r64 else None,
+            "dcl": dcl,
+            "kernel_profile_ms_per_launch": {k: (v[0] / v[1] if v[1] else 0.0) for k, v in head["prof"].items()},
+            "state_finite": head["finite"],
+        },
+        "roofline": {"bound": "hbm", "kernel": "k_residual (reconstruction + flux + gather)",
+                     "achieved": head["achieved"], "peak": peak, "unit": "GB/s", "frac": head["achieved"] / peak,
+                     "peak_kind": peak_kind, "traffic": NCU_TRAFFIC.get((precisions[0], n)),
+                     "algorithmic_bytes_per_launch": head["bytes_res"], "avg_launch_ms": head["avg_res_ms"],
+                     "time_share": head["share"]},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": int(head["info"]["launches_per_iteration"]) * args.steps,
+        "clocks": head["clocks"],
+    }
+    if r64 and precisions[0] == "fp32":
+        line["roofline_fp64"] = {"achieved": r64["achieved"], "frac": r64["achieved"] / peak,
+                                 "avg_launch_ms": r64["avg_res_ms"]}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--precision", choices=["fp32", "fp64", "both"], default="both")
+    ap.add_argument("--mesh", type=int, nargs=2, default=None, help="n_circ n_radial of a smaller mesh")
+    ap.add_argument("--dcl-iters", type=int, default=300)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-flush", action="store_true")
+    ap.add_argument("--no-clocks", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

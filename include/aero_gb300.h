@@ -30,6 +30,12 @@ extern "C" {
 
 #define AERO_ABI_VERSION 1
 
+#if defined(__GNUC__)
+#define AERO_API __attribute__((visibility("default")))
+#else
+#define AERO_API
+#endif
+
 enum aero_status {
   AERO_OK = 0,
   AERO_ERR_INVALID = 1,   /* bad argument (std::invalid_argument in the reference) */
@@ -107,7 +113,8 @@ typedef struct aero_case_desc {
   int aoa0_symmetry_enforce, aoa0_symmetry_enforce_interval;
   int precision; /* enum aero_precision */
   int ordering;  /* enum aero_ordering */
-  int block_size; /* threads per block of the cell kernels; 0 = library default */
+  int block_size; /* threads per block of the cell kernels (64, 128 or 256); 0 = default */
+  int diagnostics; /* 1: also form the pressure-jump energies of every iteration */
 } aero_case_desc;
 
 /* One record per pseudo-time iteration: the rows of residuals.csv and forces.csv
@@ -141,28 +148,28 @@ enum aero_record_flags {
 typedef struct aero_ctx aero_ctx;
 
 /* Library identity. */
-int aero_abi_version(void);
-const char* aero_version(void);
+AERO_API int aero_abi_version(void);
+AERO_API const char* aero_version(void);
 /* 1 when a CUDA device of compute capability 10.x is usable (the reference's
  * cuda_available(), residual_stub.cpp:300-306). */
-int aero_cuda_available(void);
+AERO_API int aero_cuda_available(void);
 
 /* Fill *c with the reference's defaults (euler_solver.hpp:14-74). */
-void aero_case_defaults(aero_case_desc* c);
+AERO_API void aero_case_defaults(aero_case_desc* c);
 
 /* Replaces init_euler_device_buffers (cuda_backend.hpp:44-46): validates and copies
  * the mesh, renumbers cells, builds the cell-owned face slots, allocates all device
  * state and sets the conserved state to the freestream. */
-int aero_create(const aero_mesh_desc* mesh, const aero_case_desc* cfg, aero_ctx** out);
+AERO_API int aero_create(const aero_mesh_desc* mesh, const aero_case_desc* cfg, aero_ctx** out);
 /* Replaces free_euler_device_buffers (cuda_backend.hpp:47). Null is a no-op. */
-void aero_destroy(aero_ctx* ctx);
-const char* aero_last_error(const aero_ctx* ctx);
+AERO_API void aero_destroy(aero_ctx* ctx);
+AERO_API const char* aero_last_error(const aero_ctx* ctx);
 
 /* Conserved state, AoS [N][5], original cell order. */
-int aero_set_state(aero_ctx* ctx, const double* conserved);
-int aero_get_state(aero_ctx* ctx, double* conserved);
+AERO_API int aero_set_state(aero_ctx* ctx, const double* conserved);
+AERO_API int aero_get_state(aero_ctx* ctx, double* conserved);
 /* Primitive fields of the current state (rho, u, v, p), each [N] original order. */
-int aero_get_primitive(aero_ctx* ctx, double* rho, double* u, double* v, double* p);
+AERO_API int aero_get_primitive(aero_ctx* ctx, double* rho, double* u, double* v, double* p);
 
 /* One residual evaluation on the given conserved state (replaces euler_residual_cuda,
  * cuda_backend.hpp:49-52, and covers the gradient and MUSCL steps the reference
@@ -170,7 +177,7 @@ int aero_get_primitive(aero_ctx* ctx, double* rho, double* u, double* v, double*
  * gradients may be null, else [N][5][2] primitive gradients (rho,u,v,w,p x,y).
  * stab_mach_floor, all_speed_f_min and all_speed_ramp_weight are the per-iteration
  * controller values (euler_solver.cpp:772-797). The context's state is unchanged. */
-int aero_residual(aero_ctx* ctx, const double* conserved, int second_order,
+AERO_API int aero_residual(aero_ctx* ctx, const double* conserved, int second_order,
                   double stab_mach_floor, int all_speed_flux_fix, double all_speed_f_min,
                   double all_speed_ramp_weight, double* residual, double* spectral_radius,
                   double* gradients);
@@ -182,23 +189,35 @@ int aero_residual(aero_ctx* ctx, const double* conserved, int second_order,
  * *n_done receives the number executed (fewer than n when the monitor converged or
  * the non-finite trap fired; then AERO_ERR_NONFINITE is returned). Calls continue
  * the same run: the iteration counter and controller state persist in the context. */
-int aero_run(aero_ctx* ctx, int n, aero_iter_record* records, int* n_done);
+AERO_API int aero_run(aero_ctx* ctx, int n, aero_iter_record* records, int* n_done);
 /* Restart the iteration counter and controller state (state is kept). */
-int aero_reset_run(aero_ctx* ctx);
+AERO_API int aero_reset_run(aero_ctx* ctx);
 
 /* Last residual (pre-preconditioning, last RK stage) and spectral radius of the
  * last executed iteration (EulerRunResult::last_residual / last_spectral_radius). */
-int aero_get_last_residual(aero_ctx* ctx, double* residual, double* spectral_radius);
+AERO_API int aero_get_last_residual(aero_ctx* ctx, double* residual, double* spectral_radius);
 
 /* Timing helper: run n iterations with no records copied out and report the device
  * time between CUDA events recorded on the context's stream around them. Uses the
- * CUDA graph of one iteration when use_graph is 1. */
-int aero_time_iterations(aero_ctx* ctx, int n, int use_graph, double* device_ms);
+ * CUDA graph of one iteration when use_graph is 1. With flush_l2 = 1 a 256 MiB buffer
+ * is overwritten before every iteration (outside the timed intervals) so that no
+ * iteration starts with its working set in L2. */
+AERO_API int aero_time_iterations(aero_ctx* ctx, int n, int use_graph, int flush_l2,
+                                  double* device_ms);
+/* Per-kernel profile of n iterations, every launch between its own CUDA events.
+ * ms[6] receives summed device time and launches[6] the launch count of the kernel
+ * classes 0 gradient, 1 residual, 2 update, 3 global-time-step reduction,
+ * 4 symmetry/pressure-jump, 5 controller. */
+AERO_API int aero_profile_kernels(aero_ctx* ctx, int n, int flush_l2, double* ms, int* launches);
+
+/* Make `device` the current device of the library's CUDA runtime for this host thread
+ * (contexts created afterwards on this thread live there). */
+AERO_API int aero_select_device(int device);
 
 /* Sizes and kernel-launch counts of the context, for roofline accounting:
  * info[0] cells, [1] faces, [2] slots per cell (padded), [3] kernel launches per
  * iteration, [4] bytes of device memory held, [5] precision, [6] block size. */
-int aero_get_info(aero_ctx* ctx, long long* info, int n_info);
+AERO_API int aero_get_info(aero_ctx* ctx, long long* info, int n_info);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,77 @@
+"""C-ABI library checks that need no GPU: it loads, exports every symbol the public
+headers declare, its defaults match the reference's, and it refuses to run without a
+device instead of falling back to the CPU."""
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import aero_gb300
+from aero_gb300 import capi
+
+REPO = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return aero_gb300.load(build_if_missing=True)
+
+
+def declared_symbols():
+    names = []
+    for header in sorted((REPO / "include").glob("*.h")):
+        text = header.read_text()
+        names += re.findall(r"^AERO_API\s+[\w\s\*]+?\b(aero_\w+)\s*\(", text, flags=re.M)
+    return names
+
+
+def test_headers_declare_symbols():
+    names = declared_symbols()
+    assert "aero_create" in names and "aero_run" in names and "aero_mesh_ogrid_reference" in names
+    assert len(names) == len(set(names))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+
+
+def test_identity(lib):
+    assert lib.aero_abi_version() == 1
+    assert lib.aero_version().decode().endswith("gb300")
+
+
+def test_case_defaults_match_reference(lib):
+    c = capi.CaseDesc()
+    lib.aero_case_defaults(C.byref(c))
+    got = capi.case_to_dict(c)
+    for key, val in capi.CASE_DEFAULTS.items():
+        assert got[key] == val, key
+
+
+def test_no_cpu_fallback_without_device(lib):
+    if lib.aero_cuda_available():
+        pytest.skip("a CUDA device is present")
+    mesh = aero_gb300.ogrid_reference(n_circ=32, n_radial=4, farfield_radius=10.0, radial_stretch=1.25)
+    with pytest.raises(aero_gb300.AeroError) as exc:
+        aero_gb300.Solver(mesh, capi.make_case())
+    assert exc.value.code == capi.AERO_ERR_CUDA
+
+
+def test_invalid_arguments_are_rejected(lib):
+    mesh = aero_gb300.ogrid_reference(n_circ=32, n_radial=4, farfield_radius=10.0, radial_stretch=1.25)
+    with pytest.raises(aero_gb300.AeroError) as exc:
+        aero_gb300.Solver(mesh, capi.make_case(rk_stages=2))
+    assert exc.value.code == capi.AERO_ERR_INVALID
+    with pytest.raises(aero_gb300.AeroError) as exc:
+        aero_gb300.Solver(mesh, capi.make_case(rho_inf=-1.0, p_inf=-1.0))
+    assert exc.value.code == capi.AERO_ERR_INVALID
+
+
+def test_record_struct_size_matches_header():
+    # aero_iter_record: 4 ints + 34 doubles
+    assert C.sizeof(capi.IterRecord) == 4 * 4 + 34 * 8
+    assert np.dtype(capi.RECORD_DTYPE).itemsize == C.sizeof(capi.IterRecord)

@@ -1,0 +1,277 @@
+"""Parity of the sm_103a path (through the C ABI) with the CPU oracle and with the
+reference's golden vectors.
+
+Tolerances (per cell and component, relative to the cell's flux scale
+S_c = SR_c * max_k |U_c,k|, an upper bound of sum_faces |F_k A| up to a constant):
+  FP64 path vs FP64 oracle : 1e-12 (residual), 1e-12 (spectral radius, relative)
+  FP32 path vs float reference (golden) : 2e-5; the device contracts multiply-adds
+Whole runs compare histories and states at the tolerances given in each test."""
+
+import json
+
+import numpy as np
+import pytest
+
+import aero_gb300
+from aero_gb300 import capi
+from conftest import golden_mesh
+from oracle import oracle_py as op
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _device():
+    lib = aero_gb300.load(build_if_missing=True)
+    assert lib.aero_cuda_available(), "GPU tests need an sm_103 device"
+    op.build()
+
+
+def scale(sr, u):
+    return np.abs(sr)[:, None] * np.abs(u).max(axis=1, keepdims=True) + 1e-300
+
+
+def rel_err(a, b, sr, u):
+    return float(np.max(np.abs(a - b) / scale(sr, u)))
+
+
+def seeded_state(sol_or_mesh_case, seed, amp=0.05):
+    mesh, case = sol_or_mesh_case
+    o = op.OracleSolver(op.MODE_DOUBLE, mesh, case)
+    u = o.get_state().copy()
+    rng = np.random.default_rng(seed)
+    x = mesh.cell_center.reshape(-1, 3)
+    smooth = 0.1 * np.sin(1.3 * x[:, 0]) * np.cos(0.7 * x[:, 1])
+    for k in (0, 1, 2, 4):
+        u[:, k] *= 1.0 + smooth + amp * rng.standard_normal(len(u))
+    u[:, 3] = 0.0
+    return u
+
+
+COMBOS = [dict(flux=f, limiter=l, precond_on=p, low_mach_fix=p, all_speed_flux_fix=p, precond_farfield_bc=p)
+          for f in (0, 1) for l in (0, 1) for p in (0, 1)]
+BASE = dict(mach=0.3, aoa_deg=2.0, gas_constant=1.0, p_inf=1.0, t_inf=1.0, rho_inf=1.0)
+
+
+# ------------------------------------------------------------------------------------------
+# single residual evaluations
+# ------------------------------------------------------------------------------------------
+def test_residual_fp64_vs_oracle_on_golden_states(golden_meshes, golden_residuals):
+    data, meta = golden_residuals
+    mesh = golden_mesh(golden_meshes, "ogrid_32x4")
+    worst = 0.0
+    for m in meta:
+        case = capi.make_case(**m["case"], precision=capi.PRECISION_FP64)
+        u = data[m["key"] + "/u"].astype(np.float64)
+        args = (m["second_order"], m["stab"], m["as_fix"], m["as_fmin"], m["as_ramp"])
+        with aero_gb300.Solver(mesh, case) as s:
+            r, sr, g = s.residual(u, *args)
+        ro, sro, go, _ = op.OracleSolver(op.MODE_DOUBLE, mesh, case).residual(u, *args)
+        tol = 1e-12 if "_s0_" in m["key"] else 1e-9
+        e = rel_err(r, ro, sro, u)
+        worst = max(worst, e if tol == 1e-12 else 0.0)
+        assert e <= tol, (m["key"], e)
+        np.testing.assert_allclose(sr, sro, rtol=1e-12, err_msg=m["key"])
+        if m["second_order"]:
+            gs = np.abs(go).max() + 1e-300
+            assert np.max(np.abs(g - go)) / gs < 1e-12, m["key"]
+    print("worst FP64 residual error", worst)
+
+
+def test_residual_fp32_vs_reference_golden(golden_meshes, golden_residuals):
+    data, meta = golden_residuals
+    mesh = golden_mesh(golden_meshes, "ogrid_32x4")
+    for m in meta:
+        if "_s1_" in m["key"]:
+            continue  # near-vacuum stress states: float round-off is unbounded there
+        case = capi.make_case(**m["case"], precision=capi.PRECISION_FP32)
+        u = data[m["key"] + "/u"].astype(np.float64)
+        with aero_gb300.Solver(mesh, case) as s:
+            r, sr, _ = s.residual(u, m["second_order"], m["stab"], m["as_fix"], m["as_fmin"], m["as_ramp"])
+        ref_r = data[m["key"] + "/r"].astype(np.float64)
+        ref_sr = data[m["key"] + "/sr"].astype(np.float64)
+        assert rel_err(r, ref_r, ref_sr, u) <= 2e-5, m["key"]
+        np.testing.assert_allclose(sr, ref_sr, rtol=2e-6, err_msg=m["key"])
+
+
+@pytest.mark.parametrize("cell_type", [3, 4])
+@pytest.mark.parametrize("combo", [0, 3, 4, 7])
+def test_residual_fp64_synthetic_mesh(cell_type, combo):
+    mesh = aero_gb300.ogrid_synthetic(96, 24, cell_type=cell_type, permute=True, jitter=0.1, seed=11)
+    case = capi.make_case(**BASE, **COMBOS[combo], precision=capi.PRECISION_FP64)
+    u = seeded_state((mesh, case), seed=combo)
+    for second in (0, 1):
+        with aero_gb300.Solver(mesh, case) as s:
+            r, sr, _ = s.residual(u, second, 0.02, COMBOS[combo]["all_speed_flux_fix"], 0.05, 0.7)
+        ro, sro, _, _ = op.OracleSolver(op.MODE_DOUBLE, mesh, case).residual(
+            u, second, 0.02, COMBOS[combo]["all_speed_flux_fix"], 0.05, 0.7)
+        assert rel_err(r, ro, sro, u) <= 1e-12
+        np.testing.assert_allclose(sr, sro, rtol=1e-12)
+
+
+@pytest.mark.parametrize("precision", [capi.PRECISION_FP64, capi.PRECISION_FP32])
+def test_freestream_preservation_jittered(precision):
+    """Uniform freestream on a jittered, permuted mesh: every cell not touching the wall has
+    a zero residual to round-off (the wall flux is pressure-only, so wall cells do not)."""
+    mesh = aero_gb300.ogrid_synthetic(128, 32, cell_type=3, permute=True, jitter=0.1, seed=5)
+    tol = 1e-13 if precision == capi.PRECISION_FP64 else 2e-6
+    wall_cells = set(mesh.owner[mesh.wall_faces].tolist())
+    keep = np.array([c not in wall_cells for c in range(mesh.num_cells)])
+    for flux in (0, 1):
+        case = capi.make_case(mach=0.5, aoa_deg=2.0, flux=flux, limiter=1, precision=precision)
+        with aero_gb300.Solver(mesh, case) as s:
+            u = s.get_state()
+            r, sr, _ = s.residual(u, 1, 0.0, 0, 0.05, 1.0)
+        assert np.max(np.abs(r[keep]) / scale(sr, u)[keep]) <= tol
+
+
+@pytest.mark.parametrize("precision", [capi.PRECISION_FP64, capi.PRECISION_FP32])
+def test_ordering_and_block_size_do_not_change_results(precision):
+    """Each cell sums its faces in the original face order whatever the renumbering, so the
+    residual is bit-identical across orderings and block sizes."""
+    mesh = aero_gb300.ogrid_synthetic(64, 16, cell_type=3, permute=True, seed=2)
+    ref = None
+    for ordering in (capi.ORDER_NONE, capi.ORDER_MORTON, capi.ORDER_RCM):
+        for block in (64, 128, 256):
+            case = capi.make_case(mach=0.6, flux=1, limiter=1, precision=precision, ordering=ordering,
+                                  block_size=block)
+            u = seeded_state((mesh, case), seed=9)
+            with aero_gb300.Solver(mesh, case) as s:
+                r, sr, _ = s.residual(u, 1, 0.0, 0, 0.05, 1.0)
+            if ref is None:
+                ref = (r, sr)
+            else:
+                np.testing.assert_array_equal(r, ref[0])
+                np.testing.assert_array_equal(sr, ref[1])
+
+
+# ------------------------------------------------------------------------------------------
+# whole runs
+# ------------------------------------------------------------------------------------------
+RUN_NAMES = ["parity", "regression", "aoa0", "wall_sanity", "hllc_venkat", "precond", "staged",
+             "global_dt_rk1", "low_mach_on"]
+
+
+def _run_case(meta, name):
+    m = meta[name]
+    kw = dict(m["case"])
+    if kw.get("precond_on") and not m["precond_env"]:
+        kw["precond_on"] = 0
+    return m["mesh"], kw
+
+
+@pytest.mark.parametrize("name", RUN_NAMES)
+def test_run_fp64_vs_oracle(name, golden_meshes, golden_histories):
+    data, meta = golden_histories
+    mesh_name, kw = _run_case(meta, name)
+    mesh = golden_mesh(golden_meshes, mesh_name)
+    case = capi.make_case(**kw, precision=capi.PRECISION_FP64, diagnostics=1)
+    n = case.iterations
+    with aero_gb300.Solver(mesh, case) as s:
+        _, rec = s.run(n)
+        state = s.get_state()
+        lr, lsr = s.last_residual()
+    o = op.OracleSolver(op.MODE_DOUBLE, mesh, case)
+    _, orec = o.run(n)
+    assert len(rec) == len(orec)
+    l2 = orec["residual_l2"]
+    assert np.max(np.abs(rec["residual_l2"] - l2) / (np.abs(l2) + 1e-300)) < 1e-9
+    for key in ("cl", "cd", "cm"):
+        assert np.max(np.abs(rec[key] - orec[key])) < 1e-10, key
+    np.testing.assert_allclose(rec["cfl"], orec["cfl"], rtol=1e-12)
+    np.testing.assert_array_equal(rec["flags"] & 0xff, orec["flags"] & 0xff)
+    ostate = o.get_state()
+    colscale = np.abs(ostate).max(axis=0) + 1e-300
+    assert np.max(np.abs(state - ostate) / colscale) < 1e-10
+    olr, olsr = o.last_residual()
+    assert rel_err(lr, olr, olsr, ostate) < 1e-9
+    if name == "staged":
+        np.testing.assert_allclose(rec["p_jump_energy_wall_nd"], orec["p_jump_energy_wall_nd"], rtol=1e-8,
+                                   atol=1e-30)
+
+
+@pytest.mark.parametrize("name", ["regression", "hllc_venkat", "precond", "low_mach_on"])
+def test_run_fp32_vs_mixed_oracle_and_reference(name, golden_meshes, golden_histories):
+    data, meta = golden_histories
+    mesh_name, kw = _run_case(meta, name)
+    mesh = golden_mesh(golden_meshes, mesh_name)
+    case = capi.make_case(**kw, precision=capi.PRECISION_FP32)
+    n = case.iterations
+    with aero_gb300.Solver(mesh, case) as s:
+        _, rec = s.run(n)
+    _, orec = op.OracleSolver(op.MODE_MIXED, mesh, case).run(n)
+    assert len(rec) == len(orec)
+    assert np.max(np.abs(rec["cl"] - orec["cl"])) < 1e-4
+    assert np.max(np.abs(rec["residual_l2"] - orec["residual_l2"]) / orec["residual_l2"]) < 1e-2
+    ref = data[name + "/history"]
+    assert abs(rec["cl"][-1] - ref[-1, 4]) < 1e-3
+    assert abs(rec["cd"][-1] - ref[-1, 5]) < 1e-3
+
+
+def test_reference_test_assertions_hold_on_device(golden_meshes, golden_histories):
+    """The reference's C++ test thresholds, run on the device in both precisions
+    (test_euler_regression.cpp:40-61, test_euler_aoa0_regression.cpp:78-83,
+    test_euler_low_mach_asymptotic.cpp:315-316)."""
+    data, meta = golden_histories
+    for precision in (capi.PRECISION_FP64, capi.PRECISION_FP32):
+        mesh_name, kw = _run_case(meta, "regression")
+        with aero_gb300.Solver(golden_mesh(golden_meshes, mesh_name), capi.make_case(**kw, precision=precision)) as s:
+            _, rec = s.run(kw["iterations"])
+        assert rec["residual_l2"][-1] <= rec["residual_l2"][0] * 1.2
+        assert 0.16 <= rec["cl"][-1] <= 0.30 and abs(rec["cd"][-1]) <= 0.25
+        mesh_name, kw = _run_case(meta, "aoa0")
+        with aero_gb300.Solver(golden_mesh(golden_meshes, mesh_name), capi.make_case(**kw, precision=precision)) as s:
+            _, rec = s.run(kw["iterations"])
+        assert abs(rec["cl"][-1]) < 0.05 and abs(rec["cd"][-1]) < 0.06
+        cdm = {}
+        for tag in ("low_mach_off", "low_mach_on"):
+            mesh_name, kw = _run_case(meta, tag)
+            with aero_gb300.Solver(golden_mesh(golden_meshes, mesh_name), capi.make_case(**kw, precision=precision)) as s:
+                _, rec = s.run(kw["iterations"])
+            cdm[tag] = rec["cd"][-1] * 0.01
+        assert abs(cdm["low_mach_on"]) < 0.95 * abs(cdm["low_mach_off"])
+
+
+def test_nonfinite_trap_returns_status_and_context_recovers():
+    mesh = aero_gb300.ogrid_synthetic(48, 12, seed=1)
+    case = capi.make_case(mach=0.5, iterations=10, precision=capi.PRECISION_FP64)
+    with aero_gb300.Solver(mesh, case) as s:
+        u0 = s.get_state()
+        bad = u0.copy()
+        bad[17, 0] = np.nan
+        s.set_state(bad)
+        rc, rec = s.run(5, raise_on_nonfinite=False)
+        assert rc == capi.AERO_ERR_NONFINITE
+        assert len(rec) == 1 and rec["flags"][0] & capi.REC_NONFINITE
+        rc, rec = s.run(5, raise_on_nonfinite=False)  # trapped runs stay stopped
+        assert len(rec) == 0
+        s.set_state(u0)
+        s.reset_run()
+        _, rec = s.run(5)
+        assert len(rec) == 5 and np.all(np.isfinite(rec["residual_l2"]))
+
+
+@pytest.mark.parametrize("precision", [capi.PRECISION_FP64, capi.PRECISION_FP32])
+def test_runs_are_deterministic(precision):
+    mesh = aero_gb300.ogrid_synthetic(64, 16, seed=8)
+    case = capi.make_case(mach=0.7, flux=1, limiter=1, startup_first_order_iters=3, precision=precision)
+    outs = []
+    for _ in range(2):
+        with aero_gb300.Solver(mesh, case) as s:
+            _, rec = s.run(20)
+            outs.append((rec, s.get_state()))
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+    for key in ("residual_l1", "residual_l2", "cl", "cd", "cm"):
+        np.testing.assert_array_equal(outs[0][0][key], outs[1][0][key])
+
+
+def test_run_stops_at_convergence_like_the_monitor():
+    mesh = aero_gb300.ogrid_synthetic(48, 12, seed=1)
+    case = capi.make_case(mach=0.3, min_iterations=5, residual_reduction_target=1e6, force_stability_tol=1.0,
+                          force_mean_drift_tol=1.0, force_stability_window=2, precision=capi.PRECISION_FP64)
+    with aero_gb300.Solver(mesh, case) as s:
+        _, rec = s.run(50)
+    o = op.OracleSolver(op.MODE_DOUBLE, mesh, case)
+    _, orec = o.run(50)
+    assert len(rec) == len(orec) == 5
+    assert rec["flags"][-1] & capi.REC_CONVERGED

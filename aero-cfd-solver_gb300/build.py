@@ -24,7 +24,7 @@ OBJ = PKG / "_build"
 LIB = PKG / "lib" / "libaero_gb300.so"
 
 CU_SOURCES = ["engine_f32.cu", "engine_f64.cu"]
-CPP_SOURCES = ["capi.cpp", "mesh_prep.cpp", "mesh_gen.cpp"]
+CPP_SOURCES = ["capi.cpp", "mesh_prep.cpp", "mesh_gen.cpp", "driver.cpp"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 

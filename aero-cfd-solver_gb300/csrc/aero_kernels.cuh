@@ -83,6 +83,7 @@ struct CtrlConfig {
   double st_fmin_high, st_fmin_mid, st_fmin_low;
   double pj_target, pj_spike, cfl_drop, cfl_restore, cfl_min_scale;
   double p_inf, q_inf, s_ref, chord, cos_a, sin_a, x_ref, y_ref, pressure_ref, gamma;
+  double rho_inf, u_inf, v_inf;
 };
 
 // Precondition constants in double for the residual preconditioner (preconditioning.cpp:51-76).
@@ -619,14 +620,24 @@ struct Record {
   double stab, as_fmin, as_ramp;
   double dp_dom, dp_wall;
   double pj, pj_wall;
+  double wall_un, wall_mass_flux, cp_min, cp_max;
+  double ff_dp, ff_drho, ff_du, ff_dv;
+  int cp_nonfinite, action;
+};
+
+// Owner cells of the far-field faces, for the far-field deviation monitors.
+struct FarSet {
+  const int* cell;
+  int n;
 };
 
 // Controller (one block): norms, forces, convergence monitor, adaptive CFL, staged all-speed
 // controller and the next iteration's schedule (euler_solver.cpp:948-1208, 772-797;
 // convergence_monitor.cpp:13-127).
-static __global__ void __launch_bounds__(1024) k_control(CtrlConfig cc, WallSet ws, const d4* __restrict__ Un,
-                                                  Partials part, Ctrl* __restrict__ ctrl,
-                                                  Record* __restrict__ recs, int rec_cap) {
+static __global__ void __launch_bounds__(1024) k_control(CtrlConfig cc, WallSet ws, FarSet fs,
+                                                  const d4* __restrict__ Un, Partials part,
+                                                  Ctrl* __restrict__ ctrl, Record* __restrict__ recs,
+                                                  int rec_cap) {
   __shared__ double shm[32 * 8];
   if (ctrl->done) return;
   const int tid = threadIdx.x;
@@ -653,11 +664,13 @@ static __global__ void __launch_bounds__(1024) k_control(CtrlConfig cc, WallSet 
     for (int k = 0; k < 4; ++k) pj[k] += part.pjump[4 * b + k];
   }
   block_sum<4>(pj, shm);
-  // forces
+  // forces (forces.cpp:208-294) and wall monitors (euler_solver.cpp:976-1006)
   double fsum[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // snx sny fxa fya fxg fyg ma mg
+  double un_max = 0.0, cp_hi = -1.0e308, cp_lo_neg = -1.0e308, cp_bad = 0.0;
   for (int i = tid; i < cc.n_wall; i += blockDim.x) {
     const d4 u = Un[ws.cell[i]];
-    const double p = cons_to_prim(Cons<double>{u.x, u.y, u.z, u.w}, cc.gamma).p;
+    const Prim<double> w = cons_to_prim(Cons<double>{u.x, u.y, u.z, u.w}, cc.gamma);
+    const double p = w.p;
     const double nax = -ws.nx[i] * ws.area[i];
     const double nay = -ws.ny[i] * ws.area[i];
     const double gp = p - cc.p_inf;
@@ -670,8 +683,36 @@ static __global__ void __launch_bounds__(1024) k_control(CtrlConfig cc, WallSet 
     fsum[5] -= gp * nay;
     fsum[6] += x * (-p * nay) - y * (-p * nax);
     fsum[7] += x * (-gp * nay) - y * (-gp * nax);
+    un_max = smax(un_max, fabs(w.u * ws.nx[i] + w.v * ws.ny[i]));
+    const double cp = (p - cc.p_inf) / cc.q_inf;
+    if (isfinite(cp)) {
+      cp_hi = smax(cp_hi, cp);
+      cp_lo_neg = smax(cp_lo_neg, -cp);
+    } else {
+      cp_bad += 1.0;
+    }
   }
   block_sum<8>(fsum, shm);
+  un_max = block_max(un_max, shm);
+  cp_hi = block_max(cp_hi, shm);
+  cp_lo_neg = block_max(cp_lo_neg, shm);
+  {
+    double b1[1] = {cp_bad};
+    block_sum<1>(b1, shm);
+    cp_bad = b1[0];
+  }
+  // far-field monitors (euler_solver.cpp:1013-1026)
+  double ffm[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i = tid; i < fs.n; i += blockDim.x) {
+    const d4 u = Un[fs.cell[i]];
+    const Prim<double> w = cons_to_prim(Cons<double>{u.x, u.y, u.z, u.w}, cc.gamma);
+    ffm[0] = smax(ffm[0], fabs(w.p - cc.p_inf));
+    ffm[1] = smax(ffm[1], fabs(w.r - cc.rho_inf));
+    ffm[2] = smax(ffm[2], fabs(w.u - cc.u_inf));
+    ffm[3] = smax(ffm[3], fabs(w.v - cc.v_inf));
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) ffm[k] = block_max(ffm[k], shm);
   if (tid != 0) return;
 
   Ctrl& s = *ctrl;
@@ -686,6 +727,20 @@ static __global__ void __launch_bounds__(1024) k_control(CtrlConfig cc, WallSet 
   r.as_ramp = s.as_ramp;
   r.dp_dom = dpd;
   r.dp_wall = dpw;
+  r.wall_un = un_max;
+  r.wall_mass_flux = 0.0;  // the slip-wall flux has no mass component (boundary_conditions.cpp:97-110)
+  r.cp_min = cc.n_wall > 0 ? -cp_lo_neg : 0.0;
+  r.cp_max = cc.n_wall > 0 ? cp_hi : 0.0;
+  if (cc.n_wall > 0 && cp_bad == double(cc.n_wall)) {
+    r.cp_min = 3.402823466e38;  // no finite sample: the reference keeps its float sentinels
+    r.cp_max = -3.402823466e38;
+  }
+  r.cp_nonfinite = int(cp_bad);
+  r.ff_dp = ffm[0];
+  r.ff_drho = ffm[1];
+  r.ff_du = ffm[2];
+  r.ff_dv = ffm[3];
+  r.action = 0;
   const bool nonfinite = s.nonfinite != 0;
 
   const double l1 = a[0];
@@ -785,6 +840,7 @@ static __global__ void __launch_bounds__(1024) k_control(CtrlConfig cc, WallSet 
         s.stage_b_progress = 0;
         s.pjump_below = 0;
         s.freeze = 0;
+        r.action = ready ? 10 : 11;
       }
     } else {
       const double thr = (cc.pj_target > 0.0) ? cc.pj_target * cc.pj_spike : 1.0e308;
@@ -795,6 +851,7 @@ static __global__ void __launch_bounds__(1024) k_control(CtrlConfig cc, WallSet 
         s.pjump_below = 0;
         s.stage_b_fmin = smin(cc.st_fmin_high, s.stage_b_fmin + 0.05);
         s.cfl_scale = smax(s.cfl_scale * cc.cfl_drop, cc.cfl_min_scale);
+        r.action = 20;
       } else {
         if (s.freeze > 0) --s.freeze;
         s.pjump_below = good ? s.pjump_below + 1 : 0;
@@ -802,16 +859,20 @@ static __global__ void __launch_bounds__(1024) k_control(CtrlConfig cc, WallSet 
           if (s.stage_b_fmin > cc.st_fmin_mid + 1.0e-6 && s.pjump_below >= cc.pj_hold) {
             s.stage_b_fmin = cc.st_fmin_mid;
             s.pjump_below = 0;
+            r.action = 31;
           } else if (s.stage_b_fmin > cc.st_fmin_low + 1.0e-6 && s.pjump_below >= cc.pj_hold) {
             s.stage_b_fmin = cc.st_fmin_low;
             s.pjump_below = 0;
+            r.action = 32;
           } else if (s.stage_b_fmin <= cc.st_fmin_low + 1.0e-6 && good) {
             ++s.stage_b_progress;
+            if (r.action == 0) r.action = 33;
           }
           if (good) {
             s.cfl_scale = smin(s.cfl_scale * cc.cfl_restore, 1.0);
           } else if (cc.pj_target > 0.0 && r.pj_wall > cc.pj_target) {
             s.cfl_scale = smax(s.cfl_scale * cc.cfl_drop, cc.cfl_min_scale);
+            if (r.action == 0) r.action = 21;
           }
         }
       }

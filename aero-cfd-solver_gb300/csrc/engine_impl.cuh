@@ -77,6 +77,8 @@ class EngineT final : public Engine {
     ws_.area = upload(nonempty(hs_.warea));
     ws_.x = upload(nonempty(hs_.wx));
     ws_.y = upload(nonempty(hs_.wy));
+    fs_.cell = upload(nonempty(hs_.far_cell));
+    fs_.n = static_cast<int>(hs_.far_cell.size());
 
     // state
     W_ = alloc<V4>(n_);
@@ -182,6 +184,9 @@ class EngineT final : public Engine {
     c.y_ref = cfg_.y_ref;
     c.pressure_ref = rs_.pressure_ref;
     c.gamma = rs_.gamma;
+    c.rho_inf = rs_.rho_inf;
+    c.u_inf = rs_.v_inf * rs_.cos_a;
+    c.v_inf = rs_.v_inf * rs_.sin_a;
 
     // freestream initial state
     std::vector<d4> u0(static_cast<size_t>(n_), d4{rs_.cons_inf[0], rs_.cons_inf[1], rs_.cons_inf[2], rs_.cons_inf[3]});
@@ -547,7 +552,7 @@ class EngineT final : public Engine {
     if (pjump_on_) {
       wrap(4, [&] { k_pjump<T><<<nblocks_, block_, 0, st_>>>(dm_, Un_, wall_adj_, rs_.gamma, part_, ctrl_); });
     }
-    wrap(5, [&] { k_control<<<1, 1024, 0, st_>>>(cc_, ws_, Un_, part_, ctrl_, recs_, rec_cap_); });
+    wrap(5, [&] { k_control<<<1, 1024, 0, st_>>>(cc_, ws_, fs_, Un_, part_, ctrl_, recs_, rec_cap_); });
     AERO_CK(cudaGetLastError());
   }
 
@@ -631,6 +636,7 @@ class EngineT final : public Engine {
   double* vol_ = nullptr;
   unsigned char* wall_adj_ = nullptr;
   WallSet ws_{};
+  FarSet fs_{};
   V4 *W_ = nullptr, *gx_ = nullptr, *gy_ = nullptr, *R_ = nullptr;
   T* SR_ = nullptr;
   d4 *Un_ = nullptr, *Us_ = nullptr;

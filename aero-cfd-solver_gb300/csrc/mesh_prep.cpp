@@ -227,6 +227,9 @@ bool build_slots(const aero_mesh_desc& m, int ordering, HostSlots* out, std::str
       s.nbr_old[slot] = b >= 0 ? b : o;
     }
   }
+  for (int f = 0; f < nf; ++f) {
+    if (m.face_neighbor[f] < 0 && m.face_bc[f] == AERO_BC_FARFIELD) s.far_cell.push_back(s.iperm[m.face_owner[f]]);
+  }
   for (int i = 0; i < m.num_wall_faces; ++i) {
     const int f = m.wall_faces[i];
     s.wall_cell.push_back(s.iperm[m.face_owner[f]]);

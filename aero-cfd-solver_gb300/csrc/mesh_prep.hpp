@@ -26,6 +26,8 @@ struct HostSlots {
   // wall patch in patch order
   std::vector<int> wall_cell;  // new owner index
   std::vector<double> wnx, wny, warea, wx, wy;
+  // owners (new index) of the far-field faces in face order
+  std::vector<int> far_cell;
   int interior_faces = 0, boundary_faces = 0;
 };
 

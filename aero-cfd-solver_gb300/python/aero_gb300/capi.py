@@ -117,7 +117,9 @@ _REC_FIELDS = [
     "stab_mach_floor", "all_speed_f_min", "all_speed_ramp_weight",
     "max_abs_dp_domain", "max_abs_dp_wall",
     "p_jump_energy_nd", "p_jump_energy_wall_nd",
-)]
+    "max_wall_un", "max_wall_mass_flux", "wall_cp_min", "wall_cp_max",
+    "max_farfield_abs_dp", "max_farfield_abs_drho", "max_farfield_abs_du", "max_farfield_abs_dv",
+)] + [("wall_cp_nonfinite", C.c_int), ("controller_action", C.c_int)]
 
 
 class IterRecord(C.Structure):

@@ -132,6 +132,11 @@ typedef struct aero_iter_record {
   double stab_mach_floor, all_speed_f_min, all_speed_ramp_weight;
   double max_abs_dp_domain, max_abs_dp_wall;
   double p_jump_energy_nd, p_jump_energy_wall_nd;
+  /* wall and far-field monitors (euler_solver.cpp:976-1026) */
+  double max_wall_un, max_wall_mass_flux, wall_cp_min, wall_cp_max;
+  double max_farfield_abs_dp, max_farfield_abs_drho, max_farfield_abs_du, max_farfield_abs_dv;
+  int wall_cp_nonfinite;
+  int controller_action; /* all-speed controller action code (euler_solver.cpp:1068-1139) */
 } aero_iter_record;
 
 enum aero_record_flags {

@@ -559,11 +559,14 @@ struct AssemblyDiag {
 };
 
 // residual_assembly.cpp:73-182. res, sr must be sized 5N and N; they are zeroed here.
+// fscale (optional, test metric only) receives per cell and component sum_faces |F_k A|.
 template <class R>
 void assemble(const Mesh<R>& m, const std::vector<Prim<R>>& w, const std::vector<R>& g,
-              const Numerics<R>& nm, std::vector<R>* res, std::vector<R>* sr, AssemblyDiag* diag) {
+              const Numerics<R>& nm, std::vector<R>* res, std::vector<R>* sr, AssemblyDiag* diag,
+              std::vector<double>* fscale = nullptr) {
   res->assign(static_cast<size_t>(m.num_cells) * 5, R(0));
   sr->assign(static_cast<size_t>(m.num_cells), R(0));
+  if (fscale) fscale->assign(static_cast<size_t>(m.num_cells) * 5, 0.0);
   AssemblyDiag dg;
   for (int f = 0; f < m.num_faces; ++f) {
     const int o = m.owner[f], nb = m.neighbor[f];
@@ -612,6 +615,10 @@ void assemble(const Mesh<R>& m, const std::vector<Prim<R>>& w, const std::vector
       const R fa = flux[k] * area;
       (*res)[5 * o + k] += fa;
       if (nb >= 0) (*res)[5 * nb + k] -= fa;
+      if (fscale) {
+        (*fscale)[5 * o + k] += std::abs(static_cast<double>(fa));
+        if (nb >= 0) (*fscale)[5 * nb + k] += std::abs(static_cast<double>(fa));
+      }
     }
     if (nb >= 0) (*sr)[nb] += wave;
   }

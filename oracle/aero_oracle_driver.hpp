@@ -101,7 +101,8 @@ class Solver {
 
   // Residual of one stage on a given conserved state (euler_solver.cpp:802-837).
   void residual(const double* u, int second_order, double stab, int as_fix, double as_fmin,
-                double as_ramp, double* res, double* sr, double* grad, int* diag) {
+                double as_ramp, double* res, double* sr, double* grad, int* diag,
+                double* fscale = nullptr) {
     const int n = mr_.num_cells;
     std::vector<Prim<R>> w(static_cast<size_t>(n));
     for (int c = 0; c < n; ++c) {
@@ -118,8 +119,11 @@ class Solver {
     const std::vector<R> g = nm.second_order ? green_gauss(mr_, w)
                                              : std::vector<R>(static_cast<size_t>(n) * 10, R(0));
     std::vector<R> r, s;
+    std::vector<double> fs;
     AssemblyDiag dg;
-    assemble(mr_, w, g, nm, &r, &s, &dg);
+    assemble(mr_, w, g, nm, &r, &s, &dg, fscale ? &fs : nullptr);
+    if (fscale)
+      for (size_t i = 0; i < fs.size(); ++i) fscale[i] = fs[i];
     for (size_t i = 0; i < r.size(); ++i) res[i] = r[i];
     for (size_t i = 0; i < s.size(); ++i) sr[i] = s[i];
     if (grad)
@@ -220,6 +224,7 @@ class Solver {
         }
       }
       std::vector<A> p(static_cast<size_t>(n));
+      std::vector<Prim<A>> pe(static_cast<size_t>(n));
       A dp_dom = A(0), dp_wall = A(0);
       if (!bad) {
         for (int c = 0; c < n; ++c) {
@@ -230,6 +235,7 @@ class Solver {
             bad = true;
             break;
           }
+          pe[c] = pw;
           p[c] = pw.p;
           const A adp = std::abs(pw.p - p_inf_);
           dp_dom = std::max(dp_dom, adp);
@@ -268,8 +274,49 @@ class Solver {
       mon_.drift(&mdrift);
       const bool dstable = mon_.drift_stable();
 
+      // wall and far-field monitors (euler_solver.cpp:976-1026)
+      {
+        A un_max = A(0), cp_lo = std::numeric_limits<A>::max(), cp_hi = std::numeric_limits<A>::lowest();
+        int cp_bad = 0;
+        const A q = A(0.5) * ref_.rho_inf * ref_.speed_inf * ref_.speed_inf + A(1.0e-12);
+        int nwall = 0;
+        for (int f = 0; f < ma_.num_faces; ++f) {
+          if (ma_.neighbor[f] >= 0 || ma_.bc[f] != kSlipWall) continue;
+          ++nwall;
+          const Prim<A>& w = pe[ma_.owner[f]];
+          un_max = std::max(un_max, std::abs(w.u * ma_.normal[3 * f] + w.v * ma_.normal[3 * f + 1] +
+                                             w.w * ma_.normal[3 * f + 2]));
+          const A cp = (w.p - A(cfg_.p_inf)) / q;
+          if (std::isfinite(cp)) {
+            cp_lo = std::min(cp_lo, cp);
+            cp_hi = std::max(cp_hi, cp);
+          } else {
+            ++cp_bad;
+          }
+        }
+        if (nwall == 0) cp_lo = cp_hi = A(0);
+        A ff[4] = {A(0), A(0), A(0), A(0)};
+        for (int f = 0; f < ma_.num_faces; ++f) {
+          if (ma_.neighbor[f] >= 0 || ma_.bc[f] != kFarfield) continue;
+          const Prim<A>& w = pe[ma_.owner[f]];
+          ff[0] = std::max(ff[0], std::abs(w.p - A(cfg_.p_inf)));
+          ff[1] = std::max(ff[1], std::abs(w.rho - ref_.rho_inf));
+          ff[2] = std::max(ff[2], std::abs(w.u - u_inf_));
+          ff[3] = std::max(ff[3], std::abs(w.v - v_inf_));
+        }
+        rec.max_wall_un = un_max;
+        rec.max_wall_mass_flux = 0.0;
+        rec.wall_cp_min = cp_lo;
+        rec.wall_cp_max = cp_hi;
+        rec.wall_cp_nonfinite = cp_bad;
+        rec.max_farfield_abs_dp = ff[0];
+        rec.max_farfield_abs_drho = ff[1];
+        rec.max_farfield_abs_du = ff[2];
+        rec.max_farfield_abs_dv = ff[3];
+      }
+
       const A pj_all = pjump(false), pj_wall = pjump(true);
-      controller(iter, stable, pj_wall);
+      rec.controller_action = controller(iter, stable, pj_wall);
 
       rec.residual_l1 = nr.l1;
       rec.residual_l2 = nr.l2;
@@ -347,6 +394,8 @@ class Solver {
     const A v_inf = std::max(A(c.mach), A(0)) * a_inf;
     const Prim<A> pinf{rho_inf, v_inf * std::cos(alpha), v_inf * std::sin(alpha), A(0), A(c.p_inf)};
     cons_inf_ = prim_to_cons(pinf, gamma);
+    u_inf_ = pinf.u;
+    v_inf_ = pinf.v;
     p_inf_ = A(c.p_inf);
     ref_.rho_inf = rho_inf;
     ref_.p_inf = A(c.p_inf);
@@ -482,8 +531,9 @@ class Solver {
   }
 
   // All-speed staged controller (euler_solver.cpp:1068-1139).
-  void controller(int iter, bool stable, A pj_wall) {
-    if (!cfg_.all_speed_staged_controller) return;
+  // Returns the controller action code of the reference's diagnostics CSV.
+  int controller(int iter, bool stable, A pj_wall) {
+    if (!cfg_.all_speed_staged_controller) return 0;
     if (stage_ == 1) {
       const bool ready = (iter + 1 >= st_a_min_) && stable;
       const bool timeout = (st_a_max_ > 0) && (iter + 1 >= st_a_max_);
@@ -493,9 +543,11 @@ class Solver {
         stage_b_progress_ = 0;
         pjump_below_ = 0;
         freeze_ = 0;
+        return ready ? 10 : 11;
       }
-      return;
+      return 0;
     }
+    int action = 0;
     const A spike_thr = (pj_target_ > A(0)) ? pj_target_ * pj_spike_ : std::numeric_limits<A>::max();
     const bool spike = pj_wall > spike_thr;
     const bool good = (pj_target_ <= A(0)) || (pj_wall <= pj_target_);
@@ -504,7 +556,7 @@ class Solver {
       pjump_below_ = 0;
       stage_b_fmin_ = std::min(st_fmin_high_, stage_b_fmin_ + A(0.05));
       cfl_scale_ = std::max(cfl_scale_ * cfl_drop_, cfl_min_scale_);
-      return;
+      return 20;
     }
     if (freeze_ > 0) --freeze_;
     if (good) {
@@ -516,18 +568,23 @@ class Solver {
       if (stage_b_fmin_ > st_fmin_mid_ + A(1.0e-6) && pjump_below_ >= pj_hold_) {
         stage_b_fmin_ = st_fmin_mid_;
         pjump_below_ = 0;
+        action = 31;
       } else if (stage_b_fmin_ > st_fmin_low_ + A(1.0e-6) && pjump_below_ >= pj_hold_) {
         stage_b_fmin_ = st_fmin_low_;
         pjump_below_ = 0;
+        action = 32;
       } else if (stage_b_fmin_ <= st_fmin_low_ + A(1.0e-6) && good) {
         ++stage_b_progress_;
+        if (action == 0) action = 33;
       }
       if (good) {
         cfl_scale_ = std::min(cfl_scale_ * cfl_restore_, A(1));
       } else if (pj_target_ > A(0) && pj_wall > pj_target_) {
         cfl_scale_ = std::max(cfl_scale_ * cfl_drop_, cfl_min_scale_);
+        if (action == 0) action = 21;
       }
     }
+    return action;
   }
 
   aero_case_desc cfg_;
@@ -535,7 +592,7 @@ class Solver {
   Mesh<A> ma_;
   Numerics<R> nm_;
   Cons<A> cons_inf_;
-  A p_inf_ = A(0), pressure_ref_ = A(1);
+  A p_inf_ = A(0), pressure_ref_ = A(1), u_inf_ = A(0), v_inf_ = A(0);
   Reference<A> ref_;
   A cfl_start_ = A(0), cfl_max_ = A(0);
   A stab_start_ = A(0), stab_target_ = A(0);

@@ -81,12 +81,13 @@ int oracle_solver_run(void* h, int n, aero_iter_record* recs, int* n_done) {
 }
 
 // One residual evaluation (gradients + assembly) on the conserved state u [N][5].
-// diag receives {first-order fallback faces, diffusive fallback faces, first failure face}.
+// diag receives {first-order fallback faces, diffusive fallback faces, first failure face};
+// fscale (may be null) receives per cell and component sum_faces |F_k A| (parity metric).
 int oracle_solver_residual(void* h, const double* u, int second_order, double stab, int as_fix,
                            double as_fmin, double as_ramp, double* res, double* sr, double* grad,
-                           int* diag) {
+                           int* diag, double* fscale) {
   return dispatch(static_cast<Handle*>(h), [&](auto& s) {
-    s.residual(u, second_order, stab, as_fix, as_fmin, as_ramp, res, sr, grad, diag);
+    s.residual(u, second_order, stab, as_fix, as_fmin, as_ramp, res, sr, grad, diag, fscale);
     return 0;
   });
 }

@@ -54,7 +54,7 @@ def oracle_lib():
         lib.oracle_solver_reset_run.argtypes = [C.c_void_p]
         lib.oracle_solver_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(capi.IterRecord), _ip]
         lib.oracle_solver_residual.argtypes = [C.c_void_p, _dp, C.c_int, C.c_double, C.c_int,
-                                               C.c_double, C.c_double, _dp, _dp, _dp, _ip]
+                                               C.c_double, C.c_double, _dp, _dp, _dp, _ip, _dp]
         _oracle = lib
     return _oracle
 
@@ -128,17 +128,22 @@ class OracleSolver:
         status = self.lib.oracle_solver_run(self.h, n, recs, C.byref(done))
         return status, self._capi.records_to_array(recs, done.value)
 
-    def residual(self, u, second_order=True, stab=0.0, as_fix=False, as_fmin=0.05, as_ramp=1.0):
+    def residual(self, u, second_order=True, stab=0.0, as_fix=False, as_fmin=0.05, as_ramp=1.0,
+                 with_scale=False):
+        """Residual [N,5], spectral radius [N], gradients [N,5,2], fallback counters; with
+        with_scale also the per-cell, per-component sum over faces of |F_k A| [N,5]."""
         u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
         r = np.empty(self.n * 5, np.float64)
         s = np.empty(self.n, np.float64)
         g = np.empty(self.n * 10, np.float64)
+        fs = np.empty(self.n * 5, np.float64)
         diag = (C.c_int * 3)()
         self.lib.oracle_solver_residual(self.h, u.ctypes.data_as(_dp), int(second_order), float(stab),
                                         int(as_fix), float(as_fmin), float(as_ramp),
                                         r.ctypes.data_as(_dp), s.ctypes.data_as(_dp),
-                                        g.ctypes.data_as(_dp), diag)
-        return r.reshape(self.n, 5), s, g.reshape(self.n, 5, 2), tuple(diag)
+                                        g.ctypes.data_as(_dp), diag, fs.ctypes.data_as(_dp))
+        out = (r.reshape(self.n, 5), s, g.reshape(self.n, 5, 2), tuple(diag))
+        return out + (fs.reshape(self.n, 5),) if with_scale else out
 
 
 def ref_residual(mesh, case, u, second_order=True, stab=0.0, as_fix=False, as_fmin=0.05, as_ramp=1.0):

@@ -72,6 +72,6 @@ def test_invalid_arguments_are_rejected(lib):
 
 
 def test_record_struct_size_matches_header():
-    # aero_iter_record: 4 ints + 34 doubles
-    assert C.sizeof(capi.IterRecord) == 4 * 4 + 34 * 8
+    # aero_iter_record: 4 ints + 42 doubles + 2 ints
+    assert C.sizeof(capi.IterRecord) == 4 * 4 + 42 * 8 + 2 * 4
     assert np.dtype(capi.RECORD_DTYPE).itemsize == C.sizeof(capi.IterRecord)

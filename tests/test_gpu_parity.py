@@ -1,10 +1,11 @@
 """Parity of the sm_103a path (through the C ABI) with the CPU oracle and with the
 reference's golden vectors.
 
-Tolerances (per cell and component, relative to the cell's flux scale
-S_c = SR_c * max_k |U_c,k|, an upper bound of sum_faces |F_k A| up to a constant):
-  FP64 path vs FP64 oracle : 1e-12 (residual), 1e-12 (spectral radius, relative)
-  FP32 path vs float reference (golden) : 2e-5; the device contracts multiply-adds
+Residual tolerance, per cell c and component k, relative to the flux scale
+S_ck = sum over the cell's faces of |F_k A| computed by the oracle (the residual itself
+cancels towards zero, so it is no usable denominator):
+  FP64 path vs FP64 oracle               : |dR| <= 1e-12 S   (spectral radius: 1e-12 relative)
+  FP32 path vs float reference (golden)  : |dR| <= 2e-5 S    (the device contracts multiply-adds)
 Whole runs compare histories and states at the tolerances given in each test."""
 
 import json
@@ -33,6 +34,11 @@ def scale(sr, u):
 
 def rel_err(a, b, sr, u):
     return float(np.max(np.abs(a - b) / scale(sr, u)))
+
+
+def flux_err(a, b, fscale):
+    """max |a - b| / sum_faces |F_k A| over cells and components."""
+    return float(np.max(np.abs(a - b) / (fscale + 1e-300)))
 
 
 def seeded_state(sol_or_mesh_case, seed, amp=0.05):
@@ -66,11 +72,10 @@ def test_residual_fp64_vs_oracle_on_golden_states(golden_meshes, golden_residual
         args = (m["second_order"], m["stab"], m["as_fix"], m["as_fmin"], m["as_ramp"])
         with aero_gb300.Solver(mesh, case) as s:
             r, sr, g = s.residual(u, *args)
-        ro, sro, go, _ = op.OracleSolver(op.MODE_DOUBLE, mesh, case).residual(u, *args)
-        tol = 1e-12 if "_s0_" in m["key"] else 1e-9
-        e = rel_err(r, ro, sro, u)
-        worst = max(worst, e if tol == 1e-12 else 0.0)
-        assert e <= tol, (m["key"], e)
+        ro, sro, go, _, fs = op.OracleSolver(op.MODE_DOUBLE, mesh, case).residual(u, *args, with_scale=True)
+        e = flux_err(r, ro, fs)
+        worst = max(worst, e)
+        assert e <= 1e-12, (m["key"], e)
         np.testing.assert_allclose(sr, sro, rtol=1e-12, err_msg=m["key"])
         if m["second_order"]:
             gs = np.abs(go).max() + 1e-300
@@ -86,11 +91,13 @@ def test_residual_fp32_vs_reference_golden(golden_meshes, golden_residuals):
             continue  # near-vacuum stress states: float round-off is unbounded there
         case = capi.make_case(**m["case"], precision=capi.PRECISION_FP32)
         u = data[m["key"] + "/u"].astype(np.float64)
+        args = (m["second_order"], m["stab"], m["as_fix"], m["as_fmin"], m["as_ramp"])
         with aero_gb300.Solver(mesh, case) as s:
-            r, sr, _ = s.residual(u, m["second_order"], m["stab"], m["as_fix"], m["as_fmin"], m["as_ramp"])
+            r, sr, _ = s.residual(u, *args)
         ref_r = data[m["key"] + "/r"].astype(np.float64)
         ref_sr = data[m["key"] + "/sr"].astype(np.float64)
-        assert rel_err(r, ref_r, ref_sr, u) <= 2e-5, m["key"]
+        fs = op.OracleSolver(op.MODE_FLOAT, mesh, case).residual(u, *args, with_scale=True)[4]
+        assert flux_err(r, ref_r, fs) <= 2e-5, m["key"]
         np.testing.assert_allclose(sr, ref_sr, rtol=2e-6, err_msg=m["key"])
 
 
@@ -103,9 +110,9 @@ def test_residual_fp64_synthetic_mesh(cell_type, combo):
     for second in (0, 1):
         with aero_gb300.Solver(mesh, case) as s:
             r, sr, _ = s.residual(u, second, 0.02, COMBOS[combo]["all_speed_flux_fix"], 0.05, 0.7)
-        ro, sro, _, _ = op.OracleSolver(op.MODE_DOUBLE, mesh, case).residual(
-            u, second, 0.02, COMBOS[combo]["all_speed_flux_fix"], 0.05, 0.7)
-        assert rel_err(r, ro, sro, u) <= 1e-12
+        ro, sro, _, _, fs = op.OracleSolver(op.MODE_DOUBLE, mesh, case).residual(
+            u, second, 0.02, COMBOS[combo]["all_speed_flux_fix"], 0.05, 0.7, with_scale=True)
+        assert flux_err(r, ro, fs) <= 1e-12
         np.testing.assert_allclose(sr, sro, rtol=1e-12)
 
 

@@ -23,7 +23,7 @@ CSRC = PKG / "csrc"
 OBJ = PKG / "_build"
 LIB = PKG / "lib" / "libaero_gb300.so"
 
-CU_SOURCES = ["engine_f32.cu", "engine_f64.cu"]
+CU_SOURCES = ["engine_f32.cu", "engine_f64.cu", "noalloc.cu"]
 CPP_SOURCES = ["capi.cpp", "mesh_prep.cpp", "mesh_gen.cpp", "driver.cpp"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 

@@ -13,13 +13,7 @@
 #include <new>
 #include <string>
 
-struct aero_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  aero_case_desc cfg{};
-  std::unique_ptr<aero::Engine> engine;
-  std::string error;
-};
+#include "ctx.hpp"
 
 namespace {
 

@@ -24,9 +24,25 @@ struct Resolved {
   int lm;  // any low-Mach feature on
 };
 
+// Read-only device view of a context for launches issued outside the engine.
+// dm / fp point at the engine's DevMesh<T> / FaceParams<T> (T per `precision`).
+struct EngineView {
+  int n;
+  int precision;  // enum aero_precision
+  int flux;
+  int lm;
+  int block;
+  int device;
+  const void* dm;
+  const void* fp;
+  const int* perm_dev;  // new -> original cell, on the device
+  cudaStream_t stream;
+};
+
 class Engine {
  public:
   virtual ~Engine() = default;
+  virtual EngineView view() const = 0;
   virtual bool init(std::string* err) = 0;
   virtual void set_state(const double* u_orig) = 0;
   virtual void get_state(double* u_orig) = 0;

@@ -70,6 +70,7 @@ class EngineT final : public Engine {
     noff_ = upload(noff);
     vol_ = upload(hs_.vol);
     wall_adj_ = upload(hs_.wall_adj);
+    perm_dev_ = upload(hs_.perm);
     const int nw = static_cast<int>(hs_.wall_cell.size());
     ws_.cell = upload(hs_.wall_cell.empty() ? std::vector<int>{0} : hs_.wall_cell);
     ws_.nx = upload(nonempty(hs_.wnx));
@@ -199,6 +200,21 @@ class EngineT final : public Engine {
       return false;
     }
     return true;
+  }
+
+  EngineView view() const override {
+    EngineView v{};
+    v.n = n_;
+    v.precision = sizeof(T) == 4 ? AERO_PRECISION_FP32 : AERO_PRECISION_FP64;
+    v.flux = cfg_.flux;
+    v.lm = rs_.lm;
+    v.block = block_;
+    cudaGetDevice(&v.device);
+    v.dm = &dm_;
+    v.fp = &fp_;
+    v.perm_dev = perm_dev_;
+    v.stream = st_;
+    return v;
   }
 
   cudaError_t last_cuda_error() override {
@@ -635,6 +651,7 @@ class EngineT final : public Engine {
   V2* noff_ = nullptr;
   double* vol_ = nullptr;
   unsigned char* wall_adj_ = nullptr;
+  int* perm_dev_ = nullptr;
   WallSet ws_{};
   FarSet fs_{};
   V4 *W_ = nullptr, *gx_ = nullptr, *gy_ = nullptr, *R_ = nullptr;

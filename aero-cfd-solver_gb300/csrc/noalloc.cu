@@ -1,0 +1,200 @@
+// noalloc.cu -- aero_residual_noalloc: one residual evaluation on caller-owned device buffers
+// that allocates nothing. Its working arrays live in a file-scope __device__ array of fixed
+// size instead of memory obtained from cudaMalloc.
+//
+// Who needs this: code that runs the residual where device allocation is not allowed or not
+// wanted -- inside a CUDA stream capture that is later replayed, under another framework's
+// memory pool that owns all device memory, or in a time-stepping loop whose memory budget is
+// fixed up front (cudaMalloc/cudaFree can synchronise the device and fragment memory).
+//
+// Limits and sharing: the scratch array is sized for kNoallocMaxCells cells (about 8.9 MB)
+// and every GPU that loads this library holds it until the process exits. All calls on a
+// device share it and it keeps the last call's contents; the kernels clear what must start
+// at zero. Two calls whose work overlaps on the same GPU (different streams, or different
+// contexts on one device) race on the shared array and must be serialised by the caller.
+#include "aero_kernels.cuh"
+#include "ctx.hpp"
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+namespace aero {
+namespace {
+
+constexpr int kNoallocMaxCells = 65536;
+constexpr size_t kAlign = 256;
+constexpr size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+constexpr size_t kCtrlBytes = align_up(sizeof(Ctrl));
+// per cell, sized for double: W, gx, gy, R (4 reals each) and SR
+constexpr size_t kScratchBytes = kCtrlBytes + 4 * align_up(size_t(kNoallocMaxCells) * 32) +
+                                 align_up(size_t(kNoallocMaxCells) * 8);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void* g_scratch_addr[kMaxDevices] = {};
+
+// Device address of the scratch array on `device`, which must be current. The host-side
+// name g_noalloc_scratch is only a stand-in; kernels must be given this address.
+cudaError_t scratch_address(int device, void** out) {
+  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (g_scratch_addr[device] == nullptr) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_scratch_addr[device] = p;
+  }
+  *out = g_scratch_addr[device];
+  return cudaSuccess;
+}
+
+// Gathers the caller's state (original order, AoS [N][5] double) into the bulk primitive
+// state and resets the per-call fields of the scratch controller block.
+template <class T>
+__global__ void k_na_prepare(int n, const int* __restrict__ perm, const double* __restrict__ u,
+                             typename Vec<T>::v4* __restrict__ W, double gamma, Ctrl* __restrict__ ctrl,
+                             double stab, int as_fix, double as_fmin, double as_ramp) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c == 0) {
+    ctrl->done = 0;
+    ctrl->fo_fallback = 0;
+    ctrl->diff_fallback = 0;
+    ctrl->stab_floor = stab;
+    ctrl->as_fix = as_fix;
+    ctrl->as_fmin = as_fmin;
+    ctrl->as_ramp = as_ramp;
+    ctrl->sr_max = 0.0;
+  }
+  if (c >= n) return;
+  const double* s = u + 5 * static_cast<size_t>(perm[c]);
+  const Prim<T> w = cons_to_prim(Cons<T>{T(s[0]), T(s[1]), T(s[2]), T(s[4])}, T(gamma));
+  typename Vec<T>::v4 o;
+  o.x = w.r; o.y = w.u; o.z = w.v; o.w = w.p;
+  W[c] = o;
+}
+
+// Scatters the residual and spectral radius back to the caller's original order.
+template <class T>
+__global__ void k_na_store(int n, const int* __restrict__ perm, const typename Vec<T>::v4* __restrict__ R,
+                           const T* __restrict__ SR, double* __restrict__ res, double* __restrict__ sr) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const int o = perm[c];
+  const auto r = R[c];
+  double* d = res + 5 * static_cast<size_t>(o);
+  d[0] = double(r.x);
+  d[1] = double(r.y);
+  d[2] = double(r.z);
+  d[3] = 0.0;
+  d[4] = double(r.w);
+  sr[o] = double(SR[c]);
+}
+
+template <class T, int FLUX, bool SECOND, bool LM>
+void launch_residual_na(int grid, int block, cudaStream_t st, const DevMesh<T>& dm, const FaceParams<T>& fp,
+                        const typename Vec<T>::v4* W, const typename Vec<T>::v4* gx,
+                        const typename Vec<T>::v4* gy, typename Vec<T>::v4* R, T* SR, Ctrl* ctrl) {
+  k_residual<T, FLUX, SECOND, LM, false><<<grid, block, 0, st>>>(dm, fp, W, gx, gy, R, SR, Partials{}, ctrl, 0);
+}
+
+template <class T>
+cudaError_t run_na(const EngineView& v, unsigned char* base, const double* u, int second, double stab,
+                   int as_fix, double as_fmin, double as_ramp, double* res, double* sr, cudaStream_t st) {
+  using V4 = typename Vec<T>::v4;
+  const DevMesh<T>& dm = *static_cast<const DevMesh<T>*>(v.dm);
+  const FaceParams<T>& fp = *static_cast<const FaceParams<T>*>(v.fp);
+  const int n = v.n;
+  Ctrl* ctrl = reinterpret_cast<Ctrl*>(base);
+  unsigned char* p = base + kCtrlBytes;
+  auto take = [&](size_t bytes) {
+    unsigned char* q = p;
+    p += align_up(bytes);
+    return q;
+  };
+  V4* W = reinterpret_cast<V4*>(take(sizeof(V4) * n));
+  V4* gx = reinterpret_cast<V4*>(take(sizeof(V4) * n));
+  V4* gy = reinterpret_cast<V4*>(take(sizeof(V4) * n));
+  V4* R = reinterpret_cast<V4*>(take(sizeof(V4) * n));
+  T* SR = reinterpret_cast<T*>(take(sizeof(T) * n));
+  const int block = v.block;
+  const int grid = (n + block - 1) / block;
+  k_na_prepare<T><<<grid, block, 0, st>>>(n, v.perm_dev, u, W, double(fp.gamma), ctrl, stab, as_fix, as_fmin, as_ramp);
+  if (second) k_gradient<T><<<grid, block, 0, st>>>(dm, W, gx, gy, ctrl);
+  const bool lm = v.lm != 0;
+  if (v.flux == AERO_FLUX_HLLC) {
+    if (second) {
+      if (lm) launch_residual_na<T, 1, true, true>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
+      else launch_residual_na<T, 1, true, false>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
+    } else {
+      if (lm) launch_residual_na<T, 1, false, true>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
+      else launch_residual_na<T, 1, false, false>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
+    }
+  } else {
+    if (second) {
+      if (lm) launch_residual_na<T, 0, true, true>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
+      else launch_residual_na<T, 0, true, false>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
+    } else {
+      if (lm) launch_residual_na<T, 0, false, true>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
+      else launch_residual_na<T, 0, false, false>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
+    }
+  }
+  k_na_store<T><<<grid, block, 0, st>>>(n, v.perm_dev, R, SR, res, sr);
+  return cudaGetLastError();
+}
+
+}  // namespace
+}  // namespace aero
+
+extern "C" {
+
+int aero_residual_noalloc(aero_ctx* ctx, const double* conserved_dev, int second_order, double stab_mach_floor,
+                          int all_speed_flux_fix, double all_speed_f_min, double all_speed_ramp_weight,
+                          double* residual_dev, double* spectral_radius_dev, void* stream) {
+  if (ctx == nullptr) return AERO_ERR_INVALID;
+  if (conserved_dev == nullptr || residual_dev == nullptr || spectral_radius_dev == nullptr) {
+    ctx->error = "aero_residual_noalloc: null device pointer";
+    return AERO_ERR_INVALID;
+  }
+  const aero::EngineView v = ctx->engine->view();
+  if (v.n > aero::kNoallocMaxCells) {
+    ctx->error = "aero_residual_noalloc: the mesh has " + std::to_string(v.n) +
+                 " cells; the allocation-free residual supports at most " +
+                 std::to_string(aero::kNoallocMaxCells) + " cells";
+    return AERO_ERR_INVALID;
+  }
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->error = "aero_residual_noalloc: no current CUDA device";
+    return AERO_ERR_CUDA;
+  }
+  if (prev != ctx->device && cudaSetDevice(ctx->device) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->error = "aero_residual_noalloc: cannot select the context's device";
+    return AERO_ERR_CUDA;
+  }
+  void* base = nullptr;
+  cudaError_t e = aero::scratch_address(ctx->device, &base);
+  if (e == cudaSuccess) {
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : v.stream;
+    unsigned char* b = static_cast<unsigned char*>(base);
+    e = v.precision == AERO_PRECISION_FP32
+            ? aero::run_na<float>(v, b, conserved_dev, second_order, stab_mach_floor, all_speed_flux_fix,
+                                  all_speed_f_min, all_speed_ramp_weight, residual_dev, spectral_radius_dev, st)
+            : aero::run_na<double>(v, b, conserved_dev, second_order, stab_mach_floor, all_speed_flux_fix,
+                                   all_speed_f_min, all_speed_ramp_weight, residual_dev, spectral_radius_dev, st);
+  }
+  if (prev != ctx->device) cudaSetDevice(prev);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    ctx->error = std::string("aero_residual_noalloc: ") + cudaGetErrorString(e);
+    return AERO_ERR_CUDA;
+  }
+  return AERO_OK;
+}
+
+}  // extern "C"

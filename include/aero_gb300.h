@@ -219,6 +219,25 @@ AERO_API int aero_profile_kernels(aero_ctx* ctx, int n, int flush_l2, double* ms
  * (contexts created afterwards on this thread live there). */
 AERO_API int aero_select_device(int device);
 
+/* Allocation-free residual. No counterpart in the reference: an addition for callers that
+ * cannot allocate device memory while they evaluate the residual -- code being captured into
+ * a CUDA graph, code running under another framework's memory pool, or solver loops whose
+ * memory is fixed up front (cudaMalloc/cudaFree may synchronise the device).
+ * Computes what aero_residual computes (gradients only internally), but takes DEVICE
+ * pointers owned by the caller: conserved_dev [N][5] and residual_dev [N][5] double in the
+ * original cell order, spectral_radius_dev [N] double. It allocates nothing: its working
+ * arrays live in one fixed device array of the library (about 8.9 MB, held by every GPU that
+ * loads the library until exit), so meshes above 65,536 cells are rejected with
+ * AERO_ERR_INVALID. The work is queued on `stream` (null: the context's stream) and the call
+ * returns without waiting. The first call on each device looks up that array's address;
+ * make it before any stream capture. All calls on a device share the array and it keeps
+ * the last call's contents: calls whose work overlaps on the GPU race and must be ordered
+ * by the caller (one stream, or events). */
+AERO_API int aero_residual_noalloc(aero_ctx* ctx, const double* conserved_dev, int second_order,
+                                   double stab_mach_floor, int all_speed_flux_fix,
+                                   double all_speed_f_min, double all_speed_ramp_weight,
+                                   double* residual_dev, double* spectral_radius_dev, void* stream);
+
 /* Sizes and kernel-launch counts of the context, for roofline accounting:
  * info[0] cells, [1] faces, [2] slots per cell (padded), [3] kernel launches per
  * iteration, [4] bytes of device memory held, [5] precision, [6] block size. */

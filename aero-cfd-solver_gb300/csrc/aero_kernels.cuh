@@ -52,7 +52,7 @@ __device__ __forceinline__ typename Vec<T>::v4 ld4(const typename Vec<T>::v4* p)
 }
 
 // Controller and per-iteration state (device memory, one per context).
-struct Ctrl {
+struct alignas(16) Ctrl {
   int iter;        // index of the next iteration to run
   int done;        // converged or trapped: kernels return immediately
   int nonfinite;   // set by the last-stage update when the state is not finite
@@ -68,6 +68,7 @@ struct Ctrl {
   double hist[3 * 2 * kMaxForceWindow];
   double stage_b_fmin;
   int stage_b_progress, pjump_below, freeze, pad0;
+  float cfl_f, stab_f, as_fmin_f, as_ramp_f;  // float copies of the schedule values (FP32 kernels)
   double sr_max;  // global max of max(SR, floor) for global time stepping
 };
 
@@ -77,7 +78,8 @@ struct CtrlConfig {
   int cfl_ramp, stab_ramp, as_ramp_start, as_ramp_iters;
   int startup_first_order, min_iterations, window, staged;
   int st_a_min, st_a_max, pj_hold, freeze_iters;
-  int as_fix_cfg, n_blocks, pjump_blocks, pad;
+  int as_fix_cfg, n_blocks, pjump_blocks, n_wall_blocks;
+  int bulk_f32;  // partials hold float norms and float monitor bits
   double cfl_start, cfl_max, stab_start, stab_target, as_fmin;
   double residual_target, stab_tol, drift_tol;
   double st_fmin_high, st_fmin_mid, st_fmin_low;
@@ -90,6 +92,7 @@ struct CtrlConfig {
 struct PrecondD {
   int enabled;
   double gamma, mach_ref, mach_min, beta_min, beta_max;
+  float gamma_f, gm1_f;  // float(gamma), float(gamma - 1)
 };
 
 // Schedule of iteration s->iter (euler_solver.cpp:69-112 and 772-797): order switch,
@@ -140,26 +143,134 @@ __host__ __device__ inline void apply_schedule(const CtrlConfig& cc, Ctrl* sp) {
                     : sclamp(double(s.stage_b_progress) / double(cc.as_ramp_iters > 1 ? cc.as_ramp_iters : 1),
                              0.0, 1.0);
   }
+  s.cfl_f = float(s.cfl);
+  s.stab_f = float(s.stab_floor);
+  s.as_fmin_f = float(s.as_fmin);
+  s.as_ramp_f = float(s.as_ramp);
 }
 
+// Schedule values of a single residual evaluation (aero_residual and its no-allocation form).
+__host__ __device__ inline void set_eval_schedule(Ctrl* s, double stab, int as_fix, double as_fmin, double as_ramp) {
+  s->stab_floor = stab;
+  s->as_fix = as_fix;
+  s->as_fmin = as_fmin;
+  s->as_ramp = as_ramp;
+  s->stab_f = float(stab);
+  s->as_fmin_f = float(as_fmin);
+  s->as_ramp_f = float(as_ramp);
+}
+
+// Geometry as the bulk arithmetic consumes it. The face normals, areas and volumes are held
+// in double (and used in double by the forces); the T copies here are their exact
+// conversions, and inv_vol = 1/max(V, 1e-12) formed in T on the host, so FP32 kernels do
+// neither double loads nor double conversions or divides.
 template <class T>
 struct DevMesh {
   int n, d;
   const int* link;
-  const double2* nrm;
-  const double* area;
+  const typename Vec<T>::v2* nrm;
+  const T* area;
   const typename Vec<T>::v2* doff;
   const typename Vec<T>::v2* noff;
-  const double* vol;
+  const T* inv_vol;
 };
 
-// Per-block partial results reduced by the control kernel in a fixed order.
+// Per-block partial results reduced by the control kernel in a fixed order. Quantity-major
+// ([k][block]) so that the control warp reads them coalesced.
 struct Partials {
-  double* norms;   // [3 * blocks]: l1, l2 sum, linf
-  double* dp;      // [2 * blocks]: max |p - p_inf| domain, wall-adjacent
-  double* pjump;   // [4 * blocks]: sum dp^2, count, wall sum, wall count
+  double* norms;   // [3][nb]: l1, l2 sum, linf (FP64)
+  float* norms_f;  // [3][nb]: the same in float (FP32)
+  long long* mon;  // [kMon][nb]: maxima of |p - p_inf| (domain, wall-adjacent) and the far-field
+                   // deviations |dp|, |drho|, |du|, |dv|, formed in the bulk type; stored as bit
+                   // patterns (double, or float zero-extended) so that maxima are integer maxima
+  double* wall;    // [kWall][nwb]: force sums and wall monitors of blocks holding wall cells (FP64)
+  float* wall_f;   // [kWall][nwb]: the same in float (FP32)
+  double* pjump;   // [4][nb]: sum dp^2, count, wall sum, wall count
   double* srmax;   // [blocks * warps per block]: max of max(SR, floor)
+  int nb, nwb;     // blocks of the cell grid, blocks holding wall cells
 };
+constexpr int kMon = 6;
+constexpr int kWall = 12;  // snx sny fxa fya fxg fyg ma mg | un_max cp_hi -cp_lo cp_bad
+
+// End-of-iteration monitors (euler_solver.cpp:923-1026, forces.cpp:208-294) computed by the
+// cells that own wall or far-field faces, while the new state is in registers.
+struct MonitorSet {
+  const unsigned char* flags;  // per cell: bit 0 owns slip-wall faces, bit 1 owns far-field
+                               // faces, bits 2..7 number of wall entries
+  const int* wall_first;       // per cell: its first wall entry
+  const unsigned char* wkind;  // wall entries sorted by owner: bit 0 force patch face, bit 1
+                               // slip-wall face (wall monitors);
+  const double* wnx;           // unit normal out of the owner, length and centre
+  const double* wny;
+  const double* warea;
+  const double* wx;
+  const double* wy;
+  const int* block_slot;       // per update block: its slot in Partials::wall, or -1
+  double p_inf, rho_inf, u_inf, v_inf, q_inf, x_ref, y_ref, gamma;
+  float p_inf_f, rho_inf_f, u_inf_f, v_inf_f, q_inf_f, x_ref_f, y_ref_f;  // float copies (FP32)
+  const float *wnx_f, *wny_f, *warea_f, *wx_f, *wy_f;                  // float copies (FP32)
+};
+
+// Conserved state of the cells. FP64 holds it as double4; FP32 as a float-float pair: hi is
+// the float image and lo the remainder (|lo| <= ulp(hi)/2), so that the state accumulates to
+// about 2^-47 relative across iterations with float arithmetic only (a GB300 SM runs double
+// arithmetic, and float<->double conversions even more so, at a small fraction of the float
+// rate).
+struct StateRef {
+  d4* un;      // FP64
+  float4* hi;  // FP32
+  float4* lo;  // FP32
+};
+
+// Error-free float sum (Knuth's two-sum): s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float* s, float* e) {
+  const float x = __fadd_rn(a, b);
+  const float bb = __fsub_rn(x, a);
+  *e = __fadd_rn(__fsub_rn(a, __fsub_rn(x, bb)), __fsub_rn(b, bb));
+  *s = x;
+}
+// (hi, lo) + d as a renormalised float-float pair.
+__device__ __forceinline__ void ff_add(float hi, float lo, float d, float* nh, float* nl) {
+  float s, e;
+  two_sum(hi, d, &s, &e);
+  two_sum(s, __fadd_rn(lo, e), nh, nl);
+}
+// (ah, al) + (bh, bl) as a renormalised float-float pair.
+__device__ __forceinline__ void ff_add2(float ah, float al, float bh, float bl, float* nh, float* nl) {
+  float s, e;
+  two_sum(ah, bh, &s, &e);
+  two_sum(s, __fadd_rn(__fadd_rn(al, bl), e), nh, nl);
+}
+__device__ __forceinline__ void ff_split(double u, float* hi, float* lo) {
+  *hi = float(u);
+  *lo = float(u - double(*hi));
+}
+
+template <class T>
+__device__ __forceinline__ Cons<double> load_state(const StateRef& u, int c) {
+  if constexpr (sizeof(T) == 4) {
+    const float4 h = u.hi[c], l = u.lo[c];
+    return Cons<double>{double(h.x) + double(l.x), double(h.y) + double(l.y), double(h.z) + double(l.z),
+                        double(h.w) + double(l.w)};
+  } else {
+    const d4 x = u.un[c];
+    return Cons<double>{x.x, x.y, x.z, x.w};
+  }
+}
+template <class T>
+__device__ __forceinline__ void store_state(const StateRef& u, int c, const Cons<double>& s) {
+  if constexpr (sizeof(T) == 4) {
+    float4 h, l;
+    ff_split(s.r, &h.x, &l.x);
+    ff_split(s.ru, &h.y, &l.y);
+    ff_split(s.rv, &h.z, &l.z);
+    ff_split(s.rE, &h.w, &l.w);
+    u.hi[c] = h;
+    u.lo[c] = l;
+  } else {
+    u.un[c] = d4{s.r, s.ru, s.rv, s.rE};
+  }
+}
 
 // ---------------------------------------------------------------------------------------
 // warp/block reductions
@@ -178,6 +289,133 @@ __device__ __forceinline__ float warp_maxf(float x) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) x = smax(x, __shfl_xor_sync(0xffffffffu, x, o));
   return x;
+}
+template <class T>
+__device__ __forceinline__ T warp_sum_t(T x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+template <class T>
+__device__ __forceinline__ T warp_max_t(T x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x = smax(x, __shfl_xor_sync(0xffffffffu, x, o));
+  return x;
+}
+
+// Monitors of one cell after the last stage (euler_solver.cpp:923-1026, forces.cpp:208-294),
+// from the bulk primitive state w in the bulk type T, reduced per block: maxima into
+// Partials::mon (every block), force sums and wall monitors into Partials::wall / wall_f
+// (only blocks holding wall cells). FP32 forms all of it in float: a GB300 SM runs double
+// arithmetic at a small fraction of its float rate, and the blocks are combined in double by
+// the control kernel. Must be called by every thread of the block; `valid` is false past the
+// mesh.
+template <class T>
+__device__ void block_monitors(bool valid, const Prim<T>& w, int c, const MonitorSet& ms, Partials part) {
+  constexpr bool kF = sizeof(T) == 4;
+  constexpr T kLow = kF ? T(-3.0e38f) : T(-1.0e308);
+  __shared__ T shf[kMon][32];
+  __shared__ T shd[kWall][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  const T p_inf = kF ? T(ms.p_inf_f) : T(ms.p_inf);
+  T mon[kMon] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+  unsigned char fl = 0;
+  if (valid) {
+    fl = ms.flags[c];
+    const T dp = fabs(w.p - p_inf);
+    mon[0] = dp;
+    if (fl & 1) mon[1] = dp;
+    if (fl & 2) {
+      mon[2] = dp;
+      mon[3] = fabs(w.r - (kF ? T(ms.rho_inf_f) : T(ms.rho_inf)));
+      mon[4] = fabs(w.u - (kF ? T(ms.u_inf_f) : T(ms.u_inf)));
+      mon[5] = fabs(w.v - (kF ? T(ms.v_inf_f) : T(ms.v_inf)));
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kMon; ++k) mon[k] = warp_max_t(mon[k]);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < kMon; ++k) shf[k][wid] = mon[k];
+  }
+  const int slot = ms.block_slot[blockIdx.x];
+  if (slot >= 0) {
+    // snx sny fxa fya fxg fyg ma mg | un_max cp_hi -cp_lo cp_bad
+    T v[kWall] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0), kLow, kLow, T(0)};
+    if (valid && fl >= 4) {
+      const T* wnx = kF ? reinterpret_cast<const T*>(ms.wnx_f) : reinterpret_cast<const T*>(ms.wnx);
+      const T* wny = kF ? reinterpret_cast<const T*>(ms.wny_f) : reinterpret_cast<const T*>(ms.wny);
+      const T* wa = kF ? reinterpret_cast<const T*>(ms.warea_f) : reinterpret_cast<const T*>(ms.warea);
+      const T* wx = kF ? reinterpret_cast<const T*>(ms.wx_f) : reinterpret_cast<const T*>(ms.wx);
+      const T* wy = kF ? reinterpret_cast<const T*>(ms.wy_f) : reinterpret_cast<const T*>(ms.wy);
+      const T x_ref = kF ? T(ms.x_ref_f) : T(ms.x_ref), y_ref = kF ? T(ms.y_ref_f) : T(ms.y_ref);
+      const T q_inf = kF ? T(ms.q_inf_f) : T(ms.q_inf);
+      const int first = ms.wall_first[c], cnt = fl >> 2;
+      const T p = w.p, gp = w.p - p_inf;
+      for (int j = first; j < first + cnt; ++j) {
+        const unsigned char kind = ms.wkind[j];
+        if (kind & 1) {  // forces.cpp:208-294
+          const T nax = -wnx[j] * wa[j];
+          const T nay = -wny[j] * wa[j];
+          const T x = wx[j] - x_ref, y = wy[j] - y_ref;
+          v[0] += nax;
+          v[1] += nay;
+          v[2] -= p * nax;
+          v[3] -= p * nay;
+          v[4] -= gp * nax;
+          v[5] -= gp * nay;
+          v[6] += x * (-p * nay) - y * (-p * nax);
+          v[7] += x * (-gp * nay) - y * (-gp * nax);
+        }
+        if (kind & 2) {  // euler_solver.cpp:976-1006
+          v[8] = smax(v[8], fabs(w.u * wnx[j] + w.v * wny[j]));
+          const T cp = gp / q_inf;
+          if (isfinite(cp)) {
+            v[9] = smax(v[9], cp);
+            v[10] = smax(v[10], -cp);
+          } else {
+            v[11] += T(1);
+          }
+        }
+      }
+    }
+    if (__any_sync(0xffffffffu, valid && fl >= 4)) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[k] = warp_sum_t(v[k]);
+#pragma unroll
+      for (int k = 8; k < 11; ++k) v[k] = warp_max_t(v[k]);
+      v[11] = warp_sum_t(v[11]);
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < kWall; ++k) shd[k][wid] = v[k];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < kMon; ++k) {
+      T m = T(0);
+      for (int i = 0; i < nw; ++i) m = smax(m, shf[k][i]);
+      if constexpr (kF) {
+        part.mon[k * part.nb + blockIdx.x] = static_cast<long long>(__float_as_uint(m));
+      } else {
+        part.mon[k * part.nb + blockIdx.x] = __double_as_longlong(m);
+      }
+    }
+    if (slot >= 0) {
+      T* out;
+      if constexpr (kF) {
+        out = part.wall_f;
+      } else {
+        out = part.wall;
+      }
+      for (int k = 0; k < kWall; ++k) {
+        T a = (k == 9 || k == 10) ? kLow : T(0);
+        for (int i = 0; i < nw; ++i) a = (k >= 8 && k <= 10) ? smax(a, shd[k][i]) : a + shd[k][i];
+        out[k * part.nwb + slot] = a;
+      }
+    }
+  }
 }
 
 // Block sum of K doubles per thread; result valid in thread 0. shm holds 32*K doubles.
@@ -231,9 +469,9 @@ __global__ void __launch_bounds__(256) k_gradient(DevMesh<T> m, const typename V
     const int s = k * m.n + c;
     const int link = m.link[s];
     if (link == kPad) break;
-    const double2 nd = m.nrm[s];
-    const T a = T(m.area[s]);
-    const T nax = T(nd.x) * a, nay = T(nd.y) * a;
+    const auto nd = m.nrm[s];
+    const T a = m.area[s];
+    const T nax = nd.x * a, nay = nd.y * a;
     T q0 = wc.x, q1 = wc.y, q2 = wc.z, q3 = wc.w;
     bool minus = false;
     if (link >= 0) {
@@ -256,7 +494,7 @@ __global__ void __launch_bounds__(256) k_gradient(DevMesh<T> m, const typename V
       ax3 += q3 * nax; ay3 += q3 * nay;
     }
   }
-  const T inv = T(1) / smax(T(m.vol[c]), Kn<T>::vol_floor);
+  const T inv = m.inv_vol[c];
   typename Vec<T>::v4 ox, oy;
   ox.x = ax0 * inv; ox.y = ax1 * inv; ox.z = ax2 * inv; ox.w = ax3 * inv;
   oy.x = ay0 * inv; oy.y = ay1 * inv; oy.z = ay2 * inv; oy.w = ay3 * inv;
@@ -291,16 +529,21 @@ __global__ void __launch_bounds__(256) k_residual(DevMesh<T> m, FaceParams<T> fp
                                                   const typename Vec<T>::v4* __restrict__ gy,
                                                   typename Vec<T>::v4* __restrict__ R, T* __restrict__ SR,
                                                   Partials part, Ctrl* __restrict__ ctrl, int global_dt) {
-  __shared__ double shm[32 * 3];
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (ctrl->done) return;
   if (LM) {
-    fp.stab_floor = T(ctrl->stab_floor);
     fp.as_fix = ctrl->as_fix;
-    fp.as_fmin = T(ctrl->as_fmin);
-    fp.as_ramp = T(ctrl->as_ramp);
+    if constexpr (sizeof(T) == 4) {
+      fp.stab_floor = ctrl->stab_f;
+      fp.as_fmin = ctrl->as_fmin_f;
+      fp.as_ramp = ctrl->as_ramp_f;
+    } else {
+      fp.stab_floor = ctrl->stab_floor;
+      fp.as_fmin = ctrl->as_fmin;
+      fp.as_ramp = ctrl->as_ramp;
+    }
   }
-  double nl1 = 0.0, nl2 = 0.0, nlinf = 0.0;
+  T nl1 = T(0), nl2 = T(0), nlinf = T(0);  // per-cell norm terms (euler_solver.cpp:309-339)
   double srm = 0.0;
   int fo = 0, df = 0;
   if (c < m.n) {
@@ -316,9 +559,9 @@ __global__ void __launch_bounds__(256) k_residual(DevMesh<T> m, FaceParams<T> fp
       const int s = k * m.n + c;
       const int link = m.link[s];
       if (link == kPad) break;
-      const double2 nd = m.nrm[s];
-      const T nx = T(nd.x), ny = T(nd.y);
-      const T area = T(m.area[s]);
+      const auto nd = m.nrm[s];
+      const T nx = nd.x, ny = nd.y;
+      const T area = m.area[s];
       Flux<T> f;
       T mws;
       bool fb = false;
@@ -388,15 +631,12 @@ __global__ void __launch_bounds__(256) k_residual(DevMesh<T> m, FaceParams<T> fp
     SR[c] = sr;
     if (global_dt) srm = double(smax(sr, Kn<T>::wave_floor));
     if (NORMS) {
-      const double inv = 1.0 / smax(m.vol[c], 1.0e-12);
-      const double v[4] = {double(r0) * inv, double(r1) * inv, double(r2) * inv, double(r3) * inv};
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const double a = fabs(v[k]);
-        nl1 += a;
-        nl2 += a * a;
-        nlinf = smax(nlinf, a);
-      }
+      const T inv = m.inv_vol[c];
+      const T v0 = r0 * inv, v1 = r1 * inv, v2 = r2 * inv, v3 = r3 * inv;
+      const T a0 = fabs(v0), a1 = fabs(v1), a2 = fabs(v2), a3 = fabs(v3);
+      nl1 = ((a0 + a1) + a2) + a3;
+      nl2 = ((v0 * v0 + v1 * v1) + v2 * v2) + v3 * v3;
+      nlinf = smax(smax(smax(a0, a1), a2), a3);
     }
   }
   // fallback counters: one atomic per warp when any lane counted something
@@ -414,13 +654,34 @@ __global__ void __launch_bounds__(256) k_residual(DevMesh<T> m, FaceParams<T> fp
     if ((threadIdx.x & 31) == 0) part.srmax[blockIdx.x * ((blockDim.x + 31) >> 5) + (threadIdx.x >> 5)] = srm;
   }
   if (NORMS) {
-    double v3[3] = {nl1, nl2, 0.0};
-    block_sum<3>(v3, shm);
-    const double mx = block_max(nlinf, shm);
+    // block partials in T; the control kernel sums the blocks in double (FP32: float-float)
+    __shared__ T shn[3][32];
+    nl1 = warp_sum_t(nl1);
+    nl2 = warp_sum_t(nl2);
+    nlinf = warp_max_t(nlinf);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) {
+      shn[0][wid] = nl1;
+      shn[1][wid] = nl2;
+      shn[2][wid] = nlinf;
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
-      part.norms[3 * blockIdx.x + 0] = v3[0];
-      part.norms[3 * blockIdx.x + 1] = v3[1];
-      part.norms[3 * blockIdx.x + 2] = mx;
+      T a = T(0), b = T(0), mx = T(0);
+      for (int i = 0; i < nw; ++i) {
+        a += shn[0][i];
+        b += shn[1][i];
+        mx = smax(mx, shn[2][i]);
+      }
+      T* out;
+      if constexpr (sizeof(T) == 4) {
+        out = part.norms_f;
+      } else {
+        out = part.norms;
+      }
+      out[blockIdx.x] = a;
+      out[part.nb + blockIdx.x] = b;
+      out[2 * part.nb + blockIdx.x] = mx;
     }
   }
 }
@@ -435,29 +696,48 @@ static __global__ void k_srmax(const double* __restrict__ srmax, int n, Ctrl* ct
   if (threadIdx.x == 0) ctrl->sr_max = m;
 }
 
+// Positivity screen in float: true when enforce_physical (euler_flux.cpp:129-144) is provably
+// the identity on the double state s, judged from its float image f = float(s): the density
+// is above twice its floor and the internal energy is a resolved fraction (>1e-3) of the
+// total and above twice the pressure floor, so the double clamp can be skipped. NaN fails.
+__device__ __forceinline__ bool positivity_safe(const Cons<float>& f, float gm1) {
+  if (!(f.r > 2.0e-8f)) return false;
+  const float inv = 1.0f / f.r;
+  const float u = f.ru * inv, v = f.rv * inv;
+  const float ke = 0.5f * f.r * (u * u + v * v);
+  const float e = f.rE - ke;
+  return e > 1.0e-3f * f.rE && gm1 * e > 2.0e-8f;
+}
+
 // ---------------------------------------------------------------------------------------
 // Update: low-Mach residual preconditioning (preconditioning.cpp:51-76, in double), local
-// time step (time_integrator.cpp:31-59) and SSP-RK3 stage (time_integrator.cpp:61-104) on
-// the double conserved state; writes the bulk primitive state for the next stage.
-// The last stage also forms max |p - p_inf| partials and the non-finite trap
-// (euler_solver.cpp:908-946) from the new state.
+// time step (time_integrator.cpp:31-59) and SSP-RK3 stage (time_integrator.cpp:61-104);
+// writes the bulk primitive state for the next stage.
+//   FP64: the stage state Us is a double state, combined as the reference does.
+//   FP32: delta form. Us holds the stage increment delta in float; since the RK3 weights sum
+//         to one, stage k sets delta' = b_k (delta - dt R) with b = 1, 1/4, 2/3. Intermediate
+//         stage states are float: hi + delta' with hi the float image of U_n, clamped in float
+//         as the reference's float path clamps. The last stage adds delta' to the float-float
+//         pair (hi, lo) of U_n, so the conserved state accumulates beyond float precision with
+//         float arithmetic only; the double clamp runs only when the float screen fails.
+// The last stage also runs the non-finite trap (euler_solver.cpp:908-946) and the monitors.
 // ---------------------------------------------------------------------------------------
 template <class T, bool PRECOND, bool LAST>
 __global__ void __launch_bounds__(256) k_update(int n, int stage, PrecondD pc,
                                                 const typename Vec<T>::v4* __restrict__ R,
                                                 const T* __restrict__ SR, typename Vec<T>::v4* __restrict__ W,
-                                                d4* __restrict__ Un, d4* __restrict__ Us,
-                                                const unsigned char* __restrict__ wall_adj, double p_inf,
+                                                StateRef U, typename Vec<T>::v4* __restrict__ Us, MonitorSet ms,
                                                 Partials part, Ctrl* __restrict__ ctrl, int global_dt) {
-  __shared__ double shm[32];
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (ctrl->done) return;
-  double dpd = 0.0, dpw = 0.0;
   bool bad = false;
+  Cons<double> s{1.0, 0.0, 0.0, 1.0};
+  Prim<T> w{T(1), T(0), T(0), T(1)};
   if (c < n) {
     const auto r4 = R[c];
-    double r0 = double(r4.x), r1 = double(r4.y), r2 = double(r4.z), r3 = double(r4.w);
-    if (PRECOND) {
+    const T r0 = r4.x, r1 = r4.y, r2 = r4.z;
+    T r3 = r4.w;
+    if (PRECOND) {  // energy row of the preconditioned residual, in double
       const auto w4 = W[c];
       const Prim<double> w{double(w4.x), double(w4.y), double(w4.z), double(w4.w)};
       FaceParams<double> fpd;
@@ -469,10 +749,10 @@ __global__ void __launch_bounds__(256) k_update(int n, int stage, PrecondD pc,
       const double beta = cell_beta(w, fpd);
       const double b2 = beta * beta;
       const double inv_rho = 1.0 / smax(w.r, 1.0e-8);
-      const double ud = w.u * r1 + w.v * r2;
-      r3 = b2 * r3 + (b2 - 1.0) * inv_rho * ud;
+      const double ud = w.u * double(r1) + w.v * double(r2);
+      r3 = T(b2 * double(r3) + (b2 - 1.0) * inv_rho * ud);
     }
-    const T cfl = T(ctrl->cfl);
+    const T cfl = (sizeof(T) == 4) ? T(ctrl->cfl_f) : T(ctrl->cfl);
     T dt;
     if (global_dt) {
       dt = cfl / T(ctrl->sr_max);
@@ -480,49 +760,87 @@ __global__ void __launch_bounds__(256) k_update(int n, int stage, PrecondD pc,
     } else {
       dt = cfl / smax(SR[c], Kn<T>::wave_floor);
     }
-    const double d = double(dt);
-    const d4 un = Un[c];
-    const d4 us = (stage == 0) ? un : Us[c];
-    Cons<double> s{us.x - d * r0, us.y - d * r1, us.z - d * r2, us.w - d * r3};
-    if (stage == 1) {
-      s.r = 0.75 * un.x + 0.25 * s.r;
-      s.ru = 0.75 * un.y + 0.25 * s.ru;
-      s.rv = 0.75 * un.z + 0.25 * s.rv;
-      s.rE = 0.75 * un.w + 0.25 * s.rE;
-    } else if (stage >= 2) {
-      const double a = 1.0 / 3.0, b = 2.0 / 3.0;
-      s.r = a * un.x + b * s.r;
-      s.ru = a * un.y + b * s.ru;
-      s.rv = a * un.z + b * s.rv;
-      s.rE = a * un.w + b * s.rE;
-    }
-    enforce_physical(&s, pc.gamma);
-    const d4 o{s.r, s.ru, s.rv, s.rE};
-    if (LAST) {
-      Un[c] = o;
+    if constexpr (sizeof(T) == 4) {
+      float d0, d1, d2, d3;
+      if (stage == 0) {
+        d0 = -(dt * r0);
+        d1 = -(dt * r1);
+        d2 = -(dt * r2);
+        d3 = -(dt * r3);
+      } else {
+        const float b = (stage == 1) ? 0.25f : (2.0f / 3.0f);
+        const float4 dl = Us[c];
+        d0 = b * (dl.x - dt * r0);
+        d1 = b * (dl.y - dt * r1);
+        d2 = b * (dl.z - dt * r2);
+        d3 = b * (dl.w - dt * r3);
+      }
+      const float4 uh = U.hi[c];
+      if (!LAST) {
+        Cons<float> f{uh.x + d0, uh.y + d1, uh.z + d2, uh.w + d3};
+        const float fr = f.r, fe = f.rE;
+        enforce_physical(&f, pc.gamma_f);  // changes only rho and rhoE
+        if (f.r != fr) d0 = f.r - uh.x;
+        if (f.rE != fe) d3 = f.rE - uh.w;
+        Us[c] = make_float4(d0, d1, d2, d3);
+        w = cons_to_prim(f, pc.gamma_f);
+      } else {
+        const float4 ul = U.lo[c];
+        float4 h, l;
+        ff_add(uh.x, ul.x, d0, &h.x, &l.x);
+        ff_add(uh.y, ul.y, d1, &h.y, &l.y);
+        ff_add(uh.z, ul.z, d2, &h.z, &l.z);
+        ff_add(uh.w, ul.w, d3, &h.w, &l.w);
+        Cons<float> f{h.x, h.y, h.z, h.w};
+        if (!positivity_safe(f, pc.gm1_f)) {
+          s = Cons<double>{double(h.x) + double(l.x), double(h.y) + double(l.y), double(h.z) + double(l.z),
+                           double(h.w) + double(l.w)};
+          enforce_physical(&s, pc.gamma);
+          ff_split(s.r, &h.x, &l.x);
+          ff_split(s.ru, &h.y, &l.y);
+          ff_split(s.rv, &h.z, &l.z);
+          ff_split(s.rE, &h.w, &l.w);
+          f = Cons<float>{h.x, h.y, h.z, h.w};
+        }
+        U.hi[c] = h;
+        U.lo[c] = l;
+        w = cons_to_prim(f, pc.gamma_f);
+        bad = !finite4(h.x, h.y, h.z, h.w) || !finite4(l.x, l.y, l.z, l.w) || !finite4(w.r, w.u, w.v, w.p);
+      }
     } else {
-      Us[c] = o;
+      const d4 un = U.un[c];
+      const double d = double(dt);
+      const d4 us = (stage == 0) ? un : Us[c];
+      s = Cons<double>{us.x - d * r0, us.y - d * r1, us.z - d * r2, us.w - d * r3};
+      if (stage == 1) {
+        s.r = 0.75 * un.x + 0.25 * s.r;
+        s.ru = 0.75 * un.y + 0.25 * s.ru;
+        s.rv = 0.75 * un.z + 0.25 * s.rv;
+        s.rE = 0.75 * un.w + 0.25 * s.rE;
+      } else if (stage >= 2) {
+        const double a = 1.0 / 3.0, b = 2.0 / 3.0;
+        s.r = a * un.x + b * s.r;
+        s.ru = a * un.y + b * s.ru;
+        s.rv = a * un.z + b * s.rv;
+        s.rE = a * un.w + b * s.rE;
+      }
+      enforce_physical(&s, pc.gamma);
+      const d4 o{s.r, s.ru, s.rv, s.rE};
+      if (LAST) {
+        U.un[c] = o;
+      } else {
+        Us[c] = o;
+      }
+      w = cons_to_prim(Cons<T>{T(s.r), T(s.ru), T(s.rv), T(s.rE)}, T(pc.gamma));
+      if (LAST) bad = !finite4(s.r, s.ru, s.rv, s.rE) || !finite4(w.r, w.u, w.v, w.p);
     }
-    const Cons<T> ct{T(s.r), T(s.ru), T(s.rv), T(s.rE)};
-    const Prim<T> w = cons_to_prim(ct, T(pc.gamma));
     typename Vec<T>::v4 wo;
     wo.x = w.r; wo.y = w.u; wo.z = w.v; wo.w = w.p;
     W[c] = wo;
-    if (LAST) {
-      const Prim<double> wd = cons_to_prim(s, pc.gamma);
-      bad = !finite4(s.r, s.ru, s.rv, s.rE) || !finite4(wd.r, wd.u, wd.v, wd.p);
-      dpd = fabs(wd.p - p_inf);
-      if (wall_adj[c]) dpw = dpd;
-    }
   }
   if (LAST) {
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&ctrl->nonfinite, 1);
-    dpd = block_max(dpd, shm);
-    dpw = block_max(dpw, shm);
-    if (threadIdx.x == 0) {
-      part.dp[2 * blockIdx.x] = dpd;
-      part.dp[2 * blockIdx.x + 1] = dpw;
-    }
+    block_monitors<T>(c < n, w, c, ms, part);
   }
 }
 
@@ -530,63 +848,51 @@ __global__ void __launch_bounds__(256) k_update(int n, int stage, PrecondD pc,
 // v is zeroed through the primitive variables. Applied after the last stage; it redoes the
 // last stage's max |p - p_inf| partials and non-finite check on the symmetrised state.
 template <class T>
-__global__ void __launch_bounds__(256) k_symmetry(int n, int interval, double gamma, d4* __restrict__ Un,
-                                                  typename Vec<T>::v4* __restrict__ W,
-                                                  const unsigned char* __restrict__ wall_adj, double p_inf,
+__global__ void __launch_bounds__(256) k_symmetry(int n, int interval, double gamma, StateRef U,
+                                                  typename Vec<T>::v4* __restrict__ W, MonitorSet ms,
                                                   Partials part, Ctrl* __restrict__ ctrl) {
-  __shared__ double shm[32];
   if (ctrl->done) return;
   if (((ctrl->iter + 1) % interval) != 0) return;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  double dpd = 0.0, dpw = 0.0;
   bool bad = false;
+  Cons<double> s{1.0, 0.0, 0.0, 1.0};
+  Prim<T> wt{T(1), T(0), T(0), T(1)};
   if (c < n) {
-    const d4 u = Un[c];
-    Prim<double> w = cons_to_prim(Cons<double>{u.x, u.y, u.z, u.w}, gamma);
+    Prim<double> w = cons_to_prim(load_state<T>(U, c), gamma);
     w.v = 0.0;
-    const Cons<double> s = prim_to_cons(w, gamma);
-    Un[c] = d4{s.r, s.ru, s.rv, s.rE};
-    const Prim<T> wt = cons_to_prim(Cons<T>{T(s.r), T(s.ru), T(s.rv), T(s.rE)}, T(gamma));
+    s = prim_to_cons(w, gamma);
+    store_state<T>(U, c, s);
+    wt = cons_to_prim(Cons<T>{T(s.r), T(s.ru), T(s.rv), T(s.rE)}, T(gamma));
     typename Vec<T>::v4 wo;
     wo.x = wt.r; wo.y = wt.u; wo.z = wt.v; wo.w = wt.p;
     W[c] = wo;
-    const Prim<double> wd = cons_to_prim(s, gamma);
-    bad = !finite4(s.r, s.ru, s.rv, s.rE) || !finite4(wd.r, wd.u, wd.v, wd.p);
-    dpd = fabs(wd.p - p_inf);
-    if (wall_adj[c]) dpw = dpd;
+    bad = !finite4(s.r, s.ru, s.rv, s.rE) || !finite4(wt.r, wt.u, wt.v, wt.p);
   }
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&ctrl->nonfinite, 1);
-  dpd = block_max(dpd, shm);
-  dpw = block_max(dpw, shm);
-  if (threadIdx.x == 0) {
-    part.dp[2 * blockIdx.x] = dpd;
-    part.dp[2 * blockIdx.x + 1] = dpw;
-  }
+  block_monitors<T>(c < n, wt, c, ms, part);
 }
 
 // Pressure-jump energy over interior faces (euler_solver.cpp:1027-1063), per owning cell.
 template <class T>
-__global__ void __launch_bounds__(256) k_pjump(DevMesh<T> m, const d4* __restrict__ Un,
-                                               const unsigned char* __restrict__ wall_adj, double gamma,
+__global__ void __launch_bounds__(256) k_pjump(DevMesh<T> m, StateRef U,
+                                               const unsigned char* __restrict__ flags, double gamma,
                                                Partials part, const Ctrl* __restrict__ ctrl) {
   __shared__ double shm[32 * 4];
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (ctrl->done) return;
   double v[4] = {0.0, 0.0, 0.0, 0.0};
   if (c < m.n) {
-    const d4 uc = Un[c];
-    const double pc = cons_to_prim(Cons<double>{uc.x, uc.y, uc.z, uc.w}, gamma).p;
+    const double pc = cons_to_prim(load_state<T>(U, c), gamma).p;
     for (int k = 0; k < m.d; ++k) {
       const int link = m.link[k * m.n + c];
       if (link == kPad) break;
       if (link < 0 || (link & 1)) continue;  // interior faces owned by c
       const int o = link >> 1;
-      const d4 uo = Un[o];
-      const double po = cons_to_prim(Cons<double>{uo.x, uo.y, uo.z, uo.w}, gamma).p;
+      const double po = cons_to_prim(load_state<T>(U, o), gamma).p;
       const double dp = pc - po;
       v[0] += dp * dp;
       v[1] += 1.0;
-      if (wall_adj[c] || wall_adj[o]) {
+      if ((flags[c] | flags[o]) & 1) {  // bit 0: the cell owns wall faces
         v[2] += dp * dp;
         v[3] += 1.0;
       }
@@ -594,19 +900,9 @@ __global__ void __launch_bounds__(256) k_pjump(DevMesh<T> m, const d4* __restric
   }
   block_sum<4>(v, shm);
   if (threadIdx.x == 0) {
-    for (int k = 0; k < 4; ++k) part.pjump[4 * blockIdx.x + k] = v[k];
+    for (int k = 0; k < 4; ++k) part.pjump[k * part.nb + blockIdx.x] = v[k];
   }
 }
-
-// Wall faces for forces (forces.cpp:208-294), in wall-patch order.
-struct WallSet {
-  const int* cell;     // new index of the owner cell
-  const double* nx;    // unit normal out of the owner
-  const double* ny;
-  const double* area;
-  const double* x;     // face centre
-  const double* y;
-};
 
 // Host-visible iteration record (mirrors aero_iter_record of include/aero_gb300.h).
 struct Record {
@@ -625,97 +921,17 @@ struct Record {
   int cp_nonfinite, action;
 };
 
-// Owner cells of the far-field faces, for the far-field deviation monitors.
-struct FarSet {
-  const int* cell;
-  int n;
-};
+// Serial part of the controller (lane 0), on the shared copy of the controller state.
+__device__ inline void control_serial(const CtrlConfig& cc, const double (&a)[3], const double (&mon)[kMon],
+                                      const double (&pj)[4], const double (&wv)[kWall], Ctrl* sp,
+                                      Record* __restrict__ recs, int rec_cap) {
+  const double* fsum = wv;
+  const double un_max = wv[8], cp_hi = wv[9], cp_lo_neg = wv[10], cp_bad = wv[11];
+  const double lmax = a[2];
+  const double dpd = mon[0], dpw = mon[1];
+  const double ffm[4] = {mon[2], mon[3], mon[4], mon[5]};
 
-// Controller (one block): norms, forces, convergence monitor, adaptive CFL, staged all-speed
-// controller and the next iteration's schedule (euler_solver.cpp:948-1208, 772-797;
-// convergence_monitor.cpp:13-127).
-static __global__ void __launch_bounds__(1024) k_control(CtrlConfig cc, WallSet ws, FarSet fs,
-                                                  const d4* __restrict__ Un, Partials part,
-                                                  Ctrl* __restrict__ ctrl, Record* __restrict__ recs,
-                                                  int rec_cap) {
-  __shared__ double shm[32 * 8];
-  if (ctrl->done) return;
-  const int tid = threadIdx.x;
-  // residual norms
-  double a[3] = {0.0, 0.0, 0.0};
-  double lmax = 0.0;
-  for (int b = tid; b < cc.n_blocks; b += blockDim.x) {
-    a[0] += part.norms[3 * b];
-    a[1] += part.norms[3 * b + 1];
-    lmax = smax(lmax, part.norms[3 * b + 2]);
-  }
-  block_sum<3>(a, shm);
-  lmax = block_max(lmax, shm);
-  double dpd = 0.0, dpw = 0.0;
-  for (int b = tid; b < cc.n_blocks; b += blockDim.x) {
-    dpd = smax(dpd, part.dp[2 * b]);
-    dpw = smax(dpw, part.dp[2 * b + 1]);
-  }
-  dpd = block_max(dpd, shm);
-  dpw = block_max(dpw, shm);
-  double pj[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int b = tid; b < cc.pjump_blocks; b += blockDim.x) {
-#pragma unroll
-    for (int k = 0; k < 4; ++k) pj[k] += part.pjump[4 * b + k];
-  }
-  block_sum<4>(pj, shm);
-  // forces (forces.cpp:208-294) and wall monitors (euler_solver.cpp:976-1006)
-  double fsum[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // snx sny fxa fya fxg fyg ma mg
-  double un_max = 0.0, cp_hi = -1.0e308, cp_lo_neg = -1.0e308, cp_bad = 0.0;
-  for (int i = tid; i < cc.n_wall; i += blockDim.x) {
-    const d4 u = Un[ws.cell[i]];
-    const Prim<double> w = cons_to_prim(Cons<double>{u.x, u.y, u.z, u.w}, cc.gamma);
-    const double p = w.p;
-    const double nax = -ws.nx[i] * ws.area[i];
-    const double nay = -ws.ny[i] * ws.area[i];
-    const double gp = p - cc.p_inf;
-    const double x = ws.x[i] - cc.x_ref, y = ws.y[i] - cc.y_ref;
-    fsum[0] += nax;
-    fsum[1] += nay;
-    fsum[2] -= p * nax;
-    fsum[3] -= p * nay;
-    fsum[4] -= gp * nax;
-    fsum[5] -= gp * nay;
-    fsum[6] += x * (-p * nay) - y * (-p * nax);
-    fsum[7] += x * (-gp * nay) - y * (-gp * nax);
-    un_max = smax(un_max, fabs(w.u * ws.nx[i] + w.v * ws.ny[i]));
-    const double cp = (p - cc.p_inf) / cc.q_inf;
-    if (isfinite(cp)) {
-      cp_hi = smax(cp_hi, cp);
-      cp_lo_neg = smax(cp_lo_neg, -cp);
-    } else {
-      cp_bad += 1.0;
-    }
-  }
-  block_sum<8>(fsum, shm);
-  un_max = block_max(un_max, shm);
-  cp_hi = block_max(cp_hi, shm);
-  cp_lo_neg = block_max(cp_lo_neg, shm);
-  {
-    double b1[1] = {cp_bad};
-    block_sum<1>(b1, shm);
-    cp_bad = b1[0];
-  }
-  // far-field monitors (euler_solver.cpp:1013-1026)
-  double ffm[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int i = tid; i < fs.n; i += blockDim.x) {
-    const d4 u = Un[fs.cell[i]];
-    const Prim<double> w = cons_to_prim(Cons<double>{u.x, u.y, u.z, u.w}, cc.gamma);
-    ffm[0] = smax(ffm[0], fabs(w.p - cc.p_inf));
-    ffm[1] = smax(ffm[1], fabs(w.r - cc.rho_inf));
-    ffm[2] = smax(ffm[2], fabs(w.u - cc.u_inf));
-    ffm[3] = smax(ffm[3], fabs(w.v - cc.v_inf));
-  }
-#pragma unroll
-  for (int k = 0; k < 4; ++k) ffm[k] = block_max(ffm[k], shm);
-  if (tid != 0) return;
-
-  Ctrl& s = *ctrl;
+  Ctrl& s = *sp;
   Record r;
   r.iter = s.iter;
   r.flags = (s.second ? 8 : 0) | (s.as_fix ? 32 : 0) | (s.stage == 1 ? 64 : 0) | (s.stage == 2 ? 128 : 0);
@@ -797,7 +1013,10 @@ static __global__ void __launch_bounds__(1024) k_control(CtrlConfig cc, WallSet 
       s.hist_head = (s.hist_head + 1) % cap;
     }
   }
-  auto H = [&](int i, int k) { return s.hist[3 * ((s.hist_head + i) % cap) + k]; };
+  auto H = [&](int i, int k) {  // entry i of the ring (0 = oldest); head < cap, i < cap
+    const int j = s.hist_head + i;
+    return s.hist[3 * (j >= cap ? j - cap : j) + k];
+  };
   bool stable = false;
   if (s.hist_count >= req) {
     const int b = s.hist_count - req;
@@ -894,17 +1113,198 @@ static __global__ void __launch_bounds__(1024) k_control(CtrlConfig cc, WallSet 
   apply_schedule(cc, &s);
 }
 
-// Bulk primitive state from the conserved state (start of a run or after aero_set_state).
+
+// Maximum of two non-negative doubles through their bit patterns, on the integer pipe.
+__device__ __forceinline__ long long max_bits(long long a, long long b) { return a > b ? a : b; }
+__device__ __forceinline__ long long warp_max_bits(long long x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x = max_bits(x, __shfl_xor_sync(0xffffffffu, x, o));
+  return x;
+}
+
+// Controller (one block of kCtlThreads): combines the per-block partials of the norms,
+// monitors, forces and pressure jumps in a fixed order, then runs the convergence monitor,
+// adaptive CFL, staged all-speed controller and the next iteration's schedule on thread 0
+// (euler_solver.cpp:948-1208, 772-797; convergence_monitor.cpp:13-127; forces.cpp:208-294).
+// The serial part works on a shared-memory copy of the controller state, loaded and stored
+// by the whole block, so that thread 0 pays no chain of global-memory round trips. Maxima
+// of non-negative quantities are taken on the integer pipe: a GB300 SM runs double
+// arithmetic at a small fraction of its float rate.
+constexpr int kCtlThreads = 128;
+static_assert(sizeof(Ctrl) % 16 == 0, "Ctrl is copied in 16-byte words");
+static __global__ void __launch_bounds__(kCtlThreads) k_control(CtrlConfig cc, Partials part,
+                                                                Ctrl* __restrict__ ctrl,
+                                                                Record* __restrict__ recs, int rec_cap) {
+  constexpr int kWarps = kCtlThreads / 32;
+  __shared__ Ctrl sc;
+  __shared__ double s_sum[kWarps][2 + 4];   // l1, l2 sum, pressure-jump sums
+  __shared__ long long s_max[kWarps][1 + kMon];  // linf, monitors (bit patterns)
+  __shared__ double s_wall[kWarps][kWall];
+  if (ctrl->done) return;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  constexpr int kWords = int(sizeof(Ctrl) / 16);
+  {
+    const int4* src = reinterpret_cast<const int4*>(ctrl);
+    int4* dst = reinterpret_cast<int4*>(&sc);
+    for (int i = tid; i < kWords; i += kCtlThreads) dst[i] = src[i];
+  }
+  const int nb = cc.n_blocks;
+  double s1 = 0.0, s2 = 0.0;
+  long long mx[1 + kMon] = {0, 0, 0, 0, 0, 0, 0};
+  if (cc.bulk_f32) {
+    // float block partials summed in float-float, then one conversion per warp
+    float h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;
+#pragma unroll 2
+    for (int b = tid; b < nb; b += kCtlThreads) {
+      ff_add(h1, l1, part.norms_f[b], &h1, &l1);
+      ff_add(h2, l2, part.norms_f[nb + b], &h2, &l2);
+      mx[0] = max_bits(mx[0], static_cast<long long>(__float_as_uint(part.norms_f[2 * nb + b])));
+#pragma unroll
+      for (int k = 0; k < kMon; ++k) mx[k + 1] = max_bits(mx[k + 1], part.mon[k * nb + b]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float a = __shfl_xor_sync(0xffffffffu, h1, o), b = __shfl_xor_sync(0xffffffffu, l1, o);
+      const float c = __shfl_xor_sync(0xffffffffu, h2, o), d = __shfl_xor_sync(0xffffffffu, l2, o);
+      ff_add2(h1, l1, a, b, &h1, &l1);
+      ff_add2(h2, l2, c, d, &h2, &l2);
+    }
+    if (lane == 0) {
+      s1 = double(h1) + double(l1);
+      s2 = double(h2) + double(l2);
+    }
+  } else {
+#pragma unroll 2
+    for (int b = tid; b < nb; b += kCtlThreads) {
+      s1 += part.norms[b];
+      s2 += part.norms[nb + b];
+      mx[0] = max_bits(mx[0], __double_as_longlong(part.norms[2 * nb + b]));
+#pragma unroll
+      for (int k = 0; k < kMon; ++k) mx[k + 1] = max_bits(mx[k + 1], part.mon[k * nb + b]);
+    }
+    s1 = warp_sum(s1);
+    s2 = warp_sum(s2);
+  }
+#pragma unroll
+  for (int k = 0; k < 1 + kMon; ++k) mx[k] = warp_max_bits(mx[k]);
+  double pj[4] = {0.0, 0.0, 0.0, 0.0};
+  if (cc.pjump_blocks > 0) {
+    for (int b = tid; b < cc.pjump_blocks; b += kCtlThreads) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) pj[k] += part.pjump[k * nb + b];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) pj[k] = warp_sum(pj[k]);
+  }
+  // wall partials (snx sny fxa fya fxg fyg ma mg | un_max cp_hi -cp_lo cp_bad): with the
+  // wall-owning cells numbered first these come from a few blocks, summed per quantity by
+  // one thread each; otherwise by the whole block
+  const int nwb = cc.n_wall_blocks;
+  auto wall_init = [](int k) { return (k == 9 || k == 10) ? -1.0e308 : 0.0; };
+  auto wall_comb = [](int k, double acc, double x) { return (k >= 8 && k <= 10) ? smax(acc, x) : acc + x; };
+  auto wall_at = [&](int i) { return cc.bulk_f32 ? double(part.wall_f[i]) : part.wall[i]; };
+  if (nwb <= 32) {
+    if (tid < kWall) {
+      double acc = wall_init(tid);
+      for (int b = 0; b < nwb; ++b) acc = wall_comb(tid, acc, wall_at(tid * nwb + b));
+      s_wall[0][tid] = acc;
+    }
+  } else {
+    double wv[kWall];
+#pragma unroll
+    for (int k = 0; k < kWall; ++k) wv[k] = wall_init(k);
+    for (int b = tid; b < nwb; b += kCtlThreads) {
+#pragma unroll
+      for (int k = 0; k < kWall; ++k) wv[k] = wall_comb(k, wv[k], wall_at(k * nwb + b));
+    }
+#pragma unroll
+    for (int k = 0; k < kWall; ++k) wv[k] = (k >= 8 && k <= 10) ? warp_max(wv[k]) : warp_sum(wv[k]);
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < kWall; ++k) s_wall[wid][k] = wv[k];
+    }
+  }
+  if (lane == 0) {
+    s_sum[wid][0] = s1;
+    s_sum[wid][1] = s2;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) s_sum[wid][2 + k] = pj[k];
+#pragma unroll
+    for (int k = 0; k < 1 + kMon; ++k) s_max[wid][k] = mx[k];
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double a[3] = {0.0, 0.0, 0.0}, mon[kMon], p4[4] = {0.0, 0.0, 0.0, 0.0}, wv[kWall];
+    long long m[1 + kMon] = {0, 0, 0, 0, 0, 0, 0};
+    for (int w = 0; w < kWarps; ++w) {
+      a[0] += s_sum[w][0];
+      a[1] += s_sum[w][1];
+      for (int k = 0; k < 4; ++k) p4[k] += s_sum[w][2 + k];
+      for (int k = 0; k < 1 + kMon; ++k) m[k] = max_bits(m[k], s_max[w][k]);
+    }
+    auto decode = [&](long long bits) {
+      return cc.bulk_f32 ? double(__uint_as_float(static_cast<unsigned>(bits))) : __longlong_as_double(bits);
+    };
+    a[2] = decode(m[0]);
+    for (int k = 0; k < kMon; ++k) mon[k] = decode(m[k + 1]);
+    for (int k = 0; k < kWall; ++k) {
+      wv[k] = s_wall[0][k];
+      if (nwb > 32) {
+        for (int w = 1; w < kWarps; ++w) wv[k] = wall_comb(k, wv[k], s_wall[w][k]);
+      }
+    }
+    control_serial(cc, a, mon, p4, wv, &sc, recs, rec_cap);
+  }
+  __syncthreads();
+  {
+    const int4* src = reinterpret_cast<const int4*>(&sc);
+    int4* dst = reinterpret_cast<int4*>(ctrl);
+    for (int i = tid; i < kWords; i += kCtlThreads) dst[i] = src[i];
+  }
+}
+
+// Bulk primitive state from a double conserved state (FP64 state, or a state given to
+// aero_residual).
 template <class T>
 __global__ void k_refresh_prim(int n, const d4* __restrict__ Un, typename Vec<T>::v4* __restrict__ W, double gamma) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
   const d4 u = Un[c];
-  const Cons<T> ct{T(u.x), T(u.y), T(u.z), T(u.w)};
-  const Prim<T> w = cons_to_prim(ct, T(gamma));
+  const Prim<T> w = cons_to_prim(Cons<T>{T(u.x), T(u.y), T(u.z), T(u.w)}, T(gamma));
   typename Vec<T>::v4 o;
   o.x = w.r; o.y = w.u; o.z = w.v; o.w = w.p;
   W[c] = o;
+}
+
+// FP32 state: split a double state into float-float pairs, combine the pairs back into
+// doubles, and the bulk primitive state from the float image.
+static __global__ void k_split_state(int n, const d4* __restrict__ Un, float4* __restrict__ hi,
+                                     float4* __restrict__ lo) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const d4 u = Un[c];
+  float4 h, l;
+  ff_split(u.x, &h.x, &l.x);
+  ff_split(u.y, &h.y, &l.y);
+  ff_split(u.z, &h.z, &l.z);
+  ff_split(u.w, &h.w, &l.w);
+  hi[c] = h;
+  lo[c] = l;
+}
+static __global__ void k_combine_state(int n, const float4* __restrict__ hi, const float4* __restrict__ lo,
+                                       d4* __restrict__ Un) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const float4 h = hi[c], l = lo[c];
+  Un[c] = d4{double(h.x) + double(l.x), double(h.y) + double(l.y), double(h.z) + double(l.z),
+             double(h.w) + double(l.w)};
+}
+static __global__ void k_prim_from_image(int n, const float4* __restrict__ hi, float4* __restrict__ W, float gamma) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const float4 h = hi[c];
+  const Prim<float> w = cons_to_prim(Cons<float>{h.x, h.y, h.z, h.w}, gamma);
+  W[c] = make_float4(w.r, w.u, w.v, w.p);
 }
 
 }  // namespace aero

@@ -47,12 +47,20 @@ class EngineT final : public Engine {
     nblocks_ = (n_ + block_ - 1) / block_;
     const size_t ns = static_cast<size_t>(n_) * d_;
 
-    // slot table
+    // slot table; normals and areas in T (exact conversions of the double geometry)
     link_ = upload(hs_.link);
-    std::vector<double2> nrm(ns);
-    for (size_t i = 0; i < ns; ++i) nrm[i] = make_double2(hs_.nx[i], hs_.ny[i]);
+    std::vector<V2> nrm(ns);
+    std::vector<T> area(ns);
+    for (size_t i = 0; i < ns; ++i) {
+      nrm[i].x = T(hs_.nx[i]);
+      nrm[i].y = T(hs_.ny[i]);
+      area[i] = T(hs_.area[i]);
+    }
     nrm_ = upload(nrm);
-    area_ = upload(hs_.area);
+    area_ = upload(area);
+    std::vector<T> inv_vol(static_cast<size_t>(n_));
+    for (int c = 0; c < n_; ++c) inv_vol[c] = T(1) / std::max(T(hs_.vol[c]), T(1.0e-12));
+    inv_vol_ = upload(inv_vol);
     std::vector<V2> doff(ns), noff(ns);
     for (size_t i = 0; i < ns; ++i) {
       if (hs_.link[i] < 0) {
@@ -68,18 +76,57 @@ class EngineT final : public Engine {
     }
     doff_ = upload(doff);
     noff_ = upload(noff);
-    vol_ = upload(hs_.vol);
-    wall_adj_ = upload(hs_.wall_adj);
     perm_dev_ = upload(hs_.perm);
-    const int nw = static_cast<int>(hs_.wall_cell.size());
-    ws_.cell = upload(hs_.wall_cell.empty() ? std::vector<int>{0} : hs_.wall_cell);
-    ws_.nx = upload(nonempty(hs_.wnx));
-    ws_.ny = upload(nonempty(hs_.wny));
-    ws_.area = upload(nonempty(hs_.warea));
-    ws_.x = upload(nonempty(hs_.wx));
-    ws_.y = upload(nonempty(hs_.wy));
-    fs_.cell = upload(nonempty(hs_.far_cell));
-    fs_.n = static_cast<int>(hs_.far_cell.size());
+    // monitor tables: per-cell flags, owner-sorted wall entries, and a partials slot for each
+    // update block that holds wall entries
+    std::vector<int> block_slot(static_cast<size_t>(nblocks_), -1);
+    int n_wall_blocks = 0;
+    for (int b = 0; b < nblocks_; ++b) {
+      const int c0 = b * block_, c1 = std::min(n_, c0 + block_);
+      for (int c = c0; c < c1; ++c) {
+        if (hs_.flags[c] >= 4) {
+          block_slot[b] = n_wall_blocks++;
+          break;
+        }
+      }
+    }
+    flags_ = upload(hs_.flags);
+    ms_.flags = flags_;
+    ms_.wall_first = upload(hs_.wall_first);
+    ms_.wkind = upload(hs_.wkind.empty() ? std::vector<unsigned char>{0} : hs_.wkind);
+    ms_.wnx = upload(nonempty(hs_.wnx));
+    ms_.wny = upload(nonempty(hs_.wny));
+    ms_.warea = upload(nonempty(hs_.warea));
+    ms_.wx = upload(nonempty(hs_.wx));
+    ms_.wy = upload(nonempty(hs_.wy));
+    {
+      auto to_f = [](const std::vector<double>& v) {
+        std::vector<float> f(v.empty() ? 1 : v.size(), 0.0f);
+        for (size_t i = 0; i < v.size(); ++i) f[i] = float(v[i]);
+        return f;
+      };
+      ms_.wnx_f = upload(to_f(hs_.wnx));
+      ms_.wny_f = upload(to_f(hs_.wny));
+      ms_.warea_f = upload(to_f(hs_.warea));
+      ms_.wx_f = upload(to_f(hs_.wx));
+      ms_.wy_f = upload(to_f(hs_.wy));
+    }
+    ms_.block_slot = upload(block_slot);
+    ms_.p_inf = rs_.p_inf;
+    ms_.rho_inf = rs_.rho_inf;
+    ms_.u_inf = rs_.v_inf * rs_.cos_a;
+    ms_.v_inf = rs_.v_inf * rs_.sin_a;
+    ms_.q_inf = rs_.q_inf;
+    ms_.x_ref = cfg_.x_ref;
+    ms_.y_ref = cfg_.y_ref;
+    ms_.gamma = rs_.gamma;
+    ms_.p_inf_f = float(ms_.p_inf);
+    ms_.rho_inf_f = float(ms_.rho_inf);
+    ms_.u_inf_f = float(ms_.u_inf);
+    ms_.v_inf_f = float(ms_.v_inf);
+    ms_.q_inf_f = float(ms_.q_inf);
+    ms_.x_ref_f = float(ms_.x_ref);
+    ms_.y_ref_f = float(ms_.y_ref);
 
     // state
     W_ = alloc<V4>(n_);
@@ -88,9 +135,26 @@ class EngineT final : public Engine {
     R_ = alloc<V4>(n_);
     SR_ = alloc<T>(n_);
     Un_ = alloc<d4>(n_);
-    Us_ = alloc<d4>(n_);
-    part_.norms = alloc<double>(3 * nblocks_);
-    part_.dp = alloc<double>(2 * nblocks_);
+    Us_ = alloc<V4>(n_);
+    sref_.un = Un_;
+    if (sizeof(T) == 4) {
+      sref_.hi = alloc<float4>(n_);
+      sref_.lo = alloc<float4>(n_);
+    }
+    Ueval_ = alloc<d4>(n_);
+    if (sizeof(T) == 4) {
+      part_.norms_f = alloc<float>(3 * nblocks_);
+    } else {
+      part_.norms = alloc<double>(3 * nblocks_);
+    }
+    part_.mon = alloc<long long>(kMon * nblocks_);
+    if (sizeof(T) == 4) {
+      part_.wall_f = alloc<float>(kWall * std::max(n_wall_blocks, 1));
+    } else {
+      part_.wall = alloc<double>(kWall * std::max(n_wall_blocks, 1));
+    }
+    part_.nb = nblocks_;
+    part_.nwb = n_wall_blocks;
     part_.pjump = alloc<double>(4 * nblocks_);
     part_.srmax = alloc<double>(nblocks_ * (block_ / 32));
     ctrl_ = alloc<Ctrl>(1);
@@ -109,7 +173,7 @@ class EngineT final : public Engine {
     dm_.area = area_;
     dm_.doff = doff_;
     dm_.noff = noff_;
-    dm_.vol = vol_;
+    dm_.inv_vol = inv_vol_;
 
     fp_.gamma = T(rs_.gamma);
     fp_.farfield = Cons<T>{T(rs_.cons_inf[0]), T(rs_.cons_inf[1]), T(rs_.cons_inf[2]), T(rs_.cons_inf[3])};
@@ -134,11 +198,15 @@ class EngineT final : public Engine {
     pc_.mach_min = double(fp_.pc_mach_min);
     pc_.beta_min = double(fp_.pc_beta_min);
     pc_.beta_max = double(fp_.pc_beta_max);
+    pc_.gamma_f = float(rs_.gamma);
+    pc_.gm1_f = float(rs_.gamma - 1.0);
 
     CtrlConfig& c = cc_;
     std::memset(&c, 0, sizeof(c));
     c.n_cells = n_;
-    c.n_wall = nw;
+    c.n_wall = hs_.n_slip;
+    c.n_wall_blocks = n_wall_blocks;
+    c.bulk_f32 = sizeof(T) == 4 ? 1 : 0;
     c.rk_stages = cfg_.rk_stages;
     c.local_dt = cfg_.local_time_stepping;
     c.cfl_ramp = cfg_.cfl_ramp_iters;
@@ -192,6 +260,7 @@ class EngineT final : public Engine {
     // freestream initial state
     std::vector<d4> u0(static_cast<size_t>(n_), d4{rs_.cons_inf[0], rs_.cons_inf[1], rs_.cons_inf[2], rs_.cons_inf[3]});
     AERO_CK(cudaMemcpyAsync(Un_, u0.data(), sizeof(d4) * n_, cudaMemcpyHostToDevice, st_));
+    state_from_staging();
     w_valid_ = false;
     reset_run();
     AERO_CK(cudaStreamSynchronize(st_));
@@ -246,12 +315,14 @@ class EngineT final : public Engine {
       h[cn] = d4{s[0], s[1], s[2], s[4]};
     }
     AERO_CK(cudaMemcpyAsync(Un_, h, sizeof(d4) * n_, cudaMemcpyHostToDevice, st_));
+    state_from_staging();
     AERO_CK(cudaStreamSynchronize(st_));
     w_valid_ = false;
   }
 
   void get_state(double* u) override {
     d4* h = pinned_state();
+    state_to_staging();
     AERO_CK(cudaMemcpyAsync(h, Un_, sizeof(d4) * n_, cudaMemcpyDeviceToHost, st_));
     AERO_CK(cudaStreamSynchronize(st_));
     for (int cn = 0; cn < n_; ++cn) {
@@ -266,6 +337,7 @@ class EngineT final : public Engine {
 
   void get_primitive(double* rho, double* u, double* v, double* p) override {
     std::vector<d4> h(static_cast<size_t>(n_));
+    state_to_staging();
     AERO_CK(cudaMemcpyAsync(h.data(), Un_, sizeof(d4) * n_, cudaMemcpyDeviceToHost, st_));
     AERO_CK(cudaStreamSynchronize(st_));
     for (int cn = 0; cn < n_; ++cn) {
@@ -289,15 +361,12 @@ class EngineT final : public Engine {
       const double* s = u + 5 * static_cast<size_t>(hs_.perm[cn]);
       h[cn] = d4{s[0], s[1], s[2], s[4]};
     }
-    AERO_CK(cudaMemcpyAsync(Us_, h.data(), sizeof(d4) * n_, cudaMemcpyHostToDevice, st_));
+    AERO_CK(cudaMemcpyAsync(Ueval_, h.data(), sizeof(d4) * n_, cudaMemcpyHostToDevice, st_));
     Ctrl ce;
     std::memset(&ce, 0, sizeof(ce));
-    ce.stab_floor = stab;
-    ce.as_fix = as_fix;
-    ce.as_fmin = as_fmin;
-    ce.as_ramp = as_ramp;
+    set_eval_schedule(&ce, stab, as_fix, as_fmin, as_ramp);
     AERO_CK(cudaMemcpyAsync(ctrl_eval_, &ce, sizeof(Ctrl), cudaMemcpyHostToDevice, st_));
-    k_refresh_prim<T><<<nblocks_, block_, 0, st_>>>(n_, Us_, W_, rs_.gamma);
+    k_refresh_prim<T><<<nblocks_, block_, 0, st_>>>(n_, Ueval_, W_, rs_.gamma);
     if (second) k_gradient<T><<<nblocks_, block_, 0, st_>>>(dm_, W_, gx_, gy_, ctrl_eval_);
     launch_residual(second != 0, false, ctrl_eval_, 0);
     AERO_CK(cudaGetLastError());
@@ -406,24 +475,29 @@ class EngineT final : public Engine {
       ms[k] = 0.0;
       launches[k] = 0;
     }
-    cudaEvent_t e0, e1;
-    AERO_CK(cudaEventCreate(&e0));
-    AERO_CK(cudaEventCreate(&e1));
+    // every launch between its own event pair; all queued back to back, read after one sync
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
     for (int j = 0; j < n; ++j) {
       if (flush_l2) AERO_CK(cudaMemsetAsync(flush_, j & 0xff, flush_bytes_, st_));
       launch_iteration(second_at(it0 + j), [&](int cls, auto&& launch) {
-        AERO_CK(cudaEventRecord(e0, st_));
+        cudaEvent_t a = nullptr, b = nullptr;
+        AERO_CK(cudaEventCreate(&a));
+        AERO_CK(cudaEventCreate(&b));
+        AERO_CK(cudaEventRecord(a, st_));
         launch();
-        AERO_CK(cudaEventRecord(e1, st_));
-        AERO_CK(cudaEventSynchronize(e1));
-        float f = 0.0f;
-        AERO_CK(cudaEventElapsedTime(&f, e0, e1));
-        ms[cls] += f;
-        ++launches[cls];
+        AERO_CK(cudaEventRecord(b, st_));
+        marks.push_back({cls, {a, b}});
       });
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    AERO_CK(cudaStreamSynchronize(st_));
+    for (auto& mk : marks) {
+      float f = 0.0f;
+      AERO_CK(cudaEventElapsedTime(&f, mk.second.first, mk.second.second));
+      ms[mk.first] += f;
+      ++launches[mk.first];
+      cudaEventDestroy(mk.second.first);
+      cudaEventDestroy(mk.second.second);
+    }
     return end_untracked();
   }
 
@@ -468,9 +542,23 @@ class EngineT final : public Engine {
   }
 
   void refresh() {
-    k_refresh_prim<T><<<nblocks_, block_, 0, st_>>>(n_, Un_, W_, rs_.gamma);
+    if constexpr (sizeof(T) == 4) {
+      k_prim_from_image<<<nblocks_, block_, 0, st_>>>(n_, sref_.hi, W_, pc_.gamma_f);
+    } else {
+      k_refresh_prim<T><<<nblocks_, block_, 0, st_>>>(n_, Un_, W_, rs_.gamma);
+    }
     AERO_CK(cudaGetLastError());
     w_valid_ = true;
+  }
+
+  // FP32 keeps the state as float-float pairs and uses Un_ as the double staging array.
+  void state_from_staging() {
+    if (sizeof(T) == 4) k_split_state<<<nblocks_, block_, 0, st_>>>(n_, Un_, sref_.hi, sref_.lo);
+    AERO_CK(cudaGetLastError());
+  }
+  void state_to_staging() {
+    if (sizeof(T) == 4) k_combine_state<<<nblocks_, block_, 0, st_>>>(n_, sref_.hi, sref_.lo, Un_);
+    AERO_CK(cudaGetLastError());
   }
 
   void download_residual(double* res, double* sr) {
@@ -524,8 +612,8 @@ class EngineT final : public Engine {
 
   template <bool PRECOND, bool LAST>
   void update_t(int stage, int global_dt) {
-    k_update<T, PRECOND, LAST><<<nblocks_, block_, 0, st_>>>(n_, stage, pc_, R_, SR_, W_, Un_, Us_, wall_adj_,
-                                                             rs_.p_inf, part_, ctrl_, global_dt);
+    k_update<T, PRECOND, LAST><<<nblocks_, block_, 0, st_>>>(n_, stage, pc_, R_, SR_, W_, sref_, Us_, ms_, part_,
+                                                             ctrl_, global_dt);
   }
 
   struct Direct {
@@ -561,14 +649,14 @@ class EngineT final : public Engine {
     }
     if (sym_on_) {
       wrap(4, [&] {
-        k_symmetry<T><<<nblocks_, block_, 0, st_>>>(n_, cfg_.aoa0_symmetry_enforce_interval, rs_.gamma, Un_,
-                                                     W_, wall_adj_, rs_.p_inf, part_, ctrl_);
+        k_symmetry<T><<<nblocks_, block_, 0, st_>>>(n_, cfg_.aoa0_symmetry_enforce_interval, rs_.gamma, sref_,
+                                                     W_, ms_, part_, ctrl_);
       });
     }
     if (pjump_on_) {
-      wrap(4, [&] { k_pjump<T><<<nblocks_, block_, 0, st_>>>(dm_, Un_, wall_adj_, rs_.gamma, part_, ctrl_); });
+      wrap(4, [&] { k_pjump<T><<<nblocks_, block_, 0, st_>>>(dm_, sref_, flags_, rs_.gamma, part_, ctrl_); });
     }
-    wrap(5, [&] { k_control<<<1, 1024, 0, st_>>>(cc_, ws_, fs_, Un_, part_, ctrl_, recs_, rec_cap_); });
+    wrap(5, [&] { k_control<<<1, kCtlThreads, 0, st_>>>(cc_, part_, ctrl_, recs_, rec_cap_); });
     AERO_CK(cudaGetLastError());
   }
 
@@ -645,18 +733,20 @@ class EngineT final : public Engine {
   int n_ = 0, d_ = 0, block_ = 128, nblocks_ = 0, rec_cap_ = 0;
   bool pjump_on_ = false, sym_on_ = false, w_valid_ = false;
   int* link_ = nullptr;
-  double2* nrm_ = nullptr;
-  double* area_ = nullptr;
+  V2* nrm_ = nullptr;
+  T* area_ = nullptr;
   V2* doff_ = nullptr;
   V2* noff_ = nullptr;
-  double* vol_ = nullptr;
-  unsigned char* wall_adj_ = nullptr;
+  T* inv_vol_ = nullptr;
+  unsigned char* flags_ = nullptr;
   int* perm_dev_ = nullptr;
-  WallSet ws_{};
-  FarSet fs_{};
+  MonitorSet ms_{};
   V4 *W_ = nullptr, *gx_ = nullptr, *gy_ = nullptr, *R_ = nullptr;
   T* SR_ = nullptr;
-  d4 *Un_ = nullptr, *Us_ = nullptr;
+  d4* Un_ = nullptr;     // FP64: the conserved state; FP32: double staging for transfers
+  StateRef sref_{};
+  V4* Us_ = nullptr;    // FP64: stage state; FP32: stage increment (delta form)
+  d4* Ueval_ = nullptr;  // conserved state given to aero_residual
   Partials part_{};
   Ctrl* ctrl_ = nullptr;
   Ctrl* ctrl_eval_ = nullptr;

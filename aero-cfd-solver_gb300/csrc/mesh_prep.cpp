@@ -172,6 +172,16 @@ bool build_slots(const aero_mesh_desc& m, int ordering, HostSlots* out, std::str
     s.perm.resize(static_cast<size_t>(n));
     std::iota(s.perm.begin(), s.perm.end(), 0);
   }
+  if (ordering == AERO_ORDER_MORTON || ordering == AERO_ORDER_RCM) {
+    // cells that own wall faces first (each group keeps the chosen order), so that the wall
+    // force sums and monitors of the last RK stage come from a few thread blocks
+    std::vector<unsigned char> owns(static_cast<size_t>(n), 0);
+    for (int f = 0; f < nf; ++f) {
+      if (m.face_neighbor[f] < 0 && m.face_bc[f] == AERO_BC_WALL) owns[m.face_owner[f]] = 1;
+    }
+    for (int i = 0; i < m.num_wall_faces; ++i) owns[m.face_owner[m.wall_faces[i]]] = 1;
+    std::stable_partition(s.perm.begin(), s.perm.end(), [&](int c) { return owns[c] != 0; });
+  }
   s.iperm.assign(static_cast<size_t>(n), -1);
   for (int i = 0; i < n; ++i) s.iperm[s.perm[i]] = i;
 
@@ -195,7 +205,7 @@ bool build_slots(const aero_mesh_desc& m, int ordering, HostSlots* out, std::str
   s.own_old.assign(total, 0);
   s.nbr_old.assign(total, 0);
   s.vol.resize(static_cast<size_t>(n));
-  s.wall_adj.assign(static_cast<size_t>(n), 0);
+  s.flags.assign(static_cast<size_t>(n), 0);
   s.ccx.resize(static_cast<size_t>(n));
   s.ccy.resize(static_cast<size_t>(n));
   for (int c = 0; c < n; ++c) {
@@ -216,7 +226,7 @@ bool build_slots(const aero_mesh_desc& m, int ordering, HostSlots* out, std::str
         s.link[slot] = (s.iperm[other] << 1) | side;
       } else {
         s.link[slot] = (m.face_bc[f] == AERO_BC_WALL) ? -2 : -1;
-        if (m.face_bc[f] == AERO_BC_WALL) s.wall_adj[cn] = 1;
+        s.flags[cn] |= (m.face_bc[f] == AERO_BC_WALL) ? 1 : 2;
       }
       s.nx[slot] = m.face_normal[3 * f];
       s.ny[slot] = m.face_normal[3 * f + 1];
@@ -227,17 +237,50 @@ bool build_slots(const aero_mesh_desc& m, int ordering, HostSlots* out, std::str
       s.nbr_old[slot] = b >= 0 ? b : o;
     }
   }
+  // wall entries: (new owner, face, kind); a slip-wall face listed in the patch is merged
+  // into its monitor entry once, further listings get entries of their own
+  struct WallEntry {
+    int cell, face;
+    unsigned char kind;
+  };
+  std::vector<WallEntry> we;
+  std::vector<int> slip_entry(static_cast<size_t>(nf), -1);
   for (int f = 0; f < nf; ++f) {
-    if (m.face_neighbor[f] < 0 && m.face_bc[f] == AERO_BC_FARFIELD) s.far_cell.push_back(s.iperm[m.face_owner[f]]);
+    if (m.face_neighbor[f] >= 0 || m.face_bc[f] != AERO_BC_WALL) continue;
+    slip_entry[f] = static_cast<int>(we.size());
+    we.push_back({s.iperm[m.face_owner[f]], f, 2});
+    ++s.n_slip;
   }
   for (int i = 0; i < m.num_wall_faces; ++i) {
     const int f = m.wall_faces[i];
-    s.wall_cell.push_back(s.iperm[m.face_owner[f]]);
-    s.wnx.push_back(m.face_normal[3 * f]);
-    s.wny.push_back(m.face_normal[3 * f + 1]);
-    s.warea.push_back(m.face_area[f]);
-    s.wx.push_back(m.face_center[3 * f]);
-    s.wy.push_back(m.face_center[3 * f + 1]);
+    if (slip_entry[f] >= 0 && !(we[slip_entry[f]].kind & 1)) {
+      we[slip_entry[f]].kind |= 1;
+    } else {
+      we.push_back({s.iperm[m.face_owner[f]], f, 1});
+    }
+    ++s.n_patch;
+  }
+  std::stable_sort(we.begin(), we.end(), [](const WallEntry& a, const WallEntry& b) {
+    return a.cell != b.cell ? a.cell < b.cell : a.face < b.face;
+  });
+  s.wall_first.assign(static_cast<size_t>(n), 0);
+  std::vector<int> per_cell(static_cast<size_t>(n), 0);
+  for (size_t j = 0; j < we.size(); ++j) {
+    const WallEntry& e = we[j];
+    if (per_cell[e.cell]++ == 0) s.wall_first[e.cell] = static_cast<int>(j);
+    s.wkind.push_back(e.kind);
+    s.wnx.push_back(m.face_normal[3 * e.face]);
+    s.wny.push_back(m.face_normal[3 * e.face + 1]);
+    s.warea.push_back(m.face_area[e.face]);
+    s.wx.push_back(m.face_center[3 * e.face]);
+    s.wy.push_back(m.face_center[3 * e.face + 1]);
+  }
+  for (int c = 0; c < n; ++c) {
+    if (per_cell[c] > 63) {
+      *err = "a cell owns more than 63 wall faces";
+      return false;
+    }
+    s.flags[c] = static_cast<unsigned char>(s.flags[c] | (per_cell[c] << 2));
   }
   return true;
 }

@@ -22,12 +22,17 @@ struct HostSlots {
   std::vector<int> own_old, nbr_old;    // [d*n] canonical owner / neighbour (original ids)
   std::vector<double> vol;              // [n] new order
   std::vector<double> ccx, ccy;         // [n] original order (cell centres)
-  std::vector<unsigned char> wall_adj;  // [n] new order
-  // wall patch in patch order
-  std::vector<int> wall_cell;  // new owner index
+  // [n] new order: bit 0 owns slip-wall faces, bit 1 owns far-field faces, bits 2..7 number
+  // of wall entries
+  std::vector<unsigned char> flags;
+  std::vector<int> wall_first;  // [n] first wall entry of the cell
+  // Wall entries sorted by new owner index, then by face: the force patch faces (kind bit 0,
+  // once per listing) and the slip-wall boundary faces (kind bit 1, the wall monitors); a
+  // face in both sets shares one entry.
+  std::vector<unsigned char> wkind;
   std::vector<double> wnx, wny, warea, wx, wy;
-  // owners (new index) of the far-field faces in face order
-  std::vector<int> far_cell;
+  int n_patch = 0;  // force patch faces
+  int n_slip = 0;   // slip-wall boundary faces
   int interior_faces = 0, boundary_faces = 0;
 };
 

@@ -63,10 +63,7 @@ __global__ void k_na_prepare(int n, const int* __restrict__ perm, const double* 
     ctrl->done = 0;
     ctrl->fo_fallback = 0;
     ctrl->diff_fallback = 0;
-    ctrl->stab_floor = stab;
-    ctrl->as_fix = as_fix;
-    ctrl->as_fmin = as_fmin;
-    ctrl->as_ramp = as_ramp;
+    set_eval_schedule(ctrl, stab, as_fix, as_fmin, as_ramp);
     ctrl->sr_max = 0.0;
   }
   if (c >= n) return;

@@ -52,13 +52,18 @@ def algorithmic_bytes(kernel: str, n: int, slots: int, precision: str) -> float:
     """Compulsory bytes of one launch: every array element the kernel reads or writes,
     once (neighbour re-reads excluded). s = bulk real size."""
     s = 4 if precision == "fp32" else 8
-    slot_geo = 4 + 16 + 8  # link, double2 normal, double area
-    if kernel == "residual":
-        return n * (4 * s + 8 * s + slots * (slot_geo + 4 * s) + 4 * s + s)
-    if kernel == "gradient":
-        return n * (4 * s + slots * slot_geo + 8 + 8 * s)
-    if kernel == "update":  # average over the three RK stages (stage 0 reads U_n only)
-        per = [4 * s + s + 32 + 32 + 4 * s, 4 * s + s + 64 + 32 + 4 * s, 4 * s + s + 64 + 1 + 32 + 4 * s]
+    slot_geo = 4 + 2 * s + s  # link, normal, area
+    if kernel == "residual":  # W, gradients, slot geometry and MUSCL offsets, 1/vol, R, SR
+        return n * (4 * s + 8 * s + slots * (slot_geo + 4 * s) + s + 4 * s + s)
+    if kernel == "gradient":  # W, slot geometry, 1/vol, gradients
+        return n * (4 * s + slots * slot_geo + s + 8 * s)
+    if kernel == "update":
+        # average over the three RK stages: R, SR, U_n (double), stage state / increment
+        # (4 reals) read from stage 1 on and written before the last stage, U_n written and the
+        # wall flags read in the last stage, W written every stage
+        per = [4 * s + s + 32 + 4 * s + 4 * s,
+               4 * s + s + 32 + 4 * s + 4 * s + 4 * s,
+               4 * s + s + 32 + 4 * s + 32 + 1 + 4 * s]
         return n * sum(per) / 3.0
     raise KeyError(kernel)
 

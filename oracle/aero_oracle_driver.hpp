@@ -12,6 +12,7 @@
 #include "../include/aero_gb300.h"
 
 #include <string>
+#include <type_traits>
 
 namespace aero_oracle {
 
@@ -47,8 +48,95 @@ A schedule_all_speed_ramp(int on, int len, int iter) {
   return std::clamp(x, A(0), A(1));
 }
 
+// Float screen of the FP32-bulk mode: true when enforce_physical is provably the identity.
+inline bool positivity_safe(const Cons<double>& s, float gm1) {
+  const float r = static_cast<float>(s.rho);
+  if (!(r > 2.0e-8f)) return false;
+  const float inv = 1.0f / r;
+  const float u = static_cast<float>(s.ru) * inv, v = static_cast<float>(s.rv) * inv;
+  const float ke = 0.5f * r * (u * u + v * v);
+  const float e = static_cast<float>(s.rE) - ke;
+  return e > 1.0e-3f * static_cast<float>(s.rE) && gm1 * e > 2.0e-8f;
+}
+
+// Float-float arithmetic of the FP32-bulk mode's conserved state: hi is the float image,
+// lo the remainder. Knuth's error-free two-sum, so that s + e == a + b exactly.
+inline void two_sum(float a, float b, float* s, float* e) {
+  const float x = a + b;
+  const float bb = x - a;
+  *e = (a - (x - bb)) + (b - bb);
+  *s = x;
+}
+inline void ff_add(float hi, float lo, float d, float* nh, float* nl) {
+  float s, e;
+  two_sum(hi, d, &s, &e);
+  two_sum(s, lo + e, nh, nl);
+}
+inline void ff_split(double u, float* hi, float* lo) {
+  *hi = static_cast<float>(u);
+  *lo = static_cast<float>(u - static_cast<double>(*hi));
+}
+
+// RK3 stage of the FP32-bulk mode in delta form: delta' = b (delta - dt R) with b = 1, 1/4,
+// 2/3 (the RK3 weights sum to one). Intermediate stage states are float, hi + delta' with hi
+// the float image of U_n, clamped in float; the last stage adds delta' to the float-float
+// pair (hi, lo) of U_n and clamps in double only when the float screen cannot prove the clamp
+// is the identity. *us receives the stage state (the float state widened, or hi + lo).
+inline void rk_stage_delta(int stage, bool last, std::vector<float>* uhi, std::vector<float>* ulo,
+                           const std::vector<double>& rp, const std::vector<float>& dt, double gamma,
+                           std::vector<float>* delta, std::vector<double>* us) {
+  const size_t n = dt.size();
+  const float b = (stage == 1) ? 0.25f : 2.0f / 3.0f;
+  const float gm1 = static_cast<float>(gamma - 1.0);
+  const float gf = static_cast<float>(gamma);
+  for (size_t c = 0; c < n; ++c) {
+    float d[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    for (int k : {0, 1, 2, 4}) {
+      const float t = dt[c] * static_cast<float>(rp[5 * c + k]);
+      d[k] = (stage == 0) ? -t : b * ((*delta)[5 * c + k] - t);
+    }
+    float* hi = uhi->data() + 5 * c;
+    float* lo = ulo->data() + 5 * c;
+    double* o = us->data() + 5 * c;
+    if (!last) {
+      Cons<float> f{hi[0] + d[0], hi[1] + d[1], hi[2] + d[2], hi[3], hi[4] + d[4]};
+      const float fr = f.rho, fe = f.rE;
+      enforce_physical(&f, gf);
+      if (f.rho != fr) d[0] = f.rho - hi[0];
+      if (f.rE != fe) d[4] = f.rE - hi[4];
+      o[0] = f.rho;
+      o[1] = f.ru;
+      o[2] = f.rv;
+      o[3] = f.rw;
+      o[4] = f.rE;
+    } else {
+      float h[5], l[5];
+      for (int k = 0; k < 5; ++k) ff_add(hi[k], lo[k], d[k], &h[k], &l[k]);
+      const Cons<double> f{h[0], h[1], h[2], h[3], h[4]};
+      if (!positivity_safe(f, gm1)) {
+        Cons<double> s{double(h[0]) + l[0], double(h[1]) + l[1], double(h[2]) + l[2], double(h[3]) + l[3],
+                       double(h[4]) + l[4]};
+        enforce_physical(&s, gamma);
+        ff_split(s.rho, &h[0], &l[0]);
+        ff_split(s.ru, &h[1], &l[1]);
+        ff_split(s.rv, &h[2], &l[2]);
+        ff_split(s.rw, &h[3], &l[3]);
+        ff_split(s.rE, &h[4], &l[4]);
+      }
+      for (int k = 0; k < 5; ++k) {
+        hi[k] = h[k];
+        lo[k] = l[k];
+        o[k] = static_cast<double>(h[k]) + static_cast<double>(l[k]);
+      }
+    }
+    for (int k = 0; k < 5; ++k) (*delta)[5 * c + k] = d[k];
+  }
+}
+
 template <class R, class A>
 class Solver {
+  static constexpr bool kMixed = !std::is_same<R, A>::value;
+
  public:
   Solver(const aero_mesh_desc& md, const aero_case_desc& cd) : cfg_(cd) {
     load_mesh(md, &mr_);
@@ -64,12 +152,14 @@ class Solver {
       U_[5 * c + 3] = cons_inf_.rw;
       U_[5 * c + 4] = cons_inf_.rE;
     }
+    split_state();
     last_res_.assign(n * 5, R(0));
     last_sr_.assign(n, R(0));
   }
 
   void set_state(const double* u) {
     for (size_t i = 0; i < U_.size(); ++i) U_[i] = static_cast<A>(u[i]);
+    split_state();
   }
   void get_state(double* u) const {
     for (size_t i = 0; i < U_.size(); ++i) u[i] = static_cast<double>(U_[i]);
@@ -175,6 +265,7 @@ class Solver {
 
       const std::vector<A> un = U_;
       std::vector<A> us = U_, next;
+      std::vector<float> delta(kMixed ? U_.size() : 0, 0.0f);
       std::vector<Prim<R>> w(static_cast<size_t>(n));
       std::vector<R> res, sr;
       AssemblyDiag itd;
@@ -193,9 +284,14 @@ class Solver {
         std::vector<A> rp(res.begin(), res.end());
         precondition_residual<R, A>(w, nm, &rp);
         const std::vector<R> dtr = dt_over_volume(sr, R(cfl), cfg_.local_time_stepping != 0);
-        const std::vector<A> dta(dtr.begin(), dtr.end());
-        rk_stage<A>(stage, un, us, rp, dta, A(nm.gamma), &next);
-        us.swap(next);
+        if constexpr (kMixed) {
+          rk_stage_delta(stage, stage == cfg_.rk_stages - 1, &uhi_, &ulo_, rp, dtr, static_cast<double>(nm.gamma),
+                         &delta, &us);
+        } else {
+          const std::vector<A> dta(dtr.begin(), dtr.end());
+          rk_stage<A>(stage, un, us, rp, dta, A(nm.gamma), &next);
+          us.swap(next);
+        }
       }
       U_ = us;
       symmetry(iter);
@@ -225,6 +321,7 @@ class Solver {
       }
       std::vector<A> p(static_cast<size_t>(n));
       std::vector<Prim<A>> pe(static_cast<size_t>(n));
+      std::vector<Prim<R>> pr(kMixed ? static_cast<size_t>(n) : 0);
       A dp_dom = A(0), dp_wall = A(0);
       if (!bad) {
         for (int c = 0; c < n; ++c) {
@@ -237,7 +334,21 @@ class Solver {
           }
           pe[c] = pw;
           p[c] = pw.p;
-          const A adp = std::abs(pw.p - p_inf_);
+          A adp = std::abs(pw.p - p_inf_);
+          if constexpr (kMixed) {  // the FP32 mode forms these monitors from the bulk state, in R
+            const Prim<R> wr =
+                cons_to_prim(Cons<R>{R(cs.rho), R(cs.ru), R(cs.rv), R(cs.rw), R(cs.rE)}, nm.gamma);
+            if (!std::isfinite(wr.rho) || !std::isfinite(wr.u) || !std::isfinite(wr.v) ||
+                !std::isfinite(wr.p)) {
+              bad = true;
+              break;
+            }
+            pr[c] = wr;
+            adp = A(std::abs(wr.p - R(p_inf_)));
+            // forces and wall monitors from the bulk (float) primitive state as well
+            pe[c] = Prim<A>{A(wr.rho), A(wr.u), A(wr.v), A(wr.w), A(wr.p)};
+            p[c] = A(wr.p);
+          }
           dp_dom = std::max(dp_dom, adp);
           if (wall_adjacent_[c]) dp_wall = std::max(dp_wall, adp);
         }
@@ -298,11 +409,19 @@ class Solver {
         A ff[4] = {A(0), A(0), A(0), A(0)};
         for (int f = 0; f < ma_.num_faces; ++f) {
           if (ma_.neighbor[f] >= 0 || ma_.bc[f] != kFarfield) continue;
-          const Prim<A>& w = pe[ma_.owner[f]];
-          ff[0] = std::max(ff[0], std::abs(w.p - A(cfg_.p_inf)));
-          ff[1] = std::max(ff[1], std::abs(w.rho - ref_.rho_inf));
-          ff[2] = std::max(ff[2], std::abs(w.u - u_inf_));
-          ff[3] = std::max(ff[3], std::abs(w.v - v_inf_));
+          if constexpr (kMixed) {
+            const Prim<R>& w = pr[ma_.owner[f]];
+            ff[0] = std::max(ff[0], A(std::abs(w.p - R(cfg_.p_inf))));
+            ff[1] = std::max(ff[1], A(std::abs(w.rho - R(ref_.rho_inf))));
+            ff[2] = std::max(ff[2], A(std::abs(w.u - R(u_inf_))));
+            ff[3] = std::max(ff[3], A(std::abs(w.v - R(v_inf_))));
+          } else {
+            const Prim<A>& w = pe[ma_.owner[f]];
+            ff[0] = std::max(ff[0], std::abs(w.p - A(cfg_.p_inf)));
+            ff[1] = std::max(ff[1], std::abs(w.rho - ref_.rho_inf));
+            ff[2] = std::max(ff[2], std::abs(w.u - u_inf_));
+            ff[3] = std::max(ff[3], std::abs(w.v - v_inf_));
+          }
         }
         rec.max_wall_un = un_max;
         rec.max_wall_mass_flux = 0.0;
@@ -473,6 +592,22 @@ class Solver {
   // euler_solver.cpp:309-339 with the value formed in A
   Norms<A> norms(const std::vector<R>& res) const {
     double l1 = 0.0, l2s = 0.0, linf = 0.0;
+    if constexpr (kMixed) {  // per-cell terms in float, accumulated in double
+      for (int c = 0; c < mr_.num_cells; ++c) {
+        const R inv = R(1) / std::max(mr_.volume[c], K<R>::vol_floor);
+        const R v0 = res[5 * c] * inv, v1 = res[5 * c + 1] * inv, v2 = res[5 * c + 2] * inv,
+                v3 = res[5 * c + 4] * inv;
+        const R a0 = std::abs(v0), a1 = std::abs(v1), a2 = std::abs(v2), a3 = std::abs(v3);
+        l1 += static_cast<double>(((a0 + a1) + a2) + a3);
+        l2s += static_cast<double>(((v0 * v0 + v1 * v1) + v2 * v2) + v3 * v3);
+        linf = std::max(linf, static_cast<double>(std::max(std::max(std::max(a0, a1), a2), a3)));
+      }
+      Norms<A> out;
+      out.l1 = static_cast<A>(l1);
+      out.l2 = static_cast<A>(std::sqrt(l2s / std::max(1, mr_.num_cells * 5)));
+      out.linf = static_cast<A>(linf);
+      return out;
+    }
     for (int c = 0; c < ma_.num_cells; ++c) {
       const A inv = A(1) / std::max(ma_.volume[c], K<A>::vol_floor);
       for (int k = 0; k < 5; ++k) {
@@ -508,6 +643,7 @@ class Solver {
       U_[5 * c + 3] = o.rw;
       U_[5 * c + 4] = o.rE;
     }
+    split_state();
   }
 
   // Pressure-jump energy over interior faces (euler_solver.cpp:1027-1063), using the
@@ -607,6 +743,19 @@ class Solver {
   std::vector<unsigned char> wall_adjacent_;
 
   std::vector<A> U_;
+  std::vector<float> uhi_, ulo_;  // mixed mode: float-float pairs of U_ (U_ == hi + lo)
+
+  // mixed mode: split U_ into float-float pairs and set U_ to their sum
+  void split_state() {
+    if constexpr (kMixed) {
+      uhi_.resize(U_.size());
+      ulo_.resize(U_.size());
+      for (size_t i = 0; i < U_.size(); ++i) {
+        ff_split(static_cast<double>(U_[i]), &uhi_[i], &ulo_[i]);
+        U_[i] = static_cast<A>(static_cast<double>(uhi_[i]) + static_cast<double>(ulo_[i]));
+      }
+    }
+  }
   std::vector<R> last_res_, last_sr_;
   Monitor<A> mon_;
   int iter_ = 0;

@@ -59,8 +59,8 @@ struct alignas(16) Ctrl {
   int rec_base;    // iteration number stored at records[0] of the current chunk
   int second;      // second order in the current iteration
   int as_fix;      // all-speed fix effective in the current iteration
-  int fo_fallback; // per-iteration counters (summed over stages)
-  int diff_fallback;
+  int fo_fallback; // fallback counters of a single residual evaluation (the iteration loop
+  int diff_fallback;  // counts into a separate per-parity array, see k_residual)
   double cfl, stab_floor, as_fmin, as_ramp;  // current-iteration schedule values
   double cfl_scale, prev_l2, initial_l2;
   int has_prev, hist_count, hist_head, stage;  // stage: 0 single, 1 A, 2 B
@@ -528,7 +528,8 @@ __global__ void __launch_bounds__(256) k_residual(DevMesh<T> m, FaceParams<T> fp
                                                   const typename Vec<T>::v4* __restrict__ gx,
                                                   const typename Vec<T>::v4* __restrict__ gy,
                                                   typename Vec<T>::v4* __restrict__ R, T* __restrict__ SR,
-                                                  Partials part, Ctrl* __restrict__ ctrl, int global_dt) {
+                                                  Partials part, const Ctrl* __restrict__ ctrl,
+                                                  int* __restrict__ fb, int global_dt) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (ctrl->done) return;
   if (LM) {
@@ -645,8 +646,8 @@ __global__ void __launch_bounds__(256) k_residual(DevMesh<T> m, FaceParams<T> fp
     const int sfo = __reduce_add_sync(0xffffffffu, fo);
     const int sdf = __reduce_add_sync(0xffffffffu, df);
     if ((threadIdx.x & 31) == __ffs(any) - 1) {
-      if (sfo) atomicAdd(&ctrl->fo_fallback, sfo);
-      if (sdf) atomicAdd(&ctrl->diff_fallback, sdf);
+      if (sfo) atomicAdd(&fb[0], sfo);
+      if (sdf) atomicAdd(&fb[1], sdf);
     }
   }
   if (global_dt) {
@@ -924,7 +925,7 @@ struct Record {
 // Serial part of the controller (lane 0), on the shared copy of the controller state.
 __device__ inline void control_serial(const CtrlConfig& cc, const double (&a)[3], const double (&mon)[kMon],
                                       const double (&pj)[4], const double (&wv)[kWall], Ctrl* sp,
-                                      Record* __restrict__ recs, int rec_cap) {
+                                      Record* __restrict__ recs, int rec_cap, int* fb) {
   const double* fsum = wv;
   const double un_max = wv[8], cp_hi = wv[9], cp_lo_neg = wv[10], cp_bad = wv[11];
   const double lmax = a[2];
@@ -935,8 +936,10 @@ __device__ inline void control_serial(const CtrlConfig& cc, const double (&a)[3]
   Record r;
   r.iter = s.iter;
   r.flags = (s.second ? 8 : 0) | (s.as_fix ? 32 : 0) | (s.stage == 1 ? 64 : 0) | (s.stage == 2 ? 128 : 0);
-  r.fo = s.fo_fallback;
-  r.df = s.diff_fallback;
+  r.fo = fb[0];
+  r.df = fb[1];
+  fb[0] = 0;
+  fb[1] = 0;
   r.cfl = s.cfl;
   r.stab = s.stab_floor;
   r.as_fmin = s.as_fmin;
@@ -1108,8 +1111,6 @@ __device__ inline void control_serial(const CtrlConfig& cc, const double (&a)[3]
   if (conv || nonfinite) s.done = 1;
   // next iteration's schedule
   s.iter = s.iter + 1;
-  s.fo_fallback = 0;
-  s.diff_fallback = 0;
   apply_schedule(cc, &s);
 }
 
@@ -1134,7 +1135,8 @@ constexpr int kCtlThreads = 128;
 static_assert(sizeof(Ctrl) % 16 == 0, "Ctrl is copied in 16-byte words");
 static __global__ void __launch_bounds__(kCtlThreads) k_control(CtrlConfig cc, Partials part,
                                                                 Ctrl* __restrict__ ctrl,
-                                                                Record* __restrict__ recs, int rec_cap) {
+                                                                Record* __restrict__ recs, int rec_cap,
+                                                                int* __restrict__ fb) {
   constexpr int kWarps = kCtlThreads / 32;
   __shared__ Ctrl sc;
   __shared__ double s_sum[kWarps][2 + 4];   // l1, l2 sum, pressure-jump sums
@@ -1253,7 +1255,7 @@ static __global__ void __launch_bounds__(kCtlThreads) k_control(CtrlConfig cc, P
         for (int w = 1; w < kWarps; ++w) wv[k] = wall_comb(k, wv[k], s_wall[w][k]);
       }
     }
-    control_serial(cc, a, mon, p4, wv, &sc, recs, rec_cap);
+    control_serial(cc, a, mon, p4, wv, &sc, recs, rec_cap, fb);
   }
   __syncthreads();
   {

@@ -31,6 +31,9 @@ class EngineT final : public Engine {
     for (auto& g : graph_) {
       if (g) cudaGraphExecDestroy(g);
     }
+    if (ev_fork_) cudaEventDestroy(ev_fork_);
+    if (ev_join_) cudaEventDestroy(ev_join_);
+    if (side_) cudaStreamDestroy(side_);
     for (void* p : allocs_) cudaFree(p);
     if (flush_) cudaFree(flush_);
     if (pin_state_) cudaFreeHost(pin_state_);
@@ -134,6 +137,14 @@ class EngineT final : public Engine {
     gy_ = alloc<V4>(n_);
     R_ = alloc<V4>(n_);
     SR_ = alloc<T>(n_);
+    if (cfg_.rk_stages > 1) {  // the first stage's residual, kept apart from the last stage's
+      R0_ = alloc<V4>(n_);
+      SR0_ = alloc<T>(n_);
+    } else {
+      R0_ = R_;
+      SR0_ = SR_;
+    }
+    fb_ = alloc<int>(4);
     Un_ = alloc<d4>(n_);
     Us_ = alloc<V4>(n_);
     sref_.un = Un_;
@@ -257,6 +268,16 @@ class EngineT final : public Engine {
     c.u_inf = rs_.v_inf * rs_.cos_a;
     c.v_inf = rs_.v_inf * rs_.sin_a;
 
+    AERO_CK(cudaMemsetAsync(fb_, 0, 4 * sizeof(int), st_));
+    // the controller of iteration i runs beside the gradient and first residual of iteration
+    // i+1 (which need none of its outputs) when the first residual has a buffer of its own
+    // and the residual reads no controller-scheduled low-Mach weights
+    defer_control_ = cfg_.rk_stages > 1 && !rs_.lm;
+    if (defer_control_) {
+      AERO_CK(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
+      AERO_CK(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
+      AERO_CK(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
+    }
     // freestream initial state
     std::vector<d4> u0(static_cast<size_t>(n_), d4{rs_.cons_inf[0], rs_.cons_inf[1], rs_.cons_inf[2], rs_.cons_inf[3]});
     AERO_CK(cudaMemcpyAsync(Un_, u0.data(), sizeof(d4) * n_, cudaMemcpyHostToDevice, st_));
@@ -304,6 +325,7 @@ class EngineT final : public Engine {
     apply_schedule(cc_, &h);
     host_ctrl_ = h;
     AERO_CK(cudaMemcpyAsync(ctrl_, &host_ctrl_, sizeof(Ctrl), cudaMemcpyHostToDevice, st_));
+    AERO_CK(cudaMemsetAsync(fb_, 0, 4 * sizeof(int), st_));
     AERO_CK(cudaStreamSynchronize(st_));
   }
 
@@ -368,7 +390,7 @@ class EngineT final : public Engine {
     AERO_CK(cudaMemcpyAsync(ctrl_eval_, &ce, sizeof(Ctrl), cudaMemcpyHostToDevice, st_));
     k_refresh_prim<T><<<nblocks_, block_, 0, st_>>>(n_, Ueval_, W_, rs_.gamma);
     if (second) k_gradient<T><<<nblocks_, block_, 0, st_>>>(dm_, W_, gx_, gy_, ctrl_eval_);
-    launch_residual(second != 0, false, ctrl_eval_, 0);
+    launch_residual(second != 0, false, ctrl_eval_, &ctrl_eval_->fo_fallback, R_, SR_, 0);
     AERO_CK(cudaGetLastError());
     w_valid_ = false;
     download_residual(res, sr);
@@ -409,7 +431,7 @@ class EngineT final : public Engine {
       const int it0 = host_ctrl_.iter;
       host_rec_base_ = it0;
       AERO_CK(cudaMemcpyAsync(&ctrl_->rec_base, &host_rec_base_, sizeof(int), cudaMemcpyHostToDevice, st_));
-      for (int j = 0; j < chunk; ++j) launch_iteration_graph(second_at(it0 + j));
+      launch_iterations(it0, chunk, [](int) {}, [](int) {});
       AERO_CK(cudaMemcpyAsync(&host_ctrl_, ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, st_));
       AERO_CK(cudaStreamSynchronize(st_));
       const int k = host_ctrl_.iter - it0;
@@ -431,28 +453,41 @@ class EngineT final : public Engine {
   // iterations themselves are timed (one event pair per iteration, times summed).
   int time_iterations(int n, int use_graph, int flush_l2, double* ms) override {
     const int it0 = begin_untracked();
-    if (use_graph) {
-      ensure_graph(second_at(it0));
-      ensure_graph(second_at(it0 + n - 1));
+    if (use_graph) {  // instantiate every graph the loop uses before timing
+      for (int j = 0; j < std::min(n, 2); ++j) {
+        for (const int it : {it0 + j, it0 + n - 1 - j}) {
+          ensure_graph(second_at(it), it & 1, defer_control_, defer_control_ && it > it0);
+        }
+      }
     }
     if (flush_l2 && !ensure_flush_buffer()) return AERO_ERR_NOMEM;
     const int npairs = flush_l2 ? n : 1;
     std::vector<cudaEvent_t> ev(2 * static_cast<size_t>(npairs));
     for (auto& e : ev) AERO_CK(cudaEventCreate(&e));
-    if (!flush_l2) AERO_CK(cudaEventRecord(ev[0], st_));
-    for (int j = 0; j < n; ++j) {
+    auto before = [&](int j) {
       if (flush_l2) {
         AERO_CK(cudaMemsetAsync(flush_, j & 0xff, flush_bytes_, st_));
         AERO_CK(cudaEventRecord(ev[2 * j], st_));
+      } else if (j == 0) {
+        AERO_CK(cudaEventRecord(ev[0], st_));
       }
-      if (use_graph) {
-        launch_iteration_graph(second_at(it0 + j));
-      } else {
-        launch_iteration(second_at(it0 + j));
+    };
+    auto after = [&](int j) {
+      if (flush_l2) {
+        AERO_CK(cudaEventRecord(ev[2 * j + 1], st_));
+      } else if (j == n - 1) {
+        AERO_CK(cudaEventRecord(ev[1], st_));
       }
-      if (flush_l2) AERO_CK(cudaEventRecord(ev[2 * j + 1], st_));
+    };
+    if (use_graph) {
+      launch_iterations(it0, n, before, after);
+    } else {
+      for (int j = 0; j < n; ++j) {
+        before(j);
+        launch_iteration(second_at(it0 + j), (it0 + j) & 1, false, false, Direct{});
+        after(j);
+      }
     }
-    if (!flush_l2) AERO_CK(cudaEventRecord(ev[1], st_));
     AERO_CK(cudaStreamSynchronize(st_));
     double total = 0.0;
     for (int k = 0; k < npairs; ++k) {
@@ -479,7 +514,7 @@ class EngineT final : public Engine {
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
     for (int j = 0; j < n; ++j) {
       if (flush_l2) AERO_CK(cudaMemsetAsync(flush_, j & 0xff, flush_bytes_, st_));
-      launch_iteration(second_at(it0 + j), [&](int cls, auto&& launch) {
+      launch_iteration(second_at(it0 + j), (it0 + j) & 1, false, false, [&](int cls, auto&& launch) {
         cudaEvent_t a = nullptr, b = nullptr;
         AERO_CK(cudaEventCreate(&a));
         AERO_CK(cudaEventCreate(&b));
@@ -579,40 +614,48 @@ class EngineT final : public Engine {
     }
   }
 
+  struct ResOut {
+    Ctrl* ctrl;
+    int* fb;
+    V4* R;
+    T* SR;
+    int global_dt;
+  };
   template <int FLUX, bool SECOND, bool LM, bool NORMS>
-  void residual_t(Ctrl* ctrl, int global_dt) {
+  void residual_t(const ResOut& o) {
     k_residual<T, FLUX, SECOND, LM, NORMS>
-        <<<nblocks_, block_, 0, st_>>>(dm_, fp_, W_, gx_, gy_, R_, SR_, part_, ctrl, global_dt);
+        <<<nblocks_, block_, 0, st_>>>(dm_, fp_, W_, gx_, gy_, o.R, o.SR, part_, o.ctrl, o.fb, o.global_dt);
   }
   template <int FLUX, bool SECOND, bool LM>
-  void residual_n(bool norms, Ctrl* ctrl, int global_dt) {
+  void residual_n(bool norms, const ResOut& o) {
     if (norms) {
-      residual_t<FLUX, SECOND, LM, true>(ctrl, global_dt);
+      residual_t<FLUX, SECOND, LM, true>(o);
     } else {
-      residual_t<FLUX, SECOND, LM, false>(ctrl, global_dt);
+      residual_t<FLUX, SECOND, LM, false>(o);
     }
   }
   template <int FLUX, bool SECOND>
-  void residual_l(bool norms, Ctrl* ctrl, int global_dt) {
+  void residual_l(bool norms, const ResOut& o) {
     if (rs_.lm) {
-      residual_n<FLUX, SECOND, true>(norms, ctrl, global_dt);
+      residual_n<FLUX, SECOND, true>(norms, o);
     } else {
-      residual_n<FLUX, SECOND, false>(norms, ctrl, global_dt);
+      residual_n<FLUX, SECOND, false>(norms, o);
     }
   }
-  void launch_residual(bool second, bool norms, Ctrl* ctrl, int global_dt) {
+  void launch_residual(bool second, bool norms, Ctrl* ctrl, int* fb, V4* R, T* SR, int global_dt) {
+    const ResOut o{ctrl, fb, R, SR, global_dt};
     if (cfg_.flux == AERO_FLUX_HLLC) {
-      if (second) residual_l<1, true>(norms, ctrl, global_dt);
-      else residual_l<1, false>(norms, ctrl, global_dt);
+      if (second) residual_l<1, true>(norms, o);
+      else residual_l<1, false>(norms, o);
     } else {
-      if (second) residual_l<0, true>(norms, ctrl, global_dt);
-      else residual_l<0, false>(norms, ctrl, global_dt);
+      if (second) residual_l<0, true>(norms, o);
+      else residual_l<0, false>(norms, o);
     }
   }
 
   template <bool PRECOND, bool LAST>
-  void update_t(int stage, int global_dt) {
-    k_update<T, PRECOND, LAST><<<nblocks_, block_, 0, st_>>>(n_, stage, pc_, R_, SR_, W_, sref_, Us_, ms_, part_,
+  void update_t(int stage, int global_dt, const V4* R, const T* SR) {
+    k_update<T, PRECOND, LAST><<<nblocks_, block_, 0, st_>>>(n_, stage, pc_, R, SR, W_, sref_, Us_, ms_, part_,
                                                              ctrl_, global_dt);
   }
 
@@ -623,27 +666,42 @@ class EngineT final : public Engine {
     }
   };
 
-  void launch_iteration(bool second) { launch_iteration(second, Direct{}); }
-
-  // The launches of one iteration; `wrap(kernel_class, launch)` issues each one.
+  // The launches of one iteration; `wrap(kernel_class, launch)` issues each one. `parity`
+  // (iteration & 1) selects the fallback counters. With `defer`, the controller of this
+  // iteration is left to the next one (or to launch_control); with `pending`, the previous
+  // iteration's controller (parity ^ 1) is forked onto the side stream beside this
+  // iteration's gradient and first residual and joined before the first update, the first
+  // kernel that reads its outputs.
   template <class Wrap>
-  void launch_iteration(bool second, Wrap&& wrap) {
+  void launch_iteration(bool second, int parity, bool defer, bool pending, Wrap&& wrap) {
     const int global_dt = cfg_.local_time_stepping ? 0 : 1;
     const int ns = cfg_.rk_stages;
+    int* fb = fb_ + 2 * parity;
     for (int stage = 0; stage < ns; ++stage) {
       const bool last = stage == ns - 1;
+      V4* R = stage == 0 ? R0_ : R_;
+      T* SR = stage == 0 ? SR0_ : SR_;
+      if (stage == 0 && pending) {
+        AERO_CK(cudaEventRecord(ev_fork_, st_));
+        AERO_CK(cudaStreamWaitEvent(side_, ev_fork_, 0));
+        wrap(5, [&] {
+          k_control<<<1, kCtlThreads, 0, side_>>>(cc_, part_, ctrl_, recs_, rec_cap_, fb_ + 2 * (parity ^ 1));
+        });
+        AERO_CK(cudaEventRecord(ev_join_, side_));
+      }
       if (second) wrap(0, [&] { k_gradient<T><<<nblocks_, block_, 0, st_>>>(dm_, W_, gx_, gy_, ctrl_); });
-      wrap(1, [&] { launch_residual(second, last, ctrl_, global_dt); });
+      wrap(1, [&] { launch_residual(second, last, ctrl_, fb, R, SR, global_dt); });
+      if (stage == 0 && pending) AERO_CK(cudaStreamWaitEvent(st_, ev_join_, 0));
       if (global_dt) {
         wrap(3, [&] { k_srmax<<<1, 1024, 0, st_>>>(part_.srmax, nblocks_ * (block_ / 32), ctrl_); });
       }
       wrap(2, [&] {
         if (cfg_.precond_on) {
-          if (last) update_t<true, true>(stage, global_dt);
-          else update_t<true, false>(stage, global_dt);
+          if (last) update_t<true, true>(stage, global_dt, R, SR);
+          else update_t<true, false>(stage, global_dt, R, SR);
         } else {
-          if (last) update_t<false, true>(stage, global_dt);
-          else update_t<false, false>(stage, global_dt);
+          if (last) update_t<false, true>(stage, global_dt, R, SR);
+          else update_t<false, false>(stage, global_dt, R, SR);
         }
       });
     }
@@ -656,8 +714,27 @@ class EngineT final : public Engine {
     if (pjump_on_) {
       wrap(4, [&] { k_pjump<T><<<nblocks_, block_, 0, st_>>>(dm_, sref_, flags_, rs_.gamma, part_, ctrl_); });
     }
-    wrap(5, [&] { k_control<<<1, kCtlThreads, 0, st_>>>(cc_, part_, ctrl_, recs_, rec_cap_); });
+    if (!defer) launch_control(parity, wrap);
     AERO_CK(cudaGetLastError());
+  }
+  template <class Wrap>
+  void launch_control(int parity, Wrap&& wrap) {
+    wrap(5, [&] { k_control<<<1, kCtlThreads, 0, st_>>>(cc_, part_, ctrl_, recs_, rec_cap_, fb_ + 2 * parity); });
+  }
+
+  // Iterations it0 .. it0+n-1 back to back, through the per-iteration CUDA graphs; with the
+  // deferred controller, each iteration's controller overlaps the next iteration's start and
+  // the last one runs after the loop. `between(j)` runs on the stream before iteration j and
+  // `after(j)` after it (timing marks, L2 flushes).
+  template <class Before, class After>
+  void launch_iterations(int it0, int n, Before&& between, After&& after) {
+    for (int j = 0; j < n; ++j) {
+      const int it = it0 + j;
+      between(j);
+      launch_iteration_graph(second_at(it), it & 1, defer_control_, defer_control_ && j > 0);
+      if (defer_control_ && j == n - 1) launch_control(it & 1, Direct{});
+      after(j);
+    }
   }
 
   // Start/end of a run whose records are not kept (timing, profiling).
@@ -700,12 +777,15 @@ class EngineT final : public Engine {
     return true;
   }
 
-  void ensure_graph(bool second) {
-    const int i = second ? 1 : 0;
+  static int graph_index(bool second, int parity, bool defer, bool pending) {
+    return (second ? 1 : 0) | (parity << 1) | ((defer ? 1 : 0) << 2) | ((pending ? 1 : 0) << 3);
+  }
+  void ensure_graph(bool second, int parity, bool defer, bool pending) {
+    const int i = graph_index(second, parity, defer, pending);
     if (graph_[i]) return;
     cudaGraph_t g = nullptr;
     AERO_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
-    launch_iteration(second);
+    launch_iteration(second, parity, defer, pending, Direct{});
     AERO_CK(cudaStreamEndCapture(st_, &g));
     if (g) {
       AERO_CK(cudaGraphInstantiate(&graph_[i], g, 0));
@@ -713,13 +793,13 @@ class EngineT final : public Engine {
     }
   }
 
-  void launch_iteration_graph(bool second) {
-    ensure_graph(second);
-    const int i = second ? 1 : 0;
+  void launch_iteration_graph(bool second, int parity, bool defer, bool pending) {
+    ensure_graph(second, parity, defer, pending);
+    const int i = graph_index(second, parity, defer, pending);
     if (graph_[i]) {
       AERO_CK(cudaGraphLaunch(graph_[i], st_));
     } else {
-      launch_iteration(second);
+      launch_iteration(second, parity, defer, pending, Direct{});
     }
   }
 
@@ -757,7 +837,13 @@ class EngineT final : public Engine {
   FaceParams<T> fp_{};
   PrecondD pc_{};
   CtrlConfig cc_{};
-  cudaGraphExec_t graph_[2] = {nullptr, nullptr};
+  cudaGraphExec_t graph_[16] = {};
+  bool defer_control_ = false;
+  cudaStream_t side_ = nullptr;
+  cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
+  V4* R0_ = nullptr;
+  T* SR0_ = nullptr;
+  int* fb_ = nullptr;  // [2 parities][first-order, diffusive] fallback counters
   void* flush_ = nullptr;
   size_t flush_bytes_ = 0;
   d4* pin_state_ = nullptr;

@@ -95,7 +95,8 @@ template <class T, int FLUX, bool SECOND, bool LM>
 void launch_residual_na(int grid, int block, cudaStream_t st, const DevMesh<T>& dm, const FaceParams<T>& fp,
                         const typename Vec<T>::v4* W, const typename Vec<T>::v4* gx,
                         const typename Vec<T>::v4* gy, typename Vec<T>::v4* R, T* SR, Ctrl* ctrl) {
-  k_residual<T, FLUX, SECOND, LM, false><<<grid, block, 0, st>>>(dm, fp, W, gx, gy, R, SR, Partials{}, ctrl, 0);
+  k_residual<T, FLUX, SECOND, LM, false>
+      <<<grid, block, 0, st>>>(dm, fp, W, gx, gy, R, SR, Partials{}, ctrl, &ctrl->fo_fallback, 0);
 }
 
 template <class T>

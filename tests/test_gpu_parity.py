@@ -278,6 +278,27 @@ def test_nonfinite_trap_returns_status_and_context_recovers():
 
 
 @pytest.mark.parametrize("precision", [capi.PRECISION_FP64, capi.PRECISION_FP32])
+def test_chunked_runs_match_one_run(precision):
+    """The controller of iteration i overlaps iteration i+1 inside one run call and runs
+    last otherwise; records and state must not depend on how the iterations are split."""
+    mesh = aero_gb300.ogrid_synthetic(64, 16, seed=4)
+    case = capi.make_case(mach=0.7, flux=1, limiter=1, startup_first_order_iters=3, precision=precision)
+    with aero_gb300.Solver(mesh, case) as s:
+        _, rec = s.run(12)
+        state = s.get_state()
+    parts = []
+    with aero_gb300.Solver(mesh, case) as s:
+        for k in (1, 4, 2, 5):
+            _, r = s.run(k)
+            parts.append(r)
+        state2 = s.get_state()
+    rec2 = np.concatenate(parts)
+    np.testing.assert_array_equal(state, state2)
+    for key in ("residual_l2", "cl", "cfl", "flags", "first_order_fallback_faces"):
+        np.testing.assert_array_equal(rec[key], rec2[key], err_msg=key)
+
+
+@pytest.mark.parametrize("precision", [capi.PRECISION_FP64, capi.PRECISION_FP32])
 def test_runs_are_deterministic(precision):
     mesh = aero_gb300.ogrid_synthetic(64, 16, seed=8)
     case = capi.make_case(mach=0.7, flux=1, limiter=1, startup_first_order_iters=3, precision=precision)

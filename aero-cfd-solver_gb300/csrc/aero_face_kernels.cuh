@@ -1,0 +1,264 @@
+// aero_face_kernels.cuh -- the residual as two passes over a face table: the face pass
+// reconstructs, evaluates the flux of every face exactly once (residual_assembly.cpp:73-182)
+// and stores F*A and the wave-speed term; the cell pass gathers them. Each cell sums its
+// faces in ascending original face order, owner side +, neighbour side -, so the residual is
+// the same whatever the cell numbering or block size, and the flux arithmetic is half that
+// of evaluating every interior face from both of its cells.
+#pragma once
+
+#include "../../include/aero_gb300.h"
+#include "aero_kernels.cuh"
+
+namespace aero {
+
+// Faces sorted by the new index of their owner. cells = (owner, neighbour) new indices, the
+// neighbour -1 for a far-field face and -2 for a slip wall. Geometry in the bulk type T:
+// unit normal out of the owner, length, and the offsets of the face centre from the owner's
+// and the neighbour's centres (MUSCL).
+template <class T>
+struct DevFaces {
+  int nf;
+  const int2* cells;
+  const typename Vec<T>::v2* nrm;
+  const T* area;
+  const typename Vec<T>::v2* doff;
+  const typename Vec<T>::v2* noff;
+};
+
+// Per-cell gather table (ELL, slot (k, c) at k*n + c): (face << 1) | (cell is the
+// neighbour), kPad after the last face of the cell.
+template <class T>
+struct DevGather {
+  int n, d;
+  const int* slot;
+  const T* inv_vol;
+};
+
+// Face pass. FLUX 0 Rusanov / 1 HLLC; SECOND: MUSCL with the cell gradients; LM: any
+// low-Mach feature on. fb[0] / fb[1] count first-order and diffusive fallbacks.
+template <class T, int FLUX, bool SECOND, bool LM>
+__global__ void __launch_bounds__(256) k_face_flux(DevFaces<T> f, FaceParams<T> fp,
+                                                   const typename Vec<T>::v4* __restrict__ W,
+                                                   const typename Vec<T>::v4* __restrict__ gx,
+                                                   const typename Vec<T>::v4* __restrict__ gy,
+                                                   typename Vec<T>::v4* __restrict__ F, T* __restrict__ FS,
+                                                   const Ctrl* __restrict__ ctrl, int* __restrict__ fb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ctrl->done) return;
+  if (LM) {
+    fp.as_fix = ctrl->as_fix;
+    if constexpr (sizeof(T) == 4) {
+      fp.stab_floor = ctrl->stab_f;
+      fp.as_fmin = ctrl->as_fmin_f;
+      fp.as_ramp = ctrl->as_ramp_f;
+    } else {
+      fp.stab_floor = ctrl->stab_floor;
+      fp.as_fmin = ctrl->as_fmin;
+      fp.as_ramp = ctrl->as_ramp;
+    }
+  }
+  int fo = 0, df = 0;
+  if (i < f.nf) {
+    const int2 oc = f.cells[i];
+    const int o = oc.x, b = oc.y;
+    const auto nd = f.nrm[i];
+    const T nx = nd.x, ny = nd.y;
+    const T area = f.area[i];
+    const auto wo4 = W[o];
+    const Prim<T> wo{wo4.x, wo4.y, wo4.z, wo4.w};
+    Flux<T> fl;
+    T mws;
+    bool fbk = false;
+    if (b >= 0) {
+      const auto wn4 = W[b];
+      const Prim<T> wn{wn4.x, wn4.y, wn4.z, wn4.w};
+      Prim<T> L = wo, Rt = wn;
+      if (SECOND) {
+        const auto gOx = gx[o], gOy = gy[o], gNx = gx[b], gNy = gy[b];
+        const auto dO = f.doff[i];
+        const auto dN = f.noff[i];
+        muscl_var(fp.limiter, wo.r, wn.r, gOx.x, gOy.x, gNx.x, gNy.x, dO.x, dO.y, dN.x, dN.y, &L.r, &Rt.r);
+        muscl_var(fp.limiter, wo.u, wn.u, gOx.y, gOy.y, gNx.y, gNy.y, dO.x, dO.y, dN.x, dN.y, &L.u, &Rt.u);
+        muscl_var(fp.limiter, wo.v, wn.v, gOx.z, gOy.z, gNx.z, gNy.z, dO.x, dO.y, dN.x, dN.y, &L.v, &Rt.v);
+        muscl_var(fp.limiter, wo.p, wn.p, gOx.w, gOy.w, gNx.w, gNy.w, dO.x, dO.y, dN.x, dN.y, &L.p, &Rt.p);
+        L.r = smax(L.r, Kn<T>::rho_floor);
+        Rt.r = smax(Rt.r, Kn<T>::rho_floor);
+        L.p = smax(L.p, Kn<T>::p_floor);
+        Rt.p = smax(Rt.p, Kn<T>::p_floor);
+        if (!valid_prim(L) || !valid_prim(Rt)) {
+          L = wo;
+          Rt = wn;
+          ++fo;
+        }
+      }
+      const Cons<T> cl = prim_to_cons(L, fp.gamma), cr = prim_to_cons(Rt, fp.gamma);
+      const T as = face_acoustic_scale<T, LM>(cl, cr, fp);
+      fl = face_flux<T, FLUX, LM>(cl, cr, nx, ny, fp, as, &mws, &fbk);
+    } else {
+      const Cons<T> in = prim_to_cons(wo, fp.gamma);
+      if (b == -2) {  // slip wall: pressure-only flux (boundary_conditions.cpp:97-110)
+        const T as = face_acoustic_scale<T, LM>(in, in, fp);
+        const Prim<T> w = cons_to_prim(in, fp.gamma);
+        const T un = w.u * nx + w.v * ny;
+        const T a = sound_speed(w, fp.gamma);
+        fl = {T(0), w.p * nx, w.p * ny, T(0)};
+        mws = precond_speeds(un, a, as).sr;
+      } else {
+        const T as = face_acoustic_scale<T, LM>(in, fp.farfield, fp);
+        const Cons<T> bs = fp.precond_farfield_bc ? precond_farfield_state(in, nx, ny, fp, as) : fp.farfield;
+        fl = face_flux<T, FLUX, LM>(in, bs, nx, ny, fp, as, &mws, &fbk);
+      }
+    }
+    if (fbk) ++df;
+    typename Vec<T>::v4 out;
+    out.x = fl.m * area;
+    out.y = fl.fx * area;
+    out.z = fl.fy * area;
+    out.w = fl.e * area;
+    F[i] = out;
+    FS[i] = mws * area;
+  }
+  // fallback counters: one atomic per warp when any lane counted something
+  const unsigned any = __ballot_sync(0xffffffffu, (fo | df) != 0);
+  if (any) {
+    const int sfo = __reduce_add_sync(0xffffffffu, fo);
+    const int sdf = __reduce_add_sync(0xffffffffu, df);
+    if ((threadIdx.x & 31) == __ffs(any) - 1) {
+      if (sfo) atomicAdd(&fb[0], sfo);
+      if (sdf) atomicAdd(&fb[1], sdf);
+    }
+  }
+}
+
+// Cell pass: R = sum of +-F*A over the cell's faces, SR = sum of the wave-speed terms.
+// NORMS (last RK stage): also the residual-norm block partials (euler_solver.cpp:309-339).
+// global_dt: per-warp maxima of max(SR, floor) for the global time step.
+template <class T, bool NORMS>
+__global__ void __launch_bounds__(256) k_gather(DevGather<T> g, const typename Vec<T>::v4* __restrict__ F,
+                                                const T* __restrict__ FS, typename Vec<T>::v4* __restrict__ R,
+                                                T* __restrict__ SR, Partials part, const Ctrl* __restrict__ ctrl,
+                                                int global_dt) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ctrl->done) return;
+  T nl1 = T(0), nl2 = T(0), nlinf = T(0);
+  double srm = 0.0;
+  if (c < g.n) {
+    T r0 = 0, r1 = 0, r2 = 0, r3 = 0, sr = 0;
+    for (int k = 0; k < g.d; ++k) {
+      const int s = g.slot[k * g.n + c];
+      if (s == kPad) break;
+      const int fi = s >> 1;
+      const auto fv = F[fi];
+      if (s & 1) {
+        r0 -= fv.x; r1 -= fv.y; r2 -= fv.z; r3 -= fv.w;
+      } else {
+        r0 += fv.x; r1 += fv.y; r2 += fv.z; r3 += fv.w;
+      }
+      sr += FS[fi];
+    }
+    typename Vec<T>::v4 out;
+    out.x = r0; out.y = r1; out.z = r2; out.w = r3;
+    R[c] = out;
+    SR[c] = sr;
+    if (global_dt) srm = double(smax(sr, Kn<T>::wave_floor));
+    if (NORMS) {
+      const T inv = g.inv_vol[c];
+      const T v0 = r0 * inv, v1 = r1 * inv, v2 = r2 * inv, v3 = r3 * inv;
+      const T a0 = fabs(v0), a1 = fabs(v1), a2 = fabs(v2), a3 = fabs(v3);
+      nl1 = ((a0 + a1) + a2) + a3;
+      nl2 = ((v0 * v0 + v1 * v1) + v2 * v2) + v3 * v3;
+      nlinf = smax(smax(smax(a0, a1), a2), a3);
+    }
+  }
+  if (global_dt) {
+    srm = warp_max(srm);
+    if ((threadIdx.x & 31) == 0) part.srmax[blockIdx.x * ((blockDim.x + 31) >> 5) + (threadIdx.x >> 5)] = srm;
+  }
+  if (NORMS) {
+    // block partials in T; the control kernel sums the blocks in double (FP32: float-float)
+    __shared__ T shn[3][32];
+    nl1 = warp_sum_t(nl1);
+    nl2 = warp_sum_t(nl2);
+    nlinf = warp_max_t(nlinf);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) {
+      shn[0][wid] = nl1;
+      shn[1][wid] = nl2;
+      shn[2][wid] = nlinf;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T a = T(0), b = T(0), mx = T(0);
+      for (int i = 0; i < nw; ++i) {
+        a += shn[0][i];
+        b += shn[1][i];
+        mx = smax(mx, shn[2][i]);
+      }
+      T* out;
+      if constexpr (sizeof(T) == 4) {
+        out = part.norms_f;
+      } else {
+        out = part.norms;
+      }
+      out[blockIdx.x] = a;
+      out[part.nb + blockIdx.x] = b;
+      out[2 * part.nb + blockIdx.x] = mx;
+    }
+  }
+}
+
+// Launch geometry and buffers of one residual evaluation.
+template <class T>
+struct ResidualLaunch {
+  int block;
+  cudaStream_t st;
+  DevFaces<T> faces;
+  DevGather<T> gather;
+  FaceParams<T> fp;
+  const typename Vec<T>::v4 *W, *gx, *gy;
+  typename Vec<T>::v4* F;  // per face
+  T* FS;                   // per face
+  typename Vec<T>::v4* R;  // per cell
+  T* SR;                   // per cell
+  Partials part;
+  const Ctrl* ctrl;
+  int* fb;
+  int global_dt;
+};
+
+template <class T, int FLUX, bool SECOND, bool LM>
+void launch_face_flux_t(const ResidualLaunch<T>& a) {
+  const int grid = (a.faces.nf + a.block - 1) / a.block;
+  k_face_flux<T, FLUX, SECOND, LM>
+      <<<grid, a.block, 0, a.st>>>(a.faces, a.fp, a.W, a.gx, a.gy, a.F, a.FS, a.ctrl, a.fb);
+}
+
+// Face pass then cell pass, dispatched on the flux, order and low-Mach switches.
+template <class T>
+void launch_residual_passes(const ResidualLaunch<T>& a, int flux, bool second, bool lm, bool norms) {
+  if (flux == AERO_FLUX_HLLC) {
+    if (second) {
+      if (lm) launch_face_flux_t<T, 1, true, true>(a);
+      else launch_face_flux_t<T, 1, true, false>(a);
+    } else {
+      if (lm) launch_face_flux_t<T, 1, false, true>(a);
+      else launch_face_flux_t<T, 1, false, false>(a);
+    }
+  } else {
+    if (second) {
+      if (lm) launch_face_flux_t<T, 0, true, true>(a);
+      else launch_face_flux_t<T, 0, true, false>(a);
+    } else {
+      if (lm) launch_face_flux_t<T, 0, false, true>(a);
+      else launch_face_flux_t<T, 0, false, false>(a);
+    }
+  }
+  const int grid = (a.gather.n + a.block - 1) / a.block;
+  if (norms) {
+    k_gather<T, true><<<grid, a.block, 0, a.st>>>(a.gather, a.F, a.FS, a.R, a.SR, a.part, a.ctrl, a.global_dt);
+  } else {
+    k_gather<T, false><<<grid, a.block, 0, a.st>>>(a.gather, a.F, a.FS, a.R, a.SR, a.part, a.ctrl, a.global_dt);
+  }
+}
+
+}  // namespace aero

@@ -160,18 +160,16 @@ __host__ __device__ inline void set_eval_schedule(Ctrl* s, double stab, int as_f
   s->as_ramp_f = float(as_ramp);
 }
 
-// Geometry as the bulk arithmetic consumes it. The face normals, areas and volumes are held
-// in double (and used in double by the forces); the T copies here are their exact
-// conversions, and inv_vol = 1/max(V, 1e-12) formed in T on the host, so FP32 kernels do
-// neither double loads nor double conversions or divides.
+// Per-cell slot table of the gradient and pressure-jump passes, in the bulk type T: the
+// normals and areas are exact conversions of the mesh's double geometry and inv_vol =
+// 1/max(V, 1e-12) is formed in T on the host, so FP32 kernels do neither double loads nor
+// double conversions or divides.
 template <class T>
 struct DevMesh {
   int n, d;
   const int* link;
   const typename Vec<T>::v2* nrm;
   const T* area;
-  const typename Vec<T>::v2* doff;
-  const typename Vec<T>::v2* noff;
   const T* inv_vol;
 };
 
@@ -514,177 +512,6 @@ __device__ __forceinline__ void muscl_var(int lim, T qo, T qn, T gox, T goy, T g
   d_n += gny * dny;
   *ql = qo + limit(lim, d_o, dc);
   *qr = qn + limit(lim, d_n, -dc);
-}
-
-// ---------------------------------------------------------------------------------------
-// Residual: reconstruction + face flux + gather (residual_assembly.cpp:73-182).
-// FLUX 0 Rusanov / 1 HLLC; SECOND: MUSCL with gradients; LM: any low-Mach feature on
-// (preconditioning, low-Mach dissipation fix, all-speed flux fix); NORMS: last RK stage,
-// also writes the residual-norm partials (euler_solver.cpp:309-339).
-// ---------------------------------------------------------------------------------------
-template <class T, int FLUX, bool SECOND, bool LM, bool NORMS>
-__global__ void __launch_bounds__(256) k_residual(DevMesh<T> m, FaceParams<T> fp,
-                                                  const typename Vec<T>::v4* __restrict__ W,
-                                                  const typename Vec<T>::v4* __restrict__ gx,
-                                                  const typename Vec<T>::v4* __restrict__ gy,
-                                                  typename Vec<T>::v4* __restrict__ R, T* __restrict__ SR,
-                                                  Partials part, const Ctrl* __restrict__ ctrl,
-                                                  int* __restrict__ fb, int global_dt) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ctrl->done) return;
-  if (LM) {
-    fp.as_fix = ctrl->as_fix;
-    if constexpr (sizeof(T) == 4) {
-      fp.stab_floor = ctrl->stab_f;
-      fp.as_fmin = ctrl->as_fmin_f;
-      fp.as_ramp = ctrl->as_ramp_f;
-    } else {
-      fp.stab_floor = ctrl->stab_floor;
-      fp.as_fmin = ctrl->as_fmin;
-      fp.as_ramp = ctrl->as_ramp;
-    }
-  }
-  T nl1 = T(0), nl2 = T(0), nlinf = T(0);  // per-cell norm terms (euler_solver.cpp:309-339)
-  double srm = 0.0;
-  int fo = 0, df = 0;
-  if (c < m.n) {
-    const auto wc4 = W[c];
-    const Prim<T> wc{wc4.x, wc4.y, wc4.z, wc4.w};
-    typename Vec<T>::v4 gcx{}, gcy{};
-    if (SECOND) {
-      gcx = gx[c];
-      gcy = gy[c];
-    }
-    T r0 = 0, r1 = 0, r2 = 0, r3 = 0, sr = 0;
-    for (int k = 0; k < m.d; ++k) {
-      const int s = k * m.n + c;
-      const int link = m.link[s];
-      if (link == kPad) break;
-      const auto nd = m.nrm[s];
-      const T nx = nd.x, ny = nd.y;
-      const T area = m.area[s];
-      Flux<T> f;
-      T mws;
-      bool fb = false;
-      bool minus = false;
-      if (link >= 0) {
-        const int o = link >> 1;
-        minus = (link & 1) != 0;
-        const auto wo4 = W[o];
-        const Prim<T> wo{wo4.x, wo4.y, wo4.z, wo4.w};
-        const Prim<T>& pown = minus ? wo : wc;
-        const Prim<T>& pnb = minus ? wc : wo;
-        Prim<T> L = pown, Rt = pnb;
-        if (SECOND) {
-          const auto gox4 = gx[o];
-          const auto goy4 = gy[o];
-          const auto& gOx = minus ? gox4 : gcx;
-          const auto& gOy = minus ? goy4 : gcy;
-          const auto& gNx = minus ? gcx : gox4;
-          const auto& gNy = minus ? gcy : goy4;
-          const auto dO = m.doff[s];
-          const auto dN = m.noff[s];
-          muscl_var(fp.limiter, pown.r, pnb.r, gOx.x, gOy.x, gNx.x, gNy.x, dO.x, dO.y, dN.x, dN.y, &L.r, &Rt.r);
-          muscl_var(fp.limiter, pown.u, pnb.u, gOx.y, gOy.y, gNx.y, gNy.y, dO.x, dO.y, dN.x, dN.y, &L.u, &Rt.u);
-          muscl_var(fp.limiter, pown.v, pnb.v, gOx.z, gOy.z, gNx.z, gNy.z, dO.x, dO.y, dN.x, dN.y, &L.v, &Rt.v);
-          muscl_var(fp.limiter, pown.p, pnb.p, gOx.w, gOy.w, gNx.w, gNy.w, dO.x, dO.y, dN.x, dN.y, &L.p, &Rt.p);
-          L.r = smax(L.r, Kn<T>::rho_floor);
-          Rt.r = smax(Rt.r, Kn<T>::rho_floor);
-          L.p = smax(L.p, Kn<T>::p_floor);
-          Rt.p = smax(Rt.p, Kn<T>::p_floor);
-          if (!valid_prim(L) || !valid_prim(Rt)) {
-            L = pown;
-            Rt = pnb;
-            if (!minus) ++fo;
-          }
-        }
-        const Cons<T> cl = prim_to_cons(L, fp.gamma), cr = prim_to_cons(Rt, fp.gamma);
-        const T as = face_acoustic_scale<T, LM>(cl, cr, fp);
-        f = face_flux<T, FLUX, LM>(cl, cr, nx, ny, fp, as, &mws, &fb);
-        if (minus) fb = false;  // count each face once, on its owner side
-      } else {
-        const Cons<T> in = prim_to_cons(wc, fp.gamma);
-        if (link == -2) {
-          const T as = face_acoustic_scale<T, LM>(in, in, fp);
-          const Prim<T> w = cons_to_prim(in, fp.gamma);
-          const T un = w.u * nx + w.v * ny;
-          const T a = sound_speed(w, fp.gamma);
-          f = {T(0), w.p * nx, w.p * ny, T(0)};
-          mws = precond_speeds(un, a, as).sr;
-        } else {
-          const T as = face_acoustic_scale<T, LM>(in, fp.farfield, fp);
-          const Cons<T> bs = fp.precond_farfield_bc ? precond_farfield_state(in, nx, ny, fp, as) : fp.farfield;
-          f = face_flux<T, FLUX, LM>(in, bs, nx, ny, fp, as, &mws, &fb);
-        }
-      }
-      if (fb) ++df;
-      sr += mws * area;
-      const T f0 = f.m * area, f1 = f.fx * area, f2 = f.fy * area, f3 = f.e * area;
-      if (minus) {
-        r0 -= f0; r1 -= f1; r2 -= f2; r3 -= f3;
-      } else {
-        r0 += f0; r1 += f1; r2 += f2; r3 += f3;
-      }
-    }
-    typename Vec<T>::v4 out;
-    out.x = r0; out.y = r1; out.z = r2; out.w = r3;
-    R[c] = out;
-    SR[c] = sr;
-    if (global_dt) srm = double(smax(sr, Kn<T>::wave_floor));
-    if (NORMS) {
-      const T inv = m.inv_vol[c];
-      const T v0 = r0 * inv, v1 = r1 * inv, v2 = r2 * inv, v3 = r3 * inv;
-      const T a0 = fabs(v0), a1 = fabs(v1), a2 = fabs(v2), a3 = fabs(v3);
-      nl1 = ((a0 + a1) + a2) + a3;
-      nl2 = ((v0 * v0 + v1 * v1) + v2 * v2) + v3 * v3;
-      nlinf = smax(smax(smax(a0, a1), a2), a3);
-    }
-  }
-  // fallback counters: one atomic per warp when any lane counted something
-  const unsigned any = __ballot_sync(0xffffffffu, (fo | df) != 0);
-  if (any) {
-    const int sfo = __reduce_add_sync(0xffffffffu, fo);
-    const int sdf = __reduce_add_sync(0xffffffffu, df);
-    if ((threadIdx.x & 31) == __ffs(any) - 1) {
-      if (sfo) atomicAdd(&fb[0], sfo);
-      if (sdf) atomicAdd(&fb[1], sdf);
-    }
-  }
-  if (global_dt) {
-    srm = warp_max(srm);
-    if ((threadIdx.x & 31) == 0) part.srmax[blockIdx.x * ((blockDim.x + 31) >> 5) + (threadIdx.x >> 5)] = srm;
-  }
-  if (NORMS) {
-    // block partials in T; the control kernel sums the blocks in double (FP32: float-float)
-    __shared__ T shn[3][32];
-    nl1 = warp_sum_t(nl1);
-    nl2 = warp_sum_t(nl2);
-    nlinf = warp_max_t(nlinf);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-    if (lane == 0) {
-      shn[0][wid] = nl1;
-      shn[1][wid] = nl2;
-      shn[2][wid] = nlinf;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      T a = T(0), b = T(0), mx = T(0);
-      for (int i = 0; i < nw; ++i) {
-        a += shn[0][i];
-        b += shn[1][i];
-        mx = smax(mx, shn[2][i]);
-      }
-      T* out;
-      if constexpr (sizeof(T) == 4) {
-        out = part.norms_f;
-      } else {
-        out = part.norms;
-      }
-      out[blockIdx.x] = a;
-      out[part.nb + blockIdx.x] = b;
-      out[2 * part.nb + blockIdx.x] = mx;
-    }
-  }
 }
 
 // Global time step (time_integrator.cpp:45-56): maximum over per-warp maxima of max(SR, floor).

@@ -25,15 +25,19 @@ struct Resolved {
 };
 
 // Read-only device view of a context for launches issued outside the engine.
-// dm / fp point at the engine's DevMesh<T> / FaceParams<T> (T per `precision`).
+// dm / df / dg / fp point at the engine's DevMesh<T> / DevFaces<T> / DevGather<T> /
+// FaceParams<T> (T per `precision`).
 struct EngineView {
   int n;
+  int nf;
   int precision;  // enum aero_precision
   int flux;
   int lm;
   int block;
   int device;
   const void* dm;
+  const void* df;
+  const void* dg;
   const void* fp;
   const int* perm_dev;  // new -> original cell, on the device
   cudaStream_t stream;

@@ -2,7 +2,7 @@
 // engine_f32.cu and engine_f64.cu, which instantiate it.
 #pragma once
 
-#include "aero_kernels.cuh"
+#include "aero_face_kernels.cuh"
 #include "engine.hpp"
 
 #include <algorithm>
@@ -64,21 +64,39 @@ class EngineT final : public Engine {
     std::vector<T> inv_vol(static_cast<size_t>(n_));
     for (int c = 0; c < n_; ++c) inv_vol[c] = T(1) / std::max(T(hs_.vol[c]), T(1.0e-12));
     inv_vol_ = upload(inv_vol);
-    std::vector<V2> doff(ns), noff(ns);
-    for (size_t i = 0; i < ns; ++i) {
-      if (hs_.link[i] < 0) {
-        doff[i].x = doff[i].y = T(0);
-        noff[i].x = noff[i].y = T(0);
-        continue;
+    // face table in T (exact conversions; MUSCL offsets formed in T from T coordinates)
+    {
+      const size_t nf = hs_.f_orig.size();
+      std::vector<int2> fc(nf);
+      std::vector<V2> fn(nf), doff(nf), noff(nf);
+      std::vector<T> fa(nf);
+      for (size_t i = 0; i < nf; ++i) {
+        fc[i] = make_int2(hs_.f_own[i], hs_.f_nb[i]);
+        fn[i].x = T(hs_.f_nx[i]);
+        fn[i].y = T(hs_.f_ny[i]);
+        fa[i] = T(hs_.f_area[i]);
+        const int o = hs_.f_own_old[i], b = hs_.f_nb_old[i];
+        doff[i].x = T(hs_.f_cx[i]) - T(hs_.ccx[o]);
+        doff[i].y = T(hs_.f_cy[i]) - T(hs_.ccy[o]);
+        if (hs_.f_nb[i] >= 0) {
+          noff[i].x = T(hs_.f_cx[i]) - T(hs_.ccx[b]);
+          noff[i].y = T(hs_.f_cy[i]) - T(hs_.ccy[b]);
+        } else {
+          noff[i].x = noff[i].y = T(0);
+        }
       }
-      const int o = hs_.own_old[i], b = hs_.nbr_old[i];
-      doff[i].x = T(hs_.fcx[i]) - T(hs_.ccx[o]);
-      doff[i].y = T(hs_.fcy[i]) - T(hs_.ccy[o]);
-      noff[i].x = T(hs_.fcx[i]) - T(hs_.ccx[b]);
-      noff[i].y = T(hs_.fcy[i]) - T(hs_.ccy[b]);
+      df_.nf = static_cast<int>(nf);
+      df_.cells = upload(fc);
+      df_.nrm = upload(fn);
+      df_.area = upload(fa);
+      df_.doff = upload(doff);
+      df_.noff = upload(noff);
+      dg_.n = n_;
+      dg_.d = d_;
+      dg_.slot = upload(hs_.gslot);
+      F_ = alloc<V4>(nf);
+      FS_ = alloc<T>(nf);
     }
-    doff_ = upload(doff);
-    noff_ = upload(noff);
     perm_dev_ = upload(hs_.perm);
     // monitor tables: per-cell flags, owner-sorted wall entries, and a partials slot for each
     // update block that holds wall entries
@@ -182,9 +200,8 @@ class EngineT final : public Engine {
     dm_.link = link_;
     dm_.nrm = nrm_;
     dm_.area = area_;
-    dm_.doff = doff_;
-    dm_.noff = noff_;
     dm_.inv_vol = inv_vol_;
+    dg_.inv_vol = inv_vol_;
 
     fp_.gamma = T(rs_.gamma);
     fp_.farfield = Cons<T>{T(rs_.cons_inf[0]), T(rs_.cons_inf[1]), T(rs_.cons_inf[2]), T(rs_.cons_inf[3])};
@@ -301,6 +318,9 @@ class EngineT final : public Engine {
     v.block = block_;
     cudaGetDevice(&v.device);
     v.dm = &dm_;
+    v.df = &df_;
+    v.dg = &dg_;
+    v.nf = df_.nf;
     v.fp = &fp_;
     v.perm_dev = perm_dev_;
     v.stream = st_;
@@ -572,7 +592,7 @@ class EngineT final : public Engine {
   bool second_at(int it) const { return it >= std::max(cfg_.startup_first_order_iters, 0); }
 
   long long launches_per_iteration(bool second) const {
-    const int per_stage = (second ? 1 : 0) + 1 + (cfg_.local_time_stepping ? 0 : 1) + 1;
+    const int per_stage = (second ? 1 : 0) + 2 + (cfg_.local_time_stepping ? 0 : 1) + 1;  // residual: 2 passes
     return static_cast<long long>(per_stage) * cfg_.rk_stages + (pjump_on_ ? 1 : 0) + (sym_on_ ? 1 : 0) + 1;
   }
 
@@ -614,43 +634,25 @@ class EngineT final : public Engine {
     }
   }
 
-  struct ResOut {
-    Ctrl* ctrl;
-    int* fb;
-    V4* R;
-    T* SR;
-    int global_dt;
-  };
-  template <int FLUX, bool SECOND, bool LM, bool NORMS>
-  void residual_t(const ResOut& o) {
-    k_residual<T, FLUX, SECOND, LM, NORMS>
-        <<<nblocks_, block_, 0, st_>>>(dm_, fp_, W_, gx_, gy_, o.R, o.SR, part_, o.ctrl, o.fb, o.global_dt);
-  }
-  template <int FLUX, bool SECOND, bool LM>
-  void residual_n(bool norms, const ResOut& o) {
-    if (norms) {
-      residual_t<FLUX, SECOND, LM, true>(o);
-    } else {
-      residual_t<FLUX, SECOND, LM, false>(o);
-    }
-  }
-  template <int FLUX, bool SECOND>
-  void residual_l(bool norms, const ResOut& o) {
-    if (rs_.lm) {
-      residual_n<FLUX, SECOND, true>(norms, o);
-    } else {
-      residual_n<FLUX, SECOND, false>(norms, o);
-    }
-  }
   void launch_residual(bool second, bool norms, Ctrl* ctrl, int* fb, V4* R, T* SR, int global_dt) {
-    const ResOut o{ctrl, fb, R, SR, global_dt};
-    if (cfg_.flux == AERO_FLUX_HLLC) {
-      if (second) residual_l<1, true>(norms, o);
-      else residual_l<1, false>(norms, o);
-    } else {
-      if (second) residual_l<0, true>(norms, o);
-      else residual_l<0, false>(norms, o);
-    }
+    ResidualLaunch<T> a;
+    a.block = block_;
+    a.st = st_;
+    a.faces = df_;
+    a.gather = dg_;
+    a.fp = fp_;
+    a.W = W_;
+    a.gx = gx_;
+    a.gy = gy_;
+    a.F = F_;
+    a.FS = FS_;
+    a.R = R;
+    a.SR = SR;
+    a.part = part_;
+    a.ctrl = ctrl;
+    a.fb = fb;
+    a.global_dt = global_dt;
+    launch_residual_passes(a, cfg_.flux, second, rs_.lm != 0, norms);
   }
 
   template <bool PRECOND, bool LAST>
@@ -815,8 +817,10 @@ class EngineT final : public Engine {
   int* link_ = nullptr;
   V2* nrm_ = nullptr;
   T* area_ = nullptr;
-  V2* doff_ = nullptr;
-  V2* noff_ = nullptr;
+  DevFaces<T> df_{};
+  DevGather<T> dg_{};
+  V4* F_ = nullptr;   // per face: F*A
+  T* FS_ = nullptr;   // per face: wave-speed term
   T* inv_vol_ = nullptr;
   unsigned char* flags_ = nullptr;
   int* perm_dev_ = nullptr;

@@ -109,6 +109,10 @@ bool build_slots(const aero_mesh_desc& m, int ordering, HostSlots* out, std::str
     *err = "mesh must contain cells and faces";
     return false;
   }
+  if (n >= (1 << 30) || nf >= (1 << 30)) {  // cell and face ids are packed with a side bit
+    *err = "mesh too large: cell and face counts must be below 2^30";
+    return false;
+  }
   if (!m.face_owner || !m.face_neighbor || !m.face_bc || !m.face_normal || !m.face_center ||
       !m.face_area || !m.cell_volume || !m.cell_center || (m.num_wall_faces > 0 && !m.wall_faces) ||
       m.num_wall_faces < 0) {
@@ -237,6 +241,49 @@ bool build_slots(const aero_mesh_desc& m, int ordering, HostSlots* out, std::str
       s.nbr_old[slot] = b >= 0 ? b : o;
     }
   }
+  // face table sorted by new owner, and each cell's faces as gather slots in ascending
+  // original face order (the order the reference sums them in)
+  {
+    std::vector<int> order(static_cast<size_t>(nf));
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return s.iperm[m.face_owner[a]] < s.iperm[m.face_owner[b]]; });
+    std::vector<int> face_new(static_cast<size_t>(nf));
+    s.f_orig = order;
+    s.f_own.resize(static_cast<size_t>(nf));
+    s.f_nb.resize(static_cast<size_t>(nf));
+    s.f_own_old.resize(static_cast<size_t>(nf));
+    s.f_nb_old.resize(static_cast<size_t>(nf));
+    s.f_nx.resize(static_cast<size_t>(nf));
+    s.f_ny.resize(static_cast<size_t>(nf));
+    s.f_area.resize(static_cast<size_t>(nf));
+    s.f_cx.resize(static_cast<size_t>(nf));
+    s.f_cy.resize(static_cast<size_t>(nf));
+    for (int i = 0; i < nf; ++i) {
+      const int f = order[i];
+      face_new[f] = i;
+      const int o = m.face_owner[f], b = m.face_neighbor[f];
+      s.f_own[i] = s.iperm[o];
+      s.f_nb[i] = b >= 0 ? s.iperm[b] : (m.face_bc[f] == AERO_BC_WALL ? -2 : -1);
+      s.f_own_old[i] = o;
+      s.f_nb_old[i] = b >= 0 ? b : o;
+      s.f_nx[i] = m.face_normal[3 * f];
+      s.f_ny[i] = m.face_normal[3 * f + 1];
+      s.f_area[i] = m.face_area[f];
+      s.f_cx[i] = m.face_center[3 * f];
+      s.f_cy[i] = m.face_center[3 * f + 1];
+    }
+    s.gslot.assign(total, kPadLink);
+    for (int cn = 0; cn < n; ++cn) {
+      const int co = s.perm[cn];
+      int k = 0;
+      for (int j = cstart[co]; j < cstart[co + 1]; ++j, ++k) {
+        const int f = cface[j];
+        s.gslot[static_cast<size_t>(k) * n + cn] = (face_new[f] << 1) | (m.face_owner[f] == co ? 0 : 1);
+      }
+    }
+  }
+
   // wall entries: (new owner, face, kind); a slip-wall face listed in the patch is merged
   // into its monitor entry once, further listings get entries of their own
   struct WallEntry {

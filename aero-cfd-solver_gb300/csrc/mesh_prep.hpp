@@ -20,6 +20,13 @@ struct HostSlots {
   std::vector<double> nx, ny, area;     // [d*n] canonical (owner-outward) face geometry
   std::vector<double> fcx, fcy;         // [d*n] face centre
   std::vector<int> own_old, nbr_old;    // [d*n] canonical owner / neighbour (original ids)
+  // Face table: faces sorted by the new index of their owner, then by original index.
+  std::vector<int> f_orig;                  // new face -> original face
+  std::vector<int> f_own, f_nb;             // new owner; new neighbour, -1 far field, -2 wall
+  std::vector<int> f_own_old, f_nb_old;     // original owner; original neighbour (owner if none)
+  std::vector<double> f_nx, f_ny, f_area;   // unit normal out of the owner, length
+  std::vector<double> f_cx, f_cy;           // face centre
+  std::vector<int> gslot;                   // [d*n] (new face << 1) | (cell is the neighbour), kPad
   std::vector<double> vol;              // [n] new order
   std::vector<double> ccx, ccy;         // [n] original order (cell centres)
   // [n] new order: bit 0 owns slip-wall faces, bit 1 owns far-field faces, bits 2..7 number

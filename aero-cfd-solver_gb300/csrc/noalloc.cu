@@ -7,12 +7,13 @@
 // memory pool that owns all device memory, or in a time-stepping loop whose memory budget is
 // fixed up front (cudaMalloc/cudaFree can synchronise the device and fragment memory).
 //
-// Limits and sharing: the scratch array is sized for kNoallocMaxCells cells (about 8.9 MB)
-// and every GPU that loads this library holds it until the process exits. All calls on a
+// Limits and sharing: the scratch array is sized for kNoallocMaxCells cells and
+// kNoallocMaxFaces faces (about 16.8 MB) and every GPU that loads this library holds it
+// until the process exits. All calls on a
 // device share it and it keeps the last call's contents; the kernels clear what must start
 // at zero. Two calls whose work overlaps on the same GPU (different streams, or different
 // contexts on one device) race on the shared array and must be serialised by the caller.
-#include "aero_kernels.cuh"
+#include "aero_face_kernels.cuh"
 #include "ctx.hpp"
 
 #include <cuda_runtime.h>
@@ -24,12 +25,14 @@ namespace aero {
 namespace {
 
 constexpr int kNoallocMaxCells = 65536;
+constexpr int kNoallocMaxFaces = 3 * 65536;
 constexpr size_t kAlign = 256;
 constexpr size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 constexpr size_t kCtrlBytes = align_up(sizeof(Ctrl));
-// per cell, sized for double: W, gx, gy, R (4 reals each) and SR
+// sized for double: per cell W, gx, gy, R (4 reals each) and SR; per face F (4 reals) and FS
 constexpr size_t kScratchBytes = kCtrlBytes + 4 * align_up(size_t(kNoallocMaxCells) * 32) +
-                                 align_up(size_t(kNoallocMaxCells) * 8);
+                                 align_up(size_t(kNoallocMaxCells) * 8) + align_up(size_t(kNoallocMaxFaces) * 32) +
+                                 align_up(size_t(kNoallocMaxFaces) * 8);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -91,14 +94,6 @@ __global__ void k_na_store(int n, const int* __restrict__ perm, const typename V
   sr[o] = double(SR[c]);
 }
 
-template <class T, int FLUX, bool SECOND, bool LM>
-void launch_residual_na(int grid, int block, cudaStream_t st, const DevMesh<T>& dm, const FaceParams<T>& fp,
-                        const typename Vec<T>::v4* W, const typename Vec<T>::v4* gx,
-                        const typename Vec<T>::v4* gy, typename Vec<T>::v4* R, T* SR, Ctrl* ctrl) {
-  k_residual<T, FLUX, SECOND, LM, false>
-      <<<grid, block, 0, st>>>(dm, fp, W, gx, gy, R, SR, Partials{}, ctrl, &ctrl->fo_fallback, 0);
-}
-
 template <class T>
 cudaError_t run_na(const EngineView& v, unsigned char* base, const double* u, int second, double stab,
                    int as_fix, double as_fmin, double as_ramp, double* res, double* sr, cudaStream_t st) {
@@ -118,28 +113,30 @@ cudaError_t run_na(const EngineView& v, unsigned char* base, const double* u, in
   V4* gy = reinterpret_cast<V4*>(take(sizeof(V4) * n));
   V4* R = reinterpret_cast<V4*>(take(sizeof(V4) * n));
   T* SR = reinterpret_cast<T*>(take(sizeof(T) * n));
+  V4* F = reinterpret_cast<V4*>(take(sizeof(V4) * v.nf));
+  T* FS = reinterpret_cast<T*>(take(sizeof(T) * v.nf));
   const int block = v.block;
   const int grid = (n + block - 1) / block;
   k_na_prepare<T><<<grid, block, 0, st>>>(n, v.perm_dev, u, W, double(fp.gamma), ctrl, stab, as_fix, as_fmin, as_ramp);
   if (second) k_gradient<T><<<grid, block, 0, st>>>(dm, W, gx, gy, ctrl);
-  const bool lm = v.lm != 0;
-  if (v.flux == AERO_FLUX_HLLC) {
-    if (second) {
-      if (lm) launch_residual_na<T, 1, true, true>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
-      else launch_residual_na<T, 1, true, false>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
-    } else {
-      if (lm) launch_residual_na<T, 1, false, true>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
-      else launch_residual_na<T, 1, false, false>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
-    }
-  } else {
-    if (second) {
-      if (lm) launch_residual_na<T, 0, true, true>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
-      else launch_residual_na<T, 0, true, false>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
-    } else {
-      if (lm) launch_residual_na<T, 0, false, true>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
-      else launch_residual_na<T, 0, false, false>(grid, block, st, dm, fp, W, gx, gy, R, SR, ctrl);
-    }
-  }
+  ResidualLaunch<T> a;
+  a.block = block;
+  a.st = st;
+  a.faces = *static_cast<const DevFaces<T>*>(v.df);
+  a.gather = *static_cast<const DevGather<T>*>(v.dg);
+  a.fp = fp;
+  a.W = W;
+  a.gx = gx;
+  a.gy = gy;
+  a.F = F;
+  a.FS = FS;
+  a.R = R;
+  a.SR = SR;
+  a.part = Partials{};
+  a.ctrl = ctrl;
+  a.fb = &ctrl->fo_fallback;
+  a.global_dt = 0;
+  launch_residual_passes(a, v.flux, second != 0, v.lm != 0, false);
   k_na_store<T><<<grid, block, 0, st>>>(n, v.perm_dev, R, SR, res, sr);
   return cudaGetLastError();
 }
@@ -158,10 +155,11 @@ int aero_residual_noalloc(aero_ctx* ctx, const double* conserved_dev, int second
     return AERO_ERR_INVALID;
   }
   const aero::EngineView v = ctx->engine->view();
-  if (v.n > aero::kNoallocMaxCells) {
-    ctx->error = "aero_residual_noalloc: the mesh has " + std::to_string(v.n) +
-                 " cells; the allocation-free residual supports at most " +
-                 std::to_string(aero::kNoallocMaxCells) + " cells";
+  if (v.n > aero::kNoallocMaxCells || v.nf > aero::kNoallocMaxFaces) {
+    ctx->error = "aero_residual_noalloc: the mesh has " + std::to_string(v.n) + " cells and " +
+                 std::to_string(v.nf) + " faces; the allocation-free residual supports at most " +
+                 std::to_string(aero::kNoallocMaxCells) + " cells and " +
+                 std::to_string(aero::kNoallocMaxFaces) + " faces";
     return AERO_ERR_INVALID;
   }
   int prev = -1;

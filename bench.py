@@ -48,13 +48,16 @@ STARTUP = 25  # first-order start-up iterations run untimed before warm-up
 NCU_TRAFFIC = {}
 
 
-def algorithmic_bytes(kernel: str, n: int, slots: int, precision: str) -> float:
+def algorithmic_bytes(kernel: str, n: int, slots: int, precision: str, faces: int = 0) -> float:
     """Compulsory bytes of one launch: every array element the kernel reads or writes,
-    once (neighbour re-reads excluded). s = bulk real size."""
+    once (neighbour re-reads excluded). s = bulk real size; `slots` per cell."""
     s = 4 if precision == "fp32" else 8
     slot_geo = 4 + 2 * s + s  # link, normal, area
-    if kernel == "residual":  # W, gradients, slot geometry and MUSCL offsets, 1/vol, R, SR
-        return n * (4 * s + 8 * s + slots * (slot_geo + 4 * s) + s + 4 * s + s)
+    if kernel == "residual":
+        # face pass + cell pass: W and gradients per cell, per face its two cell ids, normal,
+        # length and MUSCL offsets, per cell its face list, 1/vol and R, SR; the per-face
+        # flux the two passes exchange is not counted (it is not part of the algorithm)
+        return n * (4 * s + 8 * s) + faces * (8 + 3 * s + 4 * s) + n * slots * 4 + n * (s + 4 * s + s)
     if kernel == "gradient":  # W, slot geometry, 1/vol, gradients
         return n * (4 * s + slots * slot_geo + s + 8 * s)
     if kernel == "update":
@@ -299,7 +302,7 @@ def run_gpu_arm(args):
         value = world * n * args.steps / (ms_max / 1e3) / 1e6
         res_ms, res_n = prof["residual"]
         avg_res = res_ms / max(res_n, 1)
-        bytes_res = algorithmic_bytes("residual", n, info["slots_per_cell"], prec)
+        bytes_res = algorithmic_bytes("residual", n, info["slots_per_cell"], prec, int(info["faces"]))
         achieved = bytes_res / (avg_res / 1e3) / 1e9
         total_prof = sum(v[0] for v in prof.values())
         results[prec] = dict(value=value, ms=ms_max, warm_ms=warm_ms, info=info, prof=prof, state=state,

@@ -11,29 +11,6 @@
 
 namespace aero {
 
-// Faces sorted by the new index of their owner. cells = (owner, neighbour) new indices, the
-// neighbour -1 for a far-field face and -2 for a slip wall. Geometry in the bulk type T:
-// unit normal out of the owner, length, and the offsets of the face centre from the owner's
-// and the neighbour's centres (MUSCL).
-template <class T>
-struct DevFaces {
-  int nf;
-  const int2* cells;
-  const typename Vec<T>::v2* nrm;
-  const T* area;
-  const typename Vec<T>::v2* doff;
-  const typename Vec<T>::v2* noff;
-};
-
-// Per-cell gather table (ELL, slot (k, c) at k*n + c): (face << 1) | (cell is the
-// neighbour), kPad after the last face of the cell.
-template <class T>
-struct DevGather {
-  int n, d;
-  const int* slot;
-  const T* inv_vol;
-};
-
 // Face pass. FLUX 0 Rusanov / 1 HLLC; SECOND: MUSCL with the cell gradients; LM: any
 // low-Mach feature on. fb[0] / fb[1] count first-order and diffusive fallbacks.
 template <class T, int FLUX, bool SECOND, bool LM>
@@ -143,68 +120,20 @@ __global__ void __launch_bounds__(256) k_gather(DevGather<T> g, const typename V
   T nl1 = T(0), nl2 = T(0), nlinf = T(0);
   double srm = 0.0;
   if (c < g.n) {
-    T r0 = 0, r1 = 0, r2 = 0, r3 = 0, sr = 0;
-    for (int k = 0; k < g.d; ++k) {
-      const int s = g.slot[k * g.n + c];
-      if (s == kPad) break;
-      const int fi = s >> 1;
-      const auto fv = F[fi];
-      if (s & 1) {
-        r0 -= fv.x; r1 -= fv.y; r2 -= fv.z; r3 -= fv.w;
-      } else {
-        r0 += fv.x; r1 += fv.y; r2 += fv.z; r3 += fv.w;
-      }
-      sr += FS[fi];
-    }
+    T r[4], sr;
+    gather_cell<T>(g, F, FS, c, r, &sr);
     typename Vec<T>::v4 out;
-    out.x = r0; out.y = r1; out.z = r2; out.w = r3;
+    out.x = r[0]; out.y = r[1]; out.z = r[2]; out.w = r[3];
     R[c] = out;
     SR[c] = sr;
     if (global_dt) srm = double(smax(sr, Kn<T>::wave_floor));
-    if (NORMS) {
-      const T inv = g.inv_vol[c];
-      const T v0 = r0 * inv, v1 = r1 * inv, v2 = r2 * inv, v3 = r3 * inv;
-      const T a0 = fabs(v0), a1 = fabs(v1), a2 = fabs(v2), a3 = fabs(v3);
-      nl1 = ((a0 + a1) + a2) + a3;
-      nl2 = ((v0 * v0 + v1 * v1) + v2 * v2) + v3 * v3;
-      nlinf = smax(smax(smax(a0, a1), a2), a3);
-    }
+    if (NORMS) norm_terms<T>(r, g.inv_vol[c], &nl1, &nl2, &nlinf);
   }
   if (global_dt) {
     srm = warp_max(srm);
     if ((threadIdx.x & 31) == 0) part.srmax[blockIdx.x * ((blockDim.x + 31) >> 5) + (threadIdx.x >> 5)] = srm;
   }
-  if (NORMS) {
-    // block partials in T; the control kernel sums the blocks in double (FP32: float-float)
-    __shared__ T shn[3][32];
-    nl1 = warp_sum_t(nl1);
-    nl2 = warp_sum_t(nl2);
-    nlinf = warp_max_t(nlinf);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-    if (lane == 0) {
-      shn[0][wid] = nl1;
-      shn[1][wid] = nl2;
-      shn[2][wid] = nlinf;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      T a = T(0), b = T(0), mx = T(0);
-      for (int i = 0; i < nw; ++i) {
-        a += shn[0][i];
-        b += shn[1][i];
-        mx = smax(mx, shn[2][i]);
-      }
-      T* out;
-      if constexpr (sizeof(T) == 4) {
-        out = part.norms_f;
-      } else {
-        out = part.norms;
-      }
-      out[blockIdx.x] = a;
-      out[part.nb + blockIdx.x] = b;
-      out[2 * part.nb + blockIdx.x] = mx;
-    }
-  }
+  if (NORMS) block_norms<T>(nl1, nl2, nlinf, part);
 }
 
 // Launch geometry and buffers of one residual evaluation.
@@ -233,9 +162,9 @@ void launch_face_flux_t(const ResidualLaunch<T>& a) {
       <<<grid, a.block, 0, a.st>>>(a.faces, a.fp, a.W, a.gx, a.gy, a.F, a.FS, a.ctrl, a.fb);
 }
 
-// Face pass then cell pass, dispatched on the flux, order and low-Mach switches.
+// Face pass, dispatched on the flux, order and low-Mach switches.
 template <class T>
-void launch_residual_passes(const ResidualLaunch<T>& a, int flux, bool second, bool lm, bool norms) {
+void launch_face_pass(const ResidualLaunch<T>& a, int flux, bool second, bool lm) {
   if (flux == AERO_FLUX_HLLC) {
     if (second) {
       if (lm) launch_face_flux_t<T, 1, true, true>(a);
@@ -253,12 +182,24 @@ void launch_residual_passes(const ResidualLaunch<T>& a, int flux, bool second, b
       else launch_face_flux_t<T, 0, false, false>(a);
     }
   }
+}
+
+// Cell pass into a.R / a.SR (with the norm partials when `norms`).
+template <class T>
+void launch_gather_pass(const ResidualLaunch<T>& a, bool norms) {
   const int grid = (a.gather.n + a.block - 1) / a.block;
   if (norms) {
     k_gather<T, true><<<grid, a.block, 0, a.st>>>(a.gather, a.F, a.FS, a.R, a.SR, a.part, a.ctrl, a.global_dt);
   } else {
     k_gather<T, false><<<grid, a.block, 0, a.st>>>(a.gather, a.F, a.FS, a.R, a.SR, a.part, a.ctrl, a.global_dt);
   }
+}
+
+// Face pass then cell pass.
+template <class T>
+void launch_residual_passes(const ResidualLaunch<T>& a, int flux, bool second, bool lm, bool norms) {
+  launch_face_pass(a, flux, second, lm);
+  launch_gather_pass(a, norms);
 }
 
 }  // namespace aero

@@ -173,6 +173,29 @@ struct DevMesh {
   const T* inv_vol;
 };
 
+// Faces sorted by the new index of their owner. cells = (owner, neighbour) new indices, the
+// neighbour -1 for a far-field face and -2 for a slip wall. Geometry in the bulk type T:
+// unit normal out of the owner, length, and the offsets of the face centre from the owner's
+// and the neighbour's centres (MUSCL).
+template <class T>
+struct DevFaces {
+  int nf;
+  const int2* cells;
+  const typename Vec<T>::v2* nrm;
+  const T* area;
+  const typename Vec<T>::v2* doff;
+  const typename Vec<T>::v2* noff;
+};
+
+// Per-cell gather table (ELL, slot (k, c) at k*n + c): (face << 1) | (cell is the
+// neighbour), kPad after the last face of the cell.
+template <class T>
+struct DevGather {
+  int n, d;
+  const int* slot;
+  const T* inv_vol;
+};
+
 // Per-block partial results reduced by the control kernel in a fixed order. Quantity-major
 // ([k][block]) so that the control warp reads them coalesced.
 struct Partials {
@@ -299,6 +322,86 @@ __device__ __forceinline__ T warp_max_t(T x) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) x = smax(x, __shfl_xor_sync(0xffffffffu, x, o));
   return x;
+}
+
+// Residual of cell c from the per-face fluxes: +-F*A over its faces in ascending original
+// face order, and the sum of the faces' wave-speed terms. The slots are read first so the
+// flux loads of one cell are in flight together.
+template <class T>
+__device__ __forceinline__ void gather_cell(const DevGather<T>& g, const typename Vec<T>::v4* __restrict__ F,
+                                            const T* __restrict__ FS, int c, T (&r)[4], T* sr) {
+  constexpr int kU = 4;
+  r[0] = r[1] = r[2] = r[3] = T(0);
+  *sr = T(0);
+  for (int k0 = 0; k0 < g.d; k0 += kU) {
+    int sl[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) sl[u] = (k0 + u < g.d) ? g.slot[(k0 + u) * g.n + c] : kPad;
+    typename Vec<T>::v4 fv[kU];
+    T fs[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      if (sl[u] != kPad) {
+        fv[u] = F[sl[u] >> 1];
+        fs[u] = FS[sl[u] >> 1];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      if (sl[u] == kPad) break;
+      if (sl[u] & 1) {
+        r[0] -= fv[u].x; r[1] -= fv[u].y; r[2] -= fv[u].z; r[3] -= fv[u].w;
+      } else {
+        r[0] += fv[u].x; r[1] += fv[u].y; r[2] += fv[u].z; r[3] += fv[u].w;
+      }
+      *sr += fs[u];
+    }
+    if (sl[kU - 1] == kPad) break;
+  }
+}
+
+// Residual-norm terms of one cell (euler_solver.cpp:309-339): |R|/V summed, squared, max.
+template <class T>
+__device__ __forceinline__ void norm_terms(const T (&r)[4], T inv, T* l1, T* l2, T* linf) {
+  const T v0 = r[0] * inv, v1 = r[1] * inv, v2 = r[2] * inv, v3 = r[3] * inv;
+  const T a0 = fabs(v0), a1 = fabs(v1), a2 = fabs(v2), a3 = fabs(v3);
+  *l1 = ((a0 + a1) + a2) + a3;
+  *l2 = ((v0 * v0 + v1 * v1) + v2 * v2) + v3 * v3;
+  *linf = smax(smax(smax(a0, a1), a2), a3);
+}
+
+// Block partials of the norm terms in T into Partials::norms / norms_f; the control kernel
+// sums the blocks in double (FP32: float-float). Called by every thread of the block.
+template <class T>
+__device__ void block_norms(T nl1, T nl2, T nlinf, Partials part) {
+  __shared__ T shn[3][32];
+  nl1 = warp_sum_t(nl1);
+  nl2 = warp_sum_t(nl2);
+  nlinf = warp_max_t(nlinf);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) {
+    shn[0][wid] = nl1;
+    shn[1][wid] = nl2;
+    shn[2][wid] = nlinf;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T a = T(0), b = T(0), mx = T(0);
+    for (int i = 0; i < nw; ++i) {
+      a += shn[0][i];
+      b += shn[1][i];
+      mx = smax(mx, shn[2][i]);
+    }
+    T* out;
+    if constexpr (sizeof(T) == 4) {
+      out = part.norms_f;
+    } else {
+      out = part.norms;
+    }
+    out[blockIdx.x] = a;
+    out[part.nb + blockIdx.x] = b;
+    out[2 * part.nb + blockIdx.x] = mx;
+  }
 }
 
 // Monitors of one cell after the last stage (euler_solver.cpp:923-1026, forces.cpp:208-294),
@@ -454,6 +557,67 @@ __device__ __forceinline__ double block_max(double v, double* shm) {
 // ---------------------------------------------------------------------------------------
 // Gradient: Green-Gauss primitive gradients (reconstruction.cpp:73-119), gathered per cell.
 // ---------------------------------------------------------------------------------------
+// Green-Gauss gradient of cell c (reconstruction.cpp:73-119): the face averages of the
+// primitive state times the outward face vectors, over 1/V.
+template <class T>
+__device__ __forceinline__ void cell_gradient(const DevMesh<T>& m, const typename Vec<T>::v4* __restrict__ W, int c,
+                                              typename Vec<T>::v4* gxo, typename Vec<T>::v4* gyo) {
+  const auto wc = W[c];
+  T ax0 = 0, ax1 = 0, ax2 = 0, ax3 = 0, ay0 = 0, ay1 = 0, ay2 = 0, ay3 = 0;
+  // slots in batches of kU: the links first, then every load of the batch, then the sums in
+  // slot order, so the neighbour loads of one cell are in flight together
+  constexpr int kU = 4;
+  for (int k0 = 0; k0 < m.d; k0 += kU) {
+    int lk[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) lk[u] = (k0 + u < m.d) ? m.link[(k0 + u) * m.n + c] : kPad;
+    typename Vec<T>::v2 nd[kU];
+    T ar[kU];
+    typename Vec<T>::v4 wo[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      if (lk[u] != kPad) {
+        const int s = (k0 + u) * m.n + c;
+        nd[u] = m.nrm[s];
+        ar[u] = m.area[s];
+        wo[u] = lk[u] >= 0 ? W[lk[u] >> 1] : wc;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int link = lk[u];
+      if (link == kPad) break;
+      const T nax = nd[u].x * ar[u], nay = nd[u].y * ar[u];
+      T q0 = wc.x, q1 = wc.y, q2 = wc.z, q3 = wc.w;
+      bool minus = false;
+      if (link >= 0) {
+        q0 = T(0.5) * (q0 + wo[u].x);
+        q1 = T(0.5) * (q1 + wo[u].y);
+        q2 = T(0.5) * (q2 + wo[u].z);
+        q3 = T(0.5) * (q3 + wo[u].w);
+        minus = (link & 1) != 0;
+      }
+      if (minus) {
+        ax0 -= q0 * nax; ay0 -= q0 * nay;
+        ax1 -= q1 * nax; ay1 -= q1 * nay;
+        ax2 -= q2 * nax; ay2 -= q2 * nay;
+        ax3 -= q3 * nax; ay3 -= q3 * nay;
+      } else {
+        ax0 += q0 * nax; ay0 += q0 * nay;
+        ax1 += q1 * nax; ay1 += q1 * nay;
+        ax2 += q2 * nax; ay2 += q2 * nay;
+        ax3 += q3 * nax; ay3 += q3 * nay;
+      }
+    }
+    if (lk[kU - 1] == kPad) break;
+  }
+  const T inv = m.inv_vol[c];
+  typename Vec<T>::v4& ox = *gxo;
+  typename Vec<T>::v4& oy = *gyo;
+  ox.x = ax0 * inv; ox.y = ax1 * inv; ox.z = ax2 * inv; ox.w = ax3 * inv;
+  oy.x = ay0 * inv; oy.y = ay1 * inv; oy.z = ay2 * inv; oy.w = ay3 * inv;
+}
+
 template <class T>
 __global__ void __launch_bounds__(256) k_gradient(DevMesh<T> m, const typename Vec<T>::v4* __restrict__ W,
                                                   typename Vec<T>::v4* __restrict__ gx,
@@ -461,41 +625,8 @@ __global__ void __launch_bounds__(256) k_gradient(DevMesh<T> m, const typename V
                                                   const Ctrl* __restrict__ ctrl) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.n || ctrl->done) return;
-  const auto wc = W[c];
-  T ax0 = 0, ax1 = 0, ax2 = 0, ax3 = 0, ay0 = 0, ay1 = 0, ay2 = 0, ay3 = 0;
-  for (int k = 0; k < m.d; ++k) {
-    const int s = k * m.n + c;
-    const int link = m.link[s];
-    if (link == kPad) break;
-    const auto nd = m.nrm[s];
-    const T a = m.area[s];
-    const T nax = nd.x * a, nay = nd.y * a;
-    T q0 = wc.x, q1 = wc.y, q2 = wc.z, q3 = wc.w;
-    bool minus = false;
-    if (link >= 0) {
-      const auto wo = W[link >> 1];
-      q0 = T(0.5) * (q0 + wo.x);
-      q1 = T(0.5) * (q1 + wo.y);
-      q2 = T(0.5) * (q2 + wo.z);
-      q3 = T(0.5) * (q3 + wo.w);
-      minus = (link & 1) != 0;
-    }
-    if (minus) {
-      ax0 -= q0 * nax; ay0 -= q0 * nay;
-      ax1 -= q1 * nax; ay1 -= q1 * nay;
-      ax2 -= q2 * nax; ay2 -= q2 * nay;
-      ax3 -= q3 * nax; ay3 -= q3 * nay;
-    } else {
-      ax0 += q0 * nax; ay0 += q0 * nay;
-      ax1 += q1 * nax; ay1 += q1 * nay;
-      ax2 += q2 * nax; ay2 += q2 * nay;
-      ax3 += q3 * nax; ay3 += q3 * nay;
-    }
-  }
-  const T inv = m.inv_vol[c];
   typename Vec<T>::v4 ox, oy;
-  ox.x = ax0 * inv; ox.y = ax1 * inv; ox.z = ax2 * inv; ox.w = ax3 * inv;
-  oy.x = ay0 * inv; oy.y = ay1 * inv; oy.z = ay2 * inv; oy.w = ay3 * inv;
+  cell_gradient<T>(m, W, c, &ox, &oy);
   gx[c] = ox;
   gy[c] = oy;
 }
@@ -549,22 +680,57 @@ __device__ __forceinline__ bool positivity_safe(const Cons<float>& f, float gm1)
 //         pair (hi, lo) of U_n, so the conserved state accumulates beyond float precision with
 //         float arithmetic only; the double clamp runs only when the float screen fails.
 // The last stage also runs the non-finite trap (euler_solver.cpp:908-946) and the monitors.
+// GATHER (local time stepping): the cell's residual is gathered here from the face pass's
+// fluxes instead of read from R/SR; the last stage stores it in R/SR (the run's last
+// residual) and forms the residual-norm partials.
 // ---------------------------------------------------------------------------------------
-template <class T, bool PRECOND, bool LAST>
-__global__ void __launch_bounds__(256) k_update(int n, int stage, PrecondD pc,
-                                                const typename Vec<T>::v4* __restrict__ R,
-                                                const T* __restrict__ SR, typename Vec<T>::v4* __restrict__ W,
-                                                StateRef U, typename Vec<T>::v4* __restrict__ Us, MonitorSet ms,
-                                                Partials part, Ctrl* __restrict__ ctrl, int global_dt) {
+template <class T, bool PRECOND, bool LAST, bool GATHER>
+__global__ void __launch_bounds__(256) k_update(int n, int stage, PrecondD pc, typename Vec<T>::v4* __restrict__ R,
+                                                T* __restrict__ SR, DevGather<T> g,
+                                                const typename Vec<T>::v4* __restrict__ F, const T* __restrict__ FS,
+                                                typename Vec<T>::v4* __restrict__ W, StateRef U,
+                                                typename Vec<T>::v4* __restrict__ Us, MonitorSet ms, Partials part,
+                                                Ctrl* __restrict__ ctrl, int global_dt) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (ctrl->done) return;
   bool bad = false;
   Cons<double> s{1.0, 0.0, 0.0, 1.0};
   Prim<T> w{T(1), T(0), T(0), T(1)};
+  T nl1 = T(0), nl2 = T(0), nlinf = T(0);
   if (c < n) {
-    const auto r4 = R[c];
-    const T r0 = r4.x, r1 = r4.y, r2 = r4.z;
-    T r3 = r4.w;
+    // the cell's own state first, so these loads overlap the gather's
+    typename Vec<T>::v4 st_hi{}, st_lo{}, st_us{};
+    d4 st_un{};
+    if constexpr (sizeof(T) == 4) {
+      st_hi = U.hi[c];
+      if (LAST) st_lo = U.lo[c];
+    } else {
+      st_un = U.un[c];
+    }
+    if (stage > 0) st_us = Us[c];
+    T r0, r1, r2, r3, src;
+    if (GATHER) {
+      T rr[4];
+      gather_cell<T>(g, F, FS, c, rr, &src);
+      r0 = rr[0];
+      r1 = rr[1];
+      r2 = rr[2];
+      r3 = rr[3];
+      if (LAST) {
+        typename Vec<T>::v4 o;
+        o.x = r0; o.y = r1; o.z = r2; o.w = r3;
+        R[c] = o;
+        SR[c] = src;
+        norm_terms<T>(rr, g.inv_vol[c], &nl1, &nl2, &nlinf);
+      }
+    } else {
+      const auto r4 = R[c];
+      r0 = r4.x;
+      r1 = r4.y;
+      r2 = r4.z;
+      r3 = r4.w;
+      if (!global_dt) src = SR[c];
+    }
     if (PRECOND) {  // energy row of the preconditioned residual, in double
       const auto w4 = W[c];
       const Prim<double> w{double(w4.x), double(w4.y), double(w4.z), double(w4.w)};
@@ -586,7 +752,7 @@ __global__ void __launch_bounds__(256) k_update(int n, int stage, PrecondD pc,
       dt = cfl / T(ctrl->sr_max);
       if (!sfinite(dt)) dt = T(0);
     } else {
-      dt = cfl / smax(SR[c], Kn<T>::wave_floor);
+      dt = cfl / smax(src, Kn<T>::wave_floor);
     }
     if constexpr (sizeof(T) == 4) {
       float d0, d1, d2, d3;
@@ -597,13 +763,13 @@ __global__ void __launch_bounds__(256) k_update(int n, int stage, PrecondD pc,
         d3 = -(dt * r3);
       } else {
         const float b = (stage == 1) ? 0.25f : (2.0f / 3.0f);
-        const float4 dl = Us[c];
+        const float4 dl = st_us;
         d0 = b * (dl.x - dt * r0);
         d1 = b * (dl.y - dt * r1);
         d2 = b * (dl.z - dt * r2);
         d3 = b * (dl.w - dt * r3);
       }
-      const float4 uh = U.hi[c];
+      const float4 uh = st_hi;
       if (!LAST) {
         Cons<float> f{uh.x + d0, uh.y + d1, uh.z + d2, uh.w + d3};
         const float fr = f.r, fe = f.rE;
@@ -613,7 +779,7 @@ __global__ void __launch_bounds__(256) k_update(int n, int stage, PrecondD pc,
         Us[c] = make_float4(d0, d1, d2, d3);
         w = cons_to_prim(f, pc.gamma_f);
       } else {
-        const float4 ul = U.lo[c];
+        const float4 ul = st_lo;
         float4 h, l;
         ff_add(uh.x, ul.x, d0, &h.x, &l.x);
         ff_add(uh.y, ul.y, d1, &h.y, &l.y);
@@ -636,9 +802,9 @@ __global__ void __launch_bounds__(256) k_update(int n, int stage, PrecondD pc,
         bad = !finite4(h.x, h.y, h.z, h.w) || !finite4(l.x, l.y, l.z, l.w) || !finite4(w.r, w.u, w.v, w.p);
       }
     } else {
-      const d4 un = U.un[c];
+      const d4 un = st_un;
       const double d = double(dt);
-      const d4 us = (stage == 0) ? un : Us[c];
+      const d4 us = (stage == 0) ? un : st_us;
       s = Cons<double>{us.x - d * r0, us.y - d * r1, us.z - d * r2, us.w - d * r3};
       if (stage == 1) {
         s.r = 0.75 * un.x + 0.25 * s.r;
@@ -668,6 +834,7 @@ __global__ void __launch_bounds__(256) k_update(int n, int stage, PrecondD pc,
   }
   if (LAST) {
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&ctrl->nonfinite, 1);
+    if (GATHER) block_norms<T>(nl1, nl2, nlinf, part);
     block_monitors<T>(c < n, w, c, ms, part);
   }
 }

@@ -521,7 +521,8 @@ class EngineT final : public Engine {
   }
 
   // Per kernel class: summed device time (ms) and launches over n iterations, each kernel
-  // bracketed by its own events. Classes: 0 gradient, 1 residual, 2 update, 3 global-dt
+  // bracketed by its own events. Classes: 0 gradient, 1 residual face pass (+ cell pass under
+  // global time stepping), 2 update (+ cell gather under local time stepping), 3 global-dt
   // reduction, 4 symmetry + pressure-jump, 5 controller.
   int profile_kernels(int n, int flush_l2, double* ms, int* launches) override {
     const int it0 = begin_untracked();
@@ -592,7 +593,8 @@ class EngineT final : public Engine {
   bool second_at(int it) const { return it >= std::max(cfg_.startup_first_order_iters, 0); }
 
   long long launches_per_iteration(bool second) const {
-    const int per_stage = (second ? 1 : 0) + 2 + (cfg_.local_time_stepping ? 0 : 1) + 1;  // residual: 2 passes
+    // gradient, face pass, update (+ cell pass and time-step reduction with a global step)
+    const int per_stage = (second ? 1 : 0) + 2 + (cfg_.local_time_stepping ? 0 : 2);
     return static_cast<long long>(per_stage) * cfg_.rk_stages + (pjump_on_ ? 1 : 0) + (sym_on_ ? 1 : 0) + 1;
   }
 
@@ -634,7 +636,7 @@ class EngineT final : public Engine {
     }
   }
 
-  void launch_residual(bool second, bool norms, Ctrl* ctrl, int* fb, V4* R, T* SR, int global_dt) {
+  ResidualLaunch<T> residual_args(Ctrl* ctrl, int* fb, V4* R, T* SR, int global_dt) {
     ResidualLaunch<T> a;
     a.block = block_;
     a.st = st_;
@@ -652,13 +654,26 @@ class EngineT final : public Engine {
     a.ctrl = ctrl;
     a.fb = fb;
     a.global_dt = global_dt;
-    launch_residual_passes(a, cfg_.flux, second, rs_.lm != 0, norms);
+    return a;
+  }
+  void launch_residual(bool second, bool norms, Ctrl* ctrl, int* fb, V4* R, T* SR, int global_dt) {
+    launch_residual_passes(residual_args(ctrl, fb, R, SR, global_dt), cfg_.flux, second, rs_.lm != 0, norms);
   }
 
-  template <bool PRECOND, bool LAST>
-  void update_t(int stage, int global_dt, const V4* R, const T* SR) {
-    k_update<T, PRECOND, LAST><<<nblocks_, block_, 0, st_>>>(n_, stage, pc_, R, SR, W_, sref_, Us_, ms_, part_,
-                                                             ctrl_, global_dt);
+  template <bool PRECOND, bool LAST, bool GATHER>
+  void update_t(int stage, int global_dt, V4* R, T* SR) {
+    k_update<T, PRECOND, LAST, GATHER><<<nblocks_, block_, 0, st_>>>(n_, stage, pc_, R, SR, dg_, F_, FS_, W_, sref_,
+                                                                     Us_, ms_, part_, ctrl_, global_dt);
+  }
+  template <bool PRECOND>
+  void update_p(int stage, bool last, int global_dt, V4* R, T* SR) {
+    if (global_dt) {  // residual already gathered (the global time step needs all of SR first)
+      if (last) update_t<PRECOND, true, false>(stage, global_dt, R, SR);
+      else update_t<PRECOND, false, false>(stage, global_dt, R, SR);
+    } else {
+      if (last) update_t<PRECOND, true, true>(stage, global_dt, R, SR);
+      else update_t<PRECOND, false, true>(stage, global_dt, R, SR);
+    }
   }
 
   struct Direct {
@@ -692,18 +707,18 @@ class EngineT final : public Engine {
         AERO_CK(cudaEventRecord(ev_join_, side_));
       }
       if (second) wrap(0, [&] { k_gradient<T><<<nblocks_, block_, 0, st_>>>(dm_, W_, gx_, gy_, ctrl_); });
-      wrap(1, [&] { launch_residual(second, last, ctrl_, fb, R, SR, global_dt); });
+      const ResidualLaunch<T> ra = residual_args(ctrl_, fb, R, SR, global_dt);
+      wrap(1, [&] { launch_face_pass(ra, cfg_.flux, second, rs_.lm != 0); });
+      if (global_dt) wrap(1, [&] { launch_gather_pass(ra, last); });
       if (stage == 0 && pending) AERO_CK(cudaStreamWaitEvent(st_, ev_join_, 0));
       if (global_dt) {
         wrap(3, [&] { k_srmax<<<1, 1024, 0, st_>>>(part_.srmax, nblocks_ * (block_ / 32), ctrl_); });
       }
       wrap(2, [&] {
         if (cfg_.precond_on) {
-          if (last) update_t<true, true>(stage, global_dt, R, SR);
-          else update_t<true, false>(stage, global_dt, R, SR);
+          update_p<true>(stage, last, global_dt, R, SR);
         } else {
-          if (last) update_t<false, true>(stage, global_dt, R, SR);
-          else update_t<false, false>(stage, global_dt, R, SR);
+          update_p<false>(stage, last, global_dt, R, SR);
         }
       });
     }

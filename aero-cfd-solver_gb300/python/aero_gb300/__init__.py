@@ -254,7 +254,9 @@ class Solver:
         self._check(self.lib.aero_time_iterations(self.h, n, int(use_graph), int(flush_l2), C.byref(ms)))
         return ms.value
 
-    KERNEL_CLASSES = ("gradient", "residual", "update", "global_dt", "symmetry_pjump", "control")
+    # face_pass: the residual face pass (and its cell pass under global time stepping);
+    # update: the RK update, which gathers the cell residual itself under local time stepping
+    KERNEL_CLASSES = ("gradient", "face_pass", "update", "global_dt", "symmetry_pjump", "control")
 
     def profile_kernels(self, n: int, flush_l2: bool = False) -> dict:
         """Summed device ms and launch counts per kernel class over n iterations."""

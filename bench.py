@@ -53,11 +53,10 @@ def algorithmic_bytes(kernel: str, n: int, slots: int, precision: str, faces: in
     once (neighbour re-reads excluded). s = bulk real size; `slots` per cell."""
     s = 4 if precision == "fp32" else 8
     slot_geo = 4 + 2 * s + s  # link, normal, area
-    if kernel == "residual":
-        # face pass + cell pass: W and gradients per cell, per face its two cell ids, normal,
-        # length and MUSCL offsets, per cell its face list, 1/vol and R, SR; the per-face
-        # flux the two passes exchange is not counted (it is not part of the algorithm)
-        return n * (4 * s + 8 * s) + faces * (8 + 3 * s + 4 * s) + n * slots * 4 + n * (s + 4 * s + s)
+    if kernel == "face":
+        # face pass: W and gradients of every cell once; per face its two cell ids, normal,
+        # length and MUSCL offsets, and the F*A (4 reals) and wave-speed term it writes
+        return n * (4 * s + 8 * s) + faces * (8 + 3 * s + 4 * s + 5 * s)
     if kernel == "gradient":  # W, slot geometry, 1/vol, gradients
         return n * (4 * s + slots * slot_geo + s + 8 * s)
     if kernel == "update":
@@ -300,9 +299,9 @@ def run_gpu_arm(args):
             state = s.get_state() if prec == "fp32" else None
             finite = bool(np.all(np.isfinite(s.get_state())))
         value = world * n * args.steps / (ms_max / 1e3) / 1e6
-        res_ms, res_n = prof["residual"]
+        res_ms, res_n = prof["face_pass"]
         avg_res = res_ms / max(res_n, 1)
-        bytes_res = algorithmic_bytes("residual", n, info["slots_per_cell"], prec, int(info["faces"]))
+        bytes_res = algorithmic_bytes("face", n, info["slots_per_cell"], prec, int(info["faces"]))
         achieved = bytes_res / (avg_res / 1e3) / 1e9
         total_prof = sum(v[0] for v in prof.values())
         results[prec] = dict(value=value, ms=ms_max, warm_ms=warm_ms, info=info, prof=prof, state=state,
@@ -372,7 +371,7 @@ def run_gpu_arm(args):
             "kernel_profile_ms_per_launch": {k: (v[0] / v[1] if v[1] else 0.0) for k, v in head["prof"].items()},
             "state_finite": head["finite"],
         },
-        "roofline": {"bound": "hbm", "kernel": "k_residual (reconstruction + flux + gather)",
+        "roofline": {"bound": "hbm", "kernel": "k_face_flux (MUSCL reconstruction + HLLC flux, one thread per face)",
                      "achieved": head["achieved"], "peak": peak, "unit": "GB/s", "frac": head["achieved"] / peak,
                      "peak_kind": peak_kind, "traffic": NCU_TRAFFIC.get((precisions[0], n)),
                      "algorithmic_bytes_per_launch": head["bytes_res"], "avg_launch_ms": head["avg_res_ms"],

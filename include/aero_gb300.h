@@ -211,8 +211,9 @@ AERO_API int aero_time_iterations(aero_ctx* ctx, int n, int use_graph, int flush
                                   double* device_ms);
 /* Per-kernel profile of n iterations, every launch between its own CUDA events.
  * ms[6] receives summed device time and launches[6] the launch count of the kernel
- * classes 0 gradient, 1 residual, 2 update, 3 global-time-step reduction,
- * 4 symmetry/pressure-jump, 5 controller. */
+ * classes 0 gradient, 1 residual face pass (and, with global time stepping, its cell
+ * pass), 2 update (which gathers the cell residual itself under local time stepping),
+ * 3 global-time-step reduction, 4 symmetry/pressure-jump, 5 controller. */
 AERO_API int aero_profile_kernels(aero_ctx* ctx, int n, int flush_l2, double* ms, int* launches);
 
 /* Make `device` the current device of the library's CUDA runtime for this host thread

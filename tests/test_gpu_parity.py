@@ -5,7 +5,10 @@ Residual tolerance, per cell c and component k, relative to the flux scale
 S_ck = sum over the cell's faces of |F_k A| computed by the oracle (the residual itself
 cancels towards zero, so it is no usable denominator):
   FP64 path vs FP64 oracle               : |dR| <= 1e-12 S   (spectral radius: 1e-12 relative)
-  FP32 path vs float reference (golden)  : |dR| <= 2e-5 S    (the device contracts multiply-adds)
+  FP32 path vs FP64 oracle and vs float reference (golden): |dR| <= 5e-5 S, where the
+                                           reference's own float path sits up to 3e-5 S
+                                           from FP64 (the device contracts multiply-adds and
+                                           divides / takes roots to 2 ulp)
 Whole runs compare histories and states at the tolerances given in each test."""
 
 import json
@@ -92,6 +95,11 @@ def test_residual_fp64_vs_oracle_on_golden_states(golden_meshes, golden_residual
 
 
 def test_residual_fp32_vs_reference_golden(golden_meshes, golden_residuals):
+    """The FP32 residual against the reference's own float residual (the golden fixture) and
+    against exact (FP64) arithmetic, both within 5e-5 of the flux scale: float-class
+    agreement, since the reference's float path itself deviates from FP64 by up to 3e-5 of
+    the flux scale on these states (the device rounds differently: contracted multiply-adds,
+    division and square root to 2 ulp)."""
     data, meta = golden_residuals
     mesh = golden_mesh(golden_meshes, "ogrid_32x4")
     for m in meta:
@@ -105,7 +113,11 @@ def test_residual_fp32_vs_reference_golden(golden_meshes, golden_residuals):
         ref_r = data[m["key"] + "/r"].astype(np.float64)
         ref_sr = data[m["key"] + "/sr"].astype(np.float64)
         fs = op.OracleSolver(op.MODE_FLOAT, mesh, case).residual(u, *args, with_scale=True)[4]
-        assert flux_err(r, ref_r, fs) <= 2e-5, m["key"]
+        r64 = op.OracleSolver(op.MODE_DOUBLE, mesh, case).residual(u, *args)[0]
+        ref_dev = flux_err(ref_r, r64, fs)
+        assert ref_dev <= 3e-5, m["key"]  # the reference's own float rounding on this state
+        assert flux_err(r, r64, fs) <= 5e-5, (m["key"], flux_err(r, r64, fs), ref_dev)
+        assert flux_err(r, ref_r, fs) <= 5e-5, m["key"]
         np.testing.assert_allclose(sr, ref_sr, rtol=2e-6, err_msg=m["key"])
 
 

@@ -43,9 +43,10 @@ CASE = dict(mach=0.8, aoa_deg=1.25, flux=1, limiter=1, precond_farfield_bc=1, cf
             residual_reduction_target=0.0)
 STARTUP = 25  # first-order start-up iterations run untimed before warm-up
 
-# DRAM traffic per launch of the residual kernel from ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum), keyed by (precision, n_cells); see profiles/.
-NCU_TRAFFIC = {}
+# DRAM traffic per launch of the face pass from one ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum; the launch's writes stay in L2), keyed by (precision, n_cells);
+# profiles/kernels_c2_512x128.md gives the command.
+NCU_TRAFFIC = {("fp32", 131072): 13413120, ("fp64", 131072): 25307904}
 
 
 def algorithmic_bytes(kernel: str, n: int, slots: int, precision: str, faces: int = 0) -> float:

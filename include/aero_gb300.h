@@ -227,9 +227,9 @@ AERO_API int aero_select_device(int device);
  * Computes what aero_residual computes (gradients only internally), but takes DEVICE
  * pointers owned by the caller: conserved_dev [N][5] and residual_dev [N][5] double in the
  * original cell order, spectral_radius_dev [N] double. It allocates nothing: its working
- * arrays live in one fixed device array of the library (about 8.9 MB, held by every GPU that
- * loads the library until exit), so meshes above 65,536 cells are rejected with
- * AERO_ERR_INVALID. The work is queued on `stream` (null: the context's stream) and the call
+ * arrays live in one fixed device array of the library (about 16.8 MB, held by every GPU that
+ * loads the library until exit), so meshes above 65,536 cells or 196,608 faces are rejected
+ * with AERO_ERR_INVALID. The work is queued on `stream` (null: the context's stream) and the call
  * returns without waiting. The first call on each device looks up that array's address;
  * make it before any stream capture. All calls on a device share the array and it keeps
  * the last call's contents: calls whose work overlaps on the GPU race and must be ordered

@@ -14,14 +14,18 @@ namespace aero {
 // Face pass. FLUX 0 Rusanov / 1 HLLC; SECOND: MUSCL with the cell gradients; LM: any
 // low-Mach feature on. fb[0] / fb[1] count first-order and diffusive fallbacks.
 template <class T, int FLUX, bool SECOND, bool LM>
-__global__ void __launch_bounds__(256) k_face_flux(DevFaces<T> f, FaceParams<T> fp,
+__global__ void __launch_bounds__(256) k_face_flux(DevFaces<T> f, Cases<T> cs,
                                                    const typename Vec<T>::v4* __restrict__ W,
                                                    const typename Vec<T>::v4* __restrict__ gx,
                                                    const typename Vec<T>::v4* __restrict__ gy,
                                                    typename Vec<T>::v4* __restrict__ F, T* __restrict__ FS,
-                                                   const Ctrl* __restrict__ ctrl, int* __restrict__ fb) {
+                                                   int* __restrict__ fb_all) {
+  const int2 bd = cs.blk[blockIdx.x];  // face blocks: (case, end of the case's faces)
+  const Ctrl* ctrl = cs.ctrl + bd.x;
+  int* fb = fb_all + 4 * bd.x;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (ctrl->done) return;
+  FaceParams<T> fp = cs.fp[bd.x];
   if (LM) {
     fp.as_fix = ctrl->as_fix;
     if constexpr (sizeof(T) == 4) {
@@ -35,7 +39,7 @@ __global__ void __launch_bounds__(256) k_face_flux(DevFaces<T> f, FaceParams<T> 
     }
   }
   int fo = 0, df = 0;
-  if (i < f.nf) {
+  if (i < bd.y) {
     const int2 oc = f.cells[i];
     const int o = oc.x, b = oc.y;
     const auto nd = f.nrm[i];
@@ -113,13 +117,13 @@ __global__ void __launch_bounds__(256) k_face_flux(DevFaces<T> f, FaceParams<T> 
 template <class T, bool NORMS>
 __global__ void __launch_bounds__(256) k_gather(DevGather<T> g, const typename Vec<T>::v4* __restrict__ F,
                                                 const T* __restrict__ FS, typename Vec<T>::v4* __restrict__ R,
-                                                T* __restrict__ SR, Partials part, const Ctrl* __restrict__ ctrl,
-                                                int global_dt) {
+                                                T* __restrict__ SR, Partials part, Cases<T> cs, int global_dt) {
+  const int2 bd = cs.blk[blockIdx.x];  // cell blocks
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ctrl->done) return;
-  T nl1 = T(0), nl2 = T(0), nlinf = T(0);
+  if (cs.ctrl[bd.x].done) return;
+  T nq[kNorm] = {T(0), T(0), T(0), T(0)};
   double srm = 0.0;
-  if (c < g.n) {
+  if (c < bd.y) {
     T r[4], sr;
     gather_cell<T>(g, F, FS, c, r, &sr);
     typename Vec<T>::v4 out;
@@ -127,31 +131,32 @@ __global__ void __launch_bounds__(256) k_gather(DevGather<T> g, const typename V
     R[c] = out;
     SR[c] = sr;
     if (global_dt) srm = double(smax(sr, Kn<T>::wave_floor));
-    if (NORMS) norm_terms<T>(r, g.inv_vol[c], &nl1, &nl2, &nlinf);
+    if (NORMS) norm_terms<T>(r, g.inv_vol[c], nq);
   }
   if (global_dt) {
     srm = warp_max(srm);
     if ((threadIdx.x & 31) == 0) part.srmax[blockIdx.x * ((blockDim.x + 31) >> 5) + (threadIdx.x >> 5)] = srm;
   }
-  if (NORMS) block_norms<T>(nl1, nl2, nlinf, part);
+  if (NORMS) block_norms<T>(nq, part);
 }
 
-// Launch geometry and buffers of one residual evaluation.
+// Launch geometry and buffers of one residual evaluation. faces.nf and gather.n are the
+// packed (block-padded) face and cell counts of all cases.
 template <class T>
 struct ResidualLaunch {
   int block;
   cudaStream_t st;
   DevFaces<T> faces;
   DevGather<T> gather;
-  FaceParams<T> fp;
+  Cases<T> face_cases;  // blk over face blocks
+  Cases<T> cell_cases;  // blk over cell blocks
   const typename Vec<T>::v4 *W, *gx, *gy;
   typename Vec<T>::v4* F;  // per face
   T* FS;                   // per face
   typename Vec<T>::v4* R;  // per cell
   T* SR;                   // per cell
   Partials part;
-  const Ctrl* ctrl;
-  int* fb;
+  int* fb;                 // [case][2]: fallback counters, stride 4 per case
   int global_dt;
 };
 
@@ -159,7 +164,7 @@ template <class T, int FLUX, bool SECOND, bool LM>
 void launch_face_flux_t(const ResidualLaunch<T>& a) {
   const int grid = (a.faces.nf + a.block - 1) / a.block;
   k_face_flux<T, FLUX, SECOND, LM>
-      <<<grid, a.block, 0, a.st>>>(a.faces, a.fp, a.W, a.gx, a.gy, a.F, a.FS, a.ctrl, a.fb);
+      <<<grid, a.block, 0, a.st>>>(a.faces, a.face_cases, a.W, a.gx, a.gy, a.F, a.FS, a.fb);
 }
 
 // Face pass, dispatched on the flux, order and low-Mach switches.
@@ -189,9 +194,11 @@ template <class T>
 void launch_gather_pass(const ResidualLaunch<T>& a, bool norms) {
   const int grid = (a.gather.n + a.block - 1) / a.block;
   if (norms) {
-    k_gather<T, true><<<grid, a.block, 0, a.st>>>(a.gather, a.F, a.FS, a.R, a.SR, a.part, a.ctrl, a.global_dt);
+    k_gather<T, true><<<grid, a.block, 0, a.st>>>(a.gather, a.F, a.FS, a.R, a.SR, a.part, a.cell_cases,
+                                                   a.global_dt);
   } else {
-    k_gather<T, false><<<grid, a.block, 0, a.st>>>(a.gather, a.F, a.FS, a.R, a.SR, a.part, a.ctrl, a.global_dt);
+    k_gather<T, false><<<grid, a.block, 0, a.st>>>(a.gather, a.F, a.FS, a.R, a.SR, a.part, a.cell_cases,
+                                                    a.global_dt);
   }
 }
 

@@ -70,6 +70,8 @@ struct alignas(16) Ctrl {
   int stage_b_progress, pjump_below, freeze, pad0;
   float cfl_f, stab_f, as_fmin_f, as_ramp_f;  // float copies of the schedule values (FP32 kernels)
   double sr_max;  // global max of max(SR, floor) for global time stepping
+  double initial_l2rho;  // first density-residual L2 (< 0: not yet seen)
+  double pad1;
 };
 
 // Run constants of the controller (euler_solver.cpp:463-566 resolved on the host).
@@ -79,13 +81,16 @@ struct CtrlConfig {
   int startup_first_order, min_iterations, window, staged;
   int st_a_min, st_a_max, pj_hold, freeze_iters;
   int as_fix_cfg, n_blocks, pjump_blocks, n_wall_blocks;
-  int bulk_f32;  // partials hold float norms and float monitor bits
+  int bulk_f32;    // partials hold float norms and float monitor bits
+  int block_base;  // the case's first cell block (its partials are blocks [base, base + n_blocks))
+  int wall_base;   // the case's first slot in Partials::wall / wall_f
   double cfl_start, cfl_max, stab_start, stab_target, as_fmin;
   double residual_target, stab_tol, drift_tol;
   double st_fmin_high, st_fmin_mid, st_fmin_low;
   double pj_target, pj_spike, cfl_drop, cfl_restore, cfl_min_scale;
   double p_inf, q_inf, s_ref, chord, cos_a, sin_a, x_ref, y_ref, pressure_ref, gamma;
   double rho_inf, u_inf, v_inf;
+  double rho_l2_target;  // > 0: also stop when the density-residual L2 ratio falls to it
 };
 
 // Precondition constants in double for the residual preconditioner (preconditioning.cpp:51-76).
@@ -199,8 +204,8 @@ struct DevGather {
 // Per-block partial results reduced by the control kernel in a fixed order. Quantity-major
 // ([k][block]) so that the control warp reads them coalesced.
 struct Partials {
-  double* norms;   // [3][nb]: l1, l2 sum, linf (FP64)
-  float* norms_f;  // [3][nb]: the same in float (FP32)
+  double* norms;   // [kNorm][nb]: l1, l2 sum, linf, density l2 sum (FP64)
+  float* norms_f;  // [kNorm][nb]: the same in float (FP32)
   long long* mon;  // [kMon][nb]: maxima of |p - p_inf| (domain, wall-adjacent) and the far-field
                    // deviations |dp|, |drho|, |du|, |dv|, formed in the bulk type; stored as bit
                    // patterns (double, or float zero-extended) so that maxima are integer maxima
@@ -210,6 +215,7 @@ struct Partials {
   double* srmax;   // [blocks * warps per block]: max of max(SR, floor)
   int nb, nwb;     // blocks of the cell grid, blocks holding wall cells
 };
+constexpr int kNorm = 4;
 constexpr int kMon = 6;
 constexpr int kWall = 12;  // snx sny fxa fya fxg fyg ma mg | un_max cp_hi -cp_lo cp_bad
 
@@ -226,10 +232,28 @@ struct MonitorSet {
   const double* warea;
   const double* wx;
   const double* wy;
-  const int* block_slot;       // per update block: its slot in Partials::wall, or -1
+  const int* block_slot;       // per cell block: its slot in Partials::wall, or -1
+  const float *wnx_f, *wny_f, *warea_f, *wx_f, *wy_f;  // float copies (FP32)
+};
+
+// Free-stream and reference constants of one case for the monitors and forces.
+struct MonitorConsts {
   double p_inf, rho_inf, u_inf, v_inf, q_inf, x_ref, y_ref, gamma;
   float p_inf_f, rho_inf_f, u_inf_f, v_inf_f, q_inf_f, x_ref_f, y_ref_f;  // float copies (FP32)
-  const float *wnx_f, *wny_f, *warea_f, *wx_f, *wy_f;                  // float copies (FP32)
+  int sym_interval;  // AoA-0 symmetry every this many iterations, 0 = off
+};
+
+// The cases of a launch. Cases are packed one after another, each padded to whole blocks,
+// so every block belongs to one case: blk[blockIdx.x] = (case, end of that case's range)
+// over cells or faces. Per-case parameters are arrays indexed by the case. A single case
+// is a batch of one.
+template <class T>
+struct Cases {
+  const int2* blk;
+  Ctrl* ctrl;
+  const FaceParams<T>* fp;
+  const PrecondD* pc;
+  const MonitorConsts* mc;
 };
 
 // Conserved state of the cells. FP64 holds it as double4; FP32 as a float-float pair: hi is
@@ -360,37 +384,40 @@ __device__ __forceinline__ void gather_cell(const DevGather<T>& g, const typenam
   }
 }
 
-// Residual-norm terms of one cell (euler_solver.cpp:309-339): |R|/V summed, squared, max.
+// Residual-norm terms of one cell (euler_solver.cpp:309-339): |R|/V summed, squared, max;
+// q[3] is the density component squared (the batched sweep's stop rule).
 template <class T>
-__device__ __forceinline__ void norm_terms(const T (&r)[4], T inv, T* l1, T* l2, T* linf) {
+__device__ __forceinline__ void norm_terms(const T (&r)[4], T inv, T (&q)[kNorm]) {
   const T v0 = r[0] * inv, v1 = r[1] * inv, v2 = r[2] * inv, v3 = r[3] * inv;
   const T a0 = fabs(v0), a1 = fabs(v1), a2 = fabs(v2), a3 = fabs(v3);
-  *l1 = ((a0 + a1) + a2) + a3;
-  *l2 = ((v0 * v0 + v1 * v1) + v2 * v2) + v3 * v3;
-  *linf = smax(smax(smax(a0, a1), a2), a3);
+  q[0] = ((a0 + a1) + a2) + a3;
+  q[1] = ((v0 * v0 + v1 * v1) + v2 * v2) + v3 * v3;
+  q[2] = smax(smax(smax(a0, a1), a2), a3);
+  q[3] = v0 * v0;
 }
 
 // Block partials of the norm terms in T into Partials::norms / norms_f; the control kernel
 // sums the blocks in double (FP32: float-float). Called by every thread of the block.
 template <class T>
-__device__ void block_norms(T nl1, T nl2, T nlinf, Partials part) {
-  __shared__ T shn[3][32];
-  nl1 = warp_sum_t(nl1);
-  nl2 = warp_sum_t(nl2);
-  nlinf = warp_max_t(nlinf);
+__device__ void block_norms(T (&q)[kNorm], Partials part) {
+  __shared__ T shn[kNorm][32];
+  q[0] = warp_sum_t(q[0]);
+  q[1] = warp_sum_t(q[1]);
+  q[2] = warp_max_t(q[2]);
+  q[3] = warp_sum_t(q[3]);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
   if (lane == 0) {
-    shn[0][wid] = nl1;
-    shn[1][wid] = nl2;
-    shn[2][wid] = nlinf;
+#pragma unroll
+    for (int k = 0; k < kNorm; ++k) shn[k][wid] = q[k];
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    T a = T(0), b = T(0), mx = T(0);
+    T a = T(0), b = T(0), mx = T(0), rr = T(0);
     for (int i = 0; i < nw; ++i) {
       a += shn[0][i];
       b += shn[1][i];
       mx = smax(mx, shn[2][i]);
+      rr += shn[3][i];
     }
     T* out;
     if constexpr (sizeof(T) == 4) {
@@ -401,6 +428,7 @@ __device__ void block_norms(T nl1, T nl2, T nlinf, Partials part) {
     out[blockIdx.x] = a;
     out[part.nb + blockIdx.x] = b;
     out[2 * part.nb + blockIdx.x] = mx;
+    out[3 * part.nb + blockIdx.x] = rr;
   }
 }
 
@@ -412,13 +440,14 @@ __device__ void block_norms(T nl1, T nl2, T nlinf, Partials part) {
 // the control kernel. Must be called by every thread of the block; `valid` is false past the
 // mesh.
 template <class T>
-__device__ void block_monitors(bool valid, const Prim<T>& w, int c, const MonitorSet& ms, Partials part) {
+__device__ void block_monitors(bool valid, const Prim<T>& w, int c, const MonitorSet& ms, const MonitorConsts& mc,
+                               Partials part) {
   constexpr bool kF = sizeof(T) == 4;
   constexpr T kLow = kF ? T(-3.0e38f) : T(-1.0e308);
   __shared__ T shf[kMon][32];
   __shared__ T shd[kWall][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-  const T p_inf = kF ? T(ms.p_inf_f) : T(ms.p_inf);
+  const T p_inf = kF ? T(mc.p_inf_f) : T(mc.p_inf);
   T mon[kMon] = {T(0), T(0), T(0), T(0), T(0), T(0)};
   unsigned char fl = 0;
   if (valid) {
@@ -428,9 +457,9 @@ __device__ void block_monitors(bool valid, const Prim<T>& w, int c, const Monito
     if (fl & 1) mon[1] = dp;
     if (fl & 2) {
       mon[2] = dp;
-      mon[3] = fabs(w.r - (kF ? T(ms.rho_inf_f) : T(ms.rho_inf)));
-      mon[4] = fabs(w.u - (kF ? T(ms.u_inf_f) : T(ms.u_inf)));
-      mon[5] = fabs(w.v - (kF ? T(ms.v_inf_f) : T(ms.v_inf)));
+      mon[3] = fabs(w.r - (kF ? T(mc.rho_inf_f) : T(mc.rho_inf)));
+      mon[4] = fabs(w.u - (kF ? T(mc.u_inf_f) : T(mc.u_inf)));
+      mon[5] = fabs(w.v - (kF ? T(mc.v_inf_f) : T(mc.v_inf)));
     }
   }
 #pragma unroll
@@ -449,8 +478,8 @@ __device__ void block_monitors(bool valid, const Prim<T>& w, int c, const Monito
       const T* wa = kF ? reinterpret_cast<const T*>(ms.warea_f) : reinterpret_cast<const T*>(ms.warea);
       const T* wx = kF ? reinterpret_cast<const T*>(ms.wx_f) : reinterpret_cast<const T*>(ms.wx);
       const T* wy = kF ? reinterpret_cast<const T*>(ms.wy_f) : reinterpret_cast<const T*>(ms.wy);
-      const T x_ref = kF ? T(ms.x_ref_f) : T(ms.x_ref), y_ref = kF ? T(ms.y_ref_f) : T(ms.y_ref);
-      const T q_inf = kF ? T(ms.q_inf_f) : T(ms.q_inf);
+      const T x_ref = kF ? T(mc.x_ref_f) : T(mc.x_ref), y_ref = kF ? T(mc.y_ref_f) : T(mc.y_ref);
+      const T q_inf = kF ? T(mc.q_inf_f) : T(mc.q_inf);
       const int first = ms.wall_first[c], cnt = fl >> 2;
       const T p = w.p, gp = w.p - p_inf;
       for (int j = first; j < first + cnt; ++j) {
@@ -621,10 +650,10 @@ __device__ __forceinline__ void cell_gradient(const DevMesh<T>& m, const typenam
 template <class T>
 __global__ void __launch_bounds__(256) k_gradient(DevMesh<T> m, const typename Vec<T>::v4* __restrict__ W,
                                                   typename Vec<T>::v4* __restrict__ gx,
-                                                  typename Vec<T>::v4* __restrict__ gy,
-                                                  const Ctrl* __restrict__ ctrl) {
+                                                  typename Vec<T>::v4* __restrict__ gy, Cases<T> cs) {
+  const int2 bd = cs.blk[blockIdx.x];
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= m.n || ctrl->done) return;
+  if (c >= bd.y || cs.ctrl[bd.x].done) return;
   typename Vec<T>::v4 ox, oy;
   cell_gradient<T>(m, W, c, &ox, &oy);
   gx[c] = ox;
@@ -646,11 +675,13 @@ __device__ __forceinline__ void muscl_var(int lim, T qo, T qn, T gox, T goy, T g
 }
 
 // Global time step (time_integrator.cpp:45-56): maximum over per-warp maxima of max(SR, floor).
-static __global__ void k_srmax(const double* __restrict__ srmax, int n, Ctrl* ctrl) {
+// One block per case; case k's warps are [first[k], first[k+1]).
+static __global__ void k_srmax(const double* __restrict__ srmax, const int* __restrict__ first, Ctrl* ctrls) {
   __shared__ double shm[32];
+  Ctrl* ctrl = ctrls + blockIdx.x;
   if (ctrl->done) return;
   double m = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) m = smax(m, srmax[i]);
+  for (int i = first[blockIdx.x] + threadIdx.x; i < first[blockIdx.x + 1]; i += blockDim.x) m = smax(m, srmax[i]);
   m = block_max(m, shm);
   if (threadIdx.x == 0) ctrl->sr_max = m;
 }
@@ -685,18 +716,22 @@ __device__ __forceinline__ bool positivity_safe(const Cons<float>& f, float gm1)
 // residual) and forms the residual-norm partials.
 // ---------------------------------------------------------------------------------------
 template <class T, bool PRECOND, bool LAST, bool GATHER>
-__global__ void __launch_bounds__(256) k_update(int n, int stage, PrecondD pc, typename Vec<T>::v4* __restrict__ R,
+__global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename Vec<T>::v4* __restrict__ R,
                                                 T* __restrict__ SR, DevGather<T> g,
                                                 const typename Vec<T>::v4* __restrict__ F, const T* __restrict__ FS,
                                                 typename Vec<T>::v4* __restrict__ W, StateRef U,
                                                 typename Vec<T>::v4* __restrict__ Us, MonitorSet ms, Partials part,
-                                                Ctrl* __restrict__ ctrl, int global_dt) {
+                                                int global_dt) {
+  const int2 bd = cs.blk[blockIdx.x];
+  Ctrl* ctrl = cs.ctrl + bd.x;
+  const PrecondD& pc = cs.pc[bd.x];
+  const int n = bd.y;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (ctrl->done) return;
   bool bad = false;
   Cons<double> s{1.0, 0.0, 0.0, 1.0};
   Prim<T> w{T(1), T(0), T(0), T(1)};
-  T nl1 = T(0), nl2 = T(0), nlinf = T(0);
+  T nq[kNorm] = {T(0), T(0), T(0), T(0)};
   if (c < n) {
     // the cell's own state first, so these loads overlap the gather's
     typename Vec<T>::v4 st_hi{}, st_lo{}, st_us{};
@@ -721,7 +756,7 @@ __global__ void __launch_bounds__(256) k_update(int n, int stage, PrecondD pc, t
         o.x = r0; o.y = r1; o.z = r2; o.w = r3;
         R[c] = o;
         SR[c] = src;
-        norm_terms<T>(rr, g.inv_vol[c], &nl1, &nl2, &nlinf);
+        norm_terms<T>(rr, g.inv_vol[c], nq);
       }
     } else {
       const auto r4 = R[c];
@@ -834,8 +869,8 @@ __global__ void __launch_bounds__(256) k_update(int n, int stage, PrecondD pc, t
   }
   if (LAST) {
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&ctrl->nonfinite, 1);
-    if (GATHER) block_norms<T>(nl1, nl2, nlinf, part);
-    block_monitors<T>(c < n, w, c, ms, part);
+    if (GATHER) block_norms<T>(nq, part);
+    block_monitors<T>(c < n, w, c, ms, cs.mc[bd.x], part);
   }
 }
 
@@ -843,10 +878,14 @@ __global__ void __launch_bounds__(256) k_update(int n, int stage, PrecondD pc, t
 // v is zeroed through the primitive variables. Applied after the last stage; it redoes the
 // last stage's max |p - p_inf| partials and non-finite check on the symmetrised state.
 template <class T>
-__global__ void __launch_bounds__(256) k_symmetry(int n, int interval, double gamma, StateRef U,
-                                                  typename Vec<T>::v4* __restrict__ W, MonitorSet ms,
-                                                  Partials part, Ctrl* __restrict__ ctrl) {
-  if (ctrl->done) return;
+__global__ void __launch_bounds__(256) k_symmetry(Cases<T> cs, StateRef U, typename Vec<T>::v4* __restrict__ W,
+                                                  MonitorSet ms, Partials part) {
+  const int2 bd = cs.blk[blockIdx.x];
+  Ctrl* ctrl = cs.ctrl + bd.x;
+  const double gamma = cs.mc[bd.x].gamma;
+  const int interval = cs.mc[bd.x].sym_interval;
+  const int n = bd.y;
+  if (ctrl->done || interval <= 0) return;
   if (((ctrl->iter + 1) % interval) != 0) return;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   bool bad = false;
@@ -864,19 +903,21 @@ __global__ void __launch_bounds__(256) k_symmetry(int n, int interval, double ga
     bad = !finite4(s.r, s.ru, s.rv, s.rE) || !finite4(wt.r, wt.u, wt.v, wt.p);
   }
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&ctrl->nonfinite, 1);
-  block_monitors<T>(c < n, wt, c, ms, part);
+  block_monitors<T>(c < n, wt, c, ms, cs.mc[bd.x], part);
 }
 
 // Pressure-jump energy over interior faces (euler_solver.cpp:1027-1063), per owning cell.
 template <class T>
 __global__ void __launch_bounds__(256) k_pjump(DevMesh<T> m, StateRef U,
-                                               const unsigned char* __restrict__ flags, double gamma,
-                                               Partials part, const Ctrl* __restrict__ ctrl) {
+                                               const unsigned char* __restrict__ flags, Cases<T> cs,
+                                               Partials part) {
   __shared__ double shm[32 * 4];
+  const int2 bd = cs.blk[blockIdx.x];
+  const double gamma = cs.mc[bd.x].gamma;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ctrl->done) return;
+  if (cs.ctrl[bd.x].done) return;
   double v[4] = {0.0, 0.0, 0.0, 0.0};
-  if (c < m.n) {
+  if (c < bd.y) {
     const double pc = cons_to_prim(load_state<T>(U, c), gamma).p;
     for (int k = 0; k < m.d; ++k) {
       const int link = m.link[k * m.n + c];
@@ -914,10 +955,11 @@ struct Record {
   double wall_un, wall_mass_flux, cp_min, cp_max;
   double ff_dp, ff_drho, ff_du, ff_dv;
   int cp_nonfinite, action;
+  double rho_ratio;
 };
 
 // Serial part of the controller (lane 0), on the shared copy of the controller state.
-__device__ inline void control_serial(const CtrlConfig& cc, const double (&a)[3], const double (&mon)[kMon],
+__device__ inline void control_serial(const CtrlConfig& cc, const double (&a)[kNorm], const double (&mon)[kMon],
                                       const double (&pj)[4], const double (&wv)[kWall], Ctrl* sp,
                                       Record* __restrict__ recs, int rec_cap, int* fb) {
   const double* fsum = wv;
@@ -967,6 +1009,11 @@ __device__ inline void control_serial(const CtrlConfig& cc, const double (&a)[3]
   if (s.initial_l2 < 0.0) s.initial_l2 = bl2;
   const double ratio = bl2 / smax(s.initial_l2, 1.0e-20);
   r.ratio = ratio;
+  // density-residual L2 ratio (the batched sweep's per-case stop rule)
+  const double l2rho = smax(sqrt(a[3] / double(cc.n_cells > 0 ? cc.n_cells : 1)), 1.0e-20);
+  if (s.initial_l2rho < 0.0) s.initial_l2rho = l2rho;
+  const double rho_ratio = l2rho / smax(s.initial_l2rho, 1.0e-20);
+  r.rho_ratio = rho_ratio;
   if (s.prev_l2 > 0.0) {
     if (l2 > s.prev_l2 * 1.05) {
       s.cfl_scale = smax(s.cfl_scale * 0.65, 0.05);
@@ -1097,7 +1144,9 @@ __device__ inline void control_serial(const CtrlConfig& cc, const double (&a)[3]
   r.cfl_scale = s.cfl_scale;
   if (stable) r.flags |= 1;
   if (dstable) r.flags |= 2;
-  const bool conv = (s.iter + 1 >= cc.min_iterations) && !(ratio > cc.residual_target) && stable && dstable;
+  const bool conv = (s.iter + 1 >= cc.min_iterations) &&
+                    ((!(ratio > cc.residual_target) && stable && dstable) ||
+                     (cc.rho_l2_target > 0.0 && !(rho_ratio > cc.rho_l2_target)));
   if (conv) r.flags |= 4;
   if (nonfinite) r.flags |= 16;
   const int slot = s.iter - s.rec_base;
@@ -1127,13 +1176,19 @@ __device__ __forceinline__ long long warp_max_bits(long long x) {
 // arithmetic at a small fraction of its float rate.
 constexpr int kCtlThreads = 128;
 static_assert(sizeof(Ctrl) % 16 == 0, "Ctrl is copied in 16-byte words");
-static __global__ void __launch_bounds__(kCtlThreads) k_control(CtrlConfig cc, Partials part,
-                                                                Ctrl* __restrict__ ctrl,
-                                                                Record* __restrict__ recs, int rec_cap,
-                                                                int* __restrict__ fb) {
+// One block per case: ccs[case], ctrls[case], records recs[case * rec_cap ...], fallback
+// counters fb[4 * case + 0/1] (fb already offset by the iteration's parity).
+static __global__ void __launch_bounds__(kCtlThreads) k_control(const CtrlConfig* __restrict__ ccs, Partials part,
+                                                                Ctrl* __restrict__ ctrls,
+                                                                Record* __restrict__ recs_all, int rec_cap,
+                                                                int* __restrict__ fb_all) {
   constexpr int kWarps = kCtlThreads / 32;
+  const CtrlConfig cc = ccs[blockIdx.x];
+  Ctrl* ctrl = ctrls + blockIdx.x;
+  Record* recs = recs_all + static_cast<size_t>(blockIdx.x) * rec_cap;
+  int* fb = fb_all + 4 * blockIdx.x;
   __shared__ Ctrl sc;
-  __shared__ double s_sum[kWarps][2 + 4];   // l1, l2 sum, pressure-jump sums
+  __shared__ double s_sum[kWarps][3 + 4];   // l1, l2 sum, density l2 sum, pressure-jump sums
   __shared__ long long s_max[kWarps][1 + kMon];  // linf, monitors (bit patterns)
   __shared__ double s_wall[kWarps][kWall];
   if (ctrl->done) return;
@@ -1144,50 +1199,58 @@ static __global__ void __launch_bounds__(kCtlThreads) k_control(CtrlConfig cc, P
     int4* dst = reinterpret_cast<int4*>(&sc);
     for (int i = tid; i < kWords; i += kCtlThreads) dst[i] = src[i];
   }
-  const int nb = cc.n_blocks;
-  double s1 = 0.0, s2 = 0.0;
+  const int nb = cc.n_blocks;      // this case's blocks: bb .. bb + nb - 1
+  const int bb = cc.block_base;
+  const int st = part.nb;          // quantity stride of the block partials
+  double s1 = 0.0, s2 = 0.0, s3 = 0.0;
   long long mx[1 + kMon] = {0, 0, 0, 0, 0, 0, 0};
   if (cc.bulk_f32) {
     // float block partials summed in float-float, then one conversion per warp
-    float h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;
+    float h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f, h3 = 0.f, l3 = 0.f;
 #pragma unroll 2
-    for (int b = tid; b < nb; b += kCtlThreads) {
+    for (int b = bb + tid; b < bb + nb; b += kCtlThreads) {
       ff_add(h1, l1, part.norms_f[b], &h1, &l1);
-      ff_add(h2, l2, part.norms_f[nb + b], &h2, &l2);
-      mx[0] = max_bits(mx[0], static_cast<long long>(__float_as_uint(part.norms_f[2 * nb + b])));
+      ff_add(h2, l2, part.norms_f[st + b], &h2, &l2);
+      ff_add(h3, l3, part.norms_f[3 * st + b], &h3, &l3);
+      mx[0] = max_bits(mx[0], static_cast<long long>(__float_as_uint(part.norms_f[2 * st + b])));
 #pragma unroll
-      for (int k = 0; k < kMon; ++k) mx[k + 1] = max_bits(mx[k + 1], part.mon[k * nb + b]);
+      for (int k = 0; k < kMon; ++k) mx[k + 1] = max_bits(mx[k + 1], part.mon[k * st + b]);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const float a = __shfl_xor_sync(0xffffffffu, h1, o), b = __shfl_xor_sync(0xffffffffu, l1, o);
       const float c = __shfl_xor_sync(0xffffffffu, h2, o), d = __shfl_xor_sync(0xffffffffu, l2, o);
+      const float e = __shfl_xor_sync(0xffffffffu, h3, o), f = __shfl_xor_sync(0xffffffffu, l3, o);
       ff_add2(h1, l1, a, b, &h1, &l1);
       ff_add2(h2, l2, c, d, &h2, &l2);
+      ff_add2(h3, l3, e, f, &h3, &l3);
     }
     if (lane == 0) {
       s1 = double(h1) + double(l1);
       s2 = double(h2) + double(l2);
+      s3 = double(h3) + double(l3);
     }
   } else {
 #pragma unroll 2
-    for (int b = tid; b < nb; b += kCtlThreads) {
+    for (int b = bb + tid; b < bb + nb; b += kCtlThreads) {
       s1 += part.norms[b];
-      s2 += part.norms[nb + b];
-      mx[0] = max_bits(mx[0], __double_as_longlong(part.norms[2 * nb + b]));
+      s2 += part.norms[st + b];
+      s3 += part.norms[3 * st + b];
+      mx[0] = max_bits(mx[0], __double_as_longlong(part.norms[2 * st + b]));
 #pragma unroll
-      for (int k = 0; k < kMon; ++k) mx[k + 1] = max_bits(mx[k + 1], part.mon[k * nb + b]);
+      for (int k = 0; k < kMon; ++k) mx[k + 1] = max_bits(mx[k + 1], part.mon[k * st + b]);
     }
     s1 = warp_sum(s1);
     s2 = warp_sum(s2);
+    s3 = warp_sum(s3);
   }
 #pragma unroll
   for (int k = 0; k < 1 + kMon; ++k) mx[k] = warp_max_bits(mx[k]);
   double pj[4] = {0.0, 0.0, 0.0, 0.0};
   if (cc.pjump_blocks > 0) {
-    for (int b = tid; b < cc.pjump_blocks; b += kCtlThreads) {
+    for (int b = bb + tid; b < bb + cc.pjump_blocks; b += kCtlThreads) {
 #pragma unroll
-      for (int k = 0; k < 4; ++k) pj[k] += part.pjump[k * nb + b];
+      for (int k = 0; k < 4; ++k) pj[k] += part.pjump[k * st + b];
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) pj[k] = warp_sum(pj[k]);
@@ -1198,11 +1261,15 @@ static __global__ void __launch_bounds__(kCtlThreads) k_control(CtrlConfig cc, P
   const int nwb = cc.n_wall_blocks;
   auto wall_init = [](int k) { return (k == 9 || k == 10) ? -1.0e308 : 0.0; };
   auto wall_comb = [](int k, double acc, double x) { return (k >= 8 && k <= 10) ? smax(acc, x) : acc + x; };
-  auto wall_at = [&](int i) { return cc.bulk_f32 ? double(part.wall_f[i]) : part.wall[i]; };
+  const int wb = cc.wall_base, wst = part.nwb;
+  auto wall_at = [&](int k, int b) {
+    const int i = k * wst + wb + b;
+    return cc.bulk_f32 ? double(part.wall_f[i]) : part.wall[i];
+  };
   if (nwb <= 32) {
     if (tid < kWall) {
       double acc = wall_init(tid);
-      for (int b = 0; b < nwb; ++b) acc = wall_comb(tid, acc, wall_at(tid * nwb + b));
+      for (int b = 0; b < nwb; ++b) acc = wall_comb(tid, acc, wall_at(tid, b));
       s_wall[0][tid] = acc;
     }
   } else {
@@ -1211,7 +1278,7 @@ static __global__ void __launch_bounds__(kCtlThreads) k_control(CtrlConfig cc, P
     for (int k = 0; k < kWall; ++k) wv[k] = wall_init(k);
     for (int b = tid; b < nwb; b += kCtlThreads) {
 #pragma unroll
-      for (int k = 0; k < kWall; ++k) wv[k] = wall_comb(k, wv[k], wall_at(k * nwb + b));
+      for (int k = 0; k < kWall; ++k) wv[k] = wall_comb(k, wv[k], wall_at(k, b));
     }
 #pragma unroll
     for (int k = 0; k < kWall; ++k) wv[k] = (k >= 8 && k <= 10) ? warp_max(wv[k]) : warp_sum(wv[k]);
@@ -1223,19 +1290,21 @@ static __global__ void __launch_bounds__(kCtlThreads) k_control(CtrlConfig cc, P
   if (lane == 0) {
     s_sum[wid][0] = s1;
     s_sum[wid][1] = s2;
+    s_sum[wid][2] = s3;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) s_sum[wid][2 + k] = pj[k];
+    for (int k = 0; k < 4; ++k) s_sum[wid][3 + k] = pj[k];
 #pragma unroll
     for (int k = 0; k < 1 + kMon; ++k) s_max[wid][k] = mx[k];
   }
   __syncthreads();
   if (tid == 0) {
-    double a[3] = {0.0, 0.0, 0.0}, mon[kMon], p4[4] = {0.0, 0.0, 0.0, 0.0}, wv[kWall];
+    double a[kNorm] = {0.0, 0.0, 0.0, 0.0}, mon[kMon], p4[4] = {0.0, 0.0, 0.0, 0.0}, wv[kWall];
     long long m[1 + kMon] = {0, 0, 0, 0, 0, 0, 0};
     for (int w = 0; w < kWarps; ++w) {
       a[0] += s_sum[w][0];
       a[1] += s_sum[w][1];
-      for (int k = 0; k < 4; ++k) p4[k] += s_sum[w][2 + k];
+      a[3] += s_sum[w][2];
+      for (int k = 0; k < 4; ++k) p4[k] += s_sum[w][3 + k];
       for (int k = 0; k < 1 + kMon; ++k) m[k] = max_bits(m[k], s_max[w][k]);
     }
     auto decode = [&](long long bits) {

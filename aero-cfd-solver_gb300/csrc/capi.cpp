@@ -1,4 +1,5 @@
 // capi.cpp -- extern "C" entry points of libaero_gb300.so (include/aero_gb300.h).
+#include "../../include/aero_batch.h"
 #include "../../include/aero_gb300.h"
 #include "engine.hpp"
 #include "mesh_prep.hpp"
@@ -175,12 +176,14 @@ void aero_case_defaults(aero_case_desc* c) {
   c->ordering = AERO_ORDER_MORTON;
   c->block_size = 0;
   c->diagnostics = 0;
+  c->density_l2_target = 0.0;
 }
 
-int aero_create(const aero_mesh_desc* mesh, const aero_case_desc* cfg, aero_ctx** out) {
-  if (out == nullptr || mesh == nullptr || cfg == nullptr)
-    return fail(nullptr, AERO_ERR_INVALID, "aero_create: null argument");
-  *out = nullptr;
+}  // extern "C"
+
+namespace {
+
+int check_case(const aero_case_desc* cfg) {
   if (cfg->rk_stages != 1 && cfg->rk_stages != 3)
     return fail(nullptr, AERO_ERR_INVALID, "Euler pseudo-time rk_stages must be 1 or 3.");
   if (cfg->flux != AERO_FLUX_RUSANOV && cfg->flux != AERO_FLUX_HLLC)
@@ -193,31 +196,52 @@ int aero_create(const aero_mesh_desc* mesh, const aero_case_desc* cfg, aero_ctx*
   if (rho_inf <= 0.0) rho_inf = cfg->p_inf / (cfg->gas_constant * cfg->t_inf);
   if (!(rho_inf > 0.0))
     return fail(nullptr, AERO_ERR_INVALID, "Invalid freestream density. Set rho_inf or p_inf/T_inf.");
+  return AERO_OK;
+}
+
+// One context over n cases (n = 1: aero_create).
+int create_ctx(int n, const aero_mesh_desc* meshes, const aero_case_desc* cfgs, aero_ctx** out) {
+  if (out == nullptr || meshes == nullptr || cfgs == nullptr || n < 1)
+    return fail(nullptr, AERO_ERR_INVALID, "aero_create: null argument");
+  *out = nullptr;
+  for (int k = 0; k < n; ++k) {
+    const int rc = check_case(&cfgs[k]);
+    if (rc != AERO_OK) return rc;
+  }
   try {
     std::unique_ptr<aero_ctx> ctx(new aero_ctx());
-    ctx->cfg = *cfg;
+    ctx->cfg = cfgs[0];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || !device_ok(dev)) {
       cudaGetLastError();
       return fail(nullptr, AERO_ERR_CUDA, "no usable CUDA device of compute capability 10.3");
     }
     ctx->device = dev;
-    aero::HostSlots hs;
+    std::vector<aero::HostSlots> hv(static_cast<size_t>(n));
+    std::vector<aero_case_desc> cv(cfgs, cfgs + n);
+    std::vector<aero::Resolved> rv;
     std::string err;
-    if (!aero::build_slots(*mesh, cfg->ordering, &hs, &err)) return fail(nullptr, AERO_ERR_INVALID, err);
-    const aero::Resolved rs = resolve(*cfg);
+    for (int k = 0; k < n; ++k) {
+      if (!aero::build_slots(meshes[k], cfgs[k].ordering, &hv[k], &err)) {
+        return fail(nullptr, AERO_ERR_INVALID, n > 1 ? "case " + std::to_string(k) + ": " + err : err);
+      }
+      rv.push_back(resolve(cfgs[k]));
+    }
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
       cudaGetLastError();
       return fail(nullptr, AERO_ERR_CUDA, "cudaStreamCreate failed");
     }
-    aero::Engine* e = cfg->precision == AERO_PRECISION_FP32 ? aero::make_engine_f32(hs, *cfg, rs, ctx->stream)
-                                                            : aero::make_engine_f64(hs, *cfg, rs, ctx->stream);
+    aero::Engine* e = cfgs[0].precision == AERO_PRECISION_FP32 ? aero::make_engine_f32(hv, cv, rv, ctx->stream)
+                                                               : aero::make_engine_f64(hv, cv, rv, ctx->stream);
     ctx->engine.reset(e);
     if (!e->init(&err)) {
-      cudaStreamDestroy(ctx->stream);
       ctx->engine.reset();
+      cudaStreamDestroy(ctx->stream);
       ctx->stream = nullptr;
-      return fail(nullptr, err.find("allocation") != std::string::npos ? AERO_ERR_NOMEM : AERO_ERR_CUDA, err);
+      const int code = err.find("allocation") != std::string::npos ? AERO_ERR_NOMEM
+                       : err.find("must share") != std::string::npos ? AERO_ERR_INVALID
+                                                                      : AERO_ERR_CUDA;
+      return fail(nullptr, code, err);
     }
     *out = ctx.release();
     return AERO_OK;
@@ -226,6 +250,50 @@ int aero_create(const aero_mesh_desc* mesh, const aero_case_desc* cfg, aero_ctx*
   } catch (const std::exception& ex) {
     return fail(nullptr, AERO_ERR_CUDA, ex.what());
   }
+}
+
+}  // namespace
+
+extern "C" {
+
+int aero_create(const aero_mesh_desc* mesh, const aero_case_desc* cfg, aero_ctx** out) {
+  return create_ctx(1, mesh, cfg, out);
+}
+
+int aero_batch_create(int n_cases, const aero_mesh_desc* meshes, const aero_case_desc* cases, aero_ctx** out) {
+  return create_ctx(n_cases, meshes, cases, out);
+}
+
+int aero_batch_size(const aero_ctx* ctx) { return ctx ? ctx->engine->n_cases() : 0; }
+
+int aero_batch_run(aero_ctx* ctx, int n, aero_iter_record* records, int* n_done) {
+  if (ctx == nullptr || n < 0) return fail(ctx, AERO_ERR_INVALID, "aero_batch_run: bad argument");
+  const int rc = ctx->engine->run(n, records, n_done);
+  const int cs = cuda_status(ctx);
+  if (cs != AERO_OK) return cs;
+  if (rc == AERO_ERR_NONFINITE) return fail(ctx, rc, "non-finite state trapped in a case");
+  return rc;
+}
+
+int aero_batch_set_state(aero_ctx* ctx, int case_index, const double* conserved) {
+  if (ctx == nullptr || conserved == nullptr || case_index < 0 || case_index >= ctx->engine->n_cases())
+    return fail(ctx, AERO_ERR_INVALID, "aero_batch_set_state: bad argument");
+  ctx->engine->set_state(case_index, conserved);
+  return cuda_status(ctx);
+}
+
+int aero_batch_get_state(aero_ctx* ctx, int case_index, double* conserved) {
+  if (ctx == nullptr || conserved == nullptr || case_index < 0 || case_index >= ctx->engine->n_cases())
+    return fail(ctx, AERO_ERR_INVALID, "aero_batch_get_state: bad argument");
+  ctx->engine->get_state(case_index, conserved);
+  return cuda_status(ctx);
+}
+
+int aero_batch_get_last_residual(aero_ctx* ctx, int case_index, double* residual, double* spectral_radius) {
+  if (ctx == nullptr || residual == nullptr || case_index < 0 || case_index >= ctx->engine->n_cases())
+    return fail(ctx, AERO_ERR_INVALID, "aero_batch_get_last_residual: bad argument");
+  ctx->engine->last_residual(case_index, residual, spectral_radius);
+  return cuda_status(ctx);
 }
 
 void aero_destroy(aero_ctx* ctx) {
@@ -243,19 +311,19 @@ const char* aero_last_error(const aero_ctx* ctx) {
 
 int aero_set_state(aero_ctx* ctx, const double* conserved) {
   if (ctx == nullptr || conserved == nullptr) return fail(ctx, AERO_ERR_INVALID, "aero_set_state: null argument");
-  ctx->engine->set_state(conserved);
+  ctx->engine->set_state(0, conserved);
   return cuda_status(ctx);
 }
 
 int aero_get_state(aero_ctx* ctx, double* conserved) {
   if (ctx == nullptr || conserved == nullptr) return fail(ctx, AERO_ERR_INVALID, "aero_get_state: null argument");
-  ctx->engine->get_state(conserved);
+  ctx->engine->get_state(0, conserved);
   return cuda_status(ctx);
 }
 
 int aero_get_primitive(aero_ctx* ctx, double* rho, double* u, double* v, double* p) {
   if (ctx == nullptr || !rho || !u || !v || !p) return fail(ctx, AERO_ERR_INVALID, "aero_get_primitive: null argument");
-  ctx->engine->get_primitive(rho, u, v, p);
+  ctx->engine->get_primitive(0, rho, u, v, p);
   return cuda_status(ctx);
 }
 
@@ -264,6 +332,7 @@ int aero_residual(aero_ctx* ctx, const double* conserved, int second_order, doub
                   double* residual, double* spectral_radius, double* gradients) {
   if (ctx == nullptr || conserved == nullptr || residual == nullptr || spectral_radius == nullptr)
     return fail(ctx, AERO_ERR_INVALID, "aero_residual: null argument");
+  if (ctx->engine->n_cases() != 1) return fail(ctx, AERO_ERR_INVALID, "aero_residual: batched context");
   ctx->engine->residual(conserved, second_order, stab_mach_floor, all_speed_flux_fix, all_speed_f_min,
                         all_speed_ramp_weight, residual, spectral_radius, gradients);
   return cuda_status(ctx);
@@ -271,6 +340,7 @@ int aero_residual(aero_ctx* ctx, const double* conserved, int second_order, doub
 
 int aero_run(aero_ctx* ctx, int n, aero_iter_record* records, int* n_done) {
   if (ctx == nullptr || n < 0) return fail(ctx, AERO_ERR_INVALID, "aero_run: bad argument");
+  if (ctx->engine->n_cases() != 1) return fail(ctx, AERO_ERR_INVALID, "aero_run: batched context (use aero_batch_run)");
   const int rc = ctx->engine->run(n, records, n_done);
   const int cs = cuda_status(ctx);
   if (cs != AERO_OK) return cs;
@@ -286,7 +356,7 @@ int aero_reset_run(aero_ctx* ctx) {
 
 int aero_get_last_residual(aero_ctx* ctx, double* residual, double* spectral_radius) {
   if (ctx == nullptr || residual == nullptr) return fail(ctx, AERO_ERR_INVALID, "aero_get_last_residual: null argument");
-  ctx->engine->last_residual(residual, spectral_radius);
+  ctx->engine->last_residual(0, residual, spectral_radius);
   return cuda_status(ctx);
 }
 

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <vector>
 
 namespace aero {
 
@@ -24,47 +25,61 @@ struct Resolved {
   int lm;  // any low-Mach feature on
 };
 
-// Read-only device view of a context for launches issued outside the engine.
-// dm / df / dg / fp point at the engine's DevMesh<T> / DevFaces<T> / DevGather<T> /
-// FaceParams<T> (T per `precision`).
+// Read-only device view of a single-case context for launches issued outside the engine.
+// dm / df / dg point at the engine's DevMesh<T> / DevFaces<T> / DevGather<T>; fps, pcs, mcs
+// at its device arrays of FaceParams<T> / PrecondD / MonitorConsts (T per `precision`);
+// cblk / fblk are the block -> (case, end) tables of the cell and face kernels.
 struct EngineView {
-  int n;
-  int nf;
+  int n;      // cells
+  int ntot;   // cells padded to whole blocks (the stride of the per-cell arrays)
+  int nf;     // faces padded to whole blocks
+  int cblocks, fblocks;
   int precision;  // enum aero_precision
   int flux;
   int lm;
   int block;
   int device;
+  double gamma;  // case 0
   const void* dm;
   const void* df;
   const void* dg;
-  const void* fp;
+  const void* fps;
+  const void* pcs;
+  const void* mcs;
+  const int2* cblk;
+  const int2* fblk;
   const int* perm_dev;  // new -> original cell, on the device
   cudaStream_t stream;
 };
 
+// Device solver for one or more cases packed into one set of arrays. Cases of one engine
+// share the numerics that select kernel variants (flux, limiter, low-Mach switches, RK
+// stages, time-step mode, start-up length, precision, block size); the flow conditions,
+// CFL schedules and stop rules are per case. Single-case functions address case 0.
 class Engine {
  public:
   virtual ~Engine() = default;
   virtual EngineView view() const = 0;
   virtual bool init(std::string* err) = 0;
-  virtual void set_state(const double* u_orig) = 0;
-  virtual void get_state(double* u_orig) = 0;
-  virtual void get_primitive(double* rho, double* u, double* v, double* p) = 0;
+  virtual int n_cases() const = 0;
+  virtual void set_state(int cs, const double* u_orig) = 0;
+  virtual void get_state(int cs, double* u_orig) = 0;
+  virtual void get_primitive(int cs, double* rho, double* u, double* v, double* p) = 0;
   virtual void residual(const double* u_orig, int second, double stab, int as_fix, double as_fmin,
                         double as_ramp, double* res, double* sr, double* grad) = 0;
+  // records: case k's records at recs + k * n (may be null); n_done[k] iterations run
   virtual int run(int n, aero_iter_record* recs, int* n_done) = 0;
   virtual void reset_run() = 0;
-  virtual void last_residual(double* res, double* sr) = 0;
+  virtual void last_residual(int cs, double* res, double* sr) = 0;
   virtual int time_iterations(int n, int use_graph, int flush_l2, double* ms) = 0;
   virtual int profile_kernels(int n, int flush_l2, double* ms, int* launches) = 0;
   virtual void info(long long* out, int n) = 0;
   virtual cudaError_t last_cuda_error() = 0;
 };
 
-Engine* make_engine_f32(const HostSlots& hs, const aero_case_desc& cfg, const Resolved& rs,
-                        cudaStream_t stream);
-Engine* make_engine_f64(const HostSlots& hs, const aero_case_desc& cfg, const Resolved& rs,
-                        cudaStream_t stream);
+Engine* make_engine_f32(const std::vector<HostSlots>& hs, const std::vector<aero_case_desc>& cfg,
+                        const std::vector<Resolved>& rs, cudaStream_t stream);
+Engine* make_engine_f64(const std::vector<HostSlots>& hs, const std::vector<aero_case_desc>& cfg,
+                        const std::vector<Resolved>& rs, cudaStream_t stream);
 
 }  // namespace aero

@@ -2,8 +2,8 @@
 #include "engine_impl.cuh"
 
 namespace aero {
-Engine* make_engine_f64(const HostSlots& hs, const aero_case_desc& cfg, const Resolved& rs,
-                        cudaStream_t stream) {
+Engine* make_engine_f64(const std::vector<HostSlots>& hs, const std::vector<aero_case_desc>& cfg,
+                        const std::vector<Resolved>& rs, cudaStream_t stream) {
   return new EngineT<double>(hs, cfg, rs, stream);
 }
 }  // namespace aero

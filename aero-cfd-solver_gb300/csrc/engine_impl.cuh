@@ -1,5 +1,14 @@
-// engine_impl.cuh -- device solver for one bulk precision T (float or double). Included by
-// engine_f32.cu and engine_f64.cu, which instantiate it.
+// engine_impl.cuh -- device solver for one bulk precision T (float or double), for one case or
+// a batch of cases packed into one set of arrays. Included by engine_f32.cu and
+// engine_f64.cu, which instantiate it.
+//
+// Packing: case k's cells occupy [c0_k, c0_k + n_k) of the per-cell arrays and its faces
+// [f0_k, f0_k + nf_k) of the per-face arrays; both ranges start on a block boundary, so every
+// block of the cell and face kernels belongs to exactly one case (tables cblk / fblk give its
+// case and the end of that case's range). Neighbour ids, face ids and wall entries are
+// offset by the case's bases, so the kernels see one mesh of disjoint components; per-case
+// constants (free stream, schedule, controller) are arrays indexed by the case. A case's
+// cells keep the block layout of a single-case run, so a batch reproduces single runs.
 #pragma once
 
 #include "aero_face_kernels.cuh"
@@ -23,8 +32,19 @@ class EngineT final : public Engine {
   using V4 = typename Vec<T>::v4;
   using V2 = typename Vec<T>::v2;
 
+  // Where case k lives in the packed arrays.
+  struct Pack {
+    int n, nf, d;    // cells, faces, faces per cell
+    int c0, f0;      // first cell, first face
+    int cb0, ncb;    // first cell block, cell blocks
+    int fb0, nfb;    // first face block, face blocks
+    int w0;          // first wall entry
+    int ws0, nws;    // first wall-partial slot, slots
+  };
+
  public:
-  EngineT(const HostSlots& hs, const aero_case_desc& cfg, const Resolved& rs, cudaStream_t st)
+  EngineT(const std::vector<HostSlots>& hs, const std::vector<aero_case_desc>& cfg, const std::vector<Resolved>& rs,
+          cudaStream_t st)
       : hs_(hs), cfg_(cfg), rs_(rs), st_(st) {}
 
   ~EngineT() override {
@@ -40,265 +60,307 @@ class EngineT final : public Engine {
   }
 
   bool init(std::string* err) override {
-    n_ = hs_.n;
-    d_ = hs_.d;
-    block_ = cfg_.block_size > 0 ? cfg_.block_size : 128;
+    K_ = static_cast<int>(hs_.size());
+    if (K_ < 1 || cfg_.size() != hs_.size() || rs_.size() != hs_.size()) {
+      *err = "no cases";
+      return false;
+    }
+    const aero_case_desc& c0 = cfg_[0];
+    block_ = c0.block_size > 0 ? c0.block_size : 128;
     if (block_ != 64 && block_ != 128 && block_ != 256) {
       *err = "block_size must be 64, 128 or 256";
       return false;
     }
-    nblocks_ = (n_ + block_ - 1) / block_;
-    const size_t ns = static_cast<size_t>(n_) * d_;
-
-    // slot table; normals and areas in T (exact conversions of the double geometry)
-    link_ = upload(hs_.link);
-    std::vector<V2> nrm(ns);
-    std::vector<T> area(ns);
-    for (size_t i = 0; i < ns; ++i) {
-      nrm[i].x = T(hs_.nx[i]);
-      nrm[i].y = T(hs_.ny[i]);
-      area[i] = T(hs_.area[i]);
+    lm_ = rs_[0].lm;
+    for (int k = 1; k < K_; ++k) {  // settings that select kernel variants are shared
+      const aero_case_desc& c = cfg_[k];
+      if (c.flux != c0.flux || c.limiter != c0.limiter || c.precision != c0.precision ||
+          c.rk_stages != c0.rk_stages || c.local_time_stepping != c0.local_time_stepping ||
+          c.startup_first_order_iters != c0.startup_first_order_iters || c.precond_on != c0.precond_on ||
+          rs_[k].lm != lm_ || (c.block_size > 0 ? c.block_size : 128) != block_) {
+        *err = "cases of one batch must share flux, limiter, precision, RK stages, time-step mode, "
+               "start-up length, low-Mach switches and block size";
+        return false;
+      }
     }
-    nrm_ = upload(nrm);
-    area_ = upload(area);
-    std::vector<T> inv_vol(static_cast<size_t>(n_));
-    for (int c = 0; c < n_; ++c) inv_vol[c] = T(1) / std::max(T(hs_.vol[c]), T(1.0e-12));
-    inv_vol_ = upload(inv_vol);
-    // face table in T (exact conversions; MUSCL offsets formed in T from T coordinates)
-    {
-      const size_t nf = hs_.f_orig.size();
-      std::vector<int2> fc(nf);
-      std::vector<V2> fn(nf), doff(nf), noff(nf);
-      std::vector<T> fa(nf);
-      for (size_t i = 0; i < nf; ++i) {
-        fc[i] = make_int2(hs_.f_own[i], hs_.f_nb[i]);
-        fn[i].x = T(hs_.f_nx[i]);
-        fn[i].y = T(hs_.f_ny[i]);
-        fa[i] = T(hs_.f_area[i]);
-        const int o = hs_.f_own_old[i], b = hs_.f_nb_old[i];
-        doff[i].x = T(hs_.f_cx[i]) - T(hs_.ccx[o]);
-        doff[i].y = T(hs_.f_cy[i]) - T(hs_.ccy[o]);
-        if (hs_.f_nb[i] >= 0) {
-          noff[i].x = T(hs_.f_cx[i]) - T(hs_.ccx[b]);
-          noff[i].y = T(hs_.f_cy[i]) - T(hs_.ccy[b]);
-        } else {
-          noff[i].x = noff[i].y = T(0);
+
+    // ---- packed layout
+    pk_.resize(K_);
+    int ntot = 0, ftot = 0, cb = 0, fbk = 0, wtot = 0, wslots = 0;
+    d_ = 0;
+    std::vector<std::vector<int>> case_block_slot(K_);
+    for (int k = 0; k < K_; ++k) {
+      const HostSlots& h = hs_[k];
+      Pack& p = pk_[k];
+      p.n = h.n;
+      p.nf = static_cast<int>(h.f_orig.size());
+      p.d = h.d;
+      p.c0 = ntot;
+      p.f0 = ftot;
+      p.ncb = (p.n + block_ - 1) / block_;
+      p.nfb = (p.nf + block_ - 1) / block_;
+      p.cb0 = cb;
+      p.fb0 = fbk;
+      p.w0 = wtot;
+      ntot += p.ncb * block_;
+      ftot += p.nfb * block_;
+      cb += p.ncb;
+      fbk += p.nfb;
+      wtot += static_cast<int>(h.wkind.size());
+      d_ = std::max(d_, h.d);
+      // a wall-partial slot for each cell block of the case that holds wall entries
+      std::vector<int>& bs = case_block_slot[k];
+      bs.assign(p.ncb, -1);
+      p.ws0 = wslots;
+      p.nws = 0;
+      for (int b = 0; b < p.ncb; ++b) {
+        const int e = std::min(p.n, (b + 1) * block_);
+        for (int c = b * block_; c < e; ++c) {
+          if (h.flags[c] >= 4) {
+            bs[b] = wslots + p.nws++;
+            break;
+          }
         }
       }
-      df_.nf = static_cast<int>(nf);
+      wslots += p.nws;
+    }
+    ntot_ = ntot;
+    ftot_ = ftot;
+    ncb_ = cb;
+    nfb_ = fbk;
+    ncells_ = 0;
+    nfaces_ = 0;
+    for (const Pack& p : pk_) {
+      ncells_ += p.n;
+      nfaces_ += p.nf;
+    }
+
+    // ---- slot table (gradient, pressure jump) and gather slots, stride ntot
+    {
+      const size_t ns = static_cast<size_t>(ntot_) * d_;
+      std::vector<int> link(ns, kPad), gslot(ns, kPad);
+      std::vector<V2> nrm(ns);
+      std::vector<T> area(ns, T(0));
+      std::vector<T> inv_vol(static_cast<size_t>(ntot_), T(1));
+      std::vector<unsigned char> flags(static_cast<size_t>(ntot_), 0);
+      std::vector<int> wall_first(static_cast<size_t>(ntot_), 0);
+      for (auto& v : nrm) v.x = v.y = T(0);
+      for (int k = 0; k < K_; ++k) {
+        const HostSlots& h = hs_[k];
+        const Pack& p = pk_[k];
+        for (int j = 0; j < h.d; ++j) {
+          for (int c = 0; c < h.n; ++c) {
+            const size_t src = static_cast<size_t>(j) * h.n + c;
+            const size_t dst = static_cast<size_t>(j) * ntot_ + p.c0 + c;
+            const int l = h.link[src];
+            link[dst] = l >= 0 ? ((((l >> 1) + p.c0) << 1) | (l & 1)) : l;
+            const int g = h.gslot[src];
+            gslot[dst] = g >= 0 ? ((((g >> 1) + p.f0) << 1) | (g & 1)) : g;
+            nrm[dst].x = T(h.nx[src]);
+            nrm[dst].y = T(h.ny[src]);
+            area[dst] = T(h.area[src]);
+          }
+        }
+        for (int c = 0; c < h.n; ++c) {
+          inv_vol[p.c0 + c] = T(1) / std::max(T(h.vol[c]), T(1.0e-12));
+          flags[p.c0 + c] = h.flags[c];
+          wall_first[p.c0 + c] = h.wall_first[c] + p.w0;
+        }
+      }
+      link_ = upload(link);
+      nrm_ = upload(nrm);
+      area_ = upload(area);
+      inv_vol_ = upload(inv_vol);
+      flags_ = upload(flags);
+      dg_.slot = upload(gslot);
+      ms_.flags = flags_;
+      ms_.wall_first = upload(wall_first);
+    }
+    // ---- face table in T (exact conversions; MUSCL offsets formed in T from T coordinates)
+    {
+      std::vector<int2> fc(static_cast<size_t>(ftot_), make_int2(0, -1));
+      std::vector<V2> fn(static_cast<size_t>(ftot_)), doff(static_cast<size_t>(ftot_)),
+          noff(static_cast<size_t>(ftot_));
+      std::vector<T> fa(static_cast<size_t>(ftot_), T(0));
+      for (auto* v : {&fn, &doff, &noff}) {
+        for (auto& x : *v) x.x = x.y = T(0);
+      }
+      for (int k = 0; k < K_; ++k) {
+        const HostSlots& h = hs_[k];
+        const Pack& p = pk_[k];
+        for (int i = 0; i < p.nf; ++i) {
+          const size_t q = static_cast<size_t>(p.f0) + i;
+          fc[q] = make_int2(h.f_own[i] + p.c0, h.f_nb[i] >= 0 ? h.f_nb[i] + p.c0 : h.f_nb[i]);
+          fn[q].x = T(h.f_nx[i]);
+          fn[q].y = T(h.f_ny[i]);
+          fa[q] = T(h.f_area[i]);
+          const int o = h.f_own_old[i], b = h.f_nb_old[i];
+          doff[q].x = T(h.f_cx[i]) - T(h.ccx[o]);
+          doff[q].y = T(h.f_cy[i]) - T(h.ccy[o]);
+          if (h.f_nb[i] >= 0) {
+            noff[q].x = T(h.f_cx[i]) - T(h.ccx[b]);
+            noff[q].y = T(h.f_cy[i]) - T(h.ccy[b]);
+          }
+        }
+      }
+      df_.nf = ftot_;
       df_.cells = upload(fc);
       df_.nrm = upload(fn);
       df_.area = upload(fa);
       df_.doff = upload(doff);
       df_.noff = upload(noff);
-      dg_.n = n_;
-      dg_.d = d_;
-      dg_.slot = upload(hs_.gslot);
-      F_ = alloc<V4>(nf);
-      FS_ = alloc<T>(nf);
+      F_ = alloc<V4>(ftot_);
+      FS_ = alloc<T>(ftot_);
     }
-    perm_dev_ = upload(hs_.perm);
-    // monitor tables: per-cell flags, owner-sorted wall entries, and a partials slot for each
-    // update block that holds wall entries
-    std::vector<int> block_slot(static_cast<size_t>(nblocks_), -1);
-    int n_wall_blocks = 0;
-    for (int b = 0; b < nblocks_; ++b) {
-      const int c0 = b * block_, c1 = std::min(n_, c0 + block_);
-      for (int c = c0; c < c1; ++c) {
-        if (hs_.flags[c] >= 4) {
-          block_slot[b] = n_wall_blocks++;
-          break;
-        }
-      }
-    }
-    flags_ = upload(hs_.flags);
-    ms_.flags = flags_;
-    ms_.wall_first = upload(hs_.wall_first);
-    ms_.wkind = upload(hs_.wkind.empty() ? std::vector<unsigned char>{0} : hs_.wkind);
-    ms_.wnx = upload(nonempty(hs_.wnx));
-    ms_.wny = upload(nonempty(hs_.wny));
-    ms_.warea = upload(nonempty(hs_.warea));
-    ms_.wx = upload(nonempty(hs_.wx));
-    ms_.wy = upload(nonempty(hs_.wy));
+    // ---- wall entries, block tables
     {
+      std::vector<unsigned char> wkind;
+      std::vector<double> wnx, wny, warea, wx, wy;
+      for (const HostSlots& h : hs_) {
+        wkind.insert(wkind.end(), h.wkind.begin(), h.wkind.end());
+        wnx.insert(wnx.end(), h.wnx.begin(), h.wnx.end());
+        wny.insert(wny.end(), h.wny.begin(), h.wny.end());
+        warea.insert(warea.end(), h.warea.begin(), h.warea.end());
+        wx.insert(wx.end(), h.wx.begin(), h.wx.end());
+        wy.insert(wy.end(), h.wy.begin(), h.wy.end());
+      }
+      ms_.wkind = upload(nonempty(wkind));
+      ms_.wnx = upload(nonempty(wnx));
+      ms_.wny = upload(nonempty(wny));
+      ms_.warea = upload(nonempty(warea));
+      ms_.wx = upload(nonempty(wx));
+      ms_.wy = upload(nonempty(wy));
       auto to_f = [](const std::vector<double>& v) {
         std::vector<float> f(v.empty() ? 1 : v.size(), 0.0f);
         for (size_t i = 0; i < v.size(); ++i) f[i] = float(v[i]);
         return f;
       };
-      ms_.wnx_f = upload(to_f(hs_.wnx));
-      ms_.wny_f = upload(to_f(hs_.wny));
-      ms_.warea_f = upload(to_f(hs_.warea));
-      ms_.wx_f = upload(to_f(hs_.wx));
-      ms_.wy_f = upload(to_f(hs_.wy));
+      ms_.wnx_f = upload(to_f(wnx));
+      ms_.wny_f = upload(to_f(wny));
+      ms_.warea_f = upload(to_f(warea));
+      ms_.wx_f = upload(to_f(wx));
+      ms_.wy_f = upload(to_f(wy));
+      std::vector<int> block_slot;
+      std::vector<int2> cblk, fblk;
+      std::vector<int> srfirst;
+      for (int k = 0; k < K_; ++k) {
+        const Pack& p = pk_[k];
+        block_slot.insert(block_slot.end(), case_block_slot[k].begin(), case_block_slot[k].end());
+        for (int b = 0; b < p.ncb; ++b) cblk.push_back(make_int2(k, p.c0 + p.n));
+        for (int b = 0; b < p.nfb; ++b) fblk.push_back(make_int2(k, p.f0 + p.nf));
+        srfirst.push_back(p.cb0 * (block_ / 32));
+      }
+      srfirst.push_back(ncb_ * (block_ / 32));
+      ms_.block_slot = upload(block_slot);
+      cblk_ = upload(cblk);
+      fblk_ = upload(fblk);
+      srfirst_ = upload(srfirst);
+      nwslots_ = wslots;
     }
-    ms_.block_slot = upload(block_slot);
-    ms_.p_inf = rs_.p_inf;
-    ms_.rho_inf = rs_.rho_inf;
-    ms_.u_inf = rs_.v_inf * rs_.cos_a;
-    ms_.v_inf = rs_.v_inf * rs_.sin_a;
-    ms_.q_inf = rs_.q_inf;
-    ms_.x_ref = cfg_.x_ref;
-    ms_.y_ref = cfg_.y_ref;
-    ms_.gamma = rs_.gamma;
-    ms_.p_inf_f = float(ms_.p_inf);
-    ms_.rho_inf_f = float(ms_.rho_inf);
-    ms_.u_inf_f = float(ms_.u_inf);
-    ms_.v_inf_f = float(ms_.v_inf);
-    ms_.q_inf_f = float(ms_.q_inf);
-    ms_.x_ref_f = float(ms_.x_ref);
-    ms_.y_ref_f = float(ms_.y_ref);
+    std::vector<int> perm0(hs_[0].perm);
+    perm_dev_ = upload(perm0);
 
-    // state
-    W_ = alloc<V4>(n_);
-    gx_ = alloc<V4>(n_);
-    gy_ = alloc<V4>(n_);
-    R_ = alloc<V4>(n_);
-    SR_ = alloc<T>(n_);
-    if (cfg_.rk_stages > 1) {  // the first stage's residual, kept apart from the last stage's
-      R0_ = alloc<V4>(n_);
-      SR0_ = alloc<T>(n_);
+    // ---- state and work arrays
+    W_ = alloc<V4>(ntot_);
+    gx_ = alloc<V4>(ntot_);
+    gy_ = alloc<V4>(ntot_);
+    R_ = alloc<V4>(ntot_);
+    SR_ = alloc<T>(ntot_);
+    const bool global_dt = !c0.local_time_stepping;
+    if (c0.rk_stages > 1 && global_dt) {  // the first stage's residual, kept apart from the last stage's
+      R0_ = alloc<V4>(ntot_);
+      SR0_ = alloc<T>(ntot_);
     } else {
       R0_ = R_;
       SR0_ = SR_;
     }
-    fb_ = alloc<int>(4);
-    Un_ = alloc<d4>(n_);
-    Us_ = alloc<V4>(n_);
+    fb_ = alloc<int>(4 * static_cast<size_t>(K_));
+    Un_ = alloc<d4>(ntot_);
+    Us_ = alloc<V4>(ntot_);
     sref_.un = Un_;
     if (sizeof(T) == 4) {
-      sref_.hi = alloc<float4>(n_);
-      sref_.lo = alloc<float4>(n_);
+      sref_.hi = alloc<float4>(ntot_);
+      sref_.lo = alloc<float4>(ntot_);
     }
-    Ueval_ = alloc<d4>(n_);
+    Ueval_ = alloc<d4>(ntot_);
     if (sizeof(T) == 4) {
-      part_.norms_f = alloc<float>(3 * nblocks_);
+      part_.norms_f = alloc<float>(kNorm * static_cast<size_t>(ncb_));
     } else {
-      part_.norms = alloc<double>(3 * nblocks_);
+      part_.norms = alloc<double>(kNorm * static_cast<size_t>(ncb_));
     }
-    part_.mon = alloc<long long>(kMon * nblocks_);
+    part_.mon = alloc<long long>(kMon * static_cast<size_t>(ncb_));
     if (sizeof(T) == 4) {
-      part_.wall_f = alloc<float>(kWall * std::max(n_wall_blocks, 1));
+      part_.wall_f = alloc<float>(kWall * static_cast<size_t>(std::max(nwslots_, 1)));
     } else {
-      part_.wall = alloc<double>(kWall * std::max(n_wall_blocks, 1));
+      part_.wall = alloc<double>(kWall * static_cast<size_t>(std::max(nwslots_, 1)));
     }
-    part_.nb = nblocks_;
-    part_.nwb = n_wall_blocks;
-    part_.pjump = alloc<double>(4 * nblocks_);
-    part_.srmax = alloc<double>(nblocks_ * (block_ / 32));
-    ctrl_ = alloc<Ctrl>(1);
+    part_.nb = ncb_;
+    part_.nwb = nwslots_;
+    part_.pjump = alloc<double>(4 * static_cast<size_t>(ncb_));
+    part_.srmax = alloc<double>(static_cast<size_t>(ncb_) * (block_ / 32));
+    ctrls_ = alloc<Ctrl>(K_);
     ctrl_eval_ = alloc<Ctrl>(1);
     rec_cap_ = 1024;
-    recs_ = alloc<Record>(rec_cap_);
+    recs_ = alloc<Record>(static_cast<size_t>(K_) * rec_cap_);
+    ccs_dev_ = alloc<CtrlConfig>(K_);
+    fps_dev_ = alloc<FaceParams<T>>(K_);
+    pcs_dev_ = alloc<PrecondD>(K_);
+    mcs_dev_ = alloc<MonitorConsts>(K_);
     if (err_ != cudaSuccess) {
       *err = std::string("device allocation/upload failed: ") + cudaGetErrorString(err_);
       return false;
     }
 
-    dm_.n = n_;
+    dm_.n = ntot_;
     dm_.d = d_;
     dm_.link = link_;
     dm_.nrm = nrm_;
     dm_.area = area_;
     dm_.inv_vol = inv_vol_;
+    dg_.n = ntot_;
+    dg_.d = d_;
     dg_.inv_vol = inv_vol_;
 
-    fp_.gamma = T(rs_.gamma);
-    fp_.farfield = Cons<T>{T(rs_.cons_inf[0]), T(rs_.cons_inf[1]), T(rs_.cons_inf[2]), T(rs_.cons_inf[3])};
-    fp_.limiter = cfg_.limiter;
-    fp_.precond = cfg_.precond_on;
-    fp_.low_mach_fix = cfg_.low_mach_fix;
-    fp_.precond_farfield_bc = cfg_.precond_farfield_bc;
-    fp_.as_fix = 0;
-    fp_.mach_cutoff = T(cfg_.mach_cutoff);
-    fp_.pc_mach_ref = T(rs_.pc_mach_ref);
-    fp_.pc_mach_min = T(rs_.pc_mach_min);
-    fp_.pc_beta_min = T(rs_.pc_beta_min);
-    fp_.pc_beta_max = T(rs_.pc_beta_max);
-    fp_.stab_floor = T(0);
-    fp_.as_cutoff = T(cfg_.all_speed_mach_cutoff);
-    fp_.as_fmin = T(rs_.as_fmin);
-    fp_.as_ramp = T(1);
+    // ---- per-case constants
+    ccs_.resize(K_);
+    fps_.resize(K_);
+    pcs_.resize(K_);
+    mcs_.resize(K_);
+    pjump_on_ = false;
+    sym_on_ = false;
+    for (int k = 0; k < K_; ++k) {
+      setup_case(k);
+      pjump_on_ = pjump_on_ || ccs_[k].pjump_blocks > 0;
+      sym_on_ = sym_on_ || mcs_[k].sym_interval > 0;
+    }
+    AERO_CK(cudaMemcpyAsync(ccs_dev_, ccs_.data(), sizeof(CtrlConfig) * K_, cudaMemcpyHostToDevice, st_));
+    AERO_CK(cudaMemcpyAsync(fps_dev_, fps_.data(), sizeof(FaceParams<T>) * K_, cudaMemcpyHostToDevice, st_));
+    AERO_CK(cudaMemcpyAsync(pcs_dev_, pcs_.data(), sizeof(PrecondD) * K_, cudaMemcpyHostToDevice, st_));
+    AERO_CK(cudaMemcpyAsync(mcs_dev_, mcs_.data(), sizeof(MonitorConsts) * K_, cudaMemcpyHostToDevice, st_));
+    cell_cases_ = Cases<T>{cblk_, ctrls_, fps_dev_, pcs_dev_, mcs_dev_};
+    face_cases_ = Cases<T>{fblk_, ctrls_, fps_dev_, pcs_dev_, mcs_dev_};
 
-    pc_.enabled = cfg_.precond_on;
-    pc_.gamma = rs_.gamma;
-    pc_.mach_ref = double(fp_.pc_mach_ref);
-    pc_.mach_min = double(fp_.pc_mach_min);
-    pc_.beta_min = double(fp_.pc_beta_min);
-    pc_.beta_max = double(fp_.pc_beta_max);
-    pc_.gamma_f = float(rs_.gamma);
-    pc_.gm1_f = float(rs_.gamma - 1.0);
-
-    CtrlConfig& c = cc_;
-    std::memset(&c, 0, sizeof(c));
-    c.n_cells = n_;
-    c.n_wall = hs_.n_slip;
-    c.n_wall_blocks = n_wall_blocks;
-    c.bulk_f32 = sizeof(T) == 4 ? 1 : 0;
-    c.rk_stages = cfg_.rk_stages;
-    c.local_dt = cfg_.local_time_stepping;
-    c.cfl_ramp = cfg_.cfl_ramp_iters;
-    c.stab_ramp = std::max(cfg_.stab_ramp_iters, 0);
-    c.as_ramp_start = std::max(cfg_.all_speed_ramp_start_iter, 0);
-    c.as_ramp_iters = std::max(cfg_.all_speed_ramp_iters, 0);
-    c.startup_first_order = cfg_.startup_first_order_iters;
-    c.min_iterations = cfg_.min_iterations;
-    c.window = std::min(std::max(cfg_.force_stability_window, 1), kMaxForceWindow);
-    c.staged = cfg_.all_speed_staged_controller;
-    c.st_a_min = std::max(cfg_.all_speed_stage_a_min_iters, 0);
-    c.st_a_max = std::max(cfg_.all_speed_stage_a_max_iters, 0);
-    c.pj_hold = std::max(cfg_.all_speed_pjump_hold_iters, 1);
-    c.freeze_iters = std::max(cfg_.all_speed_freeze_iters, 0);
-    c.as_fix_cfg = cfg_.all_speed_flux_fix;
-    c.n_blocks = nblocks_;
-    pjump_on_ = cfg_.all_speed_staged_controller || cfg_.diagnostics;
-    sym_on_ = cfg_.aoa0_symmetry_enforce && cfg_.aoa0_symmetry_enforce_interval > 0 &&
-              !(std::fabs(cfg_.aoa_deg) > 1.0e-12);
-    c.pjump_blocks = pjump_on_ ? nblocks_ : 0;
-    c.cfl_start = cfg_.cfl_start;
-    c.cfl_max = cfg_.cfl_max;
-    c.stab_start = rs_.stab_start;
-    c.stab_target = rs_.stab_target;
-    c.as_fmin = rs_.as_fmin;
-    c.residual_target = cfg_.residual_reduction_target;
-    c.stab_tol = cfg_.force_stability_tol;
-    c.drift_tol = cfg_.force_mean_drift_tol > 0.0 ? cfg_.force_mean_drift_tol : cfg_.force_stability_tol;
-    c.st_fmin_high = rs_.st_fmin_high;
-    c.st_fmin_mid = rs_.st_fmin_mid;
-    c.st_fmin_low = rs_.st_fmin_low;
-    c.pj_target = rs_.pj_target;
-    c.pj_spike = rs_.pj_spike;
-    c.cfl_drop = rs_.cfl_drop;
-    c.cfl_restore = rs_.cfl_restore;
-    c.cfl_min_scale = rs_.cfl_min_scale;
-    c.p_inf = rs_.p_inf;
-    c.q_inf = rs_.q_inf;
-    c.chord = std::max(cfg_.chord, 1.0e-8);
-    c.s_ref = c.chord * 1.0;
-    c.cos_a = rs_.cos_a;
-    c.sin_a = rs_.sin_a;
-    c.x_ref = cfg_.x_ref;
-    c.y_ref = cfg_.y_ref;
-    c.pressure_ref = rs_.pressure_ref;
-    c.gamma = rs_.gamma;
-    c.rho_inf = rs_.rho_inf;
-    c.u_inf = rs_.v_inf * rs_.cos_a;
-    c.v_inf = rs_.v_inf * rs_.sin_a;
-
-    AERO_CK(cudaMemsetAsync(fb_, 0, 4 * sizeof(int), st_));
-    // the controller of iteration i runs beside the gradient and first residual of iteration
-    // i+1 (which need none of its outputs) when the first residual has a buffer of its own
-    // and the residual reads no controller-scheduled low-Mach weights
-    defer_control_ = cfg_.rk_stages > 1 && !rs_.lm;
+    // the controller of iteration i runs beside the gradient and first face pass of
+    // iteration i+1 (which need none of its outputs) when the residual reads no
+    // controller-scheduled low-Mach weights and the first stage's residual is not stored
+    defer_control_ = c0.rk_stages > 1 && !lm_;
     if (defer_control_) {
       AERO_CK(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
       AERO_CK(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
       AERO_CK(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
     }
     // freestream initial state
-    std::vector<d4> u0(static_cast<size_t>(n_), d4{rs_.cons_inf[0], rs_.cons_inf[1], rs_.cons_inf[2], rs_.cons_inf[3]});
-    AERO_CK(cudaMemcpyAsync(Un_, u0.data(), sizeof(d4) * n_, cudaMemcpyHostToDevice, st_));
-    state_from_staging();
+    {
+      std::vector<d4> u0(static_cast<size_t>(ntot_));
+      for (int k = 0; k < K_; ++k) {
+        const Pack& p = pk_[k];
+        const d4 fs{rs_[k].cons_inf[0], rs_[k].cons_inf[1], rs_[k].cons_inf[2], rs_[k].cons_inf[3]};
+        for (int c = 0; c < p.ncb * block_; ++c) u0[p.c0 + c] = fs;
+      }
+      AERO_CK(cudaMemcpyAsync(Un_, u0.data(), sizeof(d4) * ntot_, cudaMemcpyHostToDevice, st_));
+      AERO_CK(cudaStreamSynchronize(st_));
+    }
+    state_from_staging(0, ntot_);
     w_valid_ = false;
     reset_run();
     AERO_CK(cudaStreamSynchronize(st_));
@@ -309,19 +371,29 @@ class EngineT final : public Engine {
     return true;
   }
 
+  int n_cases() const override { return K_; }
+
   EngineView view() const override {
     EngineView v{};
-    v.n = n_;
+    v.n = pk_[0].n;
+    v.ntot = ntot_;
+    v.nf = ftot_;
+    v.cblocks = ncb_;
+    v.fblocks = nfb_;
     v.precision = sizeof(T) == 4 ? AERO_PRECISION_FP32 : AERO_PRECISION_FP64;
-    v.flux = cfg_.flux;
-    v.lm = rs_.lm;
+    v.flux = cfg_[0].flux;
+    v.lm = lm_;
     v.block = block_;
     cudaGetDevice(&v.device);
+    v.gamma = rs_[0].gamma;
     v.dm = &dm_;
     v.df = &df_;
     v.dg = &dg_;
-    v.nf = df_.nf;
-    v.fp = &fp_;
+    v.fps = fps_dev_;
+    v.pcs = pcs_dev_;
+    v.mcs = mcs_dev_;
+    v.cblk = cblk_;
+    v.fblk = fblk_;
     v.perm_dev = perm_dev_;
     v.stream = st_;
     return v;
@@ -334,41 +406,46 @@ class EngineT final : public Engine {
   }
 
   void reset_run() override {
-    Ctrl h;
-    std::memset(&h, 0, sizeof(h));
-    h.iter = 0;
-    h.cfl_scale = 1.0;
-    h.prev_l2 = -1.0;
-    h.initial_l2 = -1.0;
-    h.stage = cfg_.all_speed_staged_controller ? 1 : 0;
-    h.stage_b_fmin = rs_.st_fmin_high;
-    apply_schedule(cc_, &h);
-    host_ctrl_ = h;
-    AERO_CK(cudaMemcpyAsync(ctrl_, &host_ctrl_, sizeof(Ctrl), cudaMemcpyHostToDevice, st_));
-    AERO_CK(cudaMemsetAsync(fb_, 0, 4 * sizeof(int), st_));
+    host_ctrls_.assign(K_, Ctrl{});
+    for (int k = 0; k < K_; ++k) {
+      Ctrl& h = host_ctrls_[k];
+      std::memset(&h, 0, sizeof(h));
+      h.iter = 0;
+      h.cfl_scale = 1.0;
+      h.prev_l2 = -1.0;
+      h.initial_l2 = -1.0;
+      h.initial_l2rho = -1.0;
+      h.stage = cfg_[k].all_speed_staged_controller ? 1 : 0;
+      h.stage_b_fmin = rs_[k].st_fmin_high;
+      apply_schedule(ccs_[k], &h);
+    }
+    AERO_CK(cudaMemcpyAsync(ctrls_, host_ctrls_.data(), sizeof(Ctrl) * K_, cudaMemcpyHostToDevice, st_));
+    AERO_CK(cudaMemsetAsync(fb_, 0, 4 * sizeof(int) * K_, st_));
     AERO_CK(cudaStreamSynchronize(st_));
   }
 
   // State transfers go through a page-locked staging buffer in the device order.
-  void set_state(const double* u) override {
+  void set_state(int k, const double* u) override {
+    const Pack& p = pk_[k];
     d4* h = pinned_state();
-    for (int cn = 0; cn < n_; ++cn) {
-      const double* s = u + 5 * static_cast<size_t>(hs_.perm[cn]);
+    for (int cn = 0; cn < p.n; ++cn) {
+      const double* s = u + 5 * static_cast<size_t>(hs_[k].perm[cn]);
       h[cn] = d4{s[0], s[1], s[2], s[4]};
     }
-    AERO_CK(cudaMemcpyAsync(Un_, h, sizeof(d4) * n_, cudaMemcpyHostToDevice, st_));
-    state_from_staging();
+    AERO_CK(cudaMemcpyAsync(Un_ + p.c0, h, sizeof(d4) * p.n, cudaMemcpyHostToDevice, st_));
+    state_from_staging(p.c0, p.n);
     AERO_CK(cudaStreamSynchronize(st_));
     w_valid_ = false;
   }
 
-  void get_state(double* u) override {
+  void get_state(int k, double* u) override {
+    const Pack& p = pk_[k];
     d4* h = pinned_state();
-    state_to_staging();
-    AERO_CK(cudaMemcpyAsync(h, Un_, sizeof(d4) * n_, cudaMemcpyDeviceToHost, st_));
+    state_to_staging(p.c0, p.n);
+    AERO_CK(cudaMemcpyAsync(h, Un_ + p.c0, sizeof(d4) * p.n, cudaMemcpyDeviceToHost, st_));
     AERO_CK(cudaStreamSynchronize(st_));
-    for (int cn = 0; cn < n_; ++cn) {
-      double* s = u + 5 * static_cast<size_t>(hs_.perm[cn]);
+    for (int cn = 0; cn < p.n; ++cn) {
+      double* s = u + 5 * static_cast<size_t>(hs_[k].perm[cn]);
       s[0] = h[cn].x;
       s[1] = h[cn].y;
       s[2] = h[cn].z;
@@ -377,13 +454,14 @@ class EngineT final : public Engine {
     }
   }
 
-  void get_primitive(double* rho, double* u, double* v, double* p) override {
-    std::vector<d4> h(static_cast<size_t>(n_));
-    state_to_staging();
-    AERO_CK(cudaMemcpyAsync(h.data(), Un_, sizeof(d4) * n_, cudaMemcpyDeviceToHost, st_));
+  void get_primitive(int k, double* rho, double* u, double* v, double* p) override {
+    const Pack& pc = pk_[k];
+    std::vector<d4> h(static_cast<size_t>(pc.n));
+    state_to_staging(pc.c0, pc.n);
+    AERO_CK(cudaMemcpyAsync(h.data(), Un_ + pc.c0, sizeof(d4) * pc.n, cudaMemcpyDeviceToHost, st_));
     AERO_CK(cudaStreamSynchronize(st_));
-    for (int cn = 0; cn < n_; ++cn) {
-      const int co = hs_.perm[cn];
+    for (int cn = 0; cn < pc.n; ++cn) {
+      const int co = hs_[k].perm[cn];
       // host restatement of cons_to_prim (euler_flux.cpp:115-127) in double
       const double r = std::max(h[cn].x, 1.0e-8);
       const double inv = 1.0 / r;
@@ -392,79 +470,109 @@ class EngineT final : public Engine {
       rho[co] = r;
       u[co] = uu;
       v[co] = vv;
-      p[co] = std::max((rs_.gamma - 1.0) * (h[cn].w - ke), 1.0e-8);
+      p[co] = std::max((rs_[k].gamma - 1.0) * (h[cn].w - ke), 1.0e-8);
     }
   }
 
+  // One residual evaluation of case 0 (single-case engines).
   void residual(const double* u, int second, double stab, int as_fix, double as_fmin, double as_ramp,
                 double* res, double* sr, double* grad) override {
-    std::vector<d4> h(static_cast<size_t>(n_));
-    for (int cn = 0; cn < n_; ++cn) {
-      const double* s = u + 5 * static_cast<size_t>(hs_.perm[cn]);
+    const Pack& p = pk_[0];
+    std::vector<d4> h(static_cast<size_t>(p.n));
+    for (int cn = 0; cn < p.n; ++cn) {
+      const double* s = u + 5 * static_cast<size_t>(hs_[0].perm[cn]);
       h[cn] = d4{s[0], s[1], s[2], s[4]};
     }
-    AERO_CK(cudaMemcpyAsync(Ueval_, h.data(), sizeof(d4) * n_, cudaMemcpyHostToDevice, st_));
+    AERO_CK(cudaMemcpyAsync(Ueval_, h.data(), sizeof(d4) * p.n, cudaMemcpyHostToDevice, st_));
     Ctrl ce;
     std::memset(&ce, 0, sizeof(ce));
     set_eval_schedule(&ce, stab, as_fix, as_fmin, as_ramp);
     AERO_CK(cudaMemcpyAsync(ctrl_eval_, &ce, sizeof(Ctrl), cudaMemcpyHostToDevice, st_));
-    k_refresh_prim<T><<<nblocks_, block_, 0, st_>>>(n_, Ueval_, W_, rs_.gamma);
-    if (second) k_gradient<T><<<nblocks_, block_, 0, st_>>>(dm_, W_, gx_, gy_, ctrl_eval_);
-    launch_residual(second != 0, false, ctrl_eval_, &ctrl_eval_->fo_fallback, R_, SR_, 0);
+    const Cases<T> ccs{cblk_, ctrl_eval_, fps_dev_, pcs_dev_, mcs_dev_};
+    const Cases<T> fcs{fblk_, ctrl_eval_, fps_dev_, pcs_dev_, mcs_dev_};
+    k_refresh_prim<T><<<ncb_, block_, 0, st_>>>(p.n, Ueval_, W_, rs_[0].gamma);
+    if (second) k_gradient<T><<<ncb_, block_, 0, st_>>>(dm_, W_, gx_, gy_, ccs);
+    ResidualLaunch<T> a = residual_args(&ctrl_eval_->fo_fallback, R_, SR_, 0);
+    a.cell_cases = ccs;
+    a.face_cases = fcs;
+    launch_residual_passes(a, cfg_[0].flux, second != 0, lm_ != 0, false);
     AERO_CK(cudaGetLastError());
     w_valid_ = false;
-    download_residual(res, sr);
+    download_residual(0, res, sr);
     if (grad) {
-      std::vector<V4> hx(static_cast<size_t>(n_)), hy(static_cast<size_t>(n_));
+      std::vector<V4> hx(static_cast<size_t>(p.n)), hy(static_cast<size_t>(p.n));
       if (second) {
-        AERO_CK(cudaMemcpyAsync(hx.data(), gx_, sizeof(V4) * n_, cudaMemcpyDeviceToHost, st_));
-        AERO_CK(cudaMemcpyAsync(hy.data(), gy_, sizeof(V4) * n_, cudaMemcpyDeviceToHost, st_));
+        AERO_CK(cudaMemcpyAsync(hx.data(), gx_, sizeof(V4) * p.n, cudaMemcpyDeviceToHost, st_));
+        AERO_CK(cudaMemcpyAsync(hy.data(), gy_, sizeof(V4) * p.n, cudaMemcpyDeviceToHost, st_));
       }
       AERO_CK(cudaStreamSynchronize(st_));
-      for (int cn = 0; cn < n_; ++cn) {
-        double* g = grad + 10 * static_cast<size_t>(hs_.perm[cn]);
+      for (int cn = 0; cn < p.n; ++cn) {
+        double* g = grad + 10 * static_cast<size_t>(hs_[0].perm[cn]);
         if (!second) {
           for (int k = 0; k < 10; ++k) g[k] = 0.0;
           continue;
         }
-        const V4 a = hx[cn], b = hy[cn];
-        g[0] = a.x; g[1] = b.x;  // rho
-        g[2] = a.y; g[3] = b.y;  // u
-        g[4] = a.z; g[5] = b.z;  // v
-        g[6] = 0.0; g[7] = 0.0;  // w
-        g[8] = a.w; g[9] = b.w;  // p
+        const V4 a4 = hx[cn], b4 = hy[cn];
+        g[0] = a4.x; g[1] = b4.x;  // rho
+        g[2] = a4.y; g[3] = b4.y;  // u
+        g[4] = a4.z; g[5] = b4.z;  // v
+        g[6] = 0.0; g[7] = 0.0;    // w
+        g[8] = a4.w; g[9] = b4.w;  // p
       }
     }
   }
 
-  void last_residual(double* res, double* sr) override { download_residual(res, sr); }
+  void last_residual(int k, double* res, double* sr) override { download_residual(k, res, sr); }
 
   int run(int n, aero_iter_record* recs, int* n_done) override {
     static_assert(sizeof(Record) == sizeof(aero_iter_record), "record layout");
-    int executed = 0;
+    std::vector<int> executed(K_, 0);
     if (!w_valid_) refresh();
-    AERO_CK(cudaMemcpyAsync(&host_ctrl_, ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, st_));
-    AERO_CK(cudaStreamSynchronize(st_));
+    download_ctrls();
     int status = AERO_OK;
-    while (executed < n && !host_ctrl_.done && err_ == cudaSuccess) {
-      const int chunk = std::min(n - executed, rec_cap_);
-      const int it0 = host_ctrl_.iter;
-      host_rec_base_ = it0;
-      AERO_CK(cudaMemcpyAsync(&ctrl_->rec_base, &host_rec_base_, sizeof(int), cudaMemcpyHostToDevice, st_));
-      launch_iterations(it0, chunk, [](int) {}, [](int) {});
-      AERO_CK(cudaMemcpyAsync(&host_ctrl_, ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, st_));
-      AERO_CK(cudaStreamSynchronize(st_));
-      const int k = host_ctrl_.iter - it0;
-      if (recs && k > 0) {
-        AERO_CK(cudaMemcpyAsync(recs + executed, recs_, sizeof(Record) * k, cudaMemcpyDeviceToHost, st_));
-        AERO_CK(cudaStreamSynchronize(st_));
+    int e = 0;  // iterations launched in this call (every running case runs all of them)
+    auto running = [&] {
+      for (const Ctrl& c : host_ctrls_) {
+        if (!c.done) return true;
       }
-      executed += k;
-      if (k < chunk && !host_ctrl_.done) break;  // should not happen
+      return false;
+    };
+    while (e < n && running() && err_ == cudaSuccess) {
+      const int chunk = std::min(n - e, rec_cap_);
+      int it0 = 0;
+      for (const Ctrl& c : host_ctrls_) {
+        if (!c.done) {
+          it0 = c.iter;
+          break;
+        }
+      }
+      std::vector<int> base(K_, it0);
+      AERO_CK(cudaMemcpy2DAsync(&ctrls_->rec_base, sizeof(Ctrl), base.data(), sizeof(int), sizeof(int), K_,
+                                cudaMemcpyHostToDevice, st_));
+      std::vector<char> was_running(K_);
+      for (int k = 0; k < K_; ++k) was_running[k] = host_ctrls_[k].done ? 0 : 1;
+      launch_iterations(it0, chunk, [](int) {}, [](int) {});
+      download_ctrls();
+      for (int k = 0; k < K_; ++k) {
+        if (!was_running[k]) continue;
+        const int got = host_ctrls_[k].iter - it0;
+        if (recs && got > 0) {
+          AERO_CK(cudaMemcpyAsync(recs + static_cast<size_t>(k) * n + executed[k],
+                                  recs_ + static_cast<size_t>(k) * rec_cap_, sizeof(Record) * got,
+                                  cudaMemcpyDeviceToHost, st_));
+        }
+        executed[k] += got;
+      }
+      AERO_CK(cudaStreamSynchronize(st_));
+      e += chunk;
     }
-    if (host_ctrl_.nonfinite) status = AERO_ERR_NONFINITE;
+    for (const Ctrl& c : host_ctrls_) {
+      if (c.nonfinite) status = AERO_ERR_NONFINITE;
+    }
     if (err_ != cudaSuccess) status = AERO_ERR_CUDA;
-    if (n_done) *n_done = executed;
+    if (n_done) {
+      for (int k = 0; k < K_; ++k) n_done[k] = executed[k];
+    }
     return status;
   }
 
@@ -557,10 +665,12 @@ class EngineT final : public Engine {
     return end_untracked();
   }
 
+  // info[0] cells, [1] faces, [2] slots per cell, [3] launches per iteration, [4] device
+  // bytes, [5] precision, [6] block size, [7] cell blocks, [8] cases
   void info(long long* out, int n) override {
-    long long v[8] = {n_, hs_.nf, d_, launches_per_iteration(true), static_cast<long long>(bytes_),
-                      sizeof(T) == 4 ? AERO_PRECISION_FP32 : AERO_PRECISION_FP64, block_, nblocks_};
-    for (int i = 0; i < n && i < 8; ++i) out[i] = v[i];
+    long long v[9] = {ncells_, nfaces_, d_, launches_per_iteration(true), static_cast<long long>(bytes_),
+                      sizeof(T) == 4 ? AERO_PRECISION_FP32 : AERO_PRECISION_FP64, block_, ncb_, K_};
+    for (int i = 0; i < n && i < 9; ++i) out[i] = v[i];
   }
 
  private:
@@ -585,47 +695,201 @@ class EngineT final : public Engine {
   template <class U>
   U* upload(const std::vector<U>& v) {
     U* p = alloc<U>(v.size());
-    if (p) AERO_CK(cudaMemcpyAsync(p, v.data(), sizeof(U) * v.size(), cudaMemcpyHostToDevice, st_));
+    if (p && !v.empty()) AERO_CK(cudaMemcpyAsync(p, v.data(), sizeof(U) * v.size(), cudaMemcpyHostToDevice, st_));
     AERO_CK(cudaStreamSynchronize(st_));
     return p;
   }
 
-  bool second_at(int it) const { return it >= std::max(cfg_.startup_first_order_iters, 0); }
+  // Per-case constants: face parameters, preconditioner, monitors, controller.
+  void setup_case(int k) {
+    const aero_case_desc& cfg = cfg_[k];
+    const Resolved& rs = rs_[k];
+    const Pack& p = pk_[k];
+    FaceParams<T>& fp = fps_[k];
+    fp.gamma = T(rs.gamma);
+    fp.farfield = Cons<T>{T(rs.cons_inf[0]), T(rs.cons_inf[1]), T(rs.cons_inf[2]), T(rs.cons_inf[3])};
+    fp.limiter = cfg.limiter;
+    fp.precond = cfg.precond_on;
+    fp.low_mach_fix = cfg.low_mach_fix;
+    fp.precond_farfield_bc = cfg.precond_farfield_bc;
+    fp.as_fix = 0;
+    fp.mach_cutoff = T(cfg.mach_cutoff);
+    fp.pc_mach_ref = T(rs.pc_mach_ref);
+    fp.pc_mach_min = T(rs.pc_mach_min);
+    fp.pc_beta_min = T(rs.pc_beta_min);
+    fp.pc_beta_max = T(rs.pc_beta_max);
+    fp.stab_floor = T(0);
+    fp.as_cutoff = T(cfg.all_speed_mach_cutoff);
+    fp.as_fmin = T(rs.as_fmin);
+    fp.as_ramp = T(1);
+
+    PrecondD& pc = pcs_[k];
+    pc.enabled = cfg.precond_on;
+    pc.gamma = rs.gamma;
+    pc.mach_ref = double(fp.pc_mach_ref);
+    pc.mach_min = double(fp.pc_mach_min);
+    pc.beta_min = double(fp.pc_beta_min);
+    pc.beta_max = double(fp.pc_beta_max);
+    pc.gamma_f = float(rs.gamma);
+    pc.gm1_f = float(rs.gamma - 1.0);
+
+    MonitorConsts& mc = mcs_[k];
+    mc.p_inf = rs.p_inf;
+    mc.rho_inf = rs.rho_inf;
+    mc.u_inf = rs.v_inf * rs.cos_a;
+    mc.v_inf = rs.v_inf * rs.sin_a;
+    mc.q_inf = rs.q_inf;
+    mc.x_ref = cfg.x_ref;
+    mc.y_ref = cfg.y_ref;
+    mc.gamma = rs.gamma;
+    mc.p_inf_f = float(mc.p_inf);
+    mc.rho_inf_f = float(mc.rho_inf);
+    mc.u_inf_f = float(mc.u_inf);
+    mc.v_inf_f = float(mc.v_inf);
+    mc.q_inf_f = float(mc.q_inf);
+    mc.x_ref_f = float(mc.x_ref);
+    mc.y_ref_f = float(mc.y_ref);
+    const bool sym = cfg.aoa0_symmetry_enforce && cfg.aoa0_symmetry_enforce_interval > 0 &&
+                     !(std::fabs(cfg.aoa_deg) > 1.0e-12);
+    mc.sym_interval = sym ? cfg.aoa0_symmetry_enforce_interval : 0;
+
+    CtrlConfig& c = ccs_[k];
+    std::memset(&c, 0, sizeof(c));
+    c.n_cells = p.n;
+    c.n_wall = hs_[k].n_slip;
+    c.n_wall_blocks = p.nws;
+    c.wall_base = p.ws0;
+    c.block_base = p.cb0;
+    c.n_blocks = p.ncb;
+    c.bulk_f32 = sizeof(T) == 4 ? 1 : 0;
+    c.rk_stages = cfg.rk_stages;
+    c.local_dt = cfg.local_time_stepping;
+    c.cfl_ramp = cfg.cfl_ramp_iters;
+    c.stab_ramp = std::max(cfg.stab_ramp_iters, 0);
+    c.as_ramp_start = std::max(cfg.all_speed_ramp_start_iter, 0);
+    c.as_ramp_iters = std::max(cfg.all_speed_ramp_iters, 0);
+    c.startup_first_order = cfg.startup_first_order_iters;
+    c.min_iterations = cfg.min_iterations;
+    c.window = std::min(std::max(cfg.force_stability_window, 1), kMaxForceWindow);
+    c.staged = cfg.all_speed_staged_controller;
+    c.st_a_min = std::max(cfg.all_speed_stage_a_min_iters, 0);
+    c.st_a_max = std::max(cfg.all_speed_stage_a_max_iters, 0);
+    c.pj_hold = std::max(cfg.all_speed_pjump_hold_iters, 1);
+    c.freeze_iters = std::max(cfg.all_speed_freeze_iters, 0);
+    c.as_fix_cfg = cfg.all_speed_flux_fix;
+    c.pjump_blocks = (cfg.all_speed_staged_controller || cfg.diagnostics) ? p.ncb : 0;
+    c.cfl_start = cfg.cfl_start;
+    c.cfl_max = cfg.cfl_max;
+    c.stab_start = rs.stab_start;
+    c.stab_target = rs.stab_target;
+    c.as_fmin = rs.as_fmin;
+    c.residual_target = cfg.residual_reduction_target;
+    c.stab_tol = cfg.force_stability_tol;
+    c.drift_tol = cfg.force_mean_drift_tol > 0.0 ? cfg.force_mean_drift_tol : cfg.force_stability_tol;
+    c.st_fmin_high = rs.st_fmin_high;
+    c.st_fmin_mid = rs.st_fmin_mid;
+    c.st_fmin_low = rs.st_fmin_low;
+    c.pj_target = rs.pj_target;
+    c.pj_spike = rs.pj_spike;
+    c.cfl_drop = rs.cfl_drop;
+    c.cfl_restore = rs.cfl_restore;
+    c.cfl_min_scale = rs.cfl_min_scale;
+    c.p_inf = rs.p_inf;
+    c.q_inf = rs.q_inf;
+    c.chord = std::max(cfg.chord, 1.0e-8);
+    c.s_ref = c.chord * 1.0;
+    c.cos_a = rs.cos_a;
+    c.sin_a = rs.sin_a;
+    c.x_ref = cfg.x_ref;
+    c.y_ref = cfg.y_ref;
+    c.pressure_ref = rs.pressure_ref;
+    c.gamma = rs.gamma;
+    c.rho_inf = rs.rho_inf;
+    c.u_inf = rs.v_inf * rs.cos_a;
+    c.v_inf = rs.v_inf * rs.sin_a;
+    c.rho_l2_target = cfg.density_l2_target;
+  }
+
+  void download_ctrls() {
+    host_ctrls_.resize(K_);
+    AERO_CK(cudaMemcpyAsync(host_ctrls_.data(), ctrls_, sizeof(Ctrl) * K_, cudaMemcpyDeviceToHost, st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+  }
+
+  // Start/end of a run whose records are not kept (timing, profiling).
+  int begin_untracked() {
+    if (!w_valid_) refresh();
+    download_ctrls();
+    std::vector<int> base(K_, -(1 << 30));
+    AERO_CK(cudaMemcpy2DAsync(&ctrls_->rec_base, sizeof(Ctrl), base.data(), sizeof(int), sizeof(int), K_,
+                              cudaMemcpyHostToDevice, st_));
+    int it0 = 0;
+    for (const Ctrl& c : host_ctrls_) it0 = std::max(it0, c.iter);
+    return it0;
+  }
+  int end_untracked() {
+    download_ctrls();
+    if (err_ != cudaSuccess) return AERO_ERR_CUDA;
+    for (const Ctrl& c : host_ctrls_) {
+      if (c.nonfinite) return AERO_ERR_NONFINITE;
+    }
+    return AERO_OK;
+  }
+
+  d4* pinned_state() {
+    if (pin_state_ == nullptr) {
+      int nmax = 0;
+      for (const Pack& p : pk_) nmax = std::max(nmax, p.n);
+      if (cudaMallocHost(reinterpret_cast<void**>(&pin_state_), sizeof(d4) * static_cast<size_t>(nmax)) !=
+          cudaSuccess) {
+        cudaGetLastError();
+        pin_state_ = nullptr;
+        pin_fallback_.resize(static_cast<size_t>(nmax));
+        return pin_fallback_.data();
+      }
+    }
+    return pin_state_;
+  }
+
+  bool second_at(int it) const { return it >= std::max(cfg_[0].startup_first_order_iters, 0); }
 
   long long launches_per_iteration(bool second) const {
     // gradient, face pass, update (+ cell pass and time-step reduction with a global step)
-    const int per_stage = (second ? 1 : 0) + 2 + (cfg_.local_time_stepping ? 0 : 2);
-    return static_cast<long long>(per_stage) * cfg_.rk_stages + (pjump_on_ ? 1 : 0) + (sym_on_ ? 1 : 0) + 1;
+    const int per_stage = (second ? 1 : 0) + 2 + (cfg_[0].local_time_stepping ? 0 : 2);
+    return static_cast<long long>(per_stage) * cfg_[0].rk_stages + (pjump_on_ ? 1 : 0) + (sym_on_ ? 1 : 0) + 1;
   }
 
   void refresh() {
     if constexpr (sizeof(T) == 4) {
-      k_prim_from_image<<<nblocks_, block_, 0, st_>>>(n_, sref_.hi, W_, pc_.gamma_f);
+      k_prim_from_image<<<ncb_, block_, 0, st_>>>(ntot_, sref_.hi, W_, pcs_[0].gamma_f);
     } else {
-      k_refresh_prim<T><<<nblocks_, block_, 0, st_>>>(n_, Un_, W_, rs_.gamma);
+      k_refresh_prim<T><<<ncb_, block_, 0, st_>>>(ntot_, Un_, W_, rs_[0].gamma);
     }
     AERO_CK(cudaGetLastError());
     w_valid_ = true;
   }
 
   // FP32 keeps the state as float-float pairs and uses Un_ as the double staging array.
-  void state_from_staging() {
-    if (sizeof(T) == 4) k_split_state<<<nblocks_, block_, 0, st_>>>(n_, Un_, sref_.hi, sref_.lo);
+  void state_from_staging(int c0, int n) {
+    const int grid = (n + block_ - 1) / block_;
+    if (sizeof(T) == 4) k_split_state<<<grid, block_, 0, st_>>>(n, Un_ + c0, sref_.hi + c0, sref_.lo + c0);
     AERO_CK(cudaGetLastError());
   }
-  void state_to_staging() {
-    if (sizeof(T) == 4) k_combine_state<<<nblocks_, block_, 0, st_>>>(n_, sref_.hi, sref_.lo, Un_);
+  void state_to_staging(int c0, int n) {
+    const int grid = (n + block_ - 1) / block_;
+    if (sizeof(T) == 4) k_combine_state<<<grid, block_, 0, st_>>>(n, sref_.hi + c0, sref_.lo + c0, Un_ + c0);
     AERO_CK(cudaGetLastError());
   }
 
-  void download_residual(double* res, double* sr) {
-    std::vector<V4> hr(static_cast<size_t>(n_));
-    std::vector<T> hs(static_cast<size_t>(n_));
-    AERO_CK(cudaMemcpyAsync(hr.data(), R_, sizeof(V4) * n_, cudaMemcpyDeviceToHost, st_));
-    AERO_CK(cudaMemcpyAsync(hs.data(), SR_, sizeof(T) * n_, cudaMemcpyDeviceToHost, st_));
+  void download_residual(int k, double* res, double* sr) {
+    const Pack& p = pk_[k];
+    std::vector<V4> hr(static_cast<size_t>(p.n));
+    std::vector<T> hs(static_cast<size_t>(p.n));
+    AERO_CK(cudaMemcpyAsync(hr.data(), R_ + p.c0, sizeof(V4) * p.n, cudaMemcpyDeviceToHost, st_));
+    AERO_CK(cudaMemcpyAsync(hs.data(), SR_ + p.c0, sizeof(T) * p.n, cudaMemcpyDeviceToHost, st_));
     AERO_CK(cudaStreamSynchronize(st_));
-    for (int cn = 0; cn < n_; ++cn) {
-      const int co = hs_.perm[cn];
+    for (int cn = 0; cn < p.n; ++cn) {
+      const int co = hs_[k].perm[cn];
       double* r = res + 5 * static_cast<size_t>(co);
       r[0] = hr[cn].x;
       r[1] = hr[cn].y;
@@ -636,13 +900,14 @@ class EngineT final : public Engine {
     }
   }
 
-  ResidualLaunch<T> residual_args(Ctrl* ctrl, int* fb, V4* R, T* SR, int global_dt) {
+  ResidualLaunch<T> residual_args(int* fb, V4* R, T* SR, int global_dt) {
     ResidualLaunch<T> a;
     a.block = block_;
     a.st = st_;
     a.faces = df_;
     a.gather = dg_;
-    a.fp = fp_;
+    a.face_cases = face_cases_;
+    a.cell_cases = cell_cases_;
     a.W = W_;
     a.gx = gx_;
     a.gy = gy_;
@@ -651,19 +916,15 @@ class EngineT final : public Engine {
     a.R = R;
     a.SR = SR;
     a.part = part_;
-    a.ctrl = ctrl;
     a.fb = fb;
     a.global_dt = global_dt;
     return a;
   }
-  void launch_residual(bool second, bool norms, Ctrl* ctrl, int* fb, V4* R, T* SR, int global_dt) {
-    launch_residual_passes(residual_args(ctrl, fb, R, SR, global_dt), cfg_.flux, second, rs_.lm != 0, norms);
-  }
 
   template <bool PRECOND, bool LAST, bool GATHER>
   void update_t(int stage, int global_dt, V4* R, T* SR) {
-    k_update<T, PRECOND, LAST, GATHER><<<nblocks_, block_, 0, st_>>>(n_, stage, pc_, R, SR, dg_, F_, FS_, W_, sref_,
-                                                                     Us_, ms_, part_, ctrl_, global_dt);
+    k_update<T, PRECOND, LAST, GATHER><<<ncb_, block_, 0, st_>>>(stage, cell_cases_, R, SR, dg_, F_, FS_, W_, sref_,
+                                                                 Us_, ms_, part_, global_dt);
   }
   template <bool PRECOND>
   void update_p(int stage, bool last, int global_dt, V4* R, T* SR) {
@@ -687,12 +948,12 @@ class EngineT final : public Engine {
   // (iteration & 1) selects the fallback counters. With `defer`, the controller of this
   // iteration is left to the next one (or to launch_control); with `pending`, the previous
   // iteration's controller (parity ^ 1) is forked onto the side stream beside this
-  // iteration's gradient and first residual and joined before the first update, the first
+  // iteration's gradient and first face pass and joined before the first update, the first
   // kernel that reads its outputs.
   template <class Wrap>
   void launch_iteration(bool second, int parity, bool defer, bool pending, Wrap&& wrap) {
-    const int global_dt = cfg_.local_time_stepping ? 0 : 1;
-    const int ns = cfg_.rk_stages;
+    const int global_dt = cfg_[0].local_time_stepping ? 0 : 1;
+    const int ns = cfg_[0].rk_stages;
     int* fb = fb_ + 2 * parity;
     for (int stage = 0; stage < ns; ++stage) {
       const bool last = stage == ns - 1;
@@ -702,20 +963,20 @@ class EngineT final : public Engine {
         AERO_CK(cudaEventRecord(ev_fork_, st_));
         AERO_CK(cudaStreamWaitEvent(side_, ev_fork_, 0));
         wrap(5, [&] {
-          k_control<<<1, kCtlThreads, 0, side_>>>(cc_, part_, ctrl_, recs_, rec_cap_, fb_ + 2 * (parity ^ 1));
+          k_control<<<K_, kCtlThreads, 0, side_>>>(ccs_dev_, part_, ctrls_, recs_, rec_cap_, fb_ + 2 * (parity ^ 1));
         });
         AERO_CK(cudaEventRecord(ev_join_, side_));
       }
-      if (second) wrap(0, [&] { k_gradient<T><<<nblocks_, block_, 0, st_>>>(dm_, W_, gx_, gy_, ctrl_); });
-      const ResidualLaunch<T> ra = residual_args(ctrl_, fb, R, SR, global_dt);
-      wrap(1, [&] { launch_face_pass(ra, cfg_.flux, second, rs_.lm != 0); });
+      if (second) wrap(0, [&] { k_gradient<T><<<ncb_, block_, 0, st_>>>(dm_, W_, gx_, gy_, cell_cases_); });
+      const ResidualLaunch<T> ra = residual_args(fb, R, SR, global_dt);
+      wrap(1, [&] { launch_face_pass(ra, cfg_[0].flux, second, lm_ != 0); });
       if (global_dt) wrap(1, [&] { launch_gather_pass(ra, last); });
       if (stage == 0 && pending) AERO_CK(cudaStreamWaitEvent(st_, ev_join_, 0));
       if (global_dt) {
-        wrap(3, [&] { k_srmax<<<1, 1024, 0, st_>>>(part_.srmax, nblocks_ * (block_ / 32), ctrl_); });
+        wrap(3, [&] { k_srmax<<<K_, 1024, 0, st_>>>(part_.srmax, srfirst_, ctrls_); });
       }
       wrap(2, [&] {
-        if (cfg_.precond_on) {
+        if (cfg_[0].precond_on) {
           update_p<true>(stage, last, global_dt, R, SR);
         } else {
           update_p<false>(stage, last, global_dt, R, SR);
@@ -723,20 +984,17 @@ class EngineT final : public Engine {
       });
     }
     if (sym_on_) {
-      wrap(4, [&] {
-        k_symmetry<T><<<nblocks_, block_, 0, st_>>>(n_, cfg_.aoa0_symmetry_enforce_interval, rs_.gamma, sref_,
-                                                     W_, ms_, part_, ctrl_);
-      });
+      wrap(4, [&] { k_symmetry<T><<<ncb_, block_, 0, st_>>>(cell_cases_, sref_, W_, ms_, part_); });
     }
     if (pjump_on_) {
-      wrap(4, [&] { k_pjump<T><<<nblocks_, block_, 0, st_>>>(dm_, sref_, flags_, rs_.gamma, part_, ctrl_); });
+      wrap(4, [&] { k_pjump<T><<<ncb_, block_, 0, st_>>>(dm_, sref_, flags_, cell_cases_, part_); });
     }
     if (!defer) launch_control(parity, wrap);
     AERO_CK(cudaGetLastError());
   }
   template <class Wrap>
   void launch_control(int parity, Wrap&& wrap) {
-    wrap(5, [&] { k_control<<<1, kCtlThreads, 0, st_>>>(cc_, part_, ctrl_, recs_, rec_cap_, fb_ + 2 * parity); });
+    wrap(5, [&] { k_control<<<K_, kCtlThreads, 0, st_>>>(ccs_dev_, part_, ctrls_, recs_, rec_cap_, fb_ + 2 * parity); });
   }
 
   // Iterations it0 .. it0+n-1 back to back, through the per-iteration CUDA graphs; with the
@@ -752,35 +1010,6 @@ class EngineT final : public Engine {
       if (defer_control_ && j == n - 1) launch_control(it & 1, Direct{});
       after(j);
     }
-  }
-
-  // Start/end of a run whose records are not kept (timing, profiling).
-  int begin_untracked() {
-    if (!w_valid_) refresh();
-    AERO_CK(cudaMemcpyAsync(&host_ctrl_, ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, st_));
-    AERO_CK(cudaStreamSynchronize(st_));
-    host_rec_base_ = -(1 << 30);
-    AERO_CK(cudaMemcpyAsync(&ctrl_->rec_base, &host_rec_base_, sizeof(int), cudaMemcpyHostToDevice, st_));
-    return host_ctrl_.iter;
-  }
-  int end_untracked() {
-    AERO_CK(cudaMemcpyAsync(&host_ctrl_, ctrl_, sizeof(Ctrl), cudaMemcpyDeviceToHost, st_));
-    AERO_CK(cudaStreamSynchronize(st_));
-    if (err_ != cudaSuccess) return AERO_ERR_CUDA;
-    return host_ctrl_.nonfinite ? AERO_ERR_NONFINITE : AERO_OK;
-  }
-
-  d4* pinned_state() {
-    if (pin_state_ == nullptr) {
-      if (cudaMallocHost(reinterpret_cast<void**>(&pin_state_), sizeof(d4) * static_cast<size_t>(n_)) !=
-          cudaSuccess) {
-        cudaGetLastError();
-        pin_state_ = nullptr;
-        pin_fallback_.resize(static_cast<size_t>(n_));
-        return pin_fallback_.data();
-      }
-    }
-    return pin_state_;
   }
 
   bool ensure_flush_buffer() {
@@ -820,14 +1049,18 @@ class EngineT final : public Engine {
     }
   }
 
-  HostSlots hs_;
-  aero_case_desc cfg_;
-  Resolved rs_;
+  std::vector<HostSlots> hs_;
+  std::vector<aero_case_desc> cfg_;
+  std::vector<Resolved> rs_;
   cudaStream_t st_;
   cudaError_t err_ = cudaSuccess;
   std::vector<void*> allocs_;
   size_t bytes_ = 0;
-  int n_ = 0, d_ = 0, block_ = 128, nblocks_ = 0, rec_cap_ = 0;
+  int K_ = 0, lm_ = 0;
+  std::vector<Pack> pk_;
+  int ntot_ = 0, ftot_ = 0, ncb_ = 0, nfb_ = 0, nwslots_ = 0, d_ = 0;
+  long long ncells_ = 0, nfaces_ = 0;
+  int block_ = 128, rec_cap_ = 0;
   bool pjump_on_ = false, sym_on_ = false, w_valid_ = false;
   int* link_ = nullptr;
   V2* nrm_ = nullptr;
@@ -838,31 +1071,39 @@ class EngineT final : public Engine {
   T* FS_ = nullptr;   // per face: wave-speed term
   T* inv_vol_ = nullptr;
   unsigned char* flags_ = nullptr;
-  int* perm_dev_ = nullptr;
+  int* perm_dev_ = nullptr;  // case 0: new -> original cell
+  int2* cblk_ = nullptr;     // per cell block: (case, end of the case's cells)
+  int2* fblk_ = nullptr;     // per face block: (case, end of the case's faces)
+  int* srfirst_ = nullptr;   // per case: first per-warp time-step partial, [K + 1]
   MonitorSet ms_{};
   V4 *W_ = nullptr, *gx_ = nullptr, *gy_ = nullptr, *R_ = nullptr;
   T* SR_ = nullptr;
   d4* Un_ = nullptr;     // FP64: the conserved state; FP32: double staging for transfers
   StateRef sref_{};
-  V4* Us_ = nullptr;    // FP64: stage state; FP32: stage increment (delta form)
+  V4* Us_ = nullptr;     // FP64: stage state; FP32: stage increment (delta form)
   d4* Ueval_ = nullptr;  // conserved state given to aero_residual
   Partials part_{};
-  Ctrl* ctrl_ = nullptr;
-  Ctrl* ctrl_eval_ = nullptr;
-  Record* recs_ = nullptr;
-  Ctrl host_ctrl_{};
-  int host_rec_base_ = 0;
+  Ctrl* ctrls_ = nullptr;      // [K]
+  Ctrl* ctrl_eval_ = nullptr;  // aero_residual
+  Record* recs_ = nullptr;     // [K][rec_cap]
+  CtrlConfig* ccs_dev_ = nullptr;
+  FaceParams<T>* fps_dev_ = nullptr;
+  PrecondD* pcs_dev_ = nullptr;
+  MonitorConsts* mcs_dev_ = nullptr;
+  std::vector<CtrlConfig> ccs_;
+  std::vector<FaceParams<T>> fps_;
+  std::vector<PrecondD> pcs_;
+  std::vector<MonitorConsts> mcs_;
+  std::vector<Ctrl> host_ctrls_;
+  Cases<T> cell_cases_{}, face_cases_{};
   DevMesh<T> dm_{};
-  FaceParams<T> fp_{};
-  PrecondD pc_{};
-  CtrlConfig cc_{};
   cudaGraphExec_t graph_[16] = {};
   bool defer_control_ = false;
   cudaStream_t side_ = nullptr;
   cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
   V4* R0_ = nullptr;
   T* SR0_ = nullptr;
-  int* fb_ = nullptr;  // [2 parities][first-order, diffusive] fallback counters
+  int* fb_ = nullptr;  // [case][2 parities][first-order, diffusive] fallback counters
   void* flush_ = nullptr;
   size_t flush_bytes_ = 0;
   d4* pin_state_ = nullptr;

@@ -99,8 +99,7 @@ cudaError_t run_na(const EngineView& v, unsigned char* base, const double* u, in
                    int as_fix, double as_fmin, double as_ramp, double* res, double* sr, cudaStream_t st) {
   using V4 = typename Vec<T>::v4;
   const DevMesh<T>& dm = *static_cast<const DevMesh<T>*>(v.dm);
-  const FaceParams<T>& fp = *static_cast<const FaceParams<T>*>(v.fp);
-  const int n = v.n;
+  const int n = v.n, ntot = v.ntot;
   Ctrl* ctrl = reinterpret_cast<Ctrl*>(base);
   unsigned char* p = base + kCtrlBytes;
   auto take = [&](size_t bytes) {
@@ -108,23 +107,28 @@ cudaError_t run_na(const EngineView& v, unsigned char* base, const double* u, in
     p += align_up(bytes);
     return q;
   };
-  V4* W = reinterpret_cast<V4*>(take(sizeof(V4) * n));
-  V4* gx = reinterpret_cast<V4*>(take(sizeof(V4) * n));
-  V4* gy = reinterpret_cast<V4*>(take(sizeof(V4) * n));
-  V4* R = reinterpret_cast<V4*>(take(sizeof(V4) * n));
-  T* SR = reinterpret_cast<T*>(take(sizeof(T) * n));
+  V4* W = reinterpret_cast<V4*>(take(sizeof(V4) * ntot));
+  V4* gx = reinterpret_cast<V4*>(take(sizeof(V4) * ntot));
+  V4* gy = reinterpret_cast<V4*>(take(sizeof(V4) * ntot));
+  V4* R = reinterpret_cast<V4*>(take(sizeof(V4) * ntot));
+  T* SR = reinterpret_cast<T*>(take(sizeof(T) * ntot));
   V4* F = reinterpret_cast<V4*>(take(sizeof(V4) * v.nf));
   T* FS = reinterpret_cast<T*>(take(sizeof(T) * v.nf));
   const int block = v.block;
-  const int grid = (n + block - 1) / block;
-  k_na_prepare<T><<<grid, block, 0, st>>>(n, v.perm_dev, u, W, double(fp.gamma), ctrl, stab, as_fix, as_fmin, as_ramp);
-  if (second) k_gradient<T><<<grid, block, 0, st>>>(dm, W, gx, gy, ctrl);
+  const FaceParams<T>* fps = static_cast<const FaceParams<T>*>(v.fps);
+  const PrecondD* pcs = static_cast<const PrecondD*>(v.pcs);
+  const MonitorConsts* mcs = static_cast<const MonitorConsts*>(v.mcs);
+  const Cases<T> cells{v.cblk, ctrl, fps, pcs, mcs};
+  const Cases<T> faces{v.fblk, ctrl, fps, pcs, mcs};
+  k_na_prepare<T><<<v.cblocks, block, 0, st>>>(n, v.perm_dev, u, W, v.gamma, ctrl, stab, as_fix, as_fmin, as_ramp);
+  if (second) k_gradient<T><<<v.cblocks, block, 0, st>>>(dm, W, gx, gy, cells);
   ResidualLaunch<T> a;
   a.block = block;
   a.st = st;
   a.faces = *static_cast<const DevFaces<T>*>(v.df);
   a.gather = *static_cast<const DevGather<T>*>(v.dg);
-  a.fp = fp;
+  a.face_cases = faces;
+  a.cell_cases = cells;
   a.W = W;
   a.gx = gx;
   a.gy = gy;
@@ -133,11 +137,10 @@ cudaError_t run_na(const EngineView& v, unsigned char* base, const double* u, in
   a.R = R;
   a.SR = SR;
   a.part = Partials{};
-  a.ctrl = ctrl;
   a.fb = &ctrl->fo_fallback;
   a.global_dt = 0;
   launch_residual_passes(a, v.flux, second != 0, v.lm != 0, false);
-  k_na_store<T><<<grid, block, 0, st>>>(n, v.perm_dev, R, SR, res, sr);
+  k_na_store<T><<<v.cblocks, block, 0, st>>>(n, v.perm_dev, R, SR, res, sr);
   return cudaGetLastError();
 }
 
@@ -155,7 +158,11 @@ int aero_residual_noalloc(aero_ctx* ctx, const double* conserved_dev, int second
     return AERO_ERR_INVALID;
   }
   const aero::EngineView v = ctx->engine->view();
-  if (v.n > aero::kNoallocMaxCells || v.nf > aero::kNoallocMaxFaces) {
+  if (ctx->engine->n_cases() != 1) {
+    ctx->error = "aero_residual_noalloc: batched context";
+    return AERO_ERR_INVALID;
+  }
+  if (v.ntot > aero::kNoallocMaxCells || v.nf > aero::kNoallocMaxFaces) {
     ctx->error = "aero_residual_noalloc: the mesh has " + std::to_string(v.n) + " cells and " +
                  std::to_string(v.nf) + " faces; the allocation-free residual supports at most " +
                  std::to_string(aero::kNoallocMaxCells) + " cells and " +

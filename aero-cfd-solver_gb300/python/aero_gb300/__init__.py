@@ -79,6 +79,12 @@ def load(build_if_missing: bool = False):
         "aero_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip]),
         "aero_select_device": (C.c_int, [C.c_int]),
         "aero_get_info": (C.c_int, [C.c_void_p, _llp, C.c_int]),
+        "aero_batch_create": (C.c_int, [C.c_int, C.POINTER(MeshDesc), C.POINTER(CaseDesc), C.POINTER(C.c_void_p)]),
+        "aero_batch_size": (C.c_int, [C.c_void_p]),
+        "aero_batch_run": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(IterRecord), _ip]),
+        "aero_batch_set_state": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+        "aero_batch_get_state": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+        "aero_batch_get_last_residual": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
         "aero_mesh_ogrid_reference": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double,
                                                 C.c_double, C.POINTER(C.c_void_p)]),
         "aero_mesh_ogrid_synthetic": (C.c_int, [C.POINTER(OgridSpec), C.POINTER(C.c_void_p)]),
@@ -266,8 +272,65 @@ class Solver:
         return {k: (ms[i], launches[i]) for i, k in enumerate(self.KERNEL_CLASSES)}
 
     def info(self) -> dict:
-        v = (C.c_longlong * 8)()
-        self._check(self.lib.aero_get_info(self.h, v, 8))
+        v = (C.c_longlong * 9)()
+        self._check(self.lib.aero_get_info(self.h, v, 9))
         keys = ("cells", "faces", "slots_per_cell", "launches_per_iteration", "device_bytes", "precision",
-                "block_size", "blocks")
+                "block_size", "blocks", "cases")
         return dict(zip(keys, list(v)))
+
+
+class Batch(Solver):
+    """Many cases advanced together in one device context (aero_batch_create): meshes of
+    uneven size and per-case flow conditions, one set of packed arrays, one CUDA graph per
+    iteration. Each case's results equal a single-case run of it."""
+
+    def __init__(self, meshes, cases):
+        assert len(meshes) == len(cases) and len(meshes) > 0
+        self.lib = load()
+        self.meshes = list(meshes)
+        self.cases = list(cases)
+        self._mdescs = (MeshDesc * len(meshes))(*[m.desc() for m in self.meshes])
+        self._cdescs = (CaseDesc * len(cases))(*self.cases)
+        h = C.c_void_p()
+        rc = self.lib.aero_batch_create(len(meshes), self._mdescs, self._cdescs, C.byref(h))
+        if rc != 0:
+            raise AeroError(rc, self.lib.aero_last_error(None).decode())
+        self.h = h
+        self.k = len(meshes)
+        self.sizes = [m.num_cells for m in self.meshes]
+
+    def set_state(self, k: int, u: np.ndarray):
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        assert u.size == 5 * self.sizes[k]
+        self._check(self.lib.aero_batch_set_state(self.h, k, u.ctypes.data_as(_dp)))
+
+    def get_state(self, k: int) -> np.ndarray:
+        u = np.empty(5 * self.sizes[k], np.float64)
+        self._check(self.lib.aero_batch_get_state(self.h, k, u.ctypes.data_as(_dp)))
+        return u.reshape(self.sizes[k], 5)
+
+    def run(self, n: int, raise_on_nonfinite: bool = True):
+        """Returns (status, [records of case k]) with each case's records as a structured array."""
+        recs = (IterRecord * max(n * self.k, 1))()
+        done = (C.c_int * self.k)()
+        rc = self.lib.aero_batch_run(self.h, n, recs, done)
+        base = capi.records_to_array(recs, n * self.k) if n > 0 else None
+        out = [base[k * n: k * n + done[k]].copy() if n > 0 else capi.records_to_array(recs, 0)
+               for k in range(self.k)]
+        if rc == capi.AERO_ERR_NONFINITE and not raise_on_nonfinite:
+            return rc, out
+        self._check(rc)
+        return rc, out
+
+    def last_residual(self, k: int):
+        n = self.sizes[k]
+        r = np.empty(5 * n, np.float64)
+        s = np.empty(n, np.float64)
+        self._check(self.lib.aero_batch_get_last_residual(self.h, k, r.ctypes.data_as(_dp), s.ctypes.data_as(_dp)))
+        return r.reshape(n, 5), s
+
+    def residual(self, *args, **kw):
+        raise NotImplementedError("single residual evaluations need a single-case Solver")
+
+    def get_primitive(self):
+        raise NotImplementedError("use get_state(k)")

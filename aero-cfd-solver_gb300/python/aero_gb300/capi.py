@@ -97,6 +97,7 @@ _CASE_FIELDS = [
     ("ordering", C.c_int),
     ("block_size", C.c_int),
     ("diagnostics", C.c_int),
+    ("density_l2_target", C.c_double),
 ]
 
 
@@ -119,7 +120,7 @@ _REC_FIELDS = [
     "p_jump_energy_nd", "p_jump_energy_wall_nd",
     "max_wall_un", "max_wall_mass_flux", "wall_cp_min", "wall_cp_max",
     "max_farfield_abs_dp", "max_farfield_abs_drho", "max_farfield_abs_du", "max_farfield_abs_dv",
-)] + [("wall_cp_nonfinite", C.c_int), ("controller_action", C.c_int)]
+)] + [("wall_cp_nonfinite", C.c_int), ("controller_action", C.c_int), ("residual_rho_ratio", C.c_double)]
 
 
 class IterRecord(C.Structure):

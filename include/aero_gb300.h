@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define AERO_ABI_VERSION 1
+#define AERO_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define AERO_API __attribute__((visibility("default")))
@@ -115,6 +115,10 @@ typedef struct aero_case_desc {
   int ordering;  /* enum aero_ordering */
   int block_size; /* threads per block of the cell kernels (64, 128 or 256); 0 = default */
   int diagnostics; /* 1: also form the pressure-jump energies of every iteration */
+  /* > 0: the run also stops (converged) once min_iterations are done and the density
+   * residual's L2 norm has fallen to this fraction of its first value (the per-case mask of
+   * a batched sweep); 0: the reference's stop rule only. No reference counterpart. */
+  double density_l2_target;
 } aero_case_desc;
 
 /* One record per pseudo-time iteration: the rows of residuals.csv and forces.csv
@@ -137,6 +141,8 @@ typedef struct aero_iter_record {
   double max_farfield_abs_dp, max_farfield_abs_drho, max_farfield_abs_du, max_farfield_abs_dv;
   int wall_cp_nonfinite;
   int controller_action; /* all-speed controller action code (euler_solver.cpp:1068-1139) */
+  /* L2 norm of the density residual / its first value (no reference counterpart) */
+  double residual_rho_ratio;
 } aero_iter_record;
 
 enum aero_record_flags {

@@ -40,7 +40,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_identity(lib):
-    assert lib.aero_abi_version() == 1
+    assert lib.aero_abi_version() == 2
     assert lib.aero_version().decode().endswith("gb300")
 
 
@@ -72,6 +72,6 @@ def test_invalid_arguments_are_rejected(lib):
 
 
 def test_record_struct_size_matches_header():
-    # aero_iter_record: 4 ints + 42 doubles + 2 ints
-    assert C.sizeof(capi.IterRecord) == 4 * 4 + 42 * 8 + 2 * 4
+    # aero_iter_record: 4 ints + 42 doubles + 2 ints + 1 double
+    assert C.sizeof(capi.IterRecord) == 4 * 4 + 42 * 8 + 2 * 4 + 8
     assert np.dtype(capi.RECORD_DTYPE).itemsize == C.sizeof(capi.IterRecord)

@@ -265,6 +265,42 @@ def run_reference_arm(args):
 
 
 # ------------------------------------------------------------------------------------------
+# Batched sweep (the AoA/Mach sweep configuration): 96 cases in one batched context
+# ------------------------------------------------------------------------------------------
+C4_SIZES = [(64, 16), (128, 32), (256, 64), (512, 128)]
+C4_CASES = 96
+
+
+def c4_sweep(args, aero_gb300, capi, rank):
+    """96 FP32 cases, mesh sizes drawn from the four O-grids, alpha ~ U[-4, 8] deg, M ~
+    U[0.3, 0.85], HLLC + MUSCL venkat, per-case CFL ramp to 0.8 and a density-residual stop
+    mask at 1e-8 relative; seeded synthetic inputs. Returns device ms of `steps` iterations
+    (L2 flushed before each) and the batch's cell count."""
+    rng = np.random.default_rng(4 + rank)
+    base = {sz: aero_gb300.ogrid_synthetic(sz[0], sz[1], cell_type=3, permute=True, jitter=0.1, seed=100 + i,
+                                           wall_spacing=0.005, farfield_radius=20.0)
+            for i, sz in enumerate(C4_SIZES)}
+    pick = rng.integers(0, len(C4_SIZES), C4_CASES)
+    alphas = rng.uniform(-4.0, 8.0, C4_CASES)
+    machs = rng.uniform(0.3, 0.85, C4_CASES)
+    meshes = [base[C4_SIZES[i]] for i in pick]
+    cases = []
+    for k in range(C4_CASES):
+        kw = dict(CASE)
+        kw.update(mach=float(machs[k]), aoa_deg=float(alphas[k]))
+        c = capi.make_case(**kw, precision=capi.PRECISION_FP32)
+        c.density_l2_target = 1e-8
+        cases.append(c)
+    with aero_gb300.Batch(meshes, cases) as b:
+        cells = b.info()["cells"]
+        b.run(STARTUP)
+        b.time_iterations(args.warmup, use_graph=True, flush_l2=True)
+        ms = b.time_iterations(args.steps, use_graph=True, flush_l2=not args.no_flush)
+        launches = b.info()["launches_per_iteration"]
+    return ms, int(cells), int(launches)
+
+
+# ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
 def run_gpu_arm(args):
@@ -343,6 +379,19 @@ def run_gpu_arm(args):
                "h2d_bytes_per_step": int(u0.nbytes / args.steps),
                "d2h_bytes_per_step": int((rec_bytes + u1.nbytes) / args.steps)}
 
+    c4 = None
+    if not args.no_c4 and "fp32" in precisions:
+        barrier(dist)
+        c4_ms, c4_cells, c4_launch = c4_sweep(args, aero_gb300, capi, rank)
+        c4_ms = reduce_max(dist, c4_ms)
+        c4 = {"cases_per_gpu": C4_CASES, "cells_per_gpu": c4_cells, "steps": args.steps,
+              "ms_per_step": c4_ms / args.steps,
+              "fp32_batched_mcell_iter_s": world * c4_cells * args.steps / (c4_ms / 1e3) / 1e6,
+              "launches_per_step": c4_launch,
+              "inputs": "96 seeded cases per GPU: sizes from {64x16,128x32,256x64,512x128} triangulated "
+                        "O-grids, alpha~U[-4,8], M~U[0.3,0.85], HLLC+MUSCL venkat, CFL ramp to 0.8, "
+                        "density-residual stop mask 1e-8; one batched context, L2 flushed per step"}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu and head["state"] is not None:
         cpu = cpu_sample(mesh, head["state"])
@@ -369,6 +418,7 @@ def run_gpu_arm(args):
             "fp32_l2_warm_mcell_iter_s": world * n * args.steps / (r32["warm_ms"] / 1e3) / 1e6 if r32 else None,
             "fp64_l2_warm_mcell_iter_s": world * n * args.steps / (r64["warm_ms"] / 1e3) / 1e6 if r64 else None,
             "dcl": dcl,
+            "c4_batched_sweep": c4,
             "kernel_profile_ms_per_launch": {k: (v[0] / v[1] if v[1] else 0.0) for k, v in head["prof"].items()},
             "state_finite": head["finite"],
         },
@@ -400,6 +450,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-flush", action="store_true")
     ap.add_argument("--no-clocks", action="store_true")
+    ap.add_argument("--no-c4", action="store_true", help="skip the 96-case batched sweep measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -231,7 +231,7 @@ def run_reference_arm(args):
 
     op.build()
     mesh = make_mesh(args)
-    procs_n = max(1, os.cpu_count() or 1)
+    procs_n = args.cpu_procs if args.cpu_procs > 0 else max(1, os.cpu_count() or 1)
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     bar = ctx.Barrier(procs_n)
@@ -271,18 +271,25 @@ C4_SIZES = [(64, 16), (128, 32), (256, 64), (512, 128)]
 C4_CASES = 96
 
 
+def c4_draw(rank: int):
+    """The sweep's cases on one rank (ranks shard the sweep, each with its own seeded draw):
+    mesh size index, alpha (deg) and Mach per case."""
+    rng = np.random.default_rng(4 + rank)
+    pick = rng.integers(0, len(C4_SIZES), C4_CASES)
+    alphas = rng.uniform(-4.0, 8.0, C4_CASES)
+    machs = rng.uniform(0.3, 0.85, C4_CASES)
+    return pick, alphas, machs
+
+
 def c4_sweep(args, aero_gb300, capi, rank):
     """96 FP32 cases, mesh sizes drawn from the four O-grids, alpha ~ U[-4, 8] deg, M ~
     U[0.3, 0.85], HLLC + MUSCL venkat, per-case CFL ramp to 0.8 and a density-residual stop
     mask at 1e-8 relative; seeded synthetic inputs. Returns device ms of `steps` iterations
     (L2 flushed before each) and the batch's cell count."""
-    rng = np.random.default_rng(4 + rank)
     base = {sz: aero_gb300.ogrid_synthetic(sz[0], sz[1], cell_type=3, permute=True, jitter=0.1, seed=100 + i,
                                            wall_spacing=0.005, farfield_radius=20.0)
             for i, sz in enumerate(C4_SIZES)}
-    pick = rng.integers(0, len(C4_SIZES), C4_CASES)
-    alphas = rng.uniform(-4.0, 8.0, C4_CASES)
-    machs = rng.uniform(0.3, 0.85, C4_CASES)
+    pick, alphas, machs = c4_draw(rank)
     meshes = [base[C4_SIZES[i]] for i in pick]
     cases = []
     for k in range(C4_CASES):
@@ -451,6 +458,7 @@ def main():
     ap.add_argument("--no-flush", action="store_true")
     ap.add_argument("--no-clocks", action="store_true")
     ap.add_argument("--no-c4", action="store_true", help="skip the 96-case batched sweep measurement")
+    ap.add_argument("--cpu-procs", type=int, default=0, help="processes of the reference arm (0: all cores)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

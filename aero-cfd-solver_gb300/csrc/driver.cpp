@@ -8,6 +8,7 @@
 #include <array>
 #include <cctype>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -28,6 +29,9 @@ namespace fs = std::filesystem;
 namespace {
 
 thread_local std::string g_driver_error;
+// State file: this magic, int64 cell count, int64 components (5), then [N][5] doubles in the
+// reference's cell order and AoS layout, host byte order (little-endian on the targets).
+constexpr char kStateMagic[16] = {'A', 'E', 'R', 'O', '-', 'S', 'T', 'A', 'T', 'E', '-', 'v', '1', 0, 0, 0};
 const char* kVersion = "0.1.1";  // version string written to run.log (version.hpp of the reference)
 
 // ---------------------------------------------------------------------------------------
@@ -351,6 +355,39 @@ void write_array(std::ofstream& o, const std::vector<T>& v) {
   }
 }
 
+// Driver options beyond the reference's case keys (no reference counterpart): a state to
+// start from, a state dump after the run, and the VTU encoding.
+struct DriverOpts {
+  std::string restart_in;   // path of a state file (aero_state_write format); empty: free stream
+  std::string restart_out;  // file name in out_dir for the final state; empty: none
+  bool vtu_binary = false;  // VTU arrays as raw appended binary instead of ASCII
+};
+
+DriverOpts map_opts(const KV& kv, const fs::path& case_dir) {
+  DriverOpts o;
+  const std::string in = trim(get_s(kv, "restart_in", ""));
+  if (!in.empty()) o.restart_in = fs::path(in).is_absolute() ? in : (case_dir / in).string();
+  o.restart_out = trim(get_s(kv, "restart_out", ""));
+  const std::string vf = lower(trim(get_s(kv, "vtu_format", "ascii")));
+  if (vf != "ascii" && vf != "binary") throw std::invalid_argument("vtu_format must be ascii or binary");
+  o.vtu_binary = vf == "binary";
+  return o;
+}
+
+// Appended raw binary data of a VTU file: each array is a UInt32 byte count followed by its
+// bytes; DataArray elements give their offsets from the start of the appended block.
+struct Appended {
+  std::string bytes;
+  template <class T>
+  size_t add(const std::vector<T>& v) {
+    const size_t off = bytes.size();
+    const uint32_t nb = static_cast<uint32_t>(v.size() * sizeof(T));
+    bytes.append(reinterpret_cast<const char*>(&nb), sizeof(nb));
+    if (nb) bytes.append(reinterpret_cast<const char*>(v.data()), nb);
+    return off;
+  }
+};
+
 struct MeshHolder {
   aero_mesh* m = nullptr;
   ~MeshHolder() { aero_mesh_free(m); }
@@ -367,7 +404,7 @@ void check(int rc, aero_ctx* ctx, const char* what) {
 
 // run_euler_airfoil_case (euler_solver.cpp:463-1487) on the device.
 void run_euler(const aero_case_desc& cfg_in, const aero_airfoil_mesh_cfg& mc, const fs::path& out_dir,
-               aero_run_summary* summary) {
+               const DriverOpts& opts, aero_run_summary* summary) {
   if (cfg_in.iterations <= 0) throw std::invalid_argument("Euler iterations must be positive.");
   if (cfg_in.rk_stages != 1 && cfg_in.rk_stages != 3)
     throw std::invalid_argument("Euler pseudo-time rk_stages must be 1 or 3.");
@@ -497,6 +534,12 @@ void run_euler(const aero_case_desc& cfg_in, const aero_airfoil_mesh_cfg& mc, co
 
   CtxHolder ch;
   check(aero_create(&md, &cfg, &ch.c), nullptr, "aero_create");
+  if (!opts.restart_in.empty()) {  // start from a dumped state instead of the free stream
+    std::vector<double> u0(5 * static_cast<size_t>(N));
+    if (aero_state_read(opts.restart_in.c_str(), N, u0.data()) != AERO_OK)
+      throw std::invalid_argument(std::string("restart_in: ") + aero_driver_last_error());
+    check(aero_set_state(ch.c, u0.data()), ch.c, "aero_set_state");
+  }
 
   std::ofstream rcsv(out_dir / "residuals.csv", std::ios::trunc);
   std::ofstream fcsv(out_dir / "forces.csv", std::ios::trunc);
@@ -688,8 +731,38 @@ void run_euler(const aero_case_desc& cfg_in, const aero_airfoil_mesh_cfg& mc, co
       s += md.face_area[f];
     }
   }
+  if (!opts.restart_out.empty()) {
+    if (aero_state_write((out_dir / opts.restart_out).string().c_str(), N, U.data()) != AERO_OK)
+      throw std::runtime_error(std::string("restart_out: ") + aero_driver_last_error());
+  }
   // field_0000.vtu (io_vtk_stub.cpp:95-166)
-  {
+  if (opts.vtu_binary) {
+    std::ofstream o(out_dir / "field_0000.vtu", std::ios::trunc | std::ios::binary);
+    if (!o) throw std::runtime_error("Failed to write Euler VTU output.");
+    std::vector<float> pf(pts.begin(), pts.end());
+    Appended ap;
+    auto da = [&](const char* type, const char* name, int ncomp, size_t off) {
+      o << "        <DataArray type=\"" << type << "\"";
+      if (name) o << " Name=\"" << name << "\"";
+      if (ncomp > 1) o << " NumberOfComponents=\"" << ncomp << "\"";
+      o << " format=\"appended\" offset=\"" << off << "\"/>\n";
+    };
+    o << "<?xml version=\"1.0\"?>\n<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" byte_order=\"LittleEndian\" "
+         "header_type=\"UInt32\">\n  <UnstructuredGrid>\n    <Piece NumberOfPoints=\"" << sz.num_points
+      << "\" NumberOfCells=\"" << N << "\">\n      <Points>\n";
+    da("Float32", nullptr, 3, ap.add(pf));
+    o << "      </Points>\n      <Cells>\n";
+    da("Int32", "connectivity", 1, ap.add(conn));
+    da("Int32", "offsets", 1, ap.add(offs));
+    da("UInt8", "types", 1, ap.add(types));
+    o << "      </Cells>\n      <PointData/>\n      <CellData Scalars=\"rho\">\n";
+    const std::pair<const char*, const std::vector<float>*> arrays[] = {
+        {"rho", &rho}, {"u", &uu}, {"v", &vv}, {"p", &pp}, {"Mach", &mach}, {"residual_magnitude", &rmag}};
+    for (const auto& a : arrays) da("Float32", a.first, 1, ap.add(*a.second));
+    o << "      </CellData>\n    </Piece>\n  </UnstructuredGrid>\n  <AppendedData encoding=\"raw\">\n   _";
+    o.write(ap.bytes.data(), static_cast<std::streamsize>(ap.bytes.size()));
+    o << "\n  </AppendedData>\n</VTKFile>\n";
+  } else {
     std::ofstream o(out_dir / "field_0000.vtu", std::ios::trunc);
     if (!o) throw std::runtime_error("Failed to write Euler VTU output.");
     std::vector<float> pf(pts.begin(), pts.end());
@@ -880,7 +953,45 @@ int aero_run_euler_airfoil_case(const aero_case_desc* cfg, const aero_airfoil_me
   }
   return guard([&] {
     std::memset(out, 0, sizeof(*out));
-    run_euler(*cfg, *mesh, out_dir, out);
+    run_euler(*cfg, *mesh, out_dir, DriverOpts{}, out);
+  });
+}
+
+int aero_state_write(const char* path, int num_cells, const double* conserved) {
+  if (!path || !conserved || num_cells <= 0) {
+    g_driver_error = "aero_state_write: bad argument";
+    return AERO_ERR_INVALID;
+  }
+  return guard([&] {
+    std::ofstream o(path, std::ios::binary | std::ios::trunc);
+    if (!o) throw std::invalid_argument(std::string("cannot write ") + path);
+    const int64_t head[2] = {num_cells, 5};
+    o.write(kStateMagic, sizeof(kStateMagic));
+    o.write(reinterpret_cast<const char*>(head), sizeof(head));
+    o.write(reinterpret_cast<const char*>(conserved), static_cast<std::streamsize>(sizeof(double) * 5 * num_cells));
+    if (!o) throw std::invalid_argument(std::string("cannot write ") + path);
+  });
+}
+
+int aero_state_read(const char* path, int num_cells, double* conserved) {
+  if (!path || !conserved || num_cells <= 0) {
+    g_driver_error = "aero_state_read: bad argument";
+    return AERO_ERR_INVALID;
+  }
+  return guard([&] {
+    std::ifstream in(path, std::ios::binary);
+    if (!in) throw std::invalid_argument(std::string("cannot read ") + path);
+    char magic[sizeof(kStateMagic)];
+    int64_t head[2] = {0, 0};
+    in.read(magic, sizeof(magic));
+    in.read(reinterpret_cast<char*>(head), sizeof(head));
+    if (!in || std::memcmp(magic, kStateMagic, sizeof(magic)) != 0)
+      throw std::invalid_argument(std::string(path) + " is not a state file");
+    if (head[0] != num_cells || head[1] != 5)
+      throw std::invalid_argument("state file holds " + std::to_string(head[0]) + " cells, the mesh has " +
+                                  std::to_string(num_cells));
+    in.read(reinterpret_cast<char*>(conserved), static_cast<std::streamsize>(sizeof(double) * 5 * num_cells));
+    if (!in) throw std::invalid_argument(std::string(path) + " is truncated");
   });
 }
 
@@ -901,9 +1012,10 @@ int aero_run_case(const char* case_path, const char* out_dir, const char* backen
     aero_case_desc c;
     aero_airfoil_mesh_cfg m;
     map_case(kv, &c, &m);
+    const DriverOpts opts = map_opts(kv, fs::path(case_path).parent_path());
     std::memset(out, 0, sizeof(*out));
     std::snprintf(out->run_log, sizeof(out->run_log), "%s", case_path);  // case_path for run.log
-    run_euler(c, m, out_dir, out);
+    run_euler(c, m, out_dir, opts, out);
   });
 }
 

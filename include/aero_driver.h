@@ -61,6 +61,17 @@ AERO_API int aero_run_case(const char* case_path, const char* out_dir, const cha
                            aero_run_summary* out);
 
 /* Message of the last failed driver call on this thread. */
+/* State dump for continuation (no reference counterpart; the reference has no restart):
+ * a 16-byte magic, int64 cell count, int64 component count (5), then the conserved state
+ * [N][5] double in the reference's cell order and AoS layout, host byte order. Read checks
+ * the magic and the cell count and returns AERO_ERR_INVALID on a mismatch or short file.
+ * The driver's case file takes restart_in = <state file> (start from it instead of the free
+ * stream; the iteration schedule starts again at 0) and restart_out = <file name in out_dir>
+ * (dump the final state), and vtu_format = ascii (default, the reference's) | binary (raw
+ * appended VTU arrays). */
+AERO_API int aero_state_write(const char* path, int num_cells, const double* conserved);
+AERO_API int aero_state_read(const char* path, int num_cells, double* conserved);
+
 AERO_API const char* aero_driver_last_error(void);
 
 #ifdef __cplusplus

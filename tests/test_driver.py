@@ -100,3 +100,92 @@ def test_run_case_cuda_writes_reference_outputs(tmp_path, golden_histories):
     assert len(drow[0]) == 64 and None not in drow[0]  # header and rows both have 64 columns
     log = dict(line.split("=", 1) for line in open(out / "run.log").read().splitlines()[1:] if "=" in line)
     assert log["backend"] == "cuda" and int(log["num_cells"]) == 2 * 72 * 18
+
+
+def _state_fns():
+    lib = aero_gb300.load()
+    lib.aero_state_write.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_double)]
+    lib.aero_state_read.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_double)]
+    lib.aero_driver_last_error.restype = C.c_char_p
+    return lib
+
+
+def test_state_file_round_trip_and_checks(tmp_path):
+    lib = _state_fns()
+    dp = C.POINTER(C.c_double)
+    u = np.random.default_rng(3).standard_normal((37, 5))
+    path = str(tmp_path / "s.state").encode()
+    assert lib.aero_state_write(path, 37, u.ctypes.data_as(dp)) == 0
+    v = np.empty_like(u)
+    assert lib.aero_state_read(path, 37, v.ctypes.data_as(dp)) == 0
+    np.testing.assert_array_equal(u, v)
+    assert lib.aero_state_read(path, 36, v.ctypes.data_as(dp)) == capi.AERO_ERR_INVALID  # wrong mesh
+    assert b"37 cells" in lib.aero_driver_last_error()
+    raw = (tmp_path / "s.state").read_bytes()
+    (tmp_path / "t.state").write_bytes(raw[:-8])
+    assert lib.aero_state_read(str(tmp_path / "t.state").encode(), 37, v.ctypes.data_as(dp)) == capi.AERO_ERR_INVALID
+    (tmp_path / "m.state").write_bytes(b"X" + raw[1:])
+    assert lib.aero_state_read(str(tmp_path / "m.state").encode(), 37, v.ctypes.data_as(dp)) == capi.AERO_ERR_INVALID
+    assert lib.aero_state_read(str(tmp_path / "none").encode(), 37, v.ctypes.data_as(dp)) == capi.AERO_ERR_INVALID
+
+
+@pytest.mark.gpu
+def test_run_case_rejects_unknown_vtu_format(tmp_path):
+    p = write_cfg(tmp_path / "c.cfg", iterations=1, vtu_format="hdf5")
+    with pytest.raises(ValueError):
+        cfd_core.run_case(str(p), str(tmp_path / "o"), "cuda")
+
+
+def _read_vtu_appended(path):
+    """Arrays of a raw-appended VTU (UInt32 byte count before each array)."""
+    import re
+
+    blob = path.read_bytes()
+    head, _, tail = blob.partition(b'<AppendedData encoding="raw">')
+    data = tail[tail.index(b"_") + 1:]
+    types = {"Float32": np.float32, "Int32": np.int32, "UInt8": np.uint8}
+    out = {}
+    for m in re.finditer(rb'<DataArray type="(\w+)"(?: Name="(\w+)")?[^>]*offset="(\d+)"', head):
+        t, name, off = m.group(1).decode(), (m.group(2) or b"Points").decode(), int(m.group(3))
+        nb = int(np.frombuffer(data[off:off + 4], np.uint32)[0])
+        out[name] = np.frombuffer(data[off + 4:off + 4 + nb], types[t])
+    return out
+
+
+def _read_vtu_ascii(path):
+    import re
+
+    text = path.read_text()
+    out = {}
+    for m in re.finditer(r'<DataArray type="(\w+)"(?: Name="(\w+)")?[^>]*format="ascii">([^<]*)</DataArray>', text):
+        out[m.group(2) or "Points"] = np.array(m.group(3).split(), dtype=np.float64)
+    return out
+
+
+@pytest.mark.gpu
+def test_restart_dump_and_binary_vtu(tmp_path):
+    base = dict(naca_code="0012", num_circumferential=48, num_radial=12, farfield_radius=12, radial_stretch=1.35,
+                min_iterations=100, residual_reduction_target=1e-9, flux="hllc", limiter="venkat", precond="off",
+                startup_first_order_iters=0, cfl_ramp_iters=0, cfl_start=0.8, cfl_max=0.8, mach=0.5, aoa_deg=2,
+                precision="fp64")
+    p1 = write_cfg(tmp_path / "a.cfg", iterations=30, restart_out="a.state", **base)
+    cfd_core.run_case(str(p1), str(tmp_path / "a"), "cuda")
+    assert (tmp_path / "a" / "a.state").exists()
+    # restart_in replaces the free-stream start: 30 + 10 iterations from the dump follow the
+    # state, so the first restarted residual continues the first run's history
+    p2 = write_cfg(tmp_path / "b.cfg", iterations=10, restart_in="a/a.state", vtu_format="binary", **base)
+    r2 = cfd_core.run_case(str(p2), str(tmp_path / "b"), "cuda")
+    p3 = write_cfg(tmp_path / "c.cfg", iterations=10, **base)
+    r3 = cfd_core.run_case(str(p3), str(tmp_path / "c"), "cuda")
+    l2_a = [float(r["residual_l2"]) for r in csv.DictReader(open(tmp_path / "a" / "residuals.csv"))]
+    l2_b = [float(r["residual_l2"]) for r in csv.DictReader(open(tmp_path / "b" / "residuals.csv"))]
+    assert l2_b[0] < 0.9 * l2_a[0] and r2["residual_l2"] != r3["residual_l2"]
+    # the binary VTU holds the same arrays as the ASCII one of the same state (ASCII carries
+    # the reference writer's default 6 significant digits)
+    p4 = write_cfg(tmp_path / "d.cfg", iterations=10, restart_in="a/a.state", **base)
+    cfd_core.run_case(str(p4), str(tmp_path / "d"), "cuda")
+    vb = _read_vtu_appended(tmp_path / "b" / "field_0000.vtu")
+    va = _read_vtu_ascii(tmp_path / "d" / "field_0000.vtu")
+    assert set(va) == set(vb) and len(va) == 10
+    for k in va:
+        np.testing.assert_allclose(vb[k].astype(np.float64), va[k], rtol=1e-5, atol=1e-12, err_msg=k)

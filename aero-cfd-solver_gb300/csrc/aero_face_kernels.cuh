@@ -11,6 +11,54 @@
 
 namespace aero {
 
+// The arithmetic of one face (residual_assembly.cpp:73-182): MUSCL reconstruction of an
+// interior face from the two cells' primitive states and gradients (gO / gN: x then y
+// gradients of rho, u, v, p; dO / dN: offsets of the face centre from the cell centres), or
+// the boundary state of a boundary face (b = -1 far field, -2 slip wall), then the face
+// flux *f and wave-speed term *mws (per unit length). *fo: first-order fallback taken, *df:
+// diffusive fallback taken. Templated on the real type: the face pass runs it in float or
+// double and the adjoint linearisation in dual numbers.
+template <class T, int FLUX, bool SECOND, bool LM>
+__device__ __forceinline__ void eval_face(const FaceParams<T>& fp, int b, const Prim<T>& wo, const Prim<T>& wn,
+                                          const T (&gO)[8], const T (&gN)[8], T nx, T ny, T dox, T doy, T dnx,
+                                          T dny, Flux<T>* f, T* mws, bool* fo, bool* df) {
+  if (b >= 0) {
+    Prim<T> L = wo, Rt = wn;
+    if (SECOND) {
+      muscl_var(fp.limiter, wo.r, wn.r, gO[0], gO[4], gN[0], gN[4], dox, doy, dnx, dny, &L.r, &Rt.r);
+      muscl_var(fp.limiter, wo.u, wn.u, gO[1], gO[5], gN[1], gN[5], dox, doy, dnx, dny, &L.u, &Rt.u);
+      muscl_var(fp.limiter, wo.v, wn.v, gO[2], gO[6], gN[2], gN[6], dox, doy, dnx, dny, &L.v, &Rt.v);
+      muscl_var(fp.limiter, wo.p, wn.p, gO[3], gO[7], gN[3], gN[7], dox, doy, dnx, dny, &L.p, &Rt.p);
+      L.r = smax(L.r, Kn<T>::rho_floor);
+      Rt.r = smax(Rt.r, Kn<T>::rho_floor);
+      L.p = smax(L.p, Kn<T>::p_floor);
+      Rt.p = smax(Rt.p, Kn<T>::p_floor);
+      if (!valid_prim(L) || !valid_prim(Rt)) {
+        L = wo;
+        Rt = wn;
+        *fo = true;
+      }
+    }
+    const Cons<T> cl = prim_to_cons(L, fp.gamma), cr = prim_to_cons(Rt, fp.gamma);
+    const T as = face_acoustic_scale<T, LM>(cl, cr, fp);
+    *f = face_flux<T, FLUX, LM>(cl, cr, nx, ny, fp, as, mws, df);
+  } else {
+    const Cons<T> in = prim_to_cons(wo, fp.gamma);
+    if (b == -2) {  // slip wall: pressure-only flux (boundary_conditions.cpp:97-110)
+      const T as = face_acoustic_scale<T, LM>(in, in, fp);
+      const Prim<T> w = cons_to_prim(in, fp.gamma);
+      const T un = w.u * nx + w.v * ny;
+      const T a = sound_speed(w, fp.gamma);
+      *f = Flux<T>{T(0), w.p * nx, w.p * ny, T(0)};
+      *mws = precond_speeds(un, a, as).sr;
+    } else {
+      const T as = face_acoustic_scale<T, LM>(in, fp.farfield, fp);
+      const Cons<T> bs = fp.precond_farfield_bc ? precond_farfield_state(in, nx, ny, fp, as) : fp.farfield;
+      *f = face_flux<T, FLUX, LM>(in, bs, nx, ny, fp, as, mws, df);
+    }
+  }
+}
+
 // Face pass. FLUX 0 Rusanov / 1 HLLC; SECOND: MUSCL with the cell gradients; LM: any
 // low-Mach feature on. fb[0] / fb[1] count first-order and diffusive fallbacks.
 template <class T, int FLUX, bool SECOND, bool LM>
@@ -47,49 +95,28 @@ __global__ void __launch_bounds__(256) k_face_flux(DevFaces<T> f, Cases<T> cs,
     const T area = f.area[i];
     const auto wo4 = W[o];
     const Prim<T> wo{wo4.x, wo4.y, wo4.z, wo4.w};
-    Flux<T> fl;
-    T mws;
-    bool fbk = false;
+    Prim<T> wn = wo;
+    T gO[8], gN[8];
+    T dox = T(0), doy = T(0), dnx = T(0), dny = T(0);
     if (b >= 0) {
       const auto wn4 = W[b];
-      const Prim<T> wn{wn4.x, wn4.y, wn4.z, wn4.w};
-      Prim<T> L = wo, Rt = wn;
+      wn = Prim<T>{wn4.x, wn4.y, wn4.z, wn4.w};
       if (SECOND) {
         const auto gOx = gx[o], gOy = gy[o], gNx = gx[b], gNy = gy[b];
+        gO[0] = gOx.x; gO[1] = gOx.y; gO[2] = gOx.z; gO[3] = gOx.w;
+        gO[4] = gOy.x; gO[5] = gOy.y; gO[6] = gOy.z; gO[7] = gOy.w;
+        gN[0] = gNx.x; gN[1] = gNx.y; gN[2] = gNx.z; gN[3] = gNx.w;
+        gN[4] = gNy.x; gN[5] = gNy.y; gN[6] = gNy.z; gN[7] = gNy.w;
         const auto dO = f.doff[i];
         const auto dN = f.noff[i];
-        muscl_var(fp.limiter, wo.r, wn.r, gOx.x, gOy.x, gNx.x, gNy.x, dO.x, dO.y, dN.x, dN.y, &L.r, &Rt.r);
-        muscl_var(fp.limiter, wo.u, wn.u, gOx.y, gOy.y, gNx.y, gNy.y, dO.x, dO.y, dN.x, dN.y, &L.u, &Rt.u);
-        muscl_var(fp.limiter, wo.v, wn.v, gOx.z, gOy.z, gNx.z, gNy.z, dO.x, dO.y, dN.x, dN.y, &L.v, &Rt.v);
-        muscl_var(fp.limiter, wo.p, wn.p, gOx.w, gOy.w, gNx.w, gNy.w, dO.x, dO.y, dN.x, dN.y, &L.p, &Rt.p);
-        L.r = smax(L.r, Kn<T>::rho_floor);
-        Rt.r = smax(Rt.r, Kn<T>::rho_floor);
-        L.p = smax(L.p, Kn<T>::p_floor);
-        Rt.p = smax(Rt.p, Kn<T>::p_floor);
-        if (!valid_prim(L) || !valid_prim(Rt)) {
-          L = wo;
-          Rt = wn;
-          ++fo;
-        }
-      }
-      const Cons<T> cl = prim_to_cons(L, fp.gamma), cr = prim_to_cons(Rt, fp.gamma);
-      const T as = face_acoustic_scale<T, LM>(cl, cr, fp);
-      fl = face_flux<T, FLUX, LM>(cl, cr, nx, ny, fp, as, &mws, &fbk);
-    } else {
-      const Cons<T> in = prim_to_cons(wo, fp.gamma);
-      if (b == -2) {  // slip wall: pressure-only flux (boundary_conditions.cpp:97-110)
-        const T as = face_acoustic_scale<T, LM>(in, in, fp);
-        const Prim<T> w = cons_to_prim(in, fp.gamma);
-        const T un = w.u * nx + w.v * ny;
-        const T a = sound_speed(w, fp.gamma);
-        fl = {T(0), w.p * nx, w.p * ny, T(0)};
-        mws = precond_speeds(un, a, as).sr;
-      } else {
-        const T as = face_acoustic_scale<T, LM>(in, fp.farfield, fp);
-        const Cons<T> bs = fp.precond_farfield_bc ? precond_farfield_state(in, nx, ny, fp, as) : fp.farfield;
-        fl = face_flux<T, FLUX, LM>(in, bs, nx, ny, fp, as, &mws, &fbk);
+        dox = dO.x; doy = dO.y; dnx = dN.x; dny = dN.y;
       }
     }
+    Flux<T> fl;
+    T mws;
+    bool fbo = false, fbk = false;
+    eval_face<T, FLUX, SECOND, LM>(fp, b, wo, wn, gO, gN, nx, ny, dox, doy, dnx, dny, &fl, &mws, &fbo, &fbk);
+    if (fbo) ++fo;
     if (fbk) ++df;
     typename Vec<T>::v4 out;
     out.x = fl.m * area;

@@ -1,4 +1,5 @@
 // capi.cpp -- extern "C" entry points of libaero_gb300.so (include/aero_gb300.h).
+#include "../../include/aero_adjoint.h"
 #include "../../include/aero_batch.h"
 #include "../../include/aero_gb300.h"
 #include "engine.hpp"
@@ -388,6 +389,104 @@ int aero_get_info(aero_ctx* ctx, long long* info, int n_info) {
   if (ctx == nullptr || info == nullptr) return fail(ctx, AERO_ERR_INVALID, "aero_get_info: null argument");
   ctx->engine->info(info, n_info);
   return AERO_OK;
+}
+
+int aero_autotune(const aero_mesh_desc* mesh, const aero_case_desc* c, int iters, aero_case_desc* best,
+                  double* ms_out) {
+  if (mesh == nullptr || c == nullptr || best == nullptr || iters <= 0)
+    return fail(nullptr, AERO_ERR_INVALID, "aero_autotune: bad argument");
+  const int orders[2] = {AERO_ORDER_MORTON, AERO_ORDER_RCM};
+  const int blocks[3] = {64, 128, 256};
+  double best_ms = 0.0;
+  int k = 0;
+  *best = *c;
+  for (int o : orders) {
+    for (int b : blocks) {
+      aero_case_desc v = *c;
+      v.ordering = o;
+      v.block_size = b;
+      aero_ctx* ctx = nullptr;
+      int rc = create_ctx(1, mesh, &v, &ctx);
+      if (rc != AERO_OK) return rc;
+      double ms = 0.0;
+      const int warm = std::max(c->startup_first_order_iters, 0);
+      if (warm > 0) rc = ctx->engine->time_iterations(warm, 1, 0, &ms);  // first-order start-up
+      if (rc == AERO_OK) rc = ctx->engine->time_iterations(2, 1, 0, &ms);  // graphs instantiated
+      if (rc == AERO_OK) rc = ctx->engine->time_iterations(iters, 1, 0, &ms);
+      const int cs = cuda_status(ctx);
+      aero_destroy(ctx);
+      if (cs != AERO_OK) return cs;
+      if (rc != AERO_OK && rc != AERO_ERR_NONFINITE) return fail(nullptr, rc, "aero_autotune: timing failed");
+      if (ms_out) ms_out[k] = ms;
+      if (k == 0 || ms < best_ms) {
+        best_ms = ms;
+        best->ordering = o;
+        best->block_size = b;
+      }
+      ++k;
+    }
+  }
+  return AERO_OK;
+}
+
+}  // extern "C"
+
+// ---- discrete adjoint (include/aero_adjoint.h)
+
+namespace {
+int adjoint_status(aero_ctx* ctx, int rc, const char* what) {
+  const int cs = cuda_status(ctx);
+  if (cs != AERO_OK) return cs;
+  if (rc == AERO_ERR_INVALID)
+    return fail(ctx, rc, std::string(what) + ": needs a single-case FP64 context linearised by aero_adjoint_linearize");
+  return rc;
+}
+}  // namespace
+
+extern "C" {
+
+int aero_adjoint_linearize(aero_ctx* ctx, double w_cd, double w_cl, int second_order) {
+  if (ctx == nullptr || second_order < -1 || second_order > 1)
+    return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_linearize: bad argument");
+  if (ctx->engine->n_cases() != 1) return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_linearize: batched context");
+  const int rc = ctx->engine->adjoint_linearize(w_cd, w_cl, second_order);
+  const int cs = cuda_status(ctx);
+  if (cs != AERO_OK) return cs;
+  if (rc == AERO_ERR_INVALID)
+    return fail(ctx, rc, "aero_adjoint_linearize: needs a single-case FP64 context and finite weights");
+  return rc;
+}
+
+int aero_adjoint_vjp(aero_ctx* ctx, const double* v, double* out) {
+  if (ctx == nullptr || v == nullptr || out == nullptr) return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_vjp: null argument");
+  return adjoint_status(ctx, ctx->engine->adjoint_vjp(v, out), "aero_adjoint_vjp");
+}
+
+int aero_adjoint_objective_gradient(aero_ctx* ctx, double* g) {
+  if (ctx == nullptr || g == nullptr) return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_objective_gradient: null argument");
+  return adjoint_status(ctx, ctx->engine->adjoint_objective_gradient(g), "aero_adjoint_objective_gradient");
+}
+
+int aero_adjoint_solve(aero_ctx* ctx, int iters, double cfl, double* history) {
+  if (ctx == nullptr || iters < 0 || !(cfl > 0.0) || !std::isfinite(cfl))
+    return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_solve: bad argument");
+  return adjoint_status(ctx, ctx->engine->adjoint_solve(iters, cfl, history), "aero_adjoint_solve");
+}
+
+int aero_adjoint_get_lambda(aero_ctx* ctx, double* lam) {
+  if (ctx == nullptr || lam == nullptr) return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_get_lambda: null argument");
+  return adjoint_status(ctx, ctx->engine->adjoint_lambda(lam), "aero_adjoint_get_lambda");
+}
+
+int aero_adjoint_dalpha(aero_ctx* ctx, double* dj_dalpha_deg) {
+  if (ctx == nullptr || dj_dalpha_deg == nullptr) return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_dalpha: null argument");
+  return adjoint_status(ctx, ctx->engine->adjoint_dalpha(dj_dalpha_deg), "aero_adjoint_dalpha");
+}
+
+int aero_adjoint_geometry(aero_ctx* ctx, const aero_mesh_desc* tangent, double* dj) {
+  if (ctx == nullptr || tangent == nullptr || dj == nullptr)
+    return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_geometry: null argument");
+  return adjoint_status(ctx, ctx->engine->adjoint_geometry(*tangent, dj), "aero_adjoint_geometry");
 }
 
 }  // extern "C"

@@ -75,6 +75,17 @@ class Engine {
   virtual int profile_kernels(int n, int flush_l2, double* ms, int* launches) = 0;
   virtual void info(long long* out, int n) = 0;
   virtual cudaError_t last_cuda_error() = 0;
+
+  // Discrete adjoint at the current state (single-case FP64 contexts; others return
+  // AERO_ERR_INVALID). Objective J = w_cd CD + w_cl CL; second_order -1: the run's scheme at
+  // the current iteration. Host arrays are [N][5] in the original order.
+  virtual int adjoint_linearize(double w_cd, double w_cl, int second_order) = 0;
+  virtual int adjoint_vjp(const double* v, double* out) = 0;
+  virtual int adjoint_objective_gradient(double* g) = 0;
+  virtual int adjoint_solve(int iters, double cfl, double* history) = 0;
+  virtual int adjoint_lambda(double* lam) = 0;
+  virtual int adjoint_dalpha(double* dj_dalpha_deg) = 0;
+  virtual int adjoint_geometry(const aero_mesh_desc& tangent, double* dj) = 0;
 };
 
 Engine* make_engine_f32(const std::vector<HostSlots>& hs, const std::vector<aero_case_desc>& cfg,

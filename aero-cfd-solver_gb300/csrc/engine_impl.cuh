@@ -11,6 +11,7 @@
 // cells keep the block layout of a single-case run, so a batch reproduces single runs.
 #pragma once
 
+#include "aero_adjoint.cuh"
 #include "aero_face_kernels.cuh"
 #include "engine.hpp"
 
@@ -51,6 +52,7 @@ class EngineT final : public Engine {
     for (auto& g : graph_) {
       if (g) cudaGraphExecDestroy(g);
     }
+    if (adj_graph_) cudaGraphExecDestroy(adj_graph_);
     if (ev_fork_) cudaEventDestroy(ev_fork_);
     if (ev_join_) cudaEventDestroy(ev_join_);
     if (side_) cudaStreamDestroy(side_);
@@ -665,6 +667,315 @@ class EngineT final : public Engine {
     return end_untracked();
   }
 
+  // ---- discrete adjoint (FP64, one case) -------------------------------------------------
+  int adjoint_linearize(double w_cd, double w_cl, int second_order) override {
+    if constexpr (sizeof(T) != 8) {
+      return AERO_ERR_INVALID;
+    } else {
+      if (K_ != 1 || !std::isfinite(w_cd) || !std::isfinite(w_cl)) return AERO_ERR_INVALID;
+      if (!adj_alloc_) {
+        Ulin_ = alloc<d4>(ntot_);
+        Wlin_ = alloc<d4>(ntot_);
+        SRlin_ = alloc<double>(ntot_);
+        gxlin_ = alloc<d4>(ntot_);
+        gylin_ = alloc<d4>(ntot_);
+        Jf_ = alloc<double>(static_cast<size_t>(ftot_) * 4 * kJac);
+        adj_face_ = alloc<double>(static_cast<size_t>(ftot_) * kJac);
+        mw_ = alloc<d4>(ntot_);
+        mgx_ = alloc<d4>(ntot_);
+        mgy_ = alloc<d4>(ntot_);
+        adj_r_ = alloc<d4>(ntot_);
+        adj_g_ = alloc<d4>(ntot_);
+        lam_ = alloc<d4>(ntot_);
+        lam_n_ = alloc<d4>(ntot_);
+        adj_v_ = alloc<d4>(ntot_);
+        adj_rn_ = alloc<double>(ncb_);
+        adj_hist_ = alloc<double>(kAdjHist);
+        adj_counter_ = alloc<int>(1);
+        adj_face_out_ = alloc<double>(ftot_);
+        ctrl_lin_ = alloc<Ctrl>(1);
+        adj_alloc_ = true;
+        if (err_ != cudaSuccess) return AERO_ERR_NOMEM;
+      }
+      // the linearisation point: the current state, its primitives, gradients and residual
+      download_ctrls();
+      Ctrl lin = host_ctrls_[0];
+      lin.done = 0;
+      lin.nonfinite = 0;
+      AERO_CK(cudaMemcpyAsync(ctrl_lin_, &lin, sizeof(Ctrl), cudaMemcpyHostToDevice, st_));
+      adj_second_ = second_order < 0 ? second_at(lin.iter) : second_order != 0;
+      adj_wcd_ = w_cd;
+      adj_wcl_ = w_cl;
+      if (adj_graph_) {  // the transpose product's launches depend on the order
+        cudaGraphExecDestroy(adj_graph_);
+        adj_graph_ = nullptr;
+      }
+      const Cases<T> ccs{cblk_, ctrl_lin_, fps_dev_, pcs_dev_, mcs_dev_};
+      const Cases<T> fcs{fblk_, ctrl_lin_, fps_dev_, pcs_dev_, mcs_dev_};
+      refresh();
+      if (adj_second_) k_gradient<T><<<ncb_, block_, 0, st_>>>(dm_, W_, gx_, gy_, ccs);
+      ResidualLaunch<T> a = residual_args(&ctrl_eval_->fo_fallback, R_, SR_, 0);
+      a.cell_cases = ccs;
+      a.face_cases = fcs;
+      launch_residual_passes(a, cfg_[0].flux, adj_second_, lm_ != 0, false);
+      AERO_CK(cudaMemcpyAsync(Ulin_, Un_, sizeof(d4) * ntot_, cudaMemcpyDeviceToDevice, st_));
+      AERO_CK(cudaMemcpyAsync(Wlin_, W_, sizeof(d4) * ntot_, cudaMemcpyDeviceToDevice, st_));
+      AERO_CK(cudaMemcpyAsync(SRlin_, SR_, sizeof(double) * ntot_, cudaMemcpyDeviceToDevice, st_));
+      if (adj_second_) {
+        AERO_CK(cudaMemcpyAsync(gxlin_, gx_, sizeof(d4) * ntot_, cudaMemcpyDeviceToDevice, st_));
+        AERO_CK(cudaMemcpyAsync(gylin_, gy_, sizeof(d4) * ntot_, cudaMemcpyDeviceToDevice, st_));
+      }
+      launch_face_jac();
+      w_valid_ = false;
+      // objective gradient dJ/dU: J is linear in the gauge force, J = (ex Fx + ey Fy) / (q S)
+      const CtrlConfig& cc = ccs_[0];
+      const double ex = w_cd * cc.cos_a - w_cl * cc.sin_a;
+      const double ey = w_cd * cc.sin_a + w_cl * cc.cos_a;
+      adj_ex_ = ex;
+      adj_ey_ = ey;
+      k_adj_objective<<<ncb_, block_, 0, st_>>>(cblk_, Ulin_, rs_[0].gamma, ms_, ex, ey,
+                                                1.0 / (cc.q_inf * cc.s_ref), adj_g_);
+      AERO_CK(cudaMemsetAsync(lam_, 0, sizeof(d4) * ntot_, st_));
+      AERO_CK(cudaGetLastError());
+      AERO_CK(cudaStreamSynchronize(st_));
+      adj_ready_ = err_ == cudaSuccess;
+      return adj_ready_ ? AERO_OK : AERO_ERR_CUDA;
+    }
+  }
+
+  int adjoint_vjp(const double* v, double* out) override {
+    if constexpr (sizeof(T) != 8) {
+      return AERO_ERR_INVALID;
+    } else {
+      if (!adj_ready_) return AERO_ERR_INVALID;
+      upload_cells(v, adj_v_);
+      apply_vjp(adj_v_, adj_r_);
+      download_cells(adj_r_, out);
+      return err_ == cudaSuccess ? AERO_OK : AERO_ERR_CUDA;
+    }
+  }
+
+  int adjoint_objective_gradient(double* g) override {
+    if constexpr (sizeof(T) != 8) {
+      return AERO_ERR_INVALID;
+    } else {
+      if (!adj_ready_) return AERO_ERR_INVALID;
+      download_cells(adj_g_, g);
+      return err_ == cudaSuccess ? AERO_OK : AERO_ERR_CUDA;
+    }
+  }
+
+  // Pseudo-time solve of (dR/dU)^T lam = -dJ/dU with the primal's SSP-RK3 and local steps,
+  // continuing from the current lam: one captured graph per iteration (copy of lam, three
+  // transpose products and stages, the residual norm into a device history), launched in
+  // chunks with one host synchronisation per chunk. history[k]: RMS over cells of
+  // (dR/dU)^T lam + dJ/dU at the start of iteration k.
+  int adjoint_solve(int iters, double cfl, double* history) override {
+    if constexpr (sizeof(T) != 8) {
+      return AERO_ERR_INVALID;
+    } else {
+      if (!adj_ready_ || iters < 0 || !(cfl > 0.0)) return AERO_ERR_INVALID;
+      if (adj_graph_ && adj_graph_cfl_ != cfl) {
+        cudaGraphExecDestroy(adj_graph_);
+        adj_graph_ = nullptr;
+      }
+      if (!adj_graph_) {
+        cudaGraph_t g = nullptr;
+        AERO_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+        adjoint_iteration(cfl);
+        AERO_CK(cudaStreamEndCapture(st_, &g));
+        if (g) {
+          AERO_CK(cudaGraphInstantiate(&adj_graph_, g, 0));
+          cudaGraphDestroy(g);
+        }
+        if (!adj_graph_) return AERO_ERR_CUDA;
+        adj_graph_cfl_ = cfl;
+      }
+      std::vector<double> h(static_cast<size_t>(kAdjHist));
+      for (int done = 0; done < iters;) {
+        const int n = std::min(kAdjHist, iters - done);
+        AERO_CK(cudaMemsetAsync(adj_counter_, 0, sizeof(int), st_));
+        for (int i = 0; i < n; ++i) AERO_CK(cudaGraphLaunch(adj_graph_, st_));
+        AERO_CK(cudaMemcpyAsync(h.data(), adj_hist_, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
+        AERO_CK(cudaStreamSynchronize(st_));
+        if (err_ != cudaSuccess) break;
+        if (history) std::copy(h.begin(), h.begin() + n, history + done);
+        done += n;
+      }
+      return err_ == cudaSuccess ? AERO_OK : AERO_ERR_CUDA;
+    }
+  }
+
+  int adjoint_lambda(double* lam) override {
+    if constexpr (sizeof(T) != 8) {
+      return AERO_ERR_INVALID;
+    } else {
+      if (!adj_ready_) return AERO_ERR_INVALID;
+      download_cells(lam_, lam);
+      return err_ == cudaSuccess ? AERO_OK : AERO_ERR_CUDA;
+    }
+  }
+
+  // dJ/d(alpha) per degree at the linearisation point: the explicit term of the force
+  // rotation plus lam^T dR/d(alpha) through the far-field state.
+  int adjoint_dalpha(double* out) override {
+    if constexpr (sizeof(T) != 8) {
+      return AERO_ERR_INVALID;
+    } else {
+      if (!adj_ready_ || out == nullptr) return AERO_ERR_INVALID;
+      const CtrlConfig& cc = ccs_[0];
+      const Resolved& rs = rs_[0];
+      const double rad = 3.14159265358979323846 / 180.0;
+      const double rho = rs.cons_inf[0], vmag = rs.v_inf;
+      const d4 dfar{0.0, -rho * vmag * cc.sin_a * rad, rho * vmag * cc.cos_a * rad, 0.0};
+      const int grid = nfb_;
+      if (cfg_[0].flux == AERO_FLUX_HLLC) {
+        if (lm_) {
+          k_adj_dalpha<1, true><<<grid, block_, 0, st_>>>(df_, fblk_, fps_dev_, ctrl_lin_, W_lin(), dfar, lam_, adj_face_out_);
+        } else {
+          k_adj_dalpha<1, false><<<grid, block_, 0, st_>>>(df_, fblk_, fps_dev_, ctrl_lin_, W_lin(), dfar, lam_, adj_face_out_);
+        }
+      } else {
+        if (lm_) {
+          k_adj_dalpha<0, true><<<grid, block_, 0, st_>>>(df_, fblk_, fps_dev_, ctrl_lin_, W_lin(), dfar, lam_, adj_face_out_);
+        } else {
+          k_adj_dalpha<0, false><<<grid, block_, 0, st_>>>(df_, fblk_, fps_dev_, ctrl_lin_, W_lin(), dfar, lam_, adj_face_out_);
+        }
+      }
+      std::vector<double> per_face(static_cast<size_t>(ftot_));
+      AERO_CK(cudaMemcpyAsync(per_face.data(), adj_face_out_, sizeof(double) * ftot_, cudaMemcpyDeviceToHost, st_));
+      AERO_CK(cudaStreamSynchronize(st_));
+      double lam_dr = 0.0;
+      for (int i = 0; i < pk_[0].nf; ++i) lam_dr += per_face[i];
+      // explicit term from the gauge force at the state
+      double fx = 0.0, fy = 0.0;
+      const std::vector<double> pw = wall_pressures();
+      const HostSlots& hs = hs_[0];
+      for (int c = 0; c < pk_[0].n; ++c) {
+        const int cnt = hs.flags[c] >> 2;
+        for (int j = hs.wall_first[c]; j < hs.wall_first[c] + cnt; ++j) {
+          if (!(hs.wkind[j] & 1)) continue;
+          fx += (pw[c] - rs.p_inf) * hs.wnx[j] * hs.warea[j];
+          fy += (pw[c] - rs.p_inf) * hs.wny[j] * hs.warea[j];
+        }
+      }
+      const double qs = cc.q_inf * cc.s_ref;
+      // dCD/d(alpha) = CL and dCL/d(alpha) = -CD per radian at a fixed force
+      const double explicit_term = (adj_wcd_ * (-fx * cc.sin_a + fy * cc.cos_a) +
+                                    adj_wcl_ * (-fx * cc.cos_a - fy * cc.sin_a)) / qs;
+      *out = explicit_term * rad + lam_dr;
+      return err_ == cudaSuccess ? AERO_OK : AERO_ERR_CUDA;
+    }
+  }
+
+  // dJ/dX . dX for a geometry tangent (same connectivity as the mesh): the force term at
+  // fixed state plus lam^T (dR/dX . dX) through the gradients, MUSCL offsets, normals and
+  // lengths.
+  int adjoint_geometry(const aero_mesh_desc& t, double* dj) override {
+    if constexpr (sizeof(T) != 8) {
+      return AERO_ERR_INVALID;
+    } else {
+      if (!adj_ready_ || dj == nullptr) return AERO_ERR_INVALID;
+      const HostSlots& hs = hs_[0];
+      const Pack& pk = pk_[0];
+      if (t.num_cells != hs.n || t.num_faces != hs.nf || !t.face_normal || !t.face_center || !t.face_area ||
+          !t.cell_volume || !t.cell_center)
+        return AERO_ERR_INVALID;
+      HostSlots g;
+      map_geometry(t, hs, &g);
+      const size_t ns = static_cast<size_t>(ntot_) * d_;
+      std::vector<double2> dnrm(ns, make_double2(0.0, 0.0));
+      std::vector<double> darea(ns, 0.0), dinv(static_cast<size_t>(ntot_), 0.0);
+      for (int j = 0; j < hs.d; ++j) {
+        for (int c = 0; c < hs.n; ++c) {
+          const size_t src = static_cast<size_t>(j) * hs.n + c, dst = static_cast<size_t>(j) * ntot_ + c;
+          dnrm[dst] = make_double2(g.nx[src], g.ny[src]);
+          darea[dst] = g.area[src];
+        }
+      }
+      for (int c = 0; c < hs.n; ++c) {
+        const double v = hs.vol[c];
+        dinv[c] = v > 1.0e-12 ? -g.vol[c] / (v * v) : 0.0;  // inv_vol = 1 / max(V, 1e-12)
+      }
+      std::vector<double2> dfn(static_cast<size_t>(ftot_), make_double2(0.0, 0.0)), ddoff(dfn), dnoff(dfn);
+      std::vector<double> dfa(static_cast<size_t>(ftot_), 0.0);
+      for (int i = 0; i < pk.nf; ++i) {
+        const int o = hs.f_own_old[i], b = hs.f_nb_old[i];
+        dfn[i] = make_double2(g.f_nx[i], g.f_ny[i]);
+        dfa[i] = g.f_area[i];
+        ddoff[i] = make_double2(g.f_cx[i] - g.ccx[o], g.f_cy[i] - g.ccy[o]);
+        if (hs.f_nb[i] >= 0) dnoff[i] = make_double2(g.f_cx[i] - g.ccx[b], g.f_cy[i] - g.ccy[b]);
+      }
+      if (!geo_alloc_) {
+        geo_nrm_ = alloc<double2>(ns);
+        geo_area_ = alloc<double>(ns);
+        geo_inv_ = alloc<double>(ntot_);
+        geo_fn_ = alloc<double2>(ftot_);
+        geo_fa_ = alloc<double>(ftot_);
+        geo_doff_ = alloc<double2>(ftot_);
+        geo_noff_ = alloc<double2>(ftot_);
+        geo_gx_ = alloc<d4>(ntot_);
+        geo_gy_ = alloc<d4>(ntot_);
+        geo_alloc_ = true;
+        if (err_ != cudaSuccess) return AERO_ERR_NOMEM;
+      }
+      AERO_CK(cudaMemcpyAsync(geo_nrm_, dnrm.data(), sizeof(double2) * ns, cudaMemcpyHostToDevice, st_));
+      AERO_CK(cudaMemcpyAsync(geo_area_, darea.data(), sizeof(double) * ns, cudaMemcpyHostToDevice, st_));
+      AERO_CK(cudaMemcpyAsync(geo_inv_, dinv.data(), sizeof(double) * ntot_, cudaMemcpyHostToDevice, st_));
+      AERO_CK(cudaMemcpyAsync(geo_fn_, dfn.data(), sizeof(double2) * ftot_, cudaMemcpyHostToDevice, st_));
+      AERO_CK(cudaMemcpyAsync(geo_fa_, dfa.data(), sizeof(double) * ftot_, cudaMemcpyHostToDevice, st_));
+      AERO_CK(cudaMemcpyAsync(geo_doff_, ddoff.data(), sizeof(double2) * ftot_, cudaMemcpyHostToDevice, st_));
+      AERO_CK(cudaMemcpyAsync(geo_noff_, dnoff.data(), sizeof(double2) * ftot_, cudaMemcpyHostToDevice, st_));
+      if (adj_second_) {
+        k_adj_geo_grad<<<ncb_, block_, 0, st_>>>(dm_, geo_nrm_, geo_area_, geo_inv_, cblk_, Wlin_, geo_gx_, geo_gy_);
+      }
+      auto go = [&](auto kern) {
+        kern<<<nfb_, block_, 0, st_>>>(df_, geo_fn_, geo_fa_, geo_doff_, geo_noff_, fblk_, fps_dev_, ctrl_lin_, Wlin_,
+                                       gxlin_, gylin_, geo_gx_, geo_gy_, lam_, adj_face_out_);
+      };
+      const bool hllc = cfg_[0].flux == AERO_FLUX_HLLC, lm = lm_ != 0, sec = adj_second_;
+      if (hllc) {
+        if (sec) {
+          if (lm) go(k_adj_geo_face<1, true, true>);
+          else go(k_adj_geo_face<1, true, false>);
+        } else {
+          if (lm) go(k_adj_geo_face<1, false, true>);
+          else go(k_adj_geo_face<1, false, false>);
+        }
+      } else {
+        if (sec) {
+          if (lm) go(k_adj_geo_face<0, true, true>);
+          else go(k_adj_geo_face<0, true, false>);
+        } else {
+          if (lm) go(k_adj_geo_face<0, false, true>);
+          else go(k_adj_geo_face<0, false, false>);
+        }
+      }
+      AERO_CK(cudaGetLastError());
+      std::vector<double> per_face(static_cast<size_t>(pk.nf));
+      AERO_CK(cudaMemcpyAsync(per_face.data(), adj_face_out_, sizeof(double) * pk.nf, cudaMemcpyDeviceToHost, st_));
+      AERO_CK(cudaStreamSynchronize(st_));
+      double lam_dr = 0.0;
+      for (double v : per_face) lam_dr += v;
+      // the objective's own dependence: the force patch's normals and lengths
+      const std::vector<double> pw = wall_pressures();
+      const double pinf = rs_[0].p_inf;
+      double s = 0.0;
+      for (int c = 0; c < pk.n; ++c) {
+        const int cnt = hs.flags[c] >> 2;
+        for (int j = hs.wall_first[c]; j < hs.wall_first[c] + cnt; ++j) {
+          if (!(hs.wkind[j] & 1)) continue;
+          const double dnax = g.wnx[j] * hs.warea[j] + hs.wnx[j] * g.warea[j];
+          const double dnay = g.wny[j] * hs.warea[j] + hs.wny[j] * g.warea[j];
+          s += (pw[c] - pinf) * (adj_ex_ * dnax + adj_ey_ * dnay);
+        }
+      }
+      const CtrlConfig& cc = ccs_[0];
+      *dj = s / (cc.q_inf * cc.s_ref) + lam_dr;
+      return err_ == cudaSuccess ? AERO_OK : AERO_ERR_CUDA;
+    }
+  }
+
   // info[0] cells, [1] faces, [2] slots per cell, [3] launches per iteration, [4] device
   // bytes, [5] precision, [6] block size, [7] cell blocks, [8] cases
   void info(long long* out, int n) override {
@@ -808,6 +1119,105 @@ class EngineT final : public Engine {
     c.u_inf = rs.v_inf * rs.cos_a;
     c.v_inf = rs.v_inf * rs.sin_a;
     c.rho_l2_target = cfg.density_l2_target;
+  }
+
+  // ---- adjoint helpers (FP64)
+  const d4* W_lin() const { return Wlin_; }
+
+  void launch_face_jac() {
+    if constexpr (sizeof(T) == 8) {
+      const int grid = nfb_;
+      auto go = [&](auto kern) {
+        kern<<<grid, block_, 0, st_>>>(df_, fblk_, fps_dev_, ctrl_lin_, W_lin(),
+                                                    reinterpret_cast<const d4*>(gx_), reinterpret_cast<const d4*>(gy_), Jf_);
+      };
+      const bool hllc = cfg_[0].flux == AERO_FLUX_HLLC, lm = lm_ != 0, sec = adj_second_;
+      if (hllc) {
+        if (sec) {
+          if (lm) go(k_adj_face_jac<1, true, true>);
+          else go(k_adj_face_jac<1, true, false>);
+        } else {
+          if (lm) go(k_adj_face_jac<1, false, true>);
+          else go(k_adj_face_jac<1, false, false>);
+        }
+      } else {
+        if (sec) {
+          if (lm) go(k_adj_face_jac<0, true, true>);
+          else go(k_adj_face_jac<0, true, false>);
+        } else {
+          if (lm) go(k_adj_face_jac<0, false, true>);
+          else go(k_adj_face_jac<0, false, false>);
+        }
+      }
+      AERO_CK(cudaGetLastError());
+    }
+  }
+
+  static constexpr int kAdjHist = 4096;  // iterations per host synchronisation
+
+  void adjoint_iteration(double cfl) {
+    if constexpr (sizeof(T) == 8) {
+      AERO_CK(cudaMemcpyAsync(lam_n_, lam_, sizeof(d4) * ntot_, cudaMemcpyDeviceToDevice, st_));
+      for (int stage = 0; stage < 3; ++stage) {
+        apply_vjp(lam_, adj_r_);
+        k_adj_stage<<<ncb_, block_, 0, st_>>>(cblk_, stage, cfl, SRlin_, adj_r_, adj_g_, lam_n_, lam_,
+                                              stage == 0 ? adj_rn_ : nullptr);
+        if (stage == 0) k_adj_norm<<<1, 256, 0, st_>>>(adj_rn_, ncb_, pk_[0].n, adj_hist_, adj_counter_, kAdjHist);
+      }
+    }
+  }
+
+  // out = (dR/dU)^T v on device arrays
+  void apply_vjp(const d4* v, d4* out) {
+    if constexpr (sizeof(T) == 8) {
+      k_adj_face_vjp<<<nfb_, block_, 0, st_>>>(df_, fblk_, Jf_, v, adj_face_);
+      k_adj_gather<<<ncb_, block_, 0, st_>>>(dg_, cblk_, adj_face_, mw_, mgx_, mgy_);
+      if (adj_second_) k_adj_green_gauss<<<ncb_, block_, 0, st_>>>(dm_, cblk_, mgx_, mgy_, mw_);
+      k_adj_prim<<<ncb_, block_, 0, st_>>>(cblk_, Ulin_, rs_[0].gamma, mw_, out);
+    }
+  }
+
+  void upload_cells(const double* u, d4* dst) {
+    const Pack& p = pk_[0];
+    std::vector<d4> h(static_cast<size_t>(ntot_), d4{0.0, 0.0, 0.0, 0.0});
+    for (int cn = 0; cn < p.n; ++cn) {
+      const double* s = u + 5 * static_cast<size_t>(hs_[0].perm[cn]);
+      h[cn] = d4{s[0], s[1], s[2], s[4]};
+    }
+    AERO_CK(cudaMemcpyAsync(dst, h.data(), sizeof(d4) * ntot_, cudaMemcpyHostToDevice, st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+  }
+  void download_cells(const d4* src, double* u) {
+    const Pack& p = pk_[0];
+    std::vector<d4> h(static_cast<size_t>(p.n));
+    AERO_CK(cudaMemcpyAsync(h.data(), src, sizeof(d4) * p.n, cudaMemcpyDeviceToHost, st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+    for (int cn = 0; cn < p.n; ++cn) {
+      double* s = u + 5 * static_cast<size_t>(hs_[0].perm[cn]);
+      s[0] = h[cn].x;
+      s[1] = h[cn].y;
+      s[2] = h[cn].z;
+      s[3] = 0.0;
+      s[4] = h[cn].w;
+    }
+  }
+
+  // Pressure of the cells that own wall entries at the linearisation point (the gauge
+  // pressure force, post/forces.cpp:208-294, integrates p_owner - p_inf); 0 elsewhere.
+  std::vector<double> wall_pressures() {
+    const Pack& pk = pk_[0];
+    std::vector<d4> h(static_cast<size_t>(pk.n));
+    AERO_CK(cudaMemcpyAsync(h.data(), Ulin_, sizeof(d4) * pk.n, cudaMemcpyDeviceToHost, st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+    const HostSlots& hs = hs_[0];
+    const double g = rs_[0].gamma;
+    std::vector<double> p(static_cast<size_t>(pk.n), 0.0);
+    for (int c = 0; c < pk.n; ++c) {
+      if (!(hs.flags[c] >> 2)) continue;
+      const double r = std::max(h[c].x, 1.0e-8), inv = 1.0 / r, u = h[c].y * inv, v = h[c].z * inv;
+      p[c] = std::max((g - 1.0) * (h[c].w - 0.5 * r * (u * u + v * v)), 1.0e-8);
+    }
+    return p;
   }
 
   void download_ctrls() {
@@ -1099,6 +1509,28 @@ class EngineT final : public Engine {
   DevMesh<T> dm_{};
   cudaGraphExec_t graph_[16] = {};
   bool defer_control_ = false;
+  // discrete adjoint (FP64)
+  bool adj_alloc_ = false, adj_ready_ = false, adj_second_ = false;
+  double adj_wcd_ = 0.0, adj_wcl_ = 0.0, adj_ex_ = 0.0, adj_ey_ = 0.0;
+  d4 *gxlin_ = nullptr, *gylin_ = nullptr;
+  // geometry tangent scratch
+  bool geo_alloc_ = false;
+  double2 *geo_nrm_ = nullptr, *geo_fn_ = nullptr, *geo_doff_ = nullptr, *geo_noff_ = nullptr;
+  double *geo_area_ = nullptr, *geo_inv_ = nullptr, *geo_fa_ = nullptr;
+  d4 *geo_gx_ = nullptr, *geo_gy_ = nullptr;
+  double* Jf_ = nullptr;        // per face: 4 x kJac local Jacobian
+  double* adj_face_ = nullptr;  // per face: kJac transpose-product contributions
+  double* adj_face_out_ = nullptr;
+  d4 *mw_ = nullptr, *mgx_ = nullptr, *mgy_ = nullptr, *adj_r_ = nullptr, *adj_g_ = nullptr;
+  d4 *lam_ = nullptr, *lam_n_ = nullptr, *adj_v_ = nullptr;
+  double* adj_rn_ = nullptr;     // per cell block: sum of the squared adjoint residual
+  double* adj_hist_ = nullptr;   // per iteration of a chunk: RMS adjoint residual
+  int* adj_counter_ = nullptr;
+  cudaGraphExec_t adj_graph_ = nullptr;
+  double adj_graph_cfl_ = 0.0;
+  Ctrl* ctrl_lin_ = nullptr;
+  d4 *Ulin_ = nullptr, *Wlin_ = nullptr;  // state and primitives at the linearisation point
+  double* SRlin_ = nullptr;               // its spectral radii (the adjoint's local steps)
   cudaStream_t side_ = nullptr;
   cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
   V4* R0_ = nullptr;

@@ -9,6 +9,7 @@
 #include <map>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -527,6 +528,161 @@ aero_mesh* synthetic_ogrid(const aero_ogrid_spec& s) {
   return m;
 }
 
+// ---------------------------------------------------------------------------------------
+// Geometry from node coordinates (the synthetic generator's double formulas) and its
+// tangent along a node displacement, through one template on the scalar type.
+// ---------------------------------------------------------------------------------------
+struct Tan {  // value and one directional derivative
+  double v, d;
+};
+inline Tan operator+(Tan a, Tan b) { return {a.v + b.v, a.d + b.d}; }
+inline Tan operator-(Tan a, Tan b) { return {a.v - b.v, a.d - b.d}; }
+inline Tan operator*(Tan a, Tan b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+inline Tan operator*(double a, Tan b) { return {a * b.v, a * b.d}; }
+inline Tan operator/(Tan a, Tan b) {
+  const double q = a.v / b.v;
+  return {q, (a.d - q * b.d) / b.v};
+}
+inline Tan operator/(Tan a, double b) { return {a.v / b, a.d / b}; }
+inline Tan operator-(Tan a) { return {-a.v, -a.d}; }
+inline double val(double x) { return x; }
+inline double val(Tan x) { return x.v; }
+inline double hyp(double x, double y) { return std::hypot(x, y); }
+inline Tan hyp(Tan x, Tan y) {
+  const double h = std::hypot(x.v, y.v);
+  return {h, h > 0.0 ? (x.v * x.d + y.v * y.d) / h : 0.0};
+}
+
+template <class S>
+void node_geometry(const aero_mesh& m, const std::vector<S>& px, const std::vector<S>& py, std::vector<S>* normal,
+                   std::vector<S>* center, std::vector<S>* area, std::vector<S>* volume,
+                   std::vector<S>* cell_center) {
+  volume->assign(static_cast<size_t>(m.nc), S{});
+  cell_center->assign(3 * static_cast<size_t>(m.nc), S{});
+  for (int k = 0; k < m.nc; ++k) {
+    const int b = k == 0 ? 0 : m.offsets[k - 1], e = m.offsets[k], nv = e - b;
+    S a2{}, sx{}, sy{};
+    for (int j = 0; j < nv; ++j) {
+      const int p = m.conn[b + j], q = m.conn[b + (j + 1) % nv];
+      const S cr = px[p] * py[q] - px[q] * py[p];
+      a2 = a2 + cr;
+      sx = sx + (px[p] + px[q]) * cr;
+      sy = sy + (py[p] + py[q]) * cr;
+    }
+    if (!(val(a2) > 0.0)) throw std::runtime_error("inverted or degenerate cell " + std::to_string(k));
+    (*volume)[k] = 0.5 * a2;
+    if (nv == 3) {
+      const int v0 = m.conn[b], v1 = m.conn[b + 1], v2 = m.conn[b + 2];
+      (*cell_center)[3 * k] = (px[v0] + px[v1] + px[v2]) / 3.0;
+      (*cell_center)[3 * k + 1] = (py[v0] + py[v1] + py[v2]) / 3.0;
+    } else {
+      (*cell_center)[3 * k] = sx / (3.0 * a2);
+      (*cell_center)[3 * k + 1] = sy / (3.0 * a2);
+    }
+  }
+  normal->assign(3 * static_cast<size_t>(m.nf), S{});
+  center->assign(3 * static_cast<size_t>(m.nf), S{});
+  area->assign(static_cast<size_t>(m.nf), S{});
+  for (int f = 0; f < m.nf; ++f) {
+    const int v0 = m.face_vertices[2 * f], v1 = m.face_vertices[2 * f + 1];
+    const S dx = px[v1] - px[v0], dy = py[v1] - py[v0];
+    const S len = hyp(dx, dy);
+    if (!(val(len) > 0.0)) throw std::runtime_error("degenerate face " + std::to_string(f));
+    (*normal)[3 * f] = dy / len;
+    (*normal)[3 * f + 1] = -dx / len;
+    (*area)[f] = len;
+    (*center)[3 * f] = 0.5 * (px[v0] + px[v1]);
+    (*center)[3 * f + 1] = 0.5 * (py[v0] + py[v1]);
+  }
+}
+
+// Hicks-Henne bump on [0, 1]: sin(pi x^(ln 0.5 / ln peak))^width, 0 at both ends.
+double hicks_henne(double x, double peak, double width) {
+  if (!(x > 0.0) || !(x < 1.0)) return 0.0;
+  const double e = std::log(0.5) / std::log(peak);
+  const double s = std::sin(3.14159265358979323846 * std::pow(x, e));
+  return std::pow(std::max(s, 0.0), width);
+}
+
+// Displacement modes of n bumps: the wall nodes move in y by the bump of their side of the
+// airfoil (unit amplitude), the far-field nodes stay, every other node moves by the
+// inverse-distance-weighted mean (weights |x - x_s|^-3) of those boundary displacements.
+void hicks_henne_modes(const aero_mesh& m, int n, const double* peak, const int* upper, double width,
+                       double* modes) {
+  const int np = m.np;
+  std::vector<char> kind(static_cast<size_t>(np), 0);  // 1 wall, 2 far field
+  for (int f : m.wall_faces) {
+    kind[m.face_vertices[2 * f]] = 1;
+    kind[m.face_vertices[2 * f + 1]] = 1;
+  }
+  for (int f = 0; f < m.nf; ++f) {
+    if (m.neighbor[f] < 0 && m.bc[f] == AERO_BC_FARFIELD) {
+      for (int s = 0; s < 2; ++s) {
+        if (kind[m.face_vertices[2 * f + s]] == 0) kind[m.face_vertices[2 * f + s]] = 2;
+      }
+    }
+  }
+  std::vector<int> wall, src;
+  for (int p = 0; p < np; ++p) {
+    if (kind[p] == 1) wall.push_back(p);
+    if (kind[p] != 0) src.push_back(p);
+  }
+  if (wall.empty()) throw std::invalid_argument("mesh has no wall patch");
+  double x0 = 1e300, x1 = -1e300;
+  for (int p : wall) {
+    x0 = std::min(x0, m.points[3 * p]);
+    x1 = std::max(x1, m.points[3 * p]);
+  }
+  const double chord = x1 - x0;
+  if (!(chord > 0.0)) throw std::invalid_argument("wall patch has no chord");
+  // boundary displacements per source node and bump
+  std::vector<double> sd(src.size() * static_cast<size_t>(n), 0.0);
+  for (size_t s = 0; s < src.size(); ++s) {
+    const int p = src[s];
+    if (kind[p] != 1) continue;
+    const double xi = (m.points[3 * p] - x0) / chord, y = m.points[3 * p + 1];
+    for (int k = 0; k < n; ++k) {
+      const bool on = upper[k] ? y > 0.0 : y < 0.0;
+      if (on) sd[s * n + k] = hicks_henne(xi, peak[k], width);
+    }
+  }
+  const size_t stride = 3 * static_cast<size_t>(np);
+  std::fill(modes, modes + stride * n, 0.0);
+  auto work = [&](int p_begin, int p_end) {
+    std::vector<double> acc(static_cast<size_t>(n));
+    for (int p = p_begin; p < p_end; ++p) {
+      if (kind[p] == 1) {
+        const size_t s = static_cast<size_t>(std::lower_bound(src.begin(), src.end(), p) - src.begin());
+        for (int k = 0; k < n; ++k) modes[k * stride + 3 * p + 1] = sd[s * n + k];
+        continue;
+      }
+      if (kind[p] == 2) continue;
+      const double x = m.points[3 * p], y = m.points[3 * p + 1];
+      double wsum = 0.0;
+      std::fill(acc.begin(), acc.end(), 0.0);
+      for (size_t s = 0; s < src.size(); ++s) {
+        const int q = src[s];
+        const double dx = x - m.points[3 * q], dy = y - m.points[3 * q + 1];
+        const double d2 = dx * dx + dy * dy;
+        const double w = 1.0 / (d2 * std::sqrt(d2));
+        wsum += w;
+        if (kind[q] == 1) {
+          for (int k = 0; k < n; ++k) acc[k] += w * sd[s * n + k];
+        }
+      }
+      for (int k = 0; k < n; ++k) modes[k * stride + 3 * p + 1] = acc[k] / wsum;
+    }
+  };
+  const int threads = static_cast<int>(std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
+  std::vector<std::thread> pool;
+  const int chunk = (np + threads - 1) / threads;
+  for (int t = 0; t < threads; ++t) {
+    const int b = t * chunk, e = std::min(np, b + chunk);
+    if (b < e) pool.emplace_back(work, b, e);
+  }
+  for (auto& th : pool) th.join();
+}
+
 template <class Fn>
 int guarded(Fn&& fn) {
   try {
@@ -597,6 +753,75 @@ int aero_mesh_describe(const aero_mesh* m, aero_mesh_desc* d) {
   d->num_wall_faces = static_cast<int>(m->wall_faces.size());
   d->wall_faces = m->wall_faces.data();
   return AERO_OK;
+}
+
+int aero_mesh_clone(const aero_mesh* m, aero_mesh** out) {
+  if (m == nullptr || out == nullptr) {
+    g_mesh_error = "null argument";
+    return AERO_ERR_INVALID;
+  }
+  *out = nullptr;
+  return guarded([&] { *out = new aero_mesh(*m); });
+}
+
+int aero_mesh_set_points(aero_mesh* m, const double* points) {
+  if (m == nullptr || points == nullptr) {
+    g_mesh_error = "null argument";
+    return AERO_ERR_INVALID;
+  }
+  return guarded([&] {
+    std::vector<double> px(static_cast<size_t>(m->np)), py(px.size());
+    for (int p = 0; p < m->np; ++p) {
+      px[p] = points[3 * p];
+      py[p] = points[3 * p + 1];
+    }
+    std::vector<double> normal, center, area, volume, cc;
+    node_geometry(*m, px, py, &normal, &center, &area, &volume, &cc);
+    m->points.assign(points, points + 3 * static_cast<size_t>(m->np));
+    m->normal.swap(normal);
+    m->center.swap(center);
+    m->area.swap(area);
+    m->volume.swap(volume);
+    m->cell_center.swap(cc);
+  });
+}
+
+int aero_mesh_geometry_tangent(const aero_mesh* m, const double* dpoints, double* d_normal, double* d_center,
+                               double* d_area, double* d_volume, double* d_cell_center) {
+  if (m == nullptr || dpoints == nullptr || !d_normal || !d_center || !d_area || !d_volume || !d_cell_center) {
+    g_mesh_error = "null argument";
+    return AERO_ERR_INVALID;
+  }
+  return guarded([&] {
+    std::vector<Tan> px(static_cast<size_t>(m->np)), py(px.size());
+    for (int p = 0; p < m->np; ++p) {
+      px[p] = Tan{m->points[3 * p], dpoints[3 * p]};
+      py[p] = Tan{m->points[3 * p + 1], dpoints[3 * p + 1]};
+    }
+    std::vector<Tan> normal, center, area, volume, cc;
+    node_geometry(*m, px, py, &normal, &center, &area, &volume, &cc);
+    for (size_t i = 0; i < normal.size(); ++i) d_normal[i] = normal[i].d;
+    for (size_t i = 0; i < center.size(); ++i) d_center[i] = center[i].d;
+    for (size_t i = 0; i < area.size(); ++i) d_area[i] = area[i].d;
+    for (size_t i = 0; i < volume.size(); ++i) d_volume[i] = volume[i].d;
+    for (size_t i = 0; i < cc.size(); ++i) d_cell_center[i] = cc[i].d;
+  });
+}
+
+int aero_mesh_hicks_henne_modes(const aero_mesh* m, int n_bumps, const double* peak_x, const int* upper,
+                                double width_exponent, double* modes) {
+  if (m == nullptr || n_bumps <= 0 || peak_x == nullptr || upper == nullptr || modes == nullptr ||
+      !(width_exponent > 0.0)) {
+    g_mesh_error = "bad argument";
+    return AERO_ERR_INVALID;
+  }
+  for (int k = 0; k < n_bumps; ++k) {
+    if (!(peak_x[k] > 0.0 && peak_x[k] < 1.0)) {
+      g_mesh_error = "bump peaks must lie in (0, 1)";
+      return AERO_ERR_INVALID;
+    }
+  }
+  return guarded([&] { hicks_henne_modes(*m, n_bumps, peak_x, upper, width_exponent, modes); });
 }
 
 int aero_mesh_get_aux(const aero_mesh* m, double* points, int* face_vertices, int* conn, int* offsets,

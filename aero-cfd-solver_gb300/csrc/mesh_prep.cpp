@@ -206,6 +206,7 @@ bool build_slots(const aero_mesh_desc& m, int ordering, HostSlots* out, std::str
   s.area.assign(total, 0.0);
   s.fcx.assign(total, 0.0);
   s.fcy.assign(total, 0.0);
+  s.slot_face.assign(total, -1);
   s.own_old.assign(total, 0);
   s.nbr_old.assign(total, 0);
   s.vol.resize(static_cast<size_t>(n));
@@ -237,6 +238,7 @@ bool build_slots(const aero_mesh_desc& m, int ordering, HostSlots* out, std::str
       s.area[slot] = m.face_area[f];
       s.fcx[slot] = m.face_center[3 * f];
       s.fcy[slot] = m.face_center[3 * f + 1];
+      s.slot_face[slot] = f;
       s.own_old[slot] = o;
       s.nbr_old[slot] = b >= 0 ? b : o;
     }
@@ -316,6 +318,7 @@ bool build_slots(const aero_mesh_desc& m, int ordering, HostSlots* out, std::str
     const WallEntry& e = we[j];
     if (per_cell[e.cell]++ == 0) s.wall_first[e.cell] = static_cast<int>(j);
     s.wkind.push_back(e.kind);
+    s.w_face.push_back(e.face);
     s.wnx.push_back(m.face_normal[3 * e.face]);
     s.wny.push_back(m.face_normal[3 * e.face + 1]);
     s.warea.push_back(m.face_area[e.face]);
@@ -330,6 +333,61 @@ bool build_slots(const aero_mesh_desc& m, int ordering, HostSlots* out, std::str
     s.flags[c] = static_cast<unsigned char>(s.flags[c] | (per_cell[c] << 2));
   }
   return true;
+}
+
+void map_geometry(const aero_mesh_desc& m, const HostSlots& s, HostSlots* geo) {
+  HostSlots& g = *geo;
+  const size_t total = s.slot_face.size();
+  g.nx.assign(total, 0.0);
+  g.ny.assign(total, 0.0);
+  g.area.assign(total, 0.0);
+  g.fcx.assign(total, 0.0);
+  g.fcy.assign(total, 0.0);
+  for (size_t k = 0; k < total; ++k) {
+    const int f = s.slot_face[k];
+    if (f < 0) continue;
+    g.nx[k] = m.face_normal[3 * f];
+    g.ny[k] = m.face_normal[3 * f + 1];
+    g.area[k] = m.face_area[f];
+    g.fcx[k] = m.face_center[3 * f];
+    g.fcy[k] = m.face_center[3 * f + 1];
+  }
+  g.vol.resize(static_cast<size_t>(s.n));
+  g.ccx.resize(static_cast<size_t>(s.n));
+  g.ccy.resize(static_cast<size_t>(s.n));
+  for (int cn = 0; cn < s.n; ++cn) g.vol[cn] = m.cell_volume[s.perm[cn]];
+  for (int c = 0; c < s.n; ++c) {
+    g.ccx[c] = m.cell_center[3 * c];
+    g.ccy[c] = m.cell_center[3 * c + 1];
+  }
+  const size_t nf = s.f_orig.size();
+  g.f_nx.resize(nf);
+  g.f_ny.resize(nf);
+  g.f_area.resize(nf);
+  g.f_cx.resize(nf);
+  g.f_cy.resize(nf);
+  for (size_t i = 0; i < nf; ++i) {
+    const int f = s.f_orig[i];
+    g.f_nx[i] = m.face_normal[3 * f];
+    g.f_ny[i] = m.face_normal[3 * f + 1];
+    g.f_area[i] = m.face_area[f];
+    g.f_cx[i] = m.face_center[3 * f];
+    g.f_cy[i] = m.face_center[3 * f + 1];
+  }
+  const size_t nw = s.w_face.size();
+  g.wnx.resize(nw);
+  g.wny.resize(nw);
+  g.warea.resize(nw);
+  g.wx.resize(nw);
+  g.wy.resize(nw);
+  for (size_t j = 0; j < nw; ++j) {
+    const int f = s.w_face[j];
+    g.wnx[j] = m.face_normal[3 * f];
+    g.wny[j] = m.face_normal[3 * f + 1];
+    g.warea[j] = m.face_area[f];
+    g.wx[j] = m.face_center[3 * f];
+    g.wy[j] = m.face_center[3 * f + 1];
+  }
 }
 
 }  // namespace aero

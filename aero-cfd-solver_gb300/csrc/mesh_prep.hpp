@@ -19,6 +19,7 @@ struct HostSlots {
   std::vector<int> link;   // [d*n] (other_new << 1 | side), -1 far field, -2 wall, kPad
   std::vector<double> nx, ny, area;     // [d*n] canonical (owner-outward) face geometry
   std::vector<double> fcx, fcy;         // [d*n] face centre
+  std::vector<int> slot_face;           // [d*n] original face of the slot, -1 padding
   std::vector<int> own_old, nbr_old;    // [d*n] canonical owner / neighbour (original ids)
   // Face table: faces sorted by the new index of their owner, then by original index.
   std::vector<int> f_orig;                  // new face -> original face
@@ -38,6 +39,7 @@ struct HostSlots {
   // face in both sets shares one entry.
   std::vector<unsigned char> wkind;
   std::vector<double> wnx, wny, warea, wx, wy;
+  std::vector<int> w_face;  // original face of each wall entry
   int n_patch = 0;  // force patch faces
   int n_slip = 0;   // slip-wall boundary faces
   int interior_faces = 0, boundary_faces = 0;
@@ -45,5 +47,11 @@ struct HostSlots {
 
 // Validates the mesh and builds the slot table. Returns false with a message on bad input.
 bool build_slots(const aero_mesh_desc& m, int ordering, HostSlots* out, std::string* err);
+
+// Refill the geometry arrays of *geo (slot, face-table and wall-entry normals, areas and
+// centres, volumes and cell centres) from m, in the numbering and layout of `layout` (a
+// build_slots result for a mesh of the same connectivity). Used for geometry tangents, whose
+// arrays map through the same copies.
+void map_geometry(const aero_mesh_desc& m, const HostSlots& layout, HostSlots* geo);
 
 }  // namespace aero

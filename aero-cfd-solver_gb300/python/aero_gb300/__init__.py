@@ -7,6 +7,7 @@ solver call goes to the CUDA path, and Solver() raises when no sm_103 device is 
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from pathlib import Path
 
 import numpy as np
@@ -80,6 +81,7 @@ def load(build_if_missing: bool = False):
         "aero_select_device": (C.c_int, [C.c_int]),
         "aero_get_info": (C.c_int, [C.c_void_p, _llp, C.c_int]),
         "aero_batch_create": (C.c_int, [C.c_int, C.POINTER(MeshDesc), C.POINTER(CaseDesc), C.POINTER(C.c_void_p)]),
+        "aero_autotune": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(CaseDesc), C.c_int, C.POINTER(CaseDesc), _dp]),
         "aero_batch_size": (C.c_int, [C.c_void_p]),
         "aero_batch_run": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(IterRecord), _ip]),
         "aero_batch_set_state": (C.c_int, [C.c_void_p, C.c_int, _dp]),
@@ -93,6 +95,17 @@ def load(build_if_missing: bool = False):
         "aero_mesh_get_sizes": (C.c_int, [C.c_void_p, C.POINTER(MeshSizes)]),
         "aero_mesh_describe": (C.c_int, [C.c_void_p, C.POINTER(MeshDesc)]),
         "aero_mesh_get_aux": (C.c_int, [C.c_void_p, _dp, _ip, _ip, _ip, C.POINTER(C.c_ubyte), _ip]),
+        "aero_mesh_clone": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+        "aero_mesh_set_points": (C.c_int, [C.c_void_p, _dp]),
+        "aero_mesh_geometry_tangent": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp]),
+        "aero_mesh_hicks_henne_modes": (C.c_int, [C.c_void_p, C.c_int, _dp, _ip, C.c_double, _dp]),
+        "aero_adjoint_linearize": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int]),
+        "aero_adjoint_vjp": (C.c_int, [C.c_void_p, _dp, _dp]),
+        "aero_adjoint_objective_gradient": (C.c_int, [C.c_void_p, _dp]),
+        "aero_adjoint_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_double, _dp]),
+        "aero_adjoint_get_lambda": (C.c_int, [C.c_void_p, _dp]),
+        "aero_adjoint_dalpha": (C.c_int, [C.c_void_p, _dp]),
+        "aero_adjoint_geometry": (C.c_int, [C.c_void_p, C.POINTER(MeshDesc), _dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -116,6 +129,8 @@ def select_device(device: int) -> None:
 # meshes
 # --------------------------------------------------------------------------------------
 def _mesh_from_handle(h) -> Mesh:
+    """Copy a generated mesh into numpy arrays; the Mesh keeps the handle (freed with it)
+    for the node-based operations (deform, geometry_tangent, hicks_henne_modes)."""
     lib = load()
     sz = MeshSizes()
     lib.aero_mesh_get_sizes(h, C.byref(sz))
@@ -143,8 +158,66 @@ def _mesh_from_handle(h) -> Mesh:
              points=points, face_vertices=fv, cell_conn=conn, cell_offsets=offs,
              farfield_faces=ff[: sz.num_farfield_faces])
     m.cell_types = types
-    lib.aero_mesh_free(h)
+    m._handle = h
+    weakref.finalize(m, lib.aero_mesh_free, h)
     return m
+
+
+def _handle(mesh: Mesh):
+    h = getattr(mesh, "_handle", None)
+    if h is None:
+        raise ValueError("mesh has no node data: generate it with ogrid_synthetic / ogrid_reference")
+    return h
+
+
+def deform(mesh: Mesh, points: np.ndarray) -> Mesh:
+    """A copy of `mesh` with its nodes moved to points [P, 3] and the geometry recomputed
+    (aero_mesh_set_points)."""
+    lib = load()
+    h = C.c_void_p()
+    rc = lib.aero_mesh_clone(_handle(mesh), C.byref(h))
+    if rc != 0:
+        raise AeroError(rc, lib.aero_mesh_last_error().decode())
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1)
+    rc = lib.aero_mesh_set_points(h, pts.ctypes.data_as(_dp))
+    if rc != 0:
+        msg = lib.aero_mesh_last_error().decode()
+        lib.aero_mesh_free(h)
+        raise AeroError(rc, msg)
+    return _mesh_from_handle(h)
+
+
+def geometry_tangent(mesh: Mesh, dpoints: np.ndarray) -> Mesh:
+    """The derivative of the mesh geometry along a node displacement dpoints [P, 3], as a
+    Mesh with the connectivity of `mesh` and the derivatives in its geometry arrays (the
+    input of Solver.adjoint_geometry)."""
+    lib = load()
+    dp = np.ascontiguousarray(dpoints, dtype=np.float64).reshape(-1)
+    nf, nc = mesh.num_faces, mesh.num_cells
+    dn, dc, da = np.empty(3 * nf), np.empty(3 * nf), np.empty(nf)
+    dv, dcc = np.empty(nc), np.empty(3 * nc)
+    rc = lib.aero_mesh_geometry_tangent(_handle(mesh), dp.ctypes.data_as(_dp), dn.ctypes.data_as(_dp),
+                                        dc.ctypes.data_as(_dp), da.ctypes.data_as(_dp), dv.ctypes.data_as(_dp),
+                                        dcc.ctypes.data_as(_dp))
+    if rc != 0:
+        raise AeroError(rc, lib.aero_mesh_last_error().decode())
+    return Mesh(mesh.owner, mesh.neighbor, mesh.bc, dn, dc, da, dv, dcc, mesh.wall_faces)
+
+
+def hicks_henne_modes(mesh: Mesh, peaks, upper, width: float = 3.0) -> np.ndarray:
+    """Node displacement modes [n, P, 3] of Hicks-Henne bumps with unit amplitude, carried
+    into the volume by inverse-distance weighting (aero_mesh_hicks_henne_modes)."""
+    lib = load()
+    pk = np.ascontiguousarray(peaks, dtype=np.float64)
+    up = np.ascontiguousarray(upper, dtype=np.int32)
+    assert pk.shape == up.shape
+    npts = mesh.points.size // 3
+    modes = np.empty((pk.size, npts, 3), np.float64)
+    rc = lib.aero_mesh_hicks_henne_modes(_handle(mesh), pk.size, pk.ctypes.data_as(_dp), up.ctypes.data_as(_ip),
+                                         float(width), modes.ctypes.data_as(_dp))
+    if rc != 0:
+        raise AeroError(rc, lib.aero_mesh_last_error().decode())
+    return modes
 
 
 def ogrid_reference(naca: str = "0012", n_circ: int = 160, n_radial: int = 48,
@@ -172,6 +245,23 @@ def ogrid_synthetic(n_circ: int, n_radial: int, cell_type: int = 3, permute: boo
     if rc != 0:
         raise AeroError(rc, lib.aero_mesh_last_error().decode())
     return _mesh_from_handle(h)
+
+
+def autotune(mesh: Mesh, case: CaseDesc, iters: int = 20):
+    """Fastest block size and cell ordering for this mesh and case (aero_autotune). Returns
+    (case with them set, {(ordering, block): device ms of `iters` iterations})."""
+    lib = load()
+    md = mesh.desc()
+    best = CaseDesc()
+    ms = (C.c_double * 6)()
+    rc = lib.aero_autotune(C.byref(md), C.byref(case), iters, C.byref(best), ms)
+    if rc != 0:
+        raise AeroError(rc, lib.aero_last_error(None).decode())
+    table = {}
+    for i, o in enumerate((capi.ORDER_MORTON, capi.ORDER_RCM)):
+        for j, b in enumerate((64, 128, 256)):
+            table[(o, b)] = ms[3 * i + j]
+    return best, table
 
 
 # --------------------------------------------------------------------------------------
@@ -277,6 +367,48 @@ class Solver:
         keys = ("cells", "faces", "slots_per_cell", "launches_per_iteration", "device_bytes", "precision",
                 "block_size", "blocks", "cases")
         return dict(zip(keys, list(v)))
+
+    # ---- discrete adjoint (include/aero_adjoint.h; FP64 contexts)
+    def adjoint_linearize(self, w_cd: float = 1.0, w_cl: float = 0.0, second_order: int = -1):
+        """Linearise at the current state for J = w_cd CD + w_cl CL; lam starts at 0."""
+        self._check(self.lib.aero_adjoint_linearize(self.h, float(w_cd), float(w_cl), int(second_order)))
+
+    def adjoint_vjp(self, v: np.ndarray) -> np.ndarray:
+        """(dR/dU)^T v at the linearisation point, [N, 5] in and out."""
+        v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
+        assert v.size == 5 * self.n
+        out = np.empty(5 * self.n, np.float64)
+        self._check(self.lib.aero_adjoint_vjp(self.h, v.ctypes.data_as(_dp), out.ctypes.data_as(_dp)))
+        return out.reshape(self.n, 5)
+
+    def adjoint_objective_gradient(self) -> np.ndarray:
+        g = np.empty(5 * self.n, np.float64)
+        self._check(self.lib.aero_adjoint_objective_gradient(self.h, g.ctypes.data_as(_dp)))
+        return g.reshape(self.n, 5)
+
+    def adjoint_solve(self, iters: int, cfl: float = 0.8) -> np.ndarray:
+        """Pseudo-time iterations of the adjoint; returns the RMS adjoint residual per iteration."""
+        hist = np.empty(max(iters, 1), np.float64)
+        self._check(self.lib.aero_adjoint_solve(self.h, int(iters), float(cfl), hist.ctypes.data_as(_dp)))
+        return hist[:iters]
+
+    def adjoint_lambda(self) -> np.ndarray:
+        lam = np.empty(5 * self.n, np.float64)
+        self._check(self.lib.aero_adjoint_get_lambda(self.h, lam.ctypes.data_as(_dp)))
+        return lam.reshape(self.n, 5)
+
+    def adjoint_dalpha(self) -> float:
+        """dJ/d(alpha) per degree."""
+        out = C.c_double(0.0)
+        self._check(self.lib.aero_adjoint_dalpha(self.h, C.byref(out)))
+        return out.value
+
+    def adjoint_geometry(self, tangent: Mesh) -> float:
+        """dJ/dX . dX for a geometry tangent (geometry_tangent(mesh, dpoints))."""
+        d = tangent.desc()
+        out = C.c_double(0.0)
+        self._check(self.lib.aero_adjoint_geometry(self.h, C.byref(d), C.byref(out)))
+        return out.value
 
 
 class Batch(Solver):

@@ -160,6 +160,7 @@ CASE_DEFAULTS = dict(
     all_speed_cfl_min_scale=_F(0.1),
     aoa0_symmetry_enforce=0, aoa0_symmetry_enforce_interval=0,
     precision=PRECISION_FP64, ordering=ORDER_MORTON, block_size=0, diagnostics=0,
+    density_l2_target=0.0,
 )
 
 

@@ -247,8 +247,17 @@ AERO_API int aero_residual_noalloc(aero_ctx* ctx, const double* conserved_dev, i
 
 /* Sizes and kernel-launch counts of the context, for roofline accounting:
  * info[0] cells, [1] faces, [2] slots per cell (padded), [3] kernel launches per
- * iteration, [4] bytes of device memory held, [5] precision, [6] block size. */
+ * iteration, [4] bytes of device memory held, [5] precision, [6] block size, [7] cell
+ * blocks, [8] cases. */
 AERO_API int aero_get_info(aero_ctx* ctx, long long* info, int n_info);
+
+/* Autotuner (no reference counterpart): times `iters` second-order iterations of the case on
+ * this mesh for every block size (64, 128, 256) and cell ordering (Morton, RCM), each in its
+ * own context after the case's first-order start-up, and writes the case with the fastest
+ * pair into *best (all other fields copied from *c). ms_out (may be NULL) receives the 6
+ * device times in ms, ordering-major: [Morton 64, 128, 256, RCM 64, 128, 256]. */
+AERO_API int aero_autotune(const aero_mesh_desc* mesh, const aero_case_desc* c, int iters, aero_case_desc* best,
+                           double* ms_out);
 
 #ifdef __cplusplus
 }

@@ -60,6 +60,30 @@ AERO_API int aero_mesh_describe(const aero_mesh* m, aero_mesh_desc* d);
 AERO_API int aero_mesh_get_aux(const aero_mesh* m, double* points, int* face_vertices, int* conn,
                       int* offsets, unsigned char* types, int* farfield_faces);
 
+/* Deep copy of a mesh (free it with aero_mesh_free). */
+AERO_API int aero_mesh_clone(const aero_mesh* m, aero_mesh** out);
+
+/* Move the nodes to points [3P] and recompute the geometry (cell areas and centres, face
+ * normals, lengths and centres) with the synthetic generator's double formulas. Fails
+ * (mesh unchanged) if a cell inverts or a face degenerates. */
+AERO_API int aero_mesh_set_points(aero_mesh* m, const double* points);
+
+/* Derivatives of that geometry along a node displacement dpoints [3P]: d_normal [3F],
+ * d_center [3F], d_area [F], d_volume [N], d_cell_center [3N]. Fill an aero_mesh_desc with
+ * them (connectivity from aero_mesh_describe) to pass to aero_adjoint_geometry. */
+AERO_API int aero_mesh_geometry_tangent(const aero_mesh* m, const double* dpoints, double* d_normal,
+                                        double* d_center, double* d_area, double* d_volume,
+                                        double* d_cell_center);
+
+/* Shape modes of n Hicks-Henne bumps, modes [n][3P]: mode k moves the wall-patch nodes of
+ * the upper (upper[k] != 0, y > 0) or lower (y < 0) surface in y by
+ * sin(pi xi^(ln 0.5 / ln peak_x[k]))^width_exponent, xi the chordwise position in [0, 1]
+ * along the patch, keeps the far-field nodes fixed and carries the displacement into the
+ * volume by inverse-distance weighting (weights |x - x_s|^-3 over the wall and far-field
+ * nodes). The deformed nodes for amplitudes a are points + sum_k a_k modes[k]. */
+AERO_API int aero_mesh_hicks_henne_modes(const aero_mesh* m, int n_bumps, const double* peak_x,
+                                         const int* upper, double width_exponent, double* modes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -84,3 +84,18 @@ def test_batch_context_refuses_single_case_calls():
         recs = (capi.IterRecord * 1)()
         done = aero_gb300.C.c_int(0)
         assert b.lib.aero_run(b.h, 1, recs, aero_gb300.C.byref(done)) == capi.AERO_ERR_INVALID
+
+
+def test_autotune_picks_the_fastest_measured_variant():
+    mesh = aero_gb300.ogrid_synthetic(96, 24, cell_type=3, permute=True, jitter=0.1, seed=7)
+    case = capi.make_case(mach=0.6, flux=capi.FLUX_HLLC, limiter=capi.LIMITER_VENKAT, startup_first_order_iters=3,
+                          precision=capi.PRECISION_FP32)
+    best, table = aero_gb300.autotune(mesh, case, iters=10)
+    assert len(table) == 6 and all(v > 0 for v in table.values())
+    assert (best.ordering, best.block_size) == min(table, key=table.get)
+    assert best.mach == case.mach and best.flux == case.flux
+    with aero_gb300.Solver(mesh, best) as s:  # the tuned case runs and matches the default's results
+        _, rec = s.run(8)
+    with aero_gb300.Solver(mesh, case) as s:
+        _, rec0 = s.run(8)
+    np.testing.assert_allclose(rec["cl"], rec0["cl"], rtol=1e-5, atol=1e-7)

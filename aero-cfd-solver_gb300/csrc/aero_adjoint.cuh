@@ -23,6 +23,11 @@
 namespace aero {
 
 constexpr int kJac = 24;  // columns of a face Jacobian: W_o, W_n, G_o (x, y), G_n (x, y)
+// Columns stored per scheme: first order has no gradient inputs.
+template <bool SECOND>
+constexpr int jac_cols() {
+  return SECOND ? kJac : 8;
+}
 
 template <int N>
 __device__ __forceinline__ FaceParams<ad::Dual<N>> dual_params(const FaceParams<double>& f) {
@@ -58,8 +63,10 @@ __device__ __forceinline__ FaceParams<double> scheduled_params(FaceParams<double
   return fp;
 }
 
-// Local Jacobian of face i: J[i][k][j] = d(F_k A) / d(input j), inputs W_o(4), W_n(4),
-// G_o(8: x then y of rho, u, v, p), G_n(8). Three dual passes of 8 seeds each.
+// Local Jacobian of face i: d(F_k A) / d(input j), inputs W_o(4), W_n(4), G_o(8: x then y of
+// rho, u, v, p), G_n(8) (second order; the first 8 only for first order). Stored by column
+// across faces, J[(k * NC + j) * nf + i], so that a warp's loads are coalesced. Three dual
+// passes of 8 seeds each.
 template <int FLUX, bool SECOND, bool LM>
 __global__ void __launch_bounds__(256) k_adj_face_jac(DevFaces<double> f, const int2* __restrict__ fblk,
                                                       const FaceParams<double>* __restrict__ fps,
@@ -94,8 +101,13 @@ __global__ void __launch_bounds__(256) k_adj_face_jac(DevFaces<double> f, const 
   } else {
     for (int k = 0; k < 8; ++k) go[k] = gn[k] = 0.0;
   }
-  double* out = J + static_cast<size_t>(i) * 4 * kJac;
-  for (int k = 0; k < 4 * kJac; ++k) out[k] = 0.0;
+  constexpr int NC = jac_cols<SECOND>();
+  const size_t nf = static_cast<size_t>(f.nf);
+  if (SECOND && b < 0) {  // no gradient inputs at a boundary face
+    for (int k = 0; k < 4; ++k) {
+      for (int j = 8; j < NC; ++j) J[(k * NC + j) * nf + i] = 0.0;
+    }
+  }
   const int passes = (b >= 0 && SECOND) ? 3 : 1;
   for (int pass = 0; pass < passes; ++pass) {
     D wo[4] = {D(w0.x), D(w0.y), D(w0.z), D(w0.w)};
@@ -122,15 +134,18 @@ __global__ void __launch_bounds__(256) k_adj_face_jac(DevFaces<double> f, const 
                                    gO, gN, D(nd.x), D(nd.y), D(dox), D(doy), D(dnx), D(dny), &fl, &mws, &fo, &df);
     const D fk[4] = {fl.m, fl.fx, fl.fy, fl.e};
     for (int k = 0; k < 4; ++k) {
-      for (int j = 0; j < 8; ++j) out[k * kJac + pass * 8 + j] = fk[k].d[j] * area;
+      for (int j = 0; j < 8; ++j) J[(k * NC + pass * 8 + j) * nf + i] = fk[k].d[j] * area;
     }
   }
 }
 
 // Face pass of the transpose product: per face, a = v_o - v_n (v_o at a boundary face) and
-// its contributions J^T a: [0,4) to W_o, [4,8) W_n, [8,16) G_o, [16,24) G_n.
-static __global__ void k_adj_face_vjp(DevFaces<double> f, const int2* __restrict__ fblk, const double* __restrict__ J,
-                               const d4* __restrict__ v, double* __restrict__ out) {
+// its NC contributions J^T a, face-contiguous: [0,4) to W_o, [4,8) W_n, [8,16) G_o,
+// [16,24) G_n.
+template <int NC>
+__global__ void __launch_bounds__(256) k_adj_face_vjp(DevFaces<double> f, const int2* __restrict__ fblk,
+                                                      const double* __restrict__ J, const d4* __restrict__ v,
+                                                      double* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= fblk[blockIdx.x].y) return;
   const int2 oc = f.cells[i];
@@ -140,30 +155,39 @@ static __global__ void k_adj_face_vjp(DevFaces<double> f, const int2* __restrict
     const d4 vn = v[oc.y];
     a = d4{vo.x - vn.x, vo.y - vn.y, vo.z - vn.z, vo.w - vn.w};
   }
-  const double* Jf = J + static_cast<size_t>(i) * 4 * kJac;
-  double* o = out + static_cast<size_t>(i) * kJac;
-  for (int j = 0; j < kJac; ++j) {
-    o[j] = Jf[j] * a.x + Jf[kJac + j] * a.y + Jf[2 * kJac + j] * a.z + Jf[3 * kJac + j] * a.w;
+  const size_t nf = static_cast<size_t>(f.nf);
+  double* o = out + static_cast<size_t>(i) * NC;
+#pragma unroll
+  for (int j = 0; j < NC; ++j) {
+    o[j] = J[j * nf + i] * a.x + J[(NC + j) * nf + i] * a.y + J[(2 * NC + j) * nf + i] * a.z +
+           J[(3 * NC + j) * nf + i] * a.w;
   }
 }
 
-// Cell gather of the face contributions, in the cell's face order: mw (4) and mg (8) per cell.
-static __global__ void k_adj_gather(DevGather<double> g, const int2* __restrict__ cblk, const double* __restrict__ out,
-                             d4* __restrict__ mw, d4* __restrict__ mgx, d4* __restrict__ mgy) {
+// Cell gather of the face contributions, in the cell's face order: mw (4) and, for second
+// order, mg (8) per cell.
+template <int NC>
+__global__ void __launch_bounds__(256) k_adj_gather(DevGather<double> g, const int2* __restrict__ cblk,
+                                                    const double* __restrict__ out, d4* __restrict__ mw,
+                                                    d4* __restrict__ mgx, d4* __restrict__ mgy) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= cblk[blockIdx.x].y) return;
   double w[4] = {0, 0, 0, 0}, q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (int k = 0; k < g.d; ++k) {
     const int s = g.slot[k * g.n + c];
     if (s == kPad) break;
-    const double* o = out + static_cast<size_t>(s >> 1) * kJac;
+    const double* o = out + static_cast<size_t>(s >> 1) * NC;
     const int wo = (s & 1) ? 4 : 0, go = (s & 1) ? 16 : 8;
     for (int j = 0; j < 4; ++j) w[j] += o[wo + j];
-    for (int j = 0; j < 8; ++j) q[j] += o[go + j];
+    if (NC > 8) {
+      for (int j = 0; j < 8; ++j) q[j] += o[go + j];
+    }
   }
   mw[c] = d4{w[0], w[1], w[2], w[3]};
-  mgx[c] = d4{q[0], q[1], q[2], q[3]};
-  mgy[c] = d4{q[4], q[5], q[6], q[7]};
+  if (NC > 8) {
+    mgx[c] = d4{q[0], q[1], q[2], q[3]};
+    mgy[c] = d4{q[4], q[5], q[6], q[7]};
+  }
 }
 
 // Transpose of the Green-Gauss gradient (cell_gradient): G_c = (1/V_c) sum_s sgn_s q_s n_s A_s,
@@ -333,6 +357,82 @@ __global__ void k_adj_dalpha(DevFaces<double> f, const int2* __restrict__ fblk, 
                                 &fo, &df);
   const d4 l = lam[oc.x];
   out[i] = f.area[i] * (l.x * fl.m.d[0] + l.y * fl.fx.d[0] + l.z * fl.fy.d[0] + l.w * fl.e.d[0]);
+}
+
+// ---- vector kernels of the Krylov adjoint solve. Vectors are d4 per cell, n cells; a set
+// of vectors is contiguous with stride `ld` cells. Reductions are two-stage with a fixed
+// order (per-block partials, then one block per row), so results are deterministic.
+
+__device__ __forceinline__ double dot4(const d4& a, const d4& b) {
+  return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+}
+
+template <int BS>
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < BS / 32; ++w) s += sh[w];
+  }
+  return s;
+}
+
+// partial[r * gridDim.x + block] = sum over the block's cells of V_r . w, r = blockIdx.y.
+static __global__ void __launch_bounds__(256) k_vdot_rows(const d4* __restrict__ V, size_t ld, const d4* __restrict__ w,
+                                                          int n, double* __restrict__ partial) {
+  __shared__ double sh[8];
+  const int c = blockIdx.x * 256 + threadIdx.x;
+  const int r = blockIdx.y;
+  const double v = c < n ? dot4(V[static_cast<size_t>(r) * ld + c], w[c]) : 0.0;
+  const double s = block_sum<256>(v, sh);
+  if (threadIdx.x == 0) partial[static_cast<size_t>(r) * gridDim.x + blockIdx.x] = s;
+}
+
+// out[r] = sum of partial[r][0 .. nb), one block per row.
+static __global__ void __launch_bounds__(256) k_rows_sum(const double* __restrict__ partial, int nb,
+                                                         double* __restrict__ out) {
+  __shared__ double sh[8];
+  double a = 0.0;
+  for (int b = threadIdx.x; b < nb; b += 256) a += partial[static_cast<size_t>(blockIdx.x) * nb + b];
+  const double s = block_sum<256>(a, sh);
+  if (threadIdx.x == 0) out[blockIdx.x] = s;
+}
+
+// w = alpha * w + sum_{r < rows} coef[r] V_r   (cells c < n)
+static __global__ void __launch_bounds__(256) k_vcombine(d4* __restrict__ w, double alpha, const d4* __restrict__ V,
+                                                         size_t ld, const double* __restrict__ coef, int rows, int n) {
+  const int c = blockIdx.x * 256 + threadIdx.x;
+  if (c >= n) return;
+  d4 a{0.0, 0.0, 0.0, 0.0};
+  if (alpha != 0.0) {  // alpha = 0 does not read w
+    a = w[c];
+    a = d4{alpha * a.x, alpha * a.y, alpha * a.z, alpha * a.w};
+  }
+  for (int r = 0; r < rows; ++r) {
+    const double k = coef[r];
+    const d4 v = V[static_cast<size_t>(r) * ld + c];
+    a.x += k * v.x;
+    a.y += k * v.y;
+    a.z += k * v.z;
+    a.w += k * v.w;
+  }
+  w[c] = a;
+}
+
+// y = a * x + b * y   (cells c < n); b = 0 does not read y
+static __global__ void __launch_bounds__(256) k_vaxpby(double a, const d4* __restrict__ x, double b,
+                                                       d4* __restrict__ y, int n) {
+  const int c = blockIdx.x * 256 + threadIdx.x;
+  if (c >= n) return;
+  const d4 u = x[c];
+  if (b == 0.0) {
+    y[c] = d4{a * u.x, a * u.y, a * u.z, a * u.w};
+    return;
+  }
+  const d4 v = y[c];
+  y[c] = d4{a * u.x + b * v.x, a * u.y + b * v.y, a * u.z + b * v.z, a * u.w + b * v.w};
 }
 
 // ---- geometry sensitivities: tangents of the residual along a mesh perturbation dX

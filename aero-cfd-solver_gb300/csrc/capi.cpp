@@ -473,6 +473,21 @@ int aero_adjoint_solve(aero_ctx* ctx, int iters, double cfl, double* history) {
   return adjoint_status(ctx, ctx->engine->adjoint_solve(iters, cfl, history), "aero_adjoint_solve");
 }
 
+int aero_adjoint_solve_krylov(aero_ctx* ctx, int max_iters, int restart, int smooth_iters, double cfl,
+                              double rel_tol, double* history, int* iters_done) {
+  if (ctx == nullptr || max_iters < 0 || restart < 1 || restart > 512 || smooth_iters < 0 || !(cfl > 0.0) ||
+      !std::isfinite(cfl) || !(rel_tol >= 0.0))
+    return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_solve_krylov: bad argument");
+  return adjoint_status(
+      ctx, ctx->engine->adjoint_solve_krylov(max_iters, restart, smooth_iters, cfl, rel_tol, history, iters_done),
+      "aero_adjoint_solve_krylov");
+}
+
+int aero_adjoint_set_lambda(aero_ctx* ctx, const double* lam) {
+  if (ctx == nullptr || lam == nullptr) return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_set_lambda: null argument");
+  return adjoint_status(ctx, ctx->engine->adjoint_set_lambda(lam), "aero_adjoint_set_lambda");
+}
+
 int aero_adjoint_get_lambda(aero_ctx* ctx, double* lam) {
   if (ctx == nullptr || lam == nullptr) return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_get_lambda: null argument");
   return adjoint_status(ctx, ctx->engine->adjoint_lambda(lam), "aero_adjoint_get_lambda");

@@ -84,6 +84,9 @@ class Engine {
   virtual int adjoint_objective_gradient(double* g) = 0;
   virtual int adjoint_solve(int iters, double cfl, double* history) = 0;
   virtual int adjoint_lambda(double* lam) = 0;
+  virtual int adjoint_set_lambda(const double* lam) = 0;
+  virtual int adjoint_solve_krylov(int max_iters, int restart, int smooth, double cfl, double rtol,
+                                   double* history, int* done) = 0;
   virtual int adjoint_dalpha(double* dj_dalpha_deg) = 0;
   virtual int adjoint_geometry(const aero_mesh_desc& tangent, double* dj) = 0;
 };

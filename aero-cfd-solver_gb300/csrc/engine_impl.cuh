@@ -53,6 +53,7 @@ class EngineT final : public Engine {
       if (g) cudaGraphExecDestroy(g);
     }
     if (adj_graph_) cudaGraphExecDestroy(adj_graph_);
+    if (kr_graph_) cudaGraphExecDestroy(kr_graph_);
     if (ev_fork_) cudaEventDestroy(ev_fork_);
     if (ev_join_) cudaEventDestroy(ev_join_);
     if (side_) cudaStreamDestroy(side_);
@@ -710,6 +711,10 @@ class EngineT final : public Engine {
         cudaGraphExecDestroy(adj_graph_);
         adj_graph_ = nullptr;
       }
+      if (kr_graph_) {
+        cudaGraphExecDestroy(kr_graph_);
+        kr_graph_ = nullptr;
+      }
       const Cases<T> ccs{cblk_, ctrl_lin_, fps_dev_, pcs_dev_, mcs_dev_};
       const Cases<T> fcs{fblk_, ctrl_lin_, fps_dev_, pcs_dev_, mcs_dev_};
       refresh();
@@ -1155,24 +1160,204 @@ class EngineT final : public Engine {
 
   static constexpr int kAdjHist = 4096;  // iterations per host synchronisation
 
-  void adjoint_iteration(double cfl) {
+  // One RK3 iteration of z toward (dR/dU)^T z + src = 0 (zn: the iteration's start copy);
+  // with_norm: the RMS of (dR/dU)^T z + src at its start into the device history.
+  void adjoint_iteration(double cfl, d4* z, d4* zn, const d4* src, bool with_norm) {
     if constexpr (sizeof(T) == 8) {
-      AERO_CK(cudaMemcpyAsync(lam_n_, lam_, sizeof(d4) * ntot_, cudaMemcpyDeviceToDevice, st_));
+      AERO_CK(cudaMemcpyAsync(zn, z, sizeof(d4) * ntot_, cudaMemcpyDeviceToDevice, st_));
       for (int stage = 0; stage < 3; ++stage) {
-        apply_vjp(lam_, adj_r_);
-        k_adj_stage<<<ncb_, block_, 0, st_>>>(cblk_, stage, cfl, SRlin_, adj_r_, adj_g_, lam_n_, lam_,
-                                              stage == 0 ? adj_rn_ : nullptr);
-        if (stage == 0) k_adj_norm<<<1, 256, 0, st_>>>(adj_rn_, ncb_, pk_[0].n, adj_hist_, adj_counter_, kAdjHist);
+        apply_vjp(z, adj_r_);
+        const bool nrm = with_norm && stage == 0;
+        k_adj_stage<<<ncb_, block_, 0, st_>>>(cblk_, stage, cfl, SRlin_, adj_r_, src, zn, z, nrm ? adj_rn_ : nullptr);
+        if (nrm) k_adj_norm<<<1, 256, 0, st_>>>(adj_rn_, ncb_, pk_[0].n, adj_hist_, adj_counter_, kAdjHist);
       }
     }
   }
+  void adjoint_iteration(double cfl) { adjoint_iteration(cfl, lam_, lam_n_, adj_g_, true); }
+
+  // ---- restarted GMRES on (dR/dU)^T lam = -dJ/dU, right-preconditioned by `smooth`
+  // iterations of the RK3 smoother from zero (a fixed linear operator P). The smoother alone
+  // diverges where the primal's own iteration has not settled (limit cycles of the limiters
+  // leave a few growing modes); the Krylov outer iteration removes them.
+  int vlen() const { return pk_[0].n; }
+  int vgrid() const { return (vlen() + 255) / 256; }
+
+  // host copies of V_r . w for r < rows (two-stage deterministic reduction)
+  void vdots(const d4* V, int rows, const d4* w, double* out) {
+    const int nb = vgrid();
+    k_vdot_rows<<<dim3(nb, rows), 256, 0, st_>>>(V, static_cast<size_t>(ntot_), w, vlen(), kr_part_);
+    k_rows_sum<<<rows, 256, 0, st_>>>(kr_part_, nb, kr_out_);
+    AERO_CK(cudaMemcpyAsync(out, kr_out_, sizeof(double) * rows, cudaMemcpyDeviceToHost, st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+  }
+  double vnorm(const d4* w) {
+    double s = 0.0;
+    vdots(w, 1, w, &s);
+    return std::sqrt(s);
+  }
+  // w = alpha w + sum coef[r] V_r
+  void vcombine(d4* w, double alpha, const d4* V, const double* coef, int rows) {
+    AERO_CK(cudaMemcpyAsync(kr_coef_, coef, sizeof(double) * rows, cudaMemcpyHostToDevice, st_));
+    k_vcombine<<<vgrid(), 256, 0, st_>>>(w, alpha, V, static_cast<size_t>(ntot_), kr_coef_, rows, vlen());
+  }
+  // z = P x: `smooth` smoother iterations on (dR/dU)^T z = x from z = 0, as one graph
+  // (smooth = 0: P = identity)
+  void precondition(const d4* x, double cfl, int smooth) {
+    if (smooth == 0) {
+      k_vaxpby<<<vgrid(), 256, 0, st_>>>(1.0, x, 0.0, kr_z_, vlen());
+      return;
+    }
+    if (kr_graph_ && (kr_graph_cfl_ != cfl || kr_graph_smooth_ != smooth)) {
+      cudaGraphExecDestroy(kr_graph_);
+      kr_graph_ = nullptr;
+    }
+    k_vaxpby<<<vgrid(), 256, 0, st_>>>(-1.0, x, 0.0, kr_src_, vlen());
+    if (!kr_graph_) {
+      cudaGraph_t g = nullptr;
+      AERO_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+      AERO_CK(cudaMemsetAsync(kr_z_, 0, sizeof(d4) * ntot_, st_));
+      for (int i = 0; i < smooth; ++i) adjoint_iteration(cfl, kr_z_, kr_zn_, kr_src_, false);
+      AERO_CK(cudaStreamEndCapture(st_, &g));
+      if (g) {
+        AERO_CK(cudaGraphInstantiate(&kr_graph_, g, 0));
+        cudaGraphDestroy(g);
+      }
+      kr_graph_cfl_ = cfl;
+      kr_graph_smooth_ = smooth;
+    }
+    if (kr_graph_) AERO_CK(cudaGraphLaunch(kr_graph_, st_));
+  }
+
+ public:
+  int adjoint_set_lambda(const double* lam) override {
+    if constexpr (sizeof(T) != 8) {
+      return AERO_ERR_INVALID;
+    } else {
+      if (!adj_ready_) return AERO_ERR_INVALID;
+      upload_cells(lam, lam_);
+      return err_ == cudaSuccess ? AERO_OK : AERO_ERR_CUDA;
+    }
+  }
+
+  int adjoint_solve_krylov(int max_iters, int restart, int smooth, double cfl, double rtol, double* history,
+                           int* done_out) override {
+    if constexpr (sizeof(T) != 8) {
+      return AERO_ERR_INVALID;
+    } else {
+      if (!adj_ready_ || max_iters < 0 || restart < 1 || restart > 512 || smooth < 0 || !(cfl > 0.0) ||
+          !(rtol >= 0.0))
+        return AERO_ERR_INVALID;
+      const int m = restart;
+      if (kr_m_ < m) {  // Krylov basis and work vectors (kept for later solves)
+        kr_V_ = alloc<d4>(static_cast<size_t>(m + 1) * ntot_);
+        kr_m_ = m;
+        if (!kr_w_) {
+          kr_w_ = alloc<d4>(ntot_);
+          kr_z_ = alloc<d4>(ntot_);
+          kr_zn_ = alloc<d4>(ntot_);
+          kr_src_ = alloc<d4>(ntot_);
+        }
+        kr_part_ = alloc<double>(static_cast<size_t>(m + 1) * vgrid());
+        kr_out_ = alloc<double>(m + 1);
+        kr_coef_ = alloc<double>(m + 1);
+        if (kr_graph_) {
+          cudaGraphExecDestroy(kr_graph_);
+          kr_graph_ = nullptr;
+        }
+        if (err_ != cudaSuccess) return AERO_ERR_NOMEM;
+      }
+      auto Vr = [&](int r) { return kr_V_ + static_cast<size_t>(r) * ntot_; };
+      // b = -g
+      k_vaxpby<<<vgrid(), 256, 0, st_>>>(-1.0, adj_g_, 0.0, kr_w_, vlen());
+      const double bnorm = vnorm(kr_w_);
+      int done = 0;
+      std::vector<double> H(static_cast<size_t>(m + 1) * m), cs(m), sn(m), gv(m + 1), h(m + 1), h2(m + 1), y(m);
+      while (err_ == cudaSuccess) {
+        // r = b - A^T lam
+        apply_vjp(lam_, kr_w_);
+        k_vaxpby<<<vgrid(), 256, 0, st_>>>(-1.0, adj_g_, -1.0, kr_w_, vlen());
+        const double beta = vnorm(kr_w_);
+        if (!(beta > rtol * bnorm) || done >= max_iters || !std::isfinite(beta)) {
+          if (history && done < max_iters && done == 0) history[0] = bnorm > 0.0 ? beta / bnorm : 0.0;
+          break;
+        }
+        k_vaxpby<<<vgrid(), 256, 0, st_>>>(1.0 / beta, kr_w_, 0.0, Vr(0), vlen());
+        std::fill(gv.begin(), gv.end(), 0.0);
+        gv[0] = beta;
+        int j = 0;
+        bool stop = false;
+        for (; j < m && done < max_iters; ++j) {
+          precondition(Vr(j), cfl, smooth);
+          apply_vjp(kr_z_, kr_w_);
+          // classical Gram-Schmidt, twice
+          vdots(Vr(0), j + 1, kr_w_, h.data());
+          for (int i = 0; i <= j; ++i) h2[i] = -h[i];
+          vcombine(kr_w_, 1.0, Vr(0), h2.data(), j + 1);
+          vdots(Vr(0), j + 1, kr_w_, h2.data());
+          for (int i = 0; i <= j; ++i) {
+            h[i] += h2[i];
+            h2[i] = -h2[i];
+          }
+          vcombine(kr_w_, 1.0, Vr(0), h2.data(), j + 1);
+          const double hn = vnorm(kr_w_);
+          if (hn > 0.0) k_vaxpby<<<vgrid(), 256, 0, st_>>>(1.0 / hn, kr_w_, 0.0, Vr(j + 1), vlen());
+          // Givens rotations on column j
+          for (int i = 0; i < j; ++i) {
+            const double t = cs[i] * h[i] + sn[i] * h[i + 1];
+            h[i + 1] = -sn[i] * h[i] + cs[i] * h[i + 1];
+            h[i] = t;
+          }
+          const double den = std::hypot(h[j], hn);
+          cs[j] = den > 0.0 ? h[j] / den : 1.0;
+          sn[j] = den > 0.0 ? hn / den : 0.0;
+          h[j] = den;
+          gv[j + 1] = -sn[j] * gv[j];
+          gv[j] = cs[j] * gv[j];
+          for (int i = 0; i <= j; ++i) H[static_cast<size_t>(i) * m + j] = h[i];
+          const double res = std::fabs(gv[j + 1]);
+          if (history) history[done] = bnorm > 0.0 ? res / bnorm : 0.0;
+          ++done;
+          if (!(res > rtol * bnorm) || !(hn > 0.0) || !std::isfinite(res)) {
+            ++j;
+            stop = true;
+            break;
+          }
+        }
+        // lam += P (V y), y = R^-1 g
+        for (int i = j - 1; i >= 0; --i) {
+          double s = gv[i];
+          for (int k = i + 1; k < j; ++k) s -= H[static_cast<size_t>(i) * m + k] * y[k];
+          y[i] = s / H[static_cast<size_t>(i) * m + i];
+        }
+        if (j > 0) {
+          AERO_CK(cudaMemsetAsync(kr_w_, 0, sizeof(d4) * ntot_, st_));
+          vcombine(kr_w_, 1.0, Vr(0), y.data(), j);
+          precondition(kr_w_, cfl, smooth);
+          k_vaxpby<<<vgrid(), 256, 0, st_>>>(1.0, kr_z_, 1.0, lam_, vlen());
+        }
+        AERO_CK(cudaGetLastError());
+        if (stop && done >= max_iters) break;
+        if (done >= max_iters) break;
+      }
+      AERO_CK(cudaStreamSynchronize(st_));
+      if (done_out) *done_out = done;
+      return err_ == cudaSuccess ? AERO_OK : AERO_ERR_CUDA;
+    }
+  }
+
+ private:
 
   // out = (dR/dU)^T v on device arrays
   void apply_vjp(const d4* v, d4* out) {
     if constexpr (sizeof(T) == 8) {
-      k_adj_face_vjp<<<nfb_, block_, 0, st_>>>(df_, fblk_, Jf_, v, adj_face_);
-      k_adj_gather<<<ncb_, block_, 0, st_>>>(dg_, cblk_, adj_face_, mw_, mgx_, mgy_);
-      if (adj_second_) k_adj_green_gauss<<<ncb_, block_, 0, st_>>>(dm_, cblk_, mgx_, mgy_, mw_);
+      if (adj_second_) {
+        k_adj_face_vjp<kJac><<<nfb_, block_, 0, st_>>>(df_, fblk_, Jf_, v, adj_face_);
+        k_adj_gather<kJac><<<ncb_, block_, 0, st_>>>(dg_, cblk_, adj_face_, mw_, mgx_, mgy_);
+        k_adj_green_gauss<<<ncb_, block_, 0, st_>>>(dm_, cblk_, mgx_, mgy_, mw_);
+      } else {
+        k_adj_face_vjp<8><<<nfb_, block_, 0, st_>>>(df_, fblk_, Jf_, v, adj_face_);
+        k_adj_gather<8><<<ncb_, block_, 0, st_>>>(dg_, cblk_, adj_face_, mw_, mgx_, mgy_);
+      }
       k_adj_prim<<<ncb_, block_, 0, st_>>>(cblk_, Ulin_, rs_[0].gamma, mw_, out);
     }
   }
@@ -1528,6 +1713,13 @@ class EngineT final : public Engine {
   int* adj_counter_ = nullptr;
   cudaGraphExec_t adj_graph_ = nullptr;
   double adj_graph_cfl_ = 0.0;
+  // Krylov solve: basis (kr_m_ + 1 vectors of ntot cells), work vectors, reductions
+  int kr_m_ = 0;
+  d4 *kr_V_ = nullptr, *kr_w_ = nullptr, *kr_z_ = nullptr, *kr_zn_ = nullptr, *kr_src_ = nullptr;
+  double *kr_part_ = nullptr, *kr_out_ = nullptr, *kr_coef_ = nullptr;
+  cudaGraphExec_t kr_graph_ = nullptr;
+  double kr_graph_cfl_ = 0.0;
+  int kr_graph_smooth_ = -1;
   Ctrl* ctrl_lin_ = nullptr;
   d4 *Ulin_ = nullptr, *Wlin_ = nullptr;  // state and primitives at the linearisation point
   double* SRlin_ = nullptr;               // its spectral radii (the adjoint's local steps)

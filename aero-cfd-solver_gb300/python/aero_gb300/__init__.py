@@ -104,6 +104,9 @@ def load(build_if_missing: bool = False):
         "aero_adjoint_objective_gradient": (C.c_int, [C.c_void_p, _dp]),
         "aero_adjoint_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_double, _dp]),
         "aero_adjoint_get_lambda": (C.c_int, [C.c_void_p, _dp]),
+        "aero_adjoint_set_lambda": (C.c_int, [C.c_void_p, _dp]),
+        "aero_adjoint_solve_krylov": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, _dp,
+                                                _ip]),
         "aero_adjoint_dalpha": (C.c_int, [C.c_void_p, _dp]),
         "aero_adjoint_geometry": (C.c_int, [C.c_void_p, C.POINTER(MeshDesc), _dp]),
     }
@@ -391,6 +394,21 @@ class Solver:
         hist = np.empty(max(iters, 1), np.float64)
         self._check(self.lib.aero_adjoint_solve(self.h, int(iters), float(cfl), hist.ctypes.data_as(_dp)))
         return hist[:iters]
+
+    def adjoint_solve_krylov(self, max_iters: int = 2000, restart: int = 40, smooth: int = 10, cfl: float = 0.8,
+                             rtol: float = 1e-10) -> np.ndarray:
+        """Restarted GMRES on the adjoint system, preconditioned by `smooth` smoother
+        iterations; returns the relative residual estimate per Arnoldi step."""
+        hist = np.empty(max(max_iters, 1), np.float64)
+        done = C.c_int(0)
+        self._check(self.lib.aero_adjoint_solve_krylov(self.h, int(max_iters), int(restart), int(smooth), float(cfl),
+                                                       float(rtol), hist.ctypes.data_as(_dp), C.byref(done)))
+        return hist[: done.value]
+
+    def adjoint_set_lambda(self, lam: np.ndarray):
+        lam = np.ascontiguousarray(lam, dtype=np.float64).reshape(-1)
+        assert lam.size == 5 * self.n
+        self._check(self.lib.aero_adjoint_set_lambda(self.h, lam.ctypes.data_as(_dp)))
 
     def adjoint_lambda(self) -> np.ndarray:
         lam = np.empty(5 * self.n, np.float64)

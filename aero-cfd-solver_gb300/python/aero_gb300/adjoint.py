@@ -63,9 +63,12 @@ class ShapeProblem:
     max_iters: int = 200000
     rho_target: float = 1e-12
     chunk: int = 5000
-    adjoint_max_iters: int = 200000
+    adjoint_max_iters: int = 4000
     adjoint_tol: float = 1e-10
     adjoint_cfl: float | None = None
+    adjoint_method: str = "krylov"  # or "smoother" (the RK3 pseudo-time iteration alone)
+    krylov_restart: int = 40
+    krylov_smooth: int = 10
     primal_precision: int = capi.PRECISION_FP64
     modes: np.ndarray = field(init=False)
     last_adjoint_seconds: float = field(init=False, default=0.0)
@@ -123,15 +126,20 @@ class ShapeProblem:
         t0 = time.perf_counter()
         s.adjoint_linearize(w_cd, w_cl, 1 if self.case.startup_first_order_iters < primal.iterations else -1)
         first, done, ratio = None, 0, 1.0
-        while done < self.adjoint_max_iters:
-            n = min(self.chunk, self.adjoint_max_iters - done)
-            h = s.adjoint_solve(n, cfl)
-            done += n
-            if first is None:
-                first = h[0] if h[0] > 0 else 1.0
-            ratio = h[-1] / first
-            if not np.isfinite(ratio) or ratio < self.adjoint_tol:
-                break
+        if self.adjoint_method == "krylov":
+            h = s.adjoint_solve_krylov(self.adjoint_max_iters, self.krylov_restart, self.krylov_smooth, cfl,
+                                       self.adjoint_tol)
+            done, ratio = h.size, (float(h[-1]) if h.size else 0.0)
+        else:
+            while done < self.adjoint_max_iters:
+                n = min(self.chunk, self.adjoint_max_iters - done)
+                h = s.adjoint_solve(n, cfl)
+                done += n
+                if first is None:
+                    first = h[0] if h[0] > 0 else 1.0
+                ratio = h[-1] / first
+                if not np.isfinite(ratio) or ratio < self.adjoint_tol:
+                    break
         dalpha = s.adjoint_dalpha()
         da = np.empty(self.peaks.size)
         for k in range(self.peaks.size):

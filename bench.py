@@ -307,6 +307,113 @@ def c4_sweep(args, aero_gb300, capi, rank):
     return ms, int(cells), int(launches)
 
 
+def c3_low_mach(args, aero_gb300, capi, peak):
+    """Low-Mach precision case on the 1024x256 triangulated O-grid (524,288 cells, jittered,
+    permuted): preconditioning, low-Mach fix and all-speed flux fix on, characteristic far
+    field, HLLC + minmod, M=0.05, alpha=3. Throughput of FP32 and FP64 (L2 flushed before each
+    timed iteration), the face pass's roofline at this size (its working set no longer fits in
+    L2), and |dCL|, |dCD|, max |dCp| at the wall between FP32 and FP64 after 400 iterations from
+    free stream."""
+    mesh = aero_gb300.ogrid_synthetic(1024, 256, cell_type=3, permute=True, jitter=0.1, seed=3)
+    wall = mesh.wall_faces
+    mach = 0.05
+    res = {}
+    for prec, code in (("fp32", capi.PRECISION_FP32), ("fp64", capi.PRECISION_FP64)):
+        case = capi.make_case(mach=mach, aoa_deg=3.0, flux=capi.FLUX_HLLC, limiter=capi.LIMITER_MINMOD, precond_on=1,
+                              low_mach_fix=1, all_speed_flux_fix=1, precond_farfield_bc=1, iterations=100000,
+                              min_iterations=100000, cfl_start=0.2, cfl_max=0.8, cfl_ramp_iters=120,
+                              startup_first_order_iters=25, precision=code)
+        with aero_gb300.Solver(mesh, case) as s:
+            info = s.info()
+            _, rec = s.run(400)
+            s.time_iterations(args.warmup, use_graph=True, flush_l2=True)
+            ms = s.time_iterations(args.steps, use_graph=True, flush_l2=not args.no_flush)
+            prof = s.profile_kernels(max(2, min(args.steps, 10)), flush_l2=not args.no_flush)
+            p = s.get_primitive()[3]
+        f_ms, f_n = prof["face_pass"]
+        avg = f_ms / max(f_n, 1)
+        nbytes = algorithmic_bytes("face", mesh.num_cells, info["slots_per_cell"], prec, int(info["faces"]))
+        res[prec] = dict(mcell=mesh.num_cells * args.steps / (ms / 1e3) / 1e6, cl=float(rec["cl"][-1]),
+                         cd=float(rec["cd"][-1]), pw=p[mesh.owner[wall]], face_ms=avg, face_gbs=nbytes / (avg / 1e3) / 1e9,
+                         kernels={k: (v[0] / v[1] if v[1] else 0.0) for k, v in prof.items()})
+    q = 0.5 * 1.4 * 101325.0 * mach * mach
+    return {"cells": mesh.num_cells, "mach": mach, "fp32_mcell_iter_s": res["fp32"]["mcell"],
+            "fp64_mcell_iter_s": res["fp64"]["mcell"], "fp32_over_fp64": res["fp32"]["mcell"] / res["fp64"]["mcell"],
+            "abs_dcl_400": abs(res["fp32"]["cl"] - res["fp64"]["cl"]),
+            "abs_dcd_400": abs(res["fp32"]["cd"] - res["fp64"]["cd"]),
+            "max_abs_dcp_wall_400": float(np.max(np.abs(res["fp32"]["pw"] - res["fp64"]["pw"])) / q),
+            "roofline_face_pass_fp32": {"achieved": res["fp32"]["face_gbs"], "peak": peak, "unit": "GB/s",
+                                        "frac": res["fp32"]["face_gbs"] / peak, "avg_launch_ms": res["fp32"]["face_ms"]},
+            "roofline_face_pass_fp64": {"achieved": res["fp64"]["face_gbs"], "frac": res["fp64"]["face_gbs"] / peak,
+                                        "avg_launch_ms": res["fp64"]["face_ms"]},
+            "kernel_ms_per_launch_fp32": res["fp32"]["kernels"]}
+
+
+def c5_adjoint(args, aero_gb300, capi):
+    """Adjoint gradient case: triangulated 512x128 O-grid, M=0.75, alpha=2, HLLC, 16 Hicks-Henne
+    bumps (8 upper, 8 lower, peaks ~U[0.05, 0.95], width exponent 3, amplitudes ~N(0, 1e-3 c),
+    seeded) with inverse-distance-weighted volume deformation; J = CD. The scheme is first
+    order throughout: with the reference's second-order limiters the primal stalls at a
+    density-residual ratio near 1e-3 and has no steady state to differentiate.
+    Primal: FP64 pseudo-time iterations to a density-residual ratio of 1e-8 (and an FP32
+    primal to 1e-6 whose state seeds an FP64 adjoint). Adjoint: linearisation, the same RK3
+    smoother to a residual reduction of 1e-8, dJ/dalpha and the 16 shape products. Wall-clock
+    seconds of each, the primal's host loop included. --c5-fd adds central differences (step
+    1e-6 in alpha [deg] and in two amplitudes) of converged primal solutions (ratio 1e-13) on
+    the 128x32 grid of the same family, against the adjoint there."""
+    from aero_gb300.adjoint import ShapeProblem
+
+    rng = np.random.default_rng(5)
+    peaks = rng.uniform(0.05, 0.95, 16)
+    upper = np.array([1] * 8 + [0] * 8)
+    amps = rng.normal(0.0, 1e-3, 16)
+    kw = dict(CASE)
+    kw.update(mach=0.75, aoa_deg=2.0, startup_first_order_iters=10 ** 9)
+    case = capi.make_case(**kw, precision=capi.PRECISION_FP64)
+
+    def problem(mesh, rho, adj_tol, prec=capi.PRECISION_FP64):
+        return ShapeProblem(mesh, case, peaks=peaks, upper=upper, width=3.0, max_iters=400000, rho_target=rho,
+                            chunk=20000, adjoint_max_iters=800000, adjoint_tol=adj_tol, adjoint_method="smoother",
+                            primal_precision=prec)
+
+    mesh = aero_gb300.ogrid_synthetic(512, 128, cell_type=3, permute=True, jitter=0.1, seed=55)
+    prob = problem(mesh, 1e-8, 1e-8)
+    base = prob.solve(amps, 2.0)
+    da, dal = prob.gradient(base, 1.0, 0.0)
+    out = {"cells": mesh.num_cells, "primal_fp64_s": base.seconds, "primal_iters": base.iterations,
+           "primal_rho_ratio": base.rho_ratio, "cd": base.cd, "cl": base.cl,
+           "adjoint_s": prob.last_adjoint_seconds, "adjoint_iters": prob.last_adjoint_iterations,
+           "adjoint_residual_ratio": prob.last_adjoint_ratio,
+           "adjoint_over_primal": prob.last_adjoint_seconds / base.seconds,
+           "dcd_dalpha_per_deg": dal, "dcd_damp": [float(x) for x in da]}
+    base.solver.close()
+    prob32 = problem(mesh, 1e-6, 1e-8, capi.PRECISION_FP32)
+    b32 = prob32.solve(amps, 2.0)
+    da32, dal32 = prob32.gradient(b32, 1.0, 0.0)
+    out.update({"primal_fp32_s": b32.seconds, "primal_fp32_iters": b32.iterations,
+                "primal_fp32_rho_ratio": b32.rho_ratio, "adjoint_after_fp32_s": prob32.last_adjoint_seconds,
+                "fp32_primal_gradient_rel_diff": float(np.linalg.norm(np.append(da32, dal32) - np.append(da, dal)) /
+                                                       np.linalg.norm(np.append(da, dal)))})
+    b32.solver.close()
+    if args.c5_fd:
+        small = aero_gb300.ogrid_synthetic(128, 32, cell_type=3, permute=True, jitter=0.1, seed=55)
+        pf = problem(small, 1e-13, 1e-12)
+        b = pf.solve(amps, 2.0)
+        sda, sdal = pf.gradient(b, 1.0, 0.0)
+        fd = {"cells": small.num_cells, "primal_rho_ratio": b.rho_ratio, "adjoint_residual_ratio": pf.last_adjoint_ratio}
+        b.solver.close()
+        h = 1e-6
+        for name, e, al in [("alpha", np.zeros(16), h)] + [(f"a{k}", np.eye(16)[k] * h, 0.0) for k in (0, 8)]:
+            p, m = pf.solve(amps + e, 2.0 + al), pf.solve(amps - e, 2.0 - al)
+            fdv = (p.cd - m.cd) / (2 * h)
+            adj = sdal if name == "alpha" else float(sda[int(name[1:])])
+            fd[name] = {"adjoint": adj, "central_fd": fdv, "rel_err": abs(adj - fdv) / abs(fdv)}
+            p.solver.close()
+            m.solver.close()
+        out["fd_check_128x32_step_1e-6"] = fd
+    return out
+
+
 # ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
@@ -399,6 +506,9 @@ def run_gpu_arm(args):
                         "O-grids, alpha~U[-4,8], M~U[0.3,0.85], HLLC+MUSCL venkat, CFL ramp to 0.8, "
                         "density-residual stop mask 1e-8; one batched context, L2 flushed per step"}
 
+    c3 = c3_low_mach(args, aero_gb300, capi, peak) if not args.no_c3 and rank == 0 else None
+    c5 = c5_adjoint(args, aero_gb300, capi) if (args.c5 or args.c5_fd) and rank == 0 else None
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu and head["state"] is not None:
         cpu = cpu_sample(mesh, head["state"])
@@ -426,6 +536,8 @@ def run_gpu_arm(args):
             "fp64_l2_warm_mcell_iter_s": world * n * args.steps / (r64["warm_ms"] / 1e3) / 1e6 if r64 else None,
             "dcl": dcl,
             "c4_batched_sweep": c4,
+            "c3_low_mach": c3,
+            "c5_adjoint": c5,
             "kernel_profile_ms_per_launch": {k: (v[0] / v[1] if v[1] else 0.0) for k, v in head["prof"].items()},
             "state_finite": head["finite"],
         },
@@ -459,6 +571,9 @@ def main():
     ap.add_argument("--no-clocks", action="store_true")
     ap.add_argument("--no-c4", action="store_true", help="skip the 96-case batched sweep measurement")
     ap.add_argument("--cpu-procs", type=int, default=0, help="processes of the reference arm (0: all cores)")
+    ap.add_argument("--no-c3", action="store_true", help="skip the 524k-cell low-Mach measurement")
+    ap.add_argument("--c5", action="store_true", help="also time the adjoint gradient case (primal + adjoint)")
+    ap.add_argument("--c5-fd", action="store_true", help="--c5 plus central differences for alpha and two bumps")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -41,8 +41,20 @@ AERO_API int aero_adjoint_objective_gradient(aero_ctx* ctx, double* g);
  * cells of (dR/dU)^T lam + dJ/dU before the iteration. Continues from the current lam. */
 AERO_API int aero_adjoint_solve(aero_ctx* ctx, int iters, double cfl, double* history);
 
-/* Current adjoint state lam. */
+/* Restarted GMRES(restart) on (dR/dU)^T lam = -dJ/dU from the current lam, right-
+ * preconditioned by smooth_iters iterations of the smoother above from zero (0: no
+ * preconditioner). Needed where the smoother alone diverges: a primal that stalls in a
+ * limiter limit cycle leaves a few growing modes in the linearisation. Stops when the
+ * residual estimate falls to rel_tol * |dJ/dU| or after max_iters Arnoldi steps.
+ * history (may be NULL, max_iters entries): residual estimate / |dJ/dU| per step;
+ * iters_done (may be NULL): steps taken. */
+AERO_API int aero_adjoint_solve_krylov(aero_ctx* ctx, int max_iters, int restart, int smooth_iters,
+                                       double cfl, double rel_tol, double* history, int* iters_done);
+
+/* Current adjoint state lam; set it (a warm start, or a given lam for the dalpha and
+ * geometry products). */
 AERO_API int aero_adjoint_get_lambda(aero_ctx* ctx, double* lam);
+AERO_API int aero_adjoint_set_lambda(aero_ctx* ctx, const double* lam);
 
 /* dJ/d(alpha) per degree with the current lam: the force-rotation term plus lam^T dR/dalpha
  * through the far-field state. */

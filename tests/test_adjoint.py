@@ -135,26 +135,31 @@ def test_adjoint_refuses_fp32_and_unlinearised_contexts():
             s.adjoint_vjp(np.zeros((mesh.num_cells, 5)))
 
 
-def _problem(flux, limiter, mach=0.5, nc=64, nr=16):
+def _problem(flux, limiter, mach=0.5, nc=64, nr=16, first_order=False):
     mesh = _mesh(nc, nr, seed=11)
-    case = capi.make_case(mach=mach, aoa_deg=2.0, flux=flux, limiter=limiter, startup_first_order_iters=20,
-                          cfl_max=0.8, precision=capi.PRECISION_FP64)
+    case = capi.make_case(mach=mach, aoa_deg=2.0, flux=flux, limiter=limiter,
+                          startup_first_order_iters=10 ** 9 if first_order else 20, cfl_max=0.8,
+                          precision=capi.PRECISION_FP64)
     return ShapeProblem(mesh, case, peaks=[0.3, 0.6], upper=[1, 0], width=3.0, max_iters=60000, rho_target=1e-13,
-                        adjoint_max_iters=60000, adjoint_tol=1e-12)
+                        adjoint_max_iters=3000, adjoint_tol=1e-12)
 
 
-@pytest.mark.parametrize("scheme", ["rusanov_first", "hllc_venkat"])
-def test_gradients_against_converged_differences(scheme):
-    sc = SCHEMES[scheme]
-    prob = _problem(sc["flux"], sc["limiter"])
-    if not sc["second"]:
-        prob.case.startup_first_order_iters = 10 ** 9  # first order throughout
+def test_gradients_against_converged_differences():
+    """End to end on a scheme whose primal converges to round-off (first-order Rusanov; the
+    reference's second-order limiters stall the primal at density-residual ratios of 1e-3 on
+    these meshes, so converged differences of second-order solutions do not exist)."""
+    prob = _problem(capi.FLUX_RUSANOV, capi.LIMITER_MINMOD, first_order=True)
     a0 = np.zeros(2)
     base = prob.solve(a0, 2.0)
     assert base.rho_ratio <= 1e-13, base.rho_ratio
     da_cd, dal_cd = prob.gradient(base, 1.0, 0.0)
     assert prob.last_adjoint_ratio <= 1e-12
     da_cl, dal_cl = prob.gradient(base, 0.0, 1.0)
+    prob.adjoint_method = "smoother"  # the plain RK3 iteration converges here too
+    prob.adjoint_max_iters = 60000
+    da_cd2, dal_cd2 = prob.gradient(base, 1.0, 0.0)
+    np.testing.assert_allclose(da_cd2, da_cd, rtol=1e-7)
+    assert abs(dal_cd2 - dal_cd) <= 1e-7 * abs(dal_cd)
 
     h_al = 1e-3
     p, m = prob.solve(a0, 2.0 + h_al), prob.solve(a0, 2.0 - h_al)
@@ -172,11 +177,102 @@ def test_gradients_against_converged_differences(scheme):
         assert abs(da_cl[k] - fd_cl) <= 1e-4 * abs(fd_cl) + 1e-7, (k, da_cl[k], fd_cl)
 
 
+def test_krylov_matches_the_smoother_and_satisfies_the_adjoint_equation():
+    """GMRES (preconditioned by smoother sweeps) and the plain RK3 smoother reach the same
+    lam on a converged first-order state, and lam satisfies (dR/dU)^T lam + dJ/dU = 0
+    through the independent transpose-product call."""
+    mesh = _mesh(64, 16, seed=11)
+    case = capi.make_case(mach=0.5, aoa_deg=2.0, flux=capi.FLUX_RUSANOV, startup_first_order_iters=10 ** 9,
+                          cfl_max=0.8, iterations=100000)
+    with aero_gb300.Solver(mesh, case) as s:
+        s.run(60000)
+        s.adjoint_linearize(1.0, 0.0, 0)
+        h = s.adjoint_solve_krylov(max_iters=2000, restart=40, smooth=10, cfl=0.8, rtol=1e-11)
+        assert h.size < 2000 and h[-1] <= 1e-11, (h.size, h[-1])
+        lam_k = s.adjoint_lambda()
+        g = s.adjoint_objective_gradient()
+        r = s.adjoint_vjp(lam_k) + g
+        assert np.linalg.norm(r) <= 1e-10 * np.linalg.norm(g)
+        s.adjoint_set_lambda(np.zeros_like(lam_k))
+        hs = s.adjoint_solve(40000, 0.8)
+        assert hs[-1] <= 1e-9 * hs[0]
+        lam_s = s.adjoint_lambda()
+        assert np.linalg.norm(lam_s - lam_k) <= 1e-7 * np.linalg.norm(lam_k)
+
+
+def _wall_force(mesh, u, gamma, p_inf):
+    r = np.maximum(u[:, 0], 1e-8)
+    p = np.maximum((gamma - 1) * (u[:, 4] - 0.5 * (u[:, 1] ** 2 + u[:, 2] ** 2) / r), 1e-8)
+    f = mesh.wall_faces
+    n = mesh.normal.reshape(-1, 3)[f]
+    dp = p[mesh.owner[f]] - p_inf
+    return np.sum(dp * n[:, 0] * mesh.area[f]), np.sum(dp * n[:, 1] * mesh.area[f])
+
+
+@pytest.mark.parametrize("scheme", ["hllc_venkat", "rusanov_first"])
+def test_parameter_partials_against_residual_differences(scheme):
+    """lam^T dR/dalpha and lam^T dR/dX . m_k for a random lam, and the explicit force terms
+    (lam = 0), against central differences of the residual and of the wall force at a fixed
+    state: far-field state at alpha +- h, and meshes deformed by +- h m_k."""
+    sc = SCHEMES[scheme]
+    mesh = _mesh(48, 12, seed=9)
+    mk = dict(mach=0.6, flux=sc["flux"], limiter=sc["limiter"], startup_first_order_iters=5, cfl_max=0.8,
+              iterations=100000)
+    case = capi.make_case(aoa_deg=2.0, **mk)
+    modes = aero_gb300.hicks_henne_modes(mesh, [0.35, 0.7], [1, 0], 3.0)
+    pts = mesh.points.reshape(-1, 3)
+    second = bool(sc["second"])
+    with aero_gb300.Solver(mesh, case) as s:
+        _, recs = s.run(200)
+        rng = np.random.default_rng(3)
+        u = s.get_state() * (1.0 + 0.02 * rng.standard_normal((mesh.num_cells, 5)))
+        u[:, 3] = 0.0
+        s.set_state(u)
+        s.adjoint_linearize(0.4, 0.6, sc["second"])
+        lam = rng.standard_normal((mesh.num_cells, 5))
+        lam[:, 3] = 0.0
+        s.adjoint_set_lambda(np.zeros_like(lam))
+        d0 = s.adjoint_dalpha()
+        g0 = [s.adjoint_geometry(aero_gb300.geometry_tangent(mesh, modes[k])) for k in range(2)]
+        s.adjoint_set_lambda(lam)
+        d1 = s.adjoint_dalpha()
+        g1 = [s.adjoint_geometry(aero_gb300.geometry_tangent(mesh, modes[k])) for k in range(2)]
+    qs = recs[-1]["drag"] / recs[-1]["cd"]
+    gamma, p_inf = case.gamma, case.p_inf
+
+    def J(m, alpha):
+        fx, fy = _wall_force(m, u, gamma, p_inf)
+        a = np.deg2rad(alpha)
+        return (0.4 * (fx * np.cos(a) + fy * np.sin(a)) + 0.6 * (-fx * np.sin(a) + fy * np.cos(a))) / qs
+
+    def R(m, alpha):
+        c = capi.make_case(**mk)
+        c.aoa_deg = alpha  # exact, not rounded to float like a case-file value
+        with aero_gb300.Solver(m, c) as t:
+            return t.residual(u, second_order=second)[0]
+
+    # incidence (per degree); the far-field state is the only residual input that moves
+    h = 1e-4
+    fd_exp = (J(mesh, 2.0 + h) - J(mesh, 2.0 - h)) / (2 * h)
+    assert abs(d0 - fd_exp) <= 1e-7 * abs(fd_exp), (d0, fd_exp)
+    fd_lam = np.sum(lam * (R(mesh, 2.0 + h) - R(mesh, 2.0 - h))) / (2 * h)
+    assert abs((d1 - d0) - fd_lam) <= 1e-6 * abs(fd_lam), (d1 - d0, fd_lam)
+    # shape modes (case aoa is the float-rounded 2.0 for both meshes)
+    hx = 1e-6
+    for k in range(2):
+        mp = aero_gb300.deform(mesh, pts + hx * modes[k])
+        mm = aero_gb300.deform(mesh, pts - hx * modes[k])
+        fd_exp = (J(mp, 2.0) - J(mm, 2.0)) / (2 * hx)
+        assert abs(g0[k] - fd_exp) <= 1e-6 * abs(fd_exp) + 1e-9, (k, g0[k], fd_exp)
+        fd_lam = np.sum(lam * (R(mp, 2.0) - R(mm, 2.0))) / (2 * hx)
+        assert abs((g1[k] - g0[k]) - fd_lam) <= 1e-5 * abs(fd_lam), (k, g1[k] - g0[k], fd_lam)
+
+
 def test_autograd_function_returns_the_adjoint_gradient():
     torch = pytest.importorskip("torch")
     from aero_gb300.adjoint import AirfoilForces
 
-    prob = _problem(capi.FLUX_RUSANOV, capi.LIMITER_MINMOD, nc=48, nr=12)
+    prob = _problem(capi.FLUX_RUSANOV, capi.LIMITER_MINMOD, nc=48, nr=12, first_order=True)
     a = torch.zeros(2, dtype=torch.float64, requires_grad=True)
     alpha = torch.tensor(2.0, dtype=torch.float64, requires_grad=True)
     out = AirfoilForces.apply(a, alpha, prob)

@@ -98,6 +98,7 @@ struct PrecondD {
   int enabled;
   double gamma, mach_ref, mach_min, beta_min, beta_max;
   float gamma_f, gm1_f;  // float(gamma), float(gamma - 1)
+  float mach_ref_f, mach_min_f, beta_min_f, beta_max_f;  // float copies (FP32 update)
 };
 
 // Schedule of iteration s->iter (euler_solver.cpp:69-112 and 772-797): order switch,
@@ -766,7 +767,24 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
       r3 = r4.w;
       if (!global_dt) src = SR[c];
     }
-    if (PRECOND) {  // energy row of the preconditioned residual, in double
+    if (PRECOND && sizeof(T) == 4) {
+      // energy row of the preconditioned residual in float: the scaling changes the
+      // pseudo-time path only, not the steady state, and the float-bulk path's reference
+      // arithmetic is float (GB300 runs double at a small fraction of the float rate)
+      const auto w4 = W[c];
+      const Prim<float> w{float(w4.x), float(w4.y), float(w4.z), float(w4.w)};
+      FaceParams<float> fpf;
+      fpf.gamma = pc.gamma_f;
+      fpf.pc_mach_ref = pc.mach_ref_f;
+      fpf.pc_mach_min = pc.mach_min_f;
+      fpf.pc_beta_min = pc.beta_min_f;
+      fpf.pc_beta_max = pc.beta_max_f;
+      const float beta = cell_beta(w, fpf);
+      const float b2 = beta * beta;
+      const float inv_rho = 1.0f / smax(w.r, 1.0e-8f);
+      const float ud = fmaf(w.u, float(r1), w.v * float(r2));
+      r3 = T(fmaf(b2, float(r3), (b2 - 1.0f) * inv_rho * ud));
+    } else if (PRECOND) {  // energy row of the preconditioned residual, in double
       const auto w4 = W[c];
       const Prim<double> w{double(w4.x), double(w4.y), double(w4.z), double(w4.w)};
       FaceParams<double> fpd;

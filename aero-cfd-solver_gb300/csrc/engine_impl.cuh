@@ -1048,6 +1048,10 @@ class EngineT final : public Engine {
     pc.beta_max = double(fp.pc_beta_max);
     pc.gamma_f = float(rs.gamma);
     pc.gm1_f = float(rs.gamma - 1.0);
+    pc.mach_ref_f = float(pc.mach_ref);
+    pc.mach_min_f = float(pc.mach_min);
+    pc.beta_min_f = float(pc.beta_min);
+    pc.beta_max_f = float(pc.beta_max);
 
     MonitorConsts& mc = mcs_[k];
     mc.p_inf = rs.p_inf;

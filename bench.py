@@ -319,11 +319,7 @@ def c3_low_mach(args, aero_gb300, capi, peak):
     mach = 0.05
     res = {}
     for prec, code in (("fp32", capi.PRECISION_FP32), ("fp64", capi.PRECISION_FP64)):
-        case = capi.make_case(mach=mach, aoa_deg=3.0, flux=capi.FLUX_HLLC, limiter=capi.LIMITER_MINMOD, precond_on=1,
-                              low_mach_fix=1, all_speed_flux_fix=1, precond_farfield_bc=1, iterations=100000,
-                              min_iterations=100000, cfl_start=0.2, cfl_max=0.8, cfl_ramp_iters=120,
-                              startup_first_order_iters=25, precision=code)
-        with aero_gb300.Solver(mesh, case) as s:
+        with aero_gb300.Solver(mesh, c3_case(capi, code)) as s:
             info = s.info()
             _, rec = s.run(400)
             s.time_iterations(args.warmup, use_graph=True, flush_l2=True)
@@ -347,6 +343,28 @@ def c3_low_mach(args, aero_gb300, capi, peak):
             "roofline_face_pass_fp64": {"achieved": res["fp64"]["face_gbs"], "frac": res["fp64"]["face_gbs"] / peak,
                                         "avg_launch_ms": res["fp64"]["face_ms"]},
             "kernel_ms_per_launch_fp32": res["fp32"]["kernels"]}
+
+
+def c3_case(capi, precision):
+    return capi.make_case(mach=0.05, aoa_deg=3.0, flux=capi.FLUX_HLLC, limiter=capi.LIMITER_MINMOD, precond_on=1,
+                          low_mach_fix=1, all_speed_flux_fix=1, precond_farfield_bc=1, iterations=100000,
+                          min_iterations=100000, cfl_start=0.2, cfl_max=0.8, cfl_ramp_iters=120,
+                          startup_first_order_iters=25, precision=precision)
+
+
+def c3_profile_run(args):
+    """The C3 case with direct (non-graph) launches, for kernel profilers: 30 iterations
+    (25 first-order start-up, 5 second-order), then 5 timed second-order iterations."""
+    import aero_gb300
+    from aero_gb300 import capi
+
+    aero_gb300.load()
+    mesh = aero_gb300.ogrid_synthetic(1024, 256, cell_type=3, permute=True, jitter=0.1, seed=3)
+    with aero_gb300.Solver(mesh, c3_case(capi, capi.PRECISION_FP32)) as s:
+        s.time_iterations(30, use_graph=False, flush_l2=False)
+        ms = s.time_iterations(5, use_graph=False, flush_l2=True)
+    print(json.dumps({"c3_profile_run": {"cells": mesh.num_cells, "ms_5_iters": ms,
+                                         "mcell_iter_s": mesh.num_cells * 5 / ms / 1e3}}))
 
 
 def c5_adjoint(args, aero_gb300, capi):
@@ -479,7 +497,11 @@ def run_gpu_arm(args):
         pcode = capi.PRECISION_FP32 if precisions[0] == "fp32" else capi.PRECISION_FP64
         with aero_gb300.Solver(mesh, capi.make_case(**CASE, precision=pcode)) as s:
             u0 = s.get_state() if head["state"] is None else head["state"]
-            s.run(STARTUP)
+            # untimed warm-up through the same calls: the start-up iterations and W
+            # second-order iterations (this instantiates the iteration graphs)
+            s.run(STARTUP + args.warmup)
+            s.set_state(u0)
+            s.get_state()
             barrier(dist)
             t0 = time.perf_counter()
             s.set_state(u0)
@@ -572,12 +594,16 @@ def main():
     ap.add_argument("--no-c4", action="store_true", help="skip the 96-case batched sweep measurement")
     ap.add_argument("--cpu-procs", type=int, default=0, help="processes of the reference arm (0: all cores)")
     ap.add_argument("--no-c3", action="store_true", help="skip the 524k-cell low-Mach measurement")
+    ap.add_argument("--c3-profile", action="store_true",
+                    help="only run the 524k-cell low-Mach case with direct launches (for ncu)")
     ap.add_argument("--c5", action="store_true", help="also time the adjoint gradient case (primal + adjoint)")
     ap.add_argument("--c5-fd", action="store_true", help="--c5 plus central differences for alpha and two bumps")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
-    if args.impl == "reference":
+    if args.c3_profile:
+        c3_profile_run(args)
+    elif args.impl == "reference":
         run_reference_arm(args)
     else:
         run_gpu_arm(args)

@@ -649,6 +649,21 @@ void precondition_residual(const std::vector<Prim<R>>& w, const Numerics<R>& nm,
   }
 }
 
+// The same energy row in float with fused multiply-adds (the FP32-bulk mode's arithmetic):
+// ud = fma(u, r1, v r2), r4 = fma(b2, r4, (b2 - 1) / rho * ud).
+template <class A>
+void precondition_residual_fma(const std::vector<Prim<float>>& w, const Numerics<float>& nm, std::vector<A>* res) {
+  if (!nm.precond) return;
+  for (size_t c = 0; c < w.size(); ++c) {
+    const float beta = cell_beta(w[c], nm);
+    const float b2 = beta * beta;
+    const float inv_rho = 1.0f / std::max(w[c].rho, K<float>::rho_floor);
+    A* r = res->data() + 5 * c;
+    const float ud = std::fma(w[c].u, float(r[1]), w[c].v * float(r[2]));
+    r[4] = A(std::fma(b2, float(r[4]), (b2 - 1.0f) * inv_rho * ud));
+  }
+}
+
 // time_integrator.cpp:31-59
 template <class R>
 std::vector<R> dt_over_volume(const std::vector<R>& sr, R cfl, bool local) {

@@ -3,9 +3,9 @@
 // The pseudo-time iteration loop of run_euler_airfoil_case
 // (src/cfd_core/solvers/euler_solver.cpp:463-1208) restated on an injected mesh.
 // R is the residual (bulk) type, A the type of the conserved state across RK stages,
-// of the preconditioned residual, of the norms/forces and of the controller scalars.
-// <float,float> is the reference, <double,double> the FP64 oracle, <float,double>
-// the FP32-bulk / FP64-accumulate oracle.
+// of the norms/forces and of the controller scalars. <float,float> is the reference,
+// <double,double> the FP64 oracle, <float,double> the FP32-bulk / FP64-accumulate oracle,
+// whose residual preconditioning is float with fused multiply-adds, as the device forms it.
 #pragma once
 
 #include "aero_oracle.hpp"
@@ -282,7 +282,11 @@ class Solver {
         itd.first_order_fallback += dg.first_order_fallback;
         itd.diffusive_fallback += dg.diffusive_fallback;
         std::vector<A> rp(res.begin(), res.end());
-        precondition_residual<R, A>(w, nm, &rp);
+        if constexpr (kMixed) {
+          precondition_residual_fma(w, nm, &rp);
+        } else {
+          precondition_residual<R, A>(w, nm, &rp);
+        }
         const std::vector<R> dtr = dt_over_volume(sr, R(cfl), cfg_.local_time_stepping != 0);
         if constexpr (kMixed) {
           rk_stage_delta(stage, stage == cfg_.rk_stages - 1, &uhi_, &ulo_, rp, dtr, static_cast<double>(nm.gamma),

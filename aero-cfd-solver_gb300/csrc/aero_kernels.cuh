@@ -588,11 +588,13 @@ __device__ __forceinline__ double block_max(double v, double* shm) {
 // Gradient: Green-Gauss primitive gradients (reconstruction.cpp:73-119), gathered per cell.
 // ---------------------------------------------------------------------------------------
 // Green-Gauss gradient of cell c (reconstruction.cpp:73-119): the face averages of the
-// primitive state times the outward face vectors, over 1/V.
+// primitive state times the outward face vectors, over 1/V. sW (may be null) holds W of the
+// cells [base, base + nsw): neighbours in that range are read from shared memory.
 template <class T>
 __device__ __forceinline__ void cell_gradient(const DevMesh<T>& m, const typename Vec<T>::v4* __restrict__ W, int c,
-                                              typename Vec<T>::v4* gxo, typename Vec<T>::v4* gyo) {
-  const auto wc = W[c];
+                                              typename Vec<T>::v4* gxo, typename Vec<T>::v4* gyo,
+                                              const typename Vec<T>::v4* sW = nullptr, int base = 0, int nsw = 0) {
+  const auto wc = sW ? sW[c - base] : W[c];
   T ax0 = 0, ax1 = 0, ax2 = 0, ax3 = 0, ay0 = 0, ay1 = 0, ay2 = 0, ay3 = 0;
   // slots in batches of kU: the links first, then every load of the batch, then the sums in
   // slot order, so the neighbour loads of one cell are in flight together
@@ -610,7 +612,13 @@ __device__ __forceinline__ void cell_gradient(const DevMesh<T>& m, const typenam
         const int s = (k0 + u) * m.n + c;
         nd[u] = m.nrm[s];
         ar[u] = m.area[s];
-        wo[u] = lk[u] >= 0 ? W[lk[u] >> 1] : wc;
+        if (lk[u] >= 0) {
+          const int o = lk[u] >> 1;
+          const unsigned off = static_cast<unsigned>(o - base);
+          wo[u] = (sW && off < static_cast<unsigned>(nsw)) ? sW[off] : W[o];
+        } else {
+          wo[u] = wc;
+        }
       }
     }
 #pragma unroll
@@ -652,11 +660,19 @@ template <class T>
 __global__ void __launch_bounds__(256) k_gradient(DevMesh<T> m, const typename Vec<T>::v4* __restrict__ W,
                                                   typename Vec<T>::v4* __restrict__ gx,
                                                   typename Vec<T>::v4* __restrict__ gy, Cases<T> cs) {
+  // the block's own cells' W staged in shared memory: with the cells in Morton / RCM order
+  // most neighbours fall inside the block, and their loads no longer go to L2
+  __shared__ typename Vec<T>::v4 sW[256];
   const int2 bd = cs.blk[blockIdx.x];
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= bd.y || cs.ctrl[bd.x].done) return;
+  const int base = blockIdx.x * blockDim.x;
+  const int c = base + threadIdx.x;
+  if (cs.ctrl[bd.x].done) return;  // uniform over the block (one case per block)
+  const int nsw = min(static_cast<int>(blockDim.x), bd.y - base);
+  if (threadIdx.x < nsw) sW[threadIdx.x] = W[c];
+  __syncthreads();
+  if (c >= bd.y) return;
   typename Vec<T>::v4 ox, oy;
-  cell_gradient<T>(m, W, c, &ox, &oy);
+  cell_gradient<T>(m, W, c, &ox, &oy, sW, base, nsw);
   gx[c] = ox;
   gy[c] = oy;
 }

@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 namespace aero {
@@ -427,14 +428,37 @@ class EngineT final : public Engine {
     AERO_CK(cudaStreamSynchronize(st_));
   }
 
-  // State transfers go through a page-locked staging buffer in the device order.
+  // fn(begin, end) over [0, n) on up to 8 host threads (one for small n)
+  template <class Fn>
+  static void host_parallel(int n, Fn&& fn) {
+    const int hw = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+    const int nt = std::min({8, hw, std::max(1, n / 16384)});
+    if (nt <= 1) {
+      fn(0, n);
+      return;
+    }
+    std::vector<std::thread> pool;
+    const int chunk = (n + nt - 1) / nt;
+    for (int t = 1; t < nt; ++t) {
+      const int b = t * chunk, e = std::min(n, b + chunk);
+      if (b < e) pool.emplace_back([&fn, b, e] { fn(b, e); });
+    }
+    fn(0, std::min(n, chunk));
+    for (auto& th : pool) th.join();
+  }
+
+  // State transfers go through a page-locked staging buffer in the device order; the
+  // renumbering copies run on several host threads.
   void set_state(int k, const double* u) override {
     const Pack& p = pk_[k];
     d4* h = pinned_state();
-    for (int cn = 0; cn < p.n; ++cn) {
-      const double* s = u + 5 * static_cast<size_t>(hs_[k].perm[cn]);
-      h[cn] = d4{s[0], s[1], s[2], s[4]};
-    }
+    const int* perm = hs_[k].perm.data();
+    host_parallel(p.n, [&](int b, int e) {
+      for (int cn = b; cn < e; ++cn) {
+        const double* s = u + 5 * static_cast<size_t>(perm[cn]);
+        h[cn] = d4{s[0], s[1], s[2], s[4]};
+      }
+    });
     AERO_CK(cudaMemcpyAsync(Un_ + p.c0, h, sizeof(d4) * p.n, cudaMemcpyHostToDevice, st_));
     state_from_staging(p.c0, p.n);
     AERO_CK(cudaStreamSynchronize(st_));
@@ -447,14 +471,17 @@ class EngineT final : public Engine {
     state_to_staging(p.c0, p.n);
     AERO_CK(cudaMemcpyAsync(h, Un_ + p.c0, sizeof(d4) * p.n, cudaMemcpyDeviceToHost, st_));
     AERO_CK(cudaStreamSynchronize(st_));
-    for (int cn = 0; cn < p.n; ++cn) {
-      double* s = u + 5 * static_cast<size_t>(hs_[k].perm[cn]);
-      s[0] = h[cn].x;
-      s[1] = h[cn].y;
-      s[2] = h[cn].z;
-      s[3] = 0.0;
-      s[4] = h[cn].w;
-    }
+    const int* perm = hs_[k].perm.data();
+    host_parallel(p.n, [&](int b, int e) {
+      for (int cn = b; cn < e; ++cn) {
+        double* s = u + 5 * static_cast<size_t>(perm[cn]);
+        s[0] = h[cn].x;
+        s[1] = h[cn].y;
+        s[2] = h[cn].z;
+        s[3] = 0.0;
+        s[4] = h[cn].w;
+      }
+    });
   }
 
   void get_primitive(int k, double* rho, double* u, double* v, double* p) override {

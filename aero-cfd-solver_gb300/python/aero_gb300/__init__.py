@@ -308,10 +308,14 @@ class Solver:
         assert u.size == 5 * self.n
         self._check(self.lib.aero_set_state(self.h, u.ctypes.data_as(_dp)))
 
-    def get_state(self) -> np.ndarray:
-        u = np.empty(5 * self.n, np.float64)
-        self._check(self.lib.aero_get_state(self.h, u.ctypes.data_as(_dp)))
-        return u.reshape(self.n, 5)
+    def get_state(self, out: np.ndarray | None = None) -> np.ndarray:
+        """The conserved state [N, 5] in the original cell order; `out` (float64, C-contiguous,
+        N*5 values) is filled and returned instead of a new array when given."""
+        if out is None:
+            out = np.empty((self.n, 5), np.float64)
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == 5 * self.n
+        self._check(self.lib.aero_get_state(self.h, out.ctypes.data_as(_dp)))
+        return out.reshape(self.n, 5)
 
     def get_primitive(self):
         out = [np.empty(self.n, np.float64) for _ in range(4)]

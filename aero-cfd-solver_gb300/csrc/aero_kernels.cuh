@@ -1390,6 +1390,29 @@ static __global__ void k_split_state(int n, const d4* __restrict__ Un, float4* _
   hi[c] = h;
   lo[c] = l;
 }
+// State exchange with a caller's host array, read and written by the GPU in place where the
+// device shares the host's page tables (Grace: NVLink-C2C with address translation): u is
+// AoS [N][5] in the original cell order, perm maps device cell -> original cell.
+static __global__ void k_state_from_host(int n, const double* __restrict__ u, const int* __restrict__ perm,
+                                         d4* __restrict__ Un) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const double* s = u + 5 * static_cast<size_t>(perm[c]);
+  Un[c] = d4{s[0], s[1], s[2], s[4]};
+}
+static __global__ void k_state_to_host(int n, const d4* __restrict__ Un, const int* __restrict__ perm,
+                                       double* __restrict__ u) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const d4 v = Un[c];
+  double* s = u + 5 * static_cast<size_t>(perm[c]);
+  s[0] = v.x;
+  s[1] = v.y;
+  s[2] = v.z;
+  s[3] = 0.0;
+  s[4] = v.w;
+}
+
 static __global__ void k_combine_state(int n, const float4* __restrict__ hi, const float4* __restrict__ lo,
                                        d4* __restrict__ Un) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;

@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <thread>
 #include <vector>
@@ -263,6 +264,26 @@ class EngineT final : public Engine {
     }
     std::vector<int> perm0(hs_[0].perm);
     perm_dev_ = upload(perm0);
+    {
+      std::vector<int> perm_all(static_cast<size_t>(ntot_), 0);
+      for (int k = 0; k < K_; ++k) {
+        std::copy(hs_[k].perm.begin(), hs_[k].perm.end(), perm_all.begin() + pk_[k].c0);
+      }
+      perm_all_dev_ = upload(perm_all);
+    }
+    // direct state exchange with host arrays where the GPU walks the host's page tables
+    {
+      int dev = 0, pageable = 0, host_tables = 0;
+      cudaGetDevice(&dev);
+      if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+          cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) !=
+              cudaSuccess) {
+        cudaGetLastError();
+        pageable = host_tables = 0;
+      }
+      const char* off = std::getenv("AERO_HOST_STAGING");
+      host_direct_ = pageable == 1 && host_tables == 1 && !(off && off[0] == '1');
+    }
 
     // ---- state and work arrays
     W_ = alloc<V4>(ntot_);
@@ -451,6 +472,14 @@ class EngineT final : public Engine {
   // renumbering copies run on several host threads.
   void set_state(int k, const double* u) override {
     const Pack& p = pk_[k];
+    if (host_direct_) {
+      k_state_from_host<<<(p.n + 255) / 256, 256, 0, st_>>>(p.n, u, perm_all_dev_ + p.c0, Un_ + p.c0);
+      AERO_CK(cudaGetLastError());
+      state_from_staging(p.c0, p.n);
+      AERO_CK(cudaStreamSynchronize(st_));
+      w_valid_ = false;
+      return;
+    }
     d4* h = pinned_state();
     const int* perm = hs_[k].perm.data();
     host_parallel(p.n, [&](int b, int e) {
@@ -467,6 +496,13 @@ class EngineT final : public Engine {
 
   void get_state(int k, double* u) override {
     const Pack& p = pk_[k];
+    if (host_direct_) {
+      state_to_staging(p.c0, p.n);
+      k_state_to_host<<<(p.n + 255) / 256, 256, 0, st_>>>(p.n, Un_ + p.c0, perm_all_dev_ + p.c0, u);
+      AERO_CK(cudaGetLastError());
+      AERO_CK(cudaStreamSynchronize(st_));
+      return;
+    }
     d4* h = pinned_state();
     state_to_staging(p.c0, p.n);
     AERO_CK(cudaMemcpyAsync(h, Un_ + p.c0, sizeof(d4) * p.n, cudaMemcpyDeviceToHost, st_));
@@ -1698,6 +1734,8 @@ class EngineT final : public Engine {
   T* inv_vol_ = nullptr;
   unsigned char* flags_ = nullptr;
   int* perm_dev_ = nullptr;  // case 0: new -> original cell
+  int* perm_all_dev_ = nullptr;  // every case's new -> original cell, at the case's cell offset
+  bool host_direct_ = false;     // the GPU reads and writes host state arrays in place
   int2* cblk_ = nullptr;     // per cell block: (case, end of the case's cells)
   int2* fblk_ = nullptr;     // per face block: (case, end of the case's faces)
   int* srfirst_ = nullptr;   // per case: first per-warp time-step partial, [K + 1]

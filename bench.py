@@ -284,8 +284,10 @@ def c4_draw(rank: int):
 def c4_sweep(args, aero_gb300, capi, rank):
     """96 FP32 cases, mesh sizes drawn from the four O-grids, alpha ~ U[-4, 8] deg, M ~
     U[0.3, 0.85], HLLC + MUSCL venkat, per-case CFL ramp to 0.8 and a density-residual stop
-    mask at 1e-8 relative; seeded synthetic inputs. Returns device ms of `steps` iterations
-    (L2 flushed before each) and the batch's cell count."""
+    mask at 1e-8 relative; seeded synthetic inputs. Block size and cell ordering come from
+    the autotuner (aero_autotune on the largest mesh of the draw with the first case's flow).
+    Returns device ms of `steps` iterations (L2 flushed before each), the batch's cell count,
+    its launches per iteration and the tuned (ordering, block size)."""
     base = {sz: aero_gb300.ogrid_synthetic(sz[0], sz[1], cell_type=3, permute=True, jitter=0.1, seed=100 + i,
                                            wall_spacing=0.005, farfield_radius=20.0)
             for i, sz in enumerate(C4_SIZES)}
@@ -298,22 +300,27 @@ def c4_sweep(args, aero_gb300, capi, rank):
         c = capi.make_case(**kw, precision=capi.PRECISION_FP32)
         c.density_l2_target = 1e-8
         cases.append(c)
+    largest = max(range(C4_CASES), key=lambda k: meshes[k].num_cells)
+    tuned, _ = aero_gb300.autotune(meshes[largest], cases[0], iters=10)
+    for c in cases:
+        c.block_size = tuned.block_size
+        c.ordering = tuned.ordering
     with aero_gb300.Batch(meshes, cases) as b:
         cells = b.info()["cells"]
         b.run(STARTUP)
         b.time_iterations(args.warmup, use_graph=True, flush_l2=True)
         ms = b.time_iterations(args.steps, use_graph=True, flush_l2=not args.no_flush)
         launches = b.info()["launches_per_iteration"]
-    return ms, int(cells), int(launches)
+    return ms, int(cells), int(launches), (int(tuned.ordering), int(tuned.block_size))
 
 
 def c3_low_mach(args, aero_gb300, capi, peak):
     """Low-Mach precision case on the 1024x256 triangulated O-grid (524,288 cells, jittered,
     permuted): preconditioning, low-Mach fix and all-speed flux fix on, characteristic far
-    field, HLLC + minmod, M=0.05, alpha=3. Throughput of FP32 and FP64 (L2 flushed before each
-    timed iteration), the face pass's roofline at this size (its working set no longer fits in
-    L2), and |dCL|, |dCD|, max |dCp| at the wall between FP32 and FP64 after 400 iterations from
-    free stream."""
+    field, HLLC + minmod, alpha=3. At M=0.05: throughput of FP32 and FP64 (L2 flushed before
+    each timed iteration) and the face pass's roofline at this size (its working set no longer
+    fits in L2). At M=0.05 and M=0.01: |dCL|, |dCD|, max |dCp| at the wall between FP32 and
+    FP64 after 400 iterations from free stream."""
     mesh = aero_gb300.ogrid_synthetic(1024, 256, cell_type=3, permute=True, jitter=0.1, seed=3)
     wall = mesh.wall_faces
     mach = 0.05
@@ -333,7 +340,18 @@ def c3_low_mach(args, aero_gb300, capi, peak):
                          cd=float(rec["cd"][-1]), pw=p[mesh.owner[wall]], face_ms=avg, face_gbs=nbytes / (avg / 1e3) / 1e9,
                          kernels={k: (v[0] / v[1] if v[1] else 0.0) for k, v in prof.items()})
     q = 0.5 * 1.4 * 101325.0 * mach * mach
+    m01 = {}
+    for prec, code in (("fp32", capi.PRECISION_FP32), ("fp64", capi.PRECISION_FP64)):
+        with aero_gb300.Solver(mesh, c3_case(capi, code, 0.01)) as s:
+            _, rec = s.run(400)
+            m01[prec] = (float(rec["cl"][-1]), float(rec["cd"][-1]), s.get_primitive()[3][mesh.owner[wall]],
+                         float(rec["residual_ratio"][-1]))
+    q01 = 0.5 * 1.4 * 101325.0 * 0.01 * 0.01
+    mach01 = {"abs_dcl_400": abs(m01["fp32"][0] - m01["fp64"][0]), "abs_dcd_400": abs(m01["fp32"][1] - m01["fp64"][1]),
+              "max_abs_dcp_wall_400": float(np.max(np.abs(m01["fp32"][2] - m01["fp64"][2])) / q01),
+              "residual_ratio_fp64_400": m01["fp64"][3]}
     return {"cells": mesh.num_cells, "mach": mach, "fp32_mcell_iter_s": res["fp32"]["mcell"],
+            "mach_0.01": mach01,
             "fp64_mcell_iter_s": res["fp64"]["mcell"], "fp32_over_fp64": res["fp32"]["mcell"] / res["fp64"]["mcell"],
             "abs_dcl_400": abs(res["fp32"]["cl"] - res["fp64"]["cl"]),
             "abs_dcd_400": abs(res["fp32"]["cd"] - res["fp64"]["cd"]),
@@ -345,8 +363,8 @@ def c3_low_mach(args, aero_gb300, capi, peak):
             "kernel_ms_per_launch_fp32": res["fp32"]["kernels"]}
 
 
-def c3_case(capi, precision):
-    return capi.make_case(mach=0.05, aoa_deg=3.0, flux=capi.FLUX_HLLC, limiter=capi.LIMITER_MINMOD, precond_on=1,
+def c3_case(capi, precision, mach=0.05):
+    return capi.make_case(mach=mach, aoa_deg=3.0, flux=capi.FLUX_HLLC, limiter=capi.LIMITER_MINMOD, precond_on=1,
                           low_mach_fix=1, all_speed_flux_fix=1, precond_farfield_bc=1, iterations=100000,
                           min_iterations=100000, cfl_start=0.2, cfl_max=0.8, cfl_ramp_iters=120,
                           startup_first_order_iters=25, precision=precision)
@@ -519,12 +537,14 @@ def run_gpu_arm(args):
     c4 = None
     if not args.no_c4 and "fp32" in precisions:
         barrier(dist)
-        c4_ms, c4_cells, c4_launch = c4_sweep(args, aero_gb300, capi, rank)
+        c4_ms, c4_cells, c4_launch, c4_tuned = c4_sweep(args, aero_gb300, capi, rank)
         c4_ms = reduce_max(dist, c4_ms)
         c4 = {"cases_per_gpu": C4_CASES, "cells_per_gpu": c4_cells, "steps": args.steps,
               "ms_per_step": c4_ms / args.steps,
               "fp32_batched_mcell_iter_s": world * c4_cells * args.steps / (c4_ms / 1e3) / 1e6,
               "launches_per_step": c4_launch,
+              "autotuned": {"ordering": {1: "morton", 2: "rcm"}.get(c4_tuned[0], c4_tuned[0]),
+                            "block_size": c4_tuned[1]},
               "inputs": "96 seeded cases per GPU: sizes from {64x16,128x32,256x64,512x128} triangulated "
                         "O-grids, alpha~U[-4,8], M~U[0.3,0.85], HLLC+MUSCL venkat, CFL ramp to 0.8, "
                         "density-residual stop mask 1e-8; one batched context, L2 flushed per step"}

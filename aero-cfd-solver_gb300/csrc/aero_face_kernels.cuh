@@ -89,10 +89,16 @@ __global__ void __launch_bounds__(256) k_face_flux(DevFaces<T> f, Cases<T> cs,
   int fo = 0, df = 0;
   if (i < bd.y) {
     const int2 oc = f.cells[i];
-    const int o = oc.x, b = oc.y;
     const auto nd = f.nrm[i];
-    const T nx = nd.x, ny = nd.y;
     const T area = f.area[i];
+    // the MUSCL offsets do not depend on the cell ids: loaded with them, not after
+    typename Vec<T>::v2 dO{}, dN{};
+    if (SECOND) {
+      dO = f.doff[i];
+      dN = f.noff[i];
+    }
+    const int o = oc.x, b = oc.y;
+    const T nx = nd.x, ny = nd.y;
     const auto wo4 = W[o];
     const Prim<T> wo{wo4.x, wo4.y, wo4.z, wo4.w};
     Prim<T> wn = wo;
@@ -107,8 +113,6 @@ __global__ void __launch_bounds__(256) k_face_flux(DevFaces<T> f, Cases<T> cs,
         gO[4] = gOy.x; gO[5] = gOy.y; gO[6] = gOy.z; gO[7] = gOy.w;
         gN[0] = gNx.x; gN[1] = gNx.y; gN[2] = gNx.z; gN[3] = gNx.w;
         gN[4] = gNy.x; gN[5] = gNy.y; gN[6] = gNy.z; gN[7] = gNy.w;
-        const auto dO = f.doff[i];
-        const auto dN = f.noff[i];
         dox = dO.x; doy = dO.y; dnx = dN.x; dny = dN.y;
       }
     }

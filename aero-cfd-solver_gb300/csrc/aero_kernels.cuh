@@ -606,19 +606,24 @@ __device__ __forceinline__ void cell_gradient(const DevMesh<T>& m, const typenam
     typename Vec<T>::v2 nd[kU];
     T ar[kU];
     typename Vec<T>::v4 wo[kU];
+    // the slot geometry does not depend on the links (padding slots hold zeros), so its loads
+    // go out with the links' and only the neighbour states wait for them
 #pragma unroll
     for (int u = 0; u < kU; ++u) {
-      if (lk[u] != kPad) {
+      if (k0 + u < m.d) {
         const int s = (k0 + u) * m.n + c;
         nd[u] = m.nrm[s];
         ar[u] = m.area[s];
-        if (lk[u] >= 0) {
-          const int o = lk[u] >> 1;
-          const unsigned off = static_cast<unsigned>(o - base);
-          wo[u] = (sW && off < static_cast<unsigned>(nsw)) ? sW[off] : W[o];
-        } else {
-          wo[u] = wc;
-        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      if (lk[u] >= 0) {
+        const int o = lk[u] >> 1;
+        const unsigned off = static_cast<unsigned>(o - base);
+        wo[u] = (sW && off < static_cast<unsigned>(nsw)) ? sW[off] : W[o];
+      } else {
+        wo[u] = wc;
       }
     }
 #pragma unroll
@@ -760,6 +765,8 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
       st_un = U.un[c];
     }
     if (stage > 0) st_us = Us[c];
+    typename Vec<T>::v4 st_w{};
+    if (PRECOND) st_w = W[c];
     T r0, r1, r2, r3, src;
     if (GATHER) {
       T rr[4];
@@ -787,7 +794,7 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
       // energy row of the preconditioned residual in float: the scaling changes the
       // pseudo-time path only, not the steady state, and the float-bulk path's reference
       // arithmetic is float (GB300 runs double at a small fraction of the float rate)
-      const auto w4 = W[c];
+      const auto w4 = st_w;
       const Prim<float> w{float(w4.x), float(w4.y), float(w4.z), float(w4.w)};
       FaceParams<float> fpf;
       fpf.gamma = pc.gamma_f;
@@ -801,7 +808,7 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
       const float ud = fmaf(w.u, float(r1), w.v * float(r2));
       r3 = T(fmaf(b2, float(r3), (b2 - 1.0f) * inv_rho * ud));
     } else if (PRECOND) {  // energy row of the preconditioned residual, in double
-      const auto w4 = W[c];
+      const auto w4 = st_w;
       const Prim<double> w{double(w4.x), double(w4.y), double(w4.z), double(w4.w)};
       FaceParams<double> fpd;
       fpd.gamma = pc.gamma;

@@ -103,40 +103,50 @@ struct PrecondD {
 
 // Schedule of iteration s->iter (euler_solver.cpp:69-112 and 772-797): order switch,
 // CFL ramp times the adaptive scale, stabilization-floor ramp, all-speed weights. Used by
-// the controller for the next iteration and by the host for iteration 0.
-__host__ __device__ inline void apply_schedule(const CtrlConfig& cc, Ctrl* sp) {
-  Ctrl& s = *sp;
-  const int it = s.iter;
-  s.second = it >= (cc.startup_first_order > 0 ? cc.startup_first_order : 0);
-  {
-    double base;
-    if (cc.cfl_ramp <= 0) {
-      base = cc.cfl_max;
-    } else {
-      const double t = smin(1.0, double(it + 1) / double(cc.cfl_ramp > 1 ? cc.cfl_ramp : 1));
-      base = cc.cfl_start + t * (cc.cfl_max - cc.cfl_start);
-    }
-    s.cfl = base * s.cfl_scale;
+// the controller for the next iteration and by the host for iteration 0. SchedBase is the
+// part that depends on the iteration index alone.
+struct SchedBase {
+  int second;
+  double cfl_base, stab_floor, as_ramp;  // as_ramp: the non-staged all-speed ramp
+};
+__host__ __device__ inline SchedBase schedule_base(const CtrlConfig& cc, int it) {
+  SchedBase b;
+  b.second = it >= (cc.startup_first_order > 0 ? cc.startup_first_order : 0);
+  if (cc.cfl_ramp <= 0) {
+    b.cfl_base = cc.cfl_max;
+  } else {
+    const double t = smin(1.0, double(it + 1) / double(cc.cfl_ramp > 1 ? cc.cfl_ramp : 1));
+    b.cfl_base = cc.cfl_start + t * (cc.cfl_max - cc.cfl_start);
   }
   {
     const double m0s = sclamp(cc.stab_start, 0.0, 1.0), m0t = sclamp(cc.stab_target, 0.0, 1.0);
     if (cc.stab_ramp <= 0) {
-      s.stab_floor = m0t;
+      b.stab_floor = m0t;
     } else {
       const double t =
           sclamp(double(it > 0 ? it : 0) / double(cc.stab_ramp > 1 ? cc.stab_ramp : 1), 0.0, 1.0);
-      s.stab_floor = m0s + t * (m0t - m0s);
+      b.stab_floor = m0s + t * (m0t - m0s);
     }
   }
+  if (cc.as_ramp_iters <= 0) {
+    b.as_ramp = (it >= cc.as_ramp_start) ? 1.0 : 0.0;
+  } else {
+    b.as_ramp = sclamp(double(it - cc.as_ramp_start) / double(cc.as_ramp_iters > 1 ? cc.as_ramp_iters : 1),
+                       0.0, 1.0);
+  }
+  return b;
+}
+
+// Schedule of iteration s->iter from its iteration-only part b = schedule_base(cc, s->iter).
+__host__ __device__ inline void apply_schedule_from(const CtrlConfig& cc, const SchedBase& b, Ctrl* sp) {
+  Ctrl& s = *sp;
+  s.second = b.second;
+  s.cfl = b.cfl_base * s.cfl_scale;
+  s.stab_floor = b.stab_floor;
   if (!cc.staged) {
     s.as_fix = cc.as_fix_cfg;
     s.as_fmin = cc.as_fmin;
-    if (cc.as_ramp_iters <= 0) {
-      s.as_ramp = (it >= cc.as_ramp_start) ? 1.0 : 0.0;
-    } else {
-      s.as_ramp = sclamp(double(it - cc.as_ramp_start) / double(cc.as_ramp_iters > 1 ? cc.as_ramp_iters : 1),
-                         0.0, 1.0);
-    }
+    s.as_ramp = b.as_ramp;
   } else if (s.stage == 1) {
     s.as_fix = 0;
     s.as_fmin = cc.st_fmin_high;
@@ -153,6 +163,10 @@ __host__ __device__ inline void apply_schedule(const CtrlConfig& cc, Ctrl* sp) {
   s.stab_f = float(s.stab_floor);
   s.as_fmin_f = float(s.as_fmin);
   s.as_ramp_f = float(s.as_ramp);
+}
+
+__host__ __device__ inline void apply_schedule(const CtrlConfig& cc, Ctrl* sp) {
+  apply_schedule_from(cc, schedule_base(cc, sp->iter), sp);
 }
 
 // Schedule values of a single residual evaluation (aero_residual and its no-allocation form).
@@ -999,18 +1013,24 @@ struct Record {
   double rho_ratio;
 };
 
-// Serial part of the controller (lane 0), on the shared copy of the controller state.
-__device__ inline void control_serial(const CtrlConfig& cc, const double (&a)[kNorm], const double (&mon)[kMon],
-                                      const double (&pj)[4], const double (&wv)[kWall], Ctrl* sp,
-                                      Record* __restrict__ recs, int rec_cap, int* fb) {
-  const double* fsum = wv;
-  const double un_max = wv[8], cp_hi = wv[9], cp_lo_neg = wv[10], cp_bad = wv[11];
-  const double lmax = a[2];
-  const double dpd = mon[0], dpw = mon[1];
-  const double ffm[4] = {mon[2], mon[3], mon[4], mon[5]};
+// The controller's serial work, split over lane 0 of the four warps (each warp on its own SM
+// sub-partition, so their double arithmetic proceeds side by side) in two phases:
+//   phase 1  ctl_forces    force coefficients and their stability window
+//            ctl_residual  residual monitor and adaptive CFL
+//            ctl_side      density-residual ratio, pressure-jump energies, the iteration-only
+//                          part of the next schedule
+//            ctl_report    the record's reporting-only fields, fallback counters
+//   phase 2  ctl_decide    staged all-speed controller, stop rule, next schedule
+// Every value is formed by the same expression as in one serial pass
+// (euler_solver.cpp:948-1208, convergence_monitor.cpp:13-127, forces.cpp:208-294); the
+// threads write disjoint fields of the shared record and controller state.
+struct CtlIn {  // the block partials combined
+  double a[kNorm], mon[kMon], pj[4], wv[kWall];
+};
 
-  Ctrl& s = *sp;
-  Record r;
+__device__ inline void ctl_report(const CtrlConfig& cc, const CtlIn& in, const Ctrl& s, Record& r, int* fb) {
+  const double* fsum = in.wv;
+  const double un_max = in.wv[8], cp_hi = in.wv[9], cp_lo_neg = in.wv[10], cp_bad = in.wv[11];
   r.iter = s.iter;
   r.flags = (s.second ? 8 : 0) | (s.as_fix ? 32 : 0) | (s.stage == 1 ? 64 : 0) | (s.stage == 2 ? 128 : 0);
   r.fo = fb[0];
@@ -1021,8 +1041,8 @@ __device__ inline void control_serial(const CtrlConfig& cc, const double (&a)[kN
   r.stab = s.stab_floor;
   r.as_fmin = s.as_fmin;
   r.as_ramp = s.as_ramp;
-  r.dp_dom = dpd;
-  r.dp_wall = dpw;
+  r.dp_dom = in.mon[0];
+  r.dp_wall = in.mon[1];
   r.wall_un = un_max;
   r.wall_mass_flux = 0.0;  // the slip-wall flux has no mass component (boundary_conditions.cpp:97-110)
   r.cp_min = cc.n_wall > 0 ? -cp_lo_neg : 0.0;
@@ -1032,29 +1052,41 @@ __device__ inline void control_serial(const CtrlConfig& cc, const double (&a)[kN
     r.cp_max = -3.402823466e38;
   }
   r.cp_nonfinite = int(cp_bad);
-  r.ff_dp = ffm[0];
-  r.ff_drho = ffm[1];
-  r.ff_du = ffm[2];
-  r.ff_dv = ffm[3];
+  r.ff_dp = in.mon[2];
+  r.ff_drho = in.mon[3];
+  r.ff_du = in.mon[4];
+  r.ff_dv = in.mon[5];
   r.action = 0;
-  const bool nonfinite = s.nonfinite != 0;
+  r.l1 = in.a[0];
+  r.linf = in.a[2];
+  // integrate_pressure_forces: gauge and absolute force components, absolute coefficients
+  const double qs = cc.q_inf * cc.s_ref;
+  const double fxg = fsum[4], fyg = fsum[5], fxa = fsum[2], fya = fsum[3];
+  r.fx_g = fxg; r.fy_g = fyg; r.fx_a = fxa; r.fy_a = fya; r.snx = fsum[0]; r.sny = fsum[1];
+  r.cd_abs = (fxa * cc.cos_a + fya * cc.sin_a) / qs;
+  r.cl_abs = (-fxa * cc.sin_a + fya * cc.cos_a) / qs;
+  r.cm_abs = fsum[6] / (qs * cc.chord);
+}
 
-  const double l1 = a[0];
-  const double l2 = sqrt(a[1] / double(cc.n_cells > 0 ? 5 * cc.n_cells : 1));
-  const double linf = lmax;
-  r.l1 = l1;
+__device__ inline void ctl_side(const CtrlConfig& cc, const CtlIn& in, Ctrl& s, Record& r, SchedBase* next) {
+  *next = schedule_base(cc, s.iter + 1);
+  // density-residual L2 ratio (the batched sweep's per-case stop rule)
+  const double l2rho = smax(sqrt(in.a[3] / double(cc.n_cells > 0 ? cc.n_cells : 1)), 1.0e-20);
+  if (s.initial_l2rho < 0.0) s.initial_l2rho = l2rho;
+  r.rho_ratio = l2rho / smax(s.initial_l2rho, 1.0e-20);
+  // pressure-jump energies
+  const double pr2 = cc.pressure_ref * cc.pressure_ref + 1.0e-24;
+  r.pj = in.pj[1] > 0.0 ? (in.pj[0] / in.pj[1]) / pr2 : 0.0;
+  r.pj_wall = in.pj[3] > 0.0 ? (in.pj[2] / in.pj[3]) / pr2 : 0.0;
+}
+
+__device__ inline void ctl_residual(const CtrlConfig& cc, const CtlIn& in, Ctrl& s, Record& r) {
+  const double l2 = sqrt(in.a[1] / double(cc.n_cells > 0 ? 5 * cc.n_cells : 1));
   r.l2 = l2;
-  r.linf = linf;
   // ConvergenceMonitor::update_residual
   const double bl2 = smax(l2, 1.0e-20);
   if (s.initial_l2 < 0.0) s.initial_l2 = bl2;
-  const double ratio = bl2 / smax(s.initial_l2, 1.0e-20);
-  r.ratio = ratio;
-  // density-residual L2 ratio (the batched sweep's per-case stop rule)
-  const double l2rho = smax(sqrt(a[3] / double(cc.n_cells > 0 ? cc.n_cells : 1)), 1.0e-20);
-  if (s.initial_l2rho < 0.0) s.initial_l2rho = l2rho;
-  const double rho_ratio = l2rho / smax(s.initial_l2rho, 1.0e-20);
-  r.rho_ratio = rho_ratio;
+  r.ratio = bl2 / smax(s.initial_l2, 1.0e-20);
   if (s.prev_l2 > 0.0) {
     if (l2 > s.prev_l2 * 1.05) {
       s.cfl_scale = smax(s.cfl_scale * 0.65, 0.05);
@@ -1063,19 +1095,20 @@ __device__ inline void control_serial(const CtrlConfig& cc, const double (&a)[kN
     }
   }
   s.prev_l2 = l2;
-  // integrate_pressure_forces (gauge -> reported, abs -> *_abs)
+}
+
+__device__ inline void ctl_forces(const CtrlConfig& cc, const CtlIn& in, Ctrl& s, Record& r, bool* stable_out,
+                                  bool* dstable_out) {
+  const double* fsum = in.wv;
+  // integrate_pressure_forces (gauge -> reported)
   const double qs = cc.q_inf * cc.s_ref;
-  const double fxg = fsum[4], fyg = fsum[5], fxa = fsum[2], fya = fsum[3];
-  r.fx_g = fxg; r.fy_g = fyg; r.fx_a = fxa; r.fy_a = fya; r.snx = fsum[0]; r.sny = fsum[1];
+  const double fxg = fsum[4], fyg = fsum[5];
   r.drag = fxg * cc.cos_a + fyg * cc.sin_a;
   r.lift = -fxg * cc.sin_a + fyg * cc.cos_a;
   r.moment = fsum[7];
   r.cd = r.drag / qs;
   r.cl = r.lift / qs;
   r.cm = fsum[7] / (qs * cc.chord);
-  r.cd_abs = (fxa * cc.cos_a + fya * cc.sin_a) / qs;
-  r.cl_abs = (-fxa * cc.sin_a + fya * cc.cos_a) / qs;
-  r.cm_abs = fsum[6] / (qs * cc.chord);
   // ConvergenceMonitor::update_forces
   r.dcl = r.dcd = r.dcm = 0.0;
   if (s.has_prev) {
@@ -1129,10 +1162,13 @@ __device__ inline void control_serial(const CtrlConfig& cc, const double (&a)[kN
     r.mdcm = fabs(ca[2] * inv - pa[2] * inv);
     dstable = r.mdcl <= cc.drift_tol && r.mdcd <= cc.drift_tol && r.mdcm <= cc.drift_tol;
   }
-  // pressure-jump energies
-  const double pr2 = cc.pressure_ref * cc.pressure_ref + 1.0e-24;
-  r.pj = pj[1] > 0.0 ? (pj[0] / pj[1]) / pr2 : 0.0;
-  r.pj_wall = pj[3] > 0.0 ? (pj[2] / pj[3]) / pr2 : 0.0;
+  *stable_out = stable;
+  *dstable_out = dstable;
+}
+
+__device__ inline void ctl_decide(const CtrlConfig& cc, Ctrl& s, Record& r, bool stable, bool dstable,
+                                  const SchedBase& next) {
+  const bool nonfinite = s.nonfinite != 0;
   // staged all-speed controller (euler_solver.cpp:1068-1139)
   if (cc.staged) {
     if (s.stage == 1) {
@@ -1186,16 +1222,14 @@ __device__ inline void control_serial(const CtrlConfig& cc, const double (&a)[kN
   if (stable) r.flags |= 1;
   if (dstable) r.flags |= 2;
   const bool conv = (s.iter + 1 >= cc.min_iterations) &&
-                    ((!(ratio > cc.residual_target) && stable && dstable) ||
-                     (cc.rho_l2_target > 0.0 && !(rho_ratio > cc.rho_l2_target)));
+                    ((!(r.ratio > cc.residual_target) && stable && dstable) ||
+                     (cc.rho_l2_target > 0.0 && !(r.rho_ratio > cc.rho_l2_target)));
   if (conv) r.flags |= 4;
   if (nonfinite) r.flags |= 16;
-  const int slot = s.iter - s.rec_base;
-  if (slot >= 0 && slot < rec_cap) recs[slot] = r;
   if (conv || nonfinite) s.done = 1;
-  // next iteration's schedule
+  // next iteration's schedule (its iteration-only part formed in phase 1)
   s.iter = s.iter + 1;
-  apply_schedule(cc, &s);
+  apply_schedule_from(cc, next, &s);
 }
 
 
@@ -1209,8 +1243,10 @@ __device__ __forceinline__ long long warp_max_bits(long long x) {
 
 // Controller (one block of kCtlThreads): combines the per-block partials of the norms,
 // monitors, forces and pressure jumps in a fixed order, then runs the convergence monitor,
-// adaptive CFL, staged all-speed controller and the next iteration's schedule on thread 0
-// (euler_solver.cpp:948-1208, 772-797; convergence_monitor.cpp:13-127; forces.cpp:208-294).
+// adaptive CFL, staged all-speed controller and the next iteration's schedule in the two
+// phases of ctl_monitor / ctl_side / ctl_report and ctl_decide (euler_solver.cpp:948-1208,
+// 772-797; convergence_monitor.cpp:13-127; forces.cpp:208-294). The record is assembled in
+// shared memory and stored by the whole block.
 // The serial part works on a shared-memory copy of the controller state, loaded and stored
 // by the whole block, so that thread 0 pays no chain of global-memory round trips. Maxima
 // of non-negative quantities are taken on the integer pipe: a GB300 SM runs double
@@ -1338,8 +1374,12 @@ static __global__ void __launch_bounds__(kCtlThreads) k_control(const CtrlConfig
     for (int k = 0; k < 1 + kMon; ++k) s_max[wid][k] = mx[k];
   }
   __syncthreads();
+  __shared__ CtlIn s_in;
+  __shared__ Record srec;
+  __shared__ SchedBase snext;
+  __shared__ int s_slot;
   if (tid == 0) {
-    double a[kNorm] = {0.0, 0.0, 0.0, 0.0}, mon[kMon], p4[4] = {0.0, 0.0, 0.0, 0.0}, wv[kWall];
+    double a[kNorm] = {0.0, 0.0, 0.0, 0.0}, p4[4] = {0.0, 0.0, 0.0, 0.0};
     long long m[1 + kMon] = {0, 0, 0, 0, 0, 0, 0};
     for (int w = 0; w < kWarps; ++w) {
       a[0] += s_sum[w][0];
@@ -1352,16 +1392,41 @@ static __global__ void __launch_bounds__(kCtlThreads) k_control(const CtrlConfig
       return cc.bulk_f32 ? double(__uint_as_float(static_cast<unsigned>(bits))) : __longlong_as_double(bits);
     };
     a[2] = decode(m[0]);
-    for (int k = 0; k < kMon; ++k) mon[k] = decode(m[k + 1]);
+    for (int k = 0; k < kNorm; ++k) s_in.a[k] = a[k];
+    for (int k = 0; k < 4; ++k) s_in.pj[k] = p4[k];
+    for (int k = 0; k < kMon; ++k) s_in.mon[k] = decode(m[k + 1]);
     for (int k = 0; k < kWall; ++k) {
-      wv[k] = s_wall[0][k];
+      double v = s_wall[0][k];
       if (nwb > 32) {
-        for (int w = 1; w < kWarps; ++w) wv[k] = wall_comb(k, wv[k], s_wall[w][k]);
+        for (int w = 1; w < kWarps; ++w) v = wall_comb(k, v, s_wall[w][k]);
       }
+      s_in.wv[k] = v;
     }
-    control_serial(cc, a, mon, p4, wv, &sc, recs, rec_cap, fb);
+    s_slot = sc.iter - sc.rec_base;  // the record slot of this iteration
   }
   __syncthreads();
+  // phase 1: four independent chains on lane 0 of warps 0..3
+  static_assert(kCtlThreads >= 128, "the controller's phase 1 uses four warps");
+  bool stable = false, dstable = false;
+  if (tid == 0) {
+    ctl_forces(cc, s_in, sc, srec, &stable, &dstable);
+  } else if (tid == 32) {
+    ctl_residual(cc, s_in, sc, srec);
+  } else if (tid == 64) {
+    ctl_side(cc, s_in, sc, srec, &snext);
+  } else if (tid == 96) {
+    ctl_report(cc, s_in, sc, srec, fb);
+  }
+  __syncthreads();
+  // phase 2: the decisions
+  if (tid == 0) ctl_decide(cc, sc, srec, stable, dstable, snext);
+  __syncthreads();
+  if (s_slot >= 0 && s_slot < rec_cap) {
+    static_assert(sizeof(Record) % 8 == 0, "Record is copied in 8-byte words");
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&srec);
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(recs + s_slot);
+    for (int i = tid; i < int(sizeof(Record) / 8); i += kCtlThreads) dst[i] = src[i];
+  }
   {
     const int4* src = reinterpret_cast<const int4*>(&sc);
     int4* dst = reinterpret_cast<int4*>(ctrl);

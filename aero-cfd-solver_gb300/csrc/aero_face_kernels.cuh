@@ -67,14 +67,27 @@ __global__ void __launch_bounds__(256) k_face_flux(DevFaces<T> f, Cases<T> cs,
                                                    const typename Vec<T>::v4* __restrict__ gx,
                                                    const typename Vec<T>::v4* __restrict__ gy,
                                                    typename Vec<T>::v4* __restrict__ F, T* __restrict__ FS,
-                                                   int* __restrict__ fb_all) {
+                                                   int* __restrict__ fb_all, const LmSched* __restrict__ lms,
+                                                   int parity) {
   const int2 bd = cs.blk[blockIdx.x];  // face blocks: (case, end of the case's faces)
   const Ctrl* ctrl = cs.ctrl + bd.x;
   int* fb = fb_all + 4 * bd.x;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (ctrl->done) return;
   FaceParams<T> fp = cs.fp[bd.x];
-  if (LM) {
+  if (LM && lms) {  // the parity slot of this iteration's low-Mach weights
+    const LmSched& q = lms[2 * bd.x + parity];
+    fp.as_fix = q.as_fix;
+    if constexpr (sizeof(T) == 4) {
+      fp.stab_floor = q.stab_f;
+      fp.as_fmin = q.as_fmin_f;
+      fp.as_ramp = q.as_ramp_f;
+    } else {
+      fp.stab_floor = q.stab_floor;
+      fp.as_fmin = q.as_fmin;
+      fp.as_ramp = q.as_ramp;
+    }
+  } else if (LM) {
     fp.as_fix = ctrl->as_fix;
     if constexpr (sizeof(T) == 4) {
       fp.stab_floor = ctrl->stab_f;
@@ -189,13 +202,15 @@ struct ResidualLaunch {
   Partials part;
   int* fb;                 // [case][2]: fallback counters, stride 4 per case
   int global_dt;
+  const LmSched* lms = nullptr;  // parity slots of the low-Mach weights (null: read the controller)
+  int parity = 0;
 };
 
 template <class T, int FLUX, bool SECOND, bool LM>
 void launch_face_flux_t(const ResidualLaunch<T>& a) {
   const int grid = (a.faces.nf + a.block - 1) / a.block;
   k_face_flux<T, FLUX, SECOND, LM>
-      <<<grid, a.block, 0, a.st>>>(a.faces, a.face_cases, a.W, a.gx, a.gy, a.F, a.FS, a.fb);
+      <<<grid, a.block, 0, a.st>>>(a.faces, a.face_cases, a.W, a.gx, a.gy, a.F, a.FS, a.fb, a.lms, a.parity);
 }
 
 // Face pass, dispatched on the flux, order and low-Mach switches.

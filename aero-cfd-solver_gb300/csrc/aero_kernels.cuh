@@ -169,6 +169,30 @@ __host__ __device__ inline void apply_schedule(const CtrlConfig& cc, Ctrl* sp) {
   apply_schedule_from(cc, schedule_base(cc, sp->iter), sp);
 }
 
+// Low-Mach weights of one iteration's face passes under a schedule without the staged
+// controller (they then depend on the iteration index alone): the values apply_schedule
+// gives, kept per iteration parity so that an iteration's face passes can read them while
+// the previous iteration's controller is still running.
+struct LmSched {
+  int as_fix, pad;
+  double stab_floor, as_fmin, as_ramp;
+  float stab_f, as_fmin_f, as_ramp_f, pad_f;
+};
+__host__ __device__ inline LmSched lm_sched_of(const CtrlConfig& cc, int it) {
+  const SchedBase b = schedule_base(cc, it);
+  LmSched q;
+  q.as_fix = cc.as_fix_cfg;
+  q.pad = 0;
+  q.stab_floor = b.stab_floor;
+  q.as_fmin = cc.as_fmin;
+  q.as_ramp = b.as_ramp;
+  q.stab_f = float(q.stab_floor);
+  q.as_fmin_f = float(q.as_fmin);
+  q.as_ramp_f = float(q.as_ramp);
+  q.pad_f = 0.0f;
+  return q;
+}
+
 // Schedule values of a single residual evaluation (aero_residual and its no-allocation form).
 __host__ __device__ inline void set_eval_schedule(Ctrl* s, double stab, int as_fix, double as_fmin, double as_ramp) {
   s->stab_floor = stab;
@@ -1016,9 +1040,9 @@ struct Record {
 // The controller's serial work, split over lane 0 of the four warps (each warp on its own SM
 // sub-partition, so their double arithmetic proceeds side by side) in two phases:
 //   phase 1  ctl_forces    force coefficients and their stability window
-//            ctl_residual  residual monitor and adaptive CFL
-//            ctl_side      density-residual ratio, pressure-jump energies, the iteration-only
-//                          part of the next schedule
+//            ctl_residual  residual monitor, adaptive CFL, the iteration-only part of the
+//                          next schedule
+//            ctl_side      density-residual ratio, wall pressure-jump energy
 //            ctl_report    the record's reporting-only fields, fallback counters
 //   phase 2  ctl_decide    staged all-speed controller, stop rule, next schedule
 // Every value is formed by the same expression as in one serial pass
@@ -1066,21 +1090,25 @@ __device__ inline void ctl_report(const CtrlConfig& cc, const CtlIn& in, const C
   r.cd_abs = (fxa * cc.cos_a + fya * cc.sin_a) / qs;
   r.cl_abs = (-fxa * cc.sin_a + fya * cc.cos_a) / qs;
   r.cm_abs = fsum[6] / (qs * cc.chord);
+  // domain pressure-jump energy
+  const double pr2 = cc.pressure_ref * cc.pressure_ref + 1.0e-24;
+  r.pj = in.pj[1] > 0.0 ? (in.pj[0] / in.pj[1]) / pr2 : 0.0;
 }
 
-__device__ inline void ctl_side(const CtrlConfig& cc, const CtlIn& in, Ctrl& s, Record& r, SchedBase* next) {
-  *next = schedule_base(cc, s.iter + 1);
+__device__ inline void ctl_side(const CtrlConfig& cc, const CtlIn& in, Ctrl& s, Record& r, LmSched* lms) {
+  // the low-Mach weights of iteration iter + 2, read by that iteration's face passes
+  if (lms) lms[(s.iter + 2) & 1] = lm_sched_of(cc, s.iter + 2);
   // density-residual L2 ratio (the batched sweep's per-case stop rule)
   const double l2rho = smax(sqrt(in.a[3] / double(cc.n_cells > 0 ? cc.n_cells : 1)), 1.0e-20);
   if (s.initial_l2rho < 0.0) s.initial_l2rho = l2rho;
   r.rho_ratio = l2rho / smax(s.initial_l2rho, 1.0e-20);
-  // pressure-jump energies
+  // wall pressure-jump energy (the staged controller's input)
   const double pr2 = cc.pressure_ref * cc.pressure_ref + 1.0e-24;
-  r.pj = in.pj[1] > 0.0 ? (in.pj[0] / in.pj[1]) / pr2 : 0.0;
   r.pj_wall = in.pj[3] > 0.0 ? (in.pj[2] / in.pj[3]) / pr2 : 0.0;
 }
 
-__device__ inline void ctl_residual(const CtrlConfig& cc, const CtlIn& in, Ctrl& s, Record& r) {
+__device__ inline void ctl_residual(const CtrlConfig& cc, const CtlIn& in, Ctrl& s, Record& r, SchedBase* next) {
+  *next = schedule_base(cc, s.iter + 1);
   const double l2 = sqrt(in.a[1] / double(cc.n_cells > 0 ? 5 * cc.n_cells : 1));
   r.l2 = l2;
   // ConvergenceMonitor::update_residual
@@ -1255,10 +1283,12 @@ constexpr int kCtlThreads = 128;
 static_assert(sizeof(Ctrl) % 16 == 0, "Ctrl is copied in 16-byte words");
 // One block per case: ccs[case], ctrls[case], records recs[case * rec_cap ...], fallback
 // counters fb[4 * case + 0/1] (fb already offset by the iteration's parity).
+// lms_all (may be null): per case, the two parity slots of LmSched.
 static __global__ void __launch_bounds__(kCtlThreads) k_control(const CtrlConfig* __restrict__ ccs, Partials part,
                                                                 Ctrl* __restrict__ ctrls,
                                                                 Record* __restrict__ recs_all, int rec_cap,
-                                                                int* __restrict__ fb_all) {
+                                                                int* __restrict__ fb_all,
+                                                                LmSched* __restrict__ lms_all) {
   constexpr int kWarps = kCtlThreads / 32;
   const CtrlConfig cc = ccs[blockIdx.x];
   Ctrl* ctrl = ctrls + blockIdx.x;
@@ -1411,9 +1441,9 @@ static __global__ void __launch_bounds__(kCtlThreads) k_control(const CtrlConfig
   if (tid == 0) {
     ctl_forces(cc, s_in, sc, srec, &stable, &dstable);
   } else if (tid == 32) {
-    ctl_residual(cc, s_in, sc, srec);
+    ctl_residual(cc, s_in, sc, srec, &snext);
   } else if (tid == 64) {
-    ctl_side(cc, s_in, sc, srec, &snext);
+    ctl_side(cc, s_in, sc, srec, lms_all ? lms_all + 2 * blockIdx.x : nullptr);
   } else if (tid == 96) {
     ctl_report(cc, s_in, sc, srec, fb);
   }

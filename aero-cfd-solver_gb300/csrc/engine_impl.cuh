@@ -366,9 +366,16 @@ class EngineT final : public Engine {
     face_cases_ = Cases<T>{fblk_, ctrls_, fps_dev_, pcs_dev_, mcs_dev_};
 
     // the controller of iteration i runs beside the gradient and first face pass of
-    // iteration i+1 (which need none of its outputs) when the residual reads no
-    // controller-scheduled low-Mach weights and the first stage's residual is not stored
-    defer_control_ = c0.rk_stages > 1 && !lm_;
+    // iteration i+1 (which need none of its outputs) for RK3 runs; with low-Mach weights in
+    // the residual only when no case runs the staged all-speed controller, whose weights
+    // depend on the previous iteration: the others depend on the iteration index alone and
+    // reach the face passes through two parity slots that the controller fills two
+    // iterations ahead
+    bool staged_any = false;
+    for (int k = 0; k < K_; ++k) staged_any = staged_any || ccs_[k].staged != 0;
+    defer_control_ = c0.rk_stages > 1 && (!lm_ || !staged_any);
+    lm_defer_ = defer_control_ && lm_;
+    if (lm_defer_) lms_ = alloc<LmSched>(2 * static_cast<size_t>(K_));
     if (defer_control_) {
       AERO_CK(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
       AERO_CK(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
@@ -1625,12 +1632,17 @@ class EngineT final : public Engine {
         AERO_CK(cudaEventRecord(ev_fork_, st_));
         AERO_CK(cudaStreamWaitEvent(side_, ev_fork_, 0));
         wrap(5, [&] {
-          k_control<<<K_, kCtlThreads, 0, side_>>>(ccs_dev_, part_, ctrls_, recs_, rec_cap_, fb_ + 2 * (parity ^ 1));
+          k_control<<<K_, kCtlThreads, 0, side_>>>(ccs_dev_, part_, ctrls_, recs_, rec_cap_, fb_ + 2 * (parity ^ 1),
+                                                   lm_defer_ ? lms_ : nullptr);
         });
         AERO_CK(cudaEventRecord(ev_join_, side_));
       }
       if (second) wrap(0, [&] { k_gradient<T><<<ncb_, block_, 0, st_>>>(dm_, W_, gx_, gy_, cell_cases_); });
-      const ResidualLaunch<T> ra = residual_args(fb, R, SR, global_dt);
+      ResidualLaunch<T> ra = residual_args(fb, R, SR, global_dt);
+      if (defer && lm_defer_) {
+        ra.lms = lms_;
+        ra.parity = parity;
+      }
       wrap(1, [&] { launch_face_pass(ra, cfg_[0].flux, second, lm_ != 0); });
       if (global_dt) wrap(1, [&] { launch_gather_pass(ra, last); });
       if (stage == 0 && pending) AERO_CK(cudaStreamWaitEvent(st_, ev_join_, 0));
@@ -1656,7 +1668,10 @@ class EngineT final : public Engine {
   }
   template <class Wrap>
   void launch_control(int parity, Wrap&& wrap) {
-    wrap(5, [&] { k_control<<<K_, kCtlThreads, 0, st_>>>(ccs_dev_, part_, ctrls_, recs_, rec_cap_, fb_ + 2 * parity); });
+    wrap(5, [&] {
+      k_control<<<K_, kCtlThreads, 0, st_>>>(ccs_dev_, part_, ctrls_, recs_, rec_cap_, fb_ + 2 * parity,
+                                             lm_defer_ ? lms_ : nullptr);
+    });
   }
 
   // Iterations it0 .. it0+n-1 back to back, through the per-iteration CUDA graphs; with the
@@ -1665,6 +1680,13 @@ class EngineT final : public Engine {
   // `after(j)` after it (timing marks, L2 flushes).
   template <class Before, class After>
   void launch_iterations(int it0, int n, Before&& between, After&& after) {
+    if (lm_defer_ && n > 0) {  // the low-Mach weights of the first two iterations
+      std::vector<LmSched> q(2 * static_cast<size_t>(K_));
+      for (int k = 0; k < K_; ++k) {
+        for (int it = it0; it < it0 + 2; ++it) q[2 * k + (it & 1)] = lm_sched_of(ccs_[k], it);
+      }
+      AERO_CK(cudaMemcpyAsync(lms_, q.data(), sizeof(LmSched) * q.size(), cudaMemcpyHostToDevice, st_));
+    }
     for (int j = 0; j < n; ++j) {
       const int it = it0 + j;
       between(j);
@@ -1763,6 +1785,8 @@ class EngineT final : public Engine {
   DevMesh<T> dm_{};
   cudaGraphExec_t graph_[16] = {};
   bool defer_control_ = false;
+  bool lm_defer_ = false;      // deferred controller with low-Mach weights from parity slots
+  LmSched* lms_ = nullptr;     // [case][2] low-Mach weights by iteration parity
   // discrete adjoint (FP64)
   bool adj_alloc_ = false, adj_ready_ = false, adj_second_ = false;
   double adj_wcd_ = 0.0, adj_wcl_ = 0.0, adj_ex_ = 0.0, adj_ey_ = 0.0;

@@ -386,6 +386,16 @@ __device__ __forceinline__ T warp_max_t(T x) {
   for (int o = 16; o > 0; o >>= 1) x = smax(x, __shfl_xor_sync(0xffffffffu, x, o));
   return x;
 }
+// Warp maximum of values that are >= 0 (or NaN): for float one warp-reduce instruction on the
+// bit patterns, which order like the values; a NaN lane makes the result NaN.
+template <class T>
+__device__ __forceinline__ T warp_max_nonneg(T x) {
+  if constexpr (sizeof(T) == 4) {
+    return __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(x)));
+  } else {
+    return warp_max_t(x);
+  }
+}
 
 // Residual of cell c from the per-face fluxes: +-F*A over its faces in ascending original
 // face order, and the sum of the faces' wave-speed terms. The slots are read first so the
@@ -442,7 +452,7 @@ __device__ void block_norms(T (&q)[kNorm], Partials part) {
   __shared__ T shn[kNorm][32];
   q[0] = warp_sum_t(q[0]);
   q[1] = warp_sum_t(q[1]);
-  q[2] = warp_max_t(q[2]);
+  q[2] = warp_max_nonneg(q[2]);
   q[3] = warp_sum_t(q[3]);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
   if (lane == 0) {
@@ -502,7 +512,7 @@ __device__ void block_monitors(bool valid, const Prim<T>& w, int c, const Monito
     }
   }
 #pragma unroll
-  for (int k = 0; k < kMon; ++k) mon[k] = warp_max_t(mon[k]);
+  for (int k = 0; k < kMon; ++k) mon[k] = warp_max_nonneg(mon[k]);
   if (lane == 0) {
 #pragma unroll
     for (int k = 0; k < kMon; ++k) shf[k][wid] = mon[k];

@@ -2,7 +2,7 @@
 
 The gradient is the discrete adjoint of the FP64 device residual (include/aero_adjoint.h):
 the primal is converged on the deformed mesh, (dR/dU)^T lam = -dJ/dU is solved with the
-primal's pseudo-time smoother, and
+primal's pseudo-time smoother (or GMRES preconditioned by it), and
 
     dJ/d(alpha) = dJ/d(alpha)|_U + lam^T dR/d(alpha)          (far-field state)
     dJ/d(a_k)   = dJ/dX . m_k   + lam^T (dR/dX . m_k)          (m_k: Hicks-Henne mode k)
@@ -63,10 +63,13 @@ class ShapeProblem:
     max_iters: int = 200000
     rho_target: float = 1e-12
     chunk: int = 5000
-    adjoint_max_iters: int = 4000
+    adjoint_max_iters: int = 400000
     adjoint_tol: float = 1e-10
     adjoint_cfl: float | None = None
-    adjoint_method: str = "krylov"  # or "smoother" (the RK3 pseudo-time iteration alone)
+    # "smoother": the primal's RK3 pseudo-time iteration, which converges at the primal's rate
+    # wherever the primal converged; "krylov": GMRES preconditioned by smoother sweeps
+    # (adjoint_max_iters then counts Arnoldi steps)
+    adjoint_method: str = "smoother"
     krylov_restart: int = 40
     krylov_smooth: int = 10
     primal_precision: int = capi.PRECISION_FP64

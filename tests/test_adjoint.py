@@ -141,7 +141,7 @@ def _problem(flux, limiter, mach=0.5, nc=64, nr=16, first_order=False):
                           startup_first_order_iters=10 ** 9 if first_order else 20, cfl_max=0.8,
                           precision=capi.PRECISION_FP64)
     return ShapeProblem(mesh, case, peaks=[0.3, 0.6], upper=[1, 0], width=3.0, max_iters=60000, rho_target=1e-13,
-                        adjoint_max_iters=3000, adjoint_tol=1e-12)
+                        adjoint_max_iters=3000, adjoint_tol=1e-12, adjoint_method="krylov")
 
 
 def test_gradients_against_converged_differences():

@@ -313,7 +313,8 @@ class Solver:
         N*5 values) is filled and returned instead of a new array when given."""
         if out is None:
             out = np.empty((self.n, 5), np.float64)
-        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == 5 * self.n
+        if not (out.dtype == np.float64 and out.flags.c_contiguous and out.flags.writeable and out.size == 5 * self.n):
+            raise ValueError("get_state: out must be a writable C-contiguous float64 array of N*5 values")
         self._check(self.lib.aero_get_state(self.h, out.ctypes.data_as(_dp)))
         return out.reshape(self.n, 5)
 

@@ -334,3 +334,36 @@ def test_run_stops_at_convergence_like_the_monitor():
     _, orec = o.run(50)
     assert len(rec) == len(orec) == 5
     assert rec["flags"][-1] & capi.REC_CONVERGED
+
+
+@pytest.mark.parametrize("precision", [capi.PRECISION_FP64, capi.PRECISION_FP32])
+def test_host_state_exchange_paths_agree(precision, monkeypatch):
+    """aero_set_state / aero_get_state through the in-place device access of the host array
+    and through the pinned staging buffer (AERO_HOST_STAGING=1, read at context creation)
+    move the same values: states, and the runs continued from them, are identical."""
+    mesh = aero_gb300.ogrid_synthetic(64, 16, seed=12)
+    case = capi.make_case(mach=0.6, flux=1, limiter=1, startup_first_order_iters=3, precision=precision)
+    rng = np.random.default_rng(3)
+    outs = []
+    for staging in ("0", "1"):
+        monkeypatch.setenv("AERO_HOST_STAGING", staging)
+        with aero_gb300.Solver(mesh, case) as s:
+            s.run(10)
+            u = s.get_state()
+            u = u * (1.0 + 1e-3 * rng.standard_normal(u.shape)) if staging == "0" else outs[0][0]
+            u[:, 3] = 0.0
+            s.set_state(u)
+            back = s.get_state()
+            buf = np.full_like(back, np.nan)
+            s.get_state(out=buf)
+            _, rec = s.run(10)
+            outs.append((u, back, buf, s.get_state(), rec["cl"]))
+    u, back0, buf0, end0, cl0 = outs[0]
+    _, back1, buf1, end1, cl1 = outs[1]
+    if precision == capi.PRECISION_FP64:
+        np.testing.assert_array_equal(back0, u)  # the double state round-trips exactly
+    np.testing.assert_array_equal(back0, back1)
+    np.testing.assert_array_equal(buf0, back0)
+    np.testing.assert_array_equal(buf1, back1)
+    np.testing.assert_array_equal(end0, end1)
+    np.testing.assert_array_equal(cl0, cl1)

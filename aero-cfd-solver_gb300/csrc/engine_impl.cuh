@@ -12,6 +12,7 @@
 #pragma once
 
 #include "aero_adjoint.cuh"
+#include "aero_tma.cuh"
 #include "aero_face_kernels.cuh"
 #include "engine.hpp"
 
@@ -345,6 +346,28 @@ class EngineT final : public Engine {
     dg_.n = ntot_;
     dg_.d = d_;
     dg_.inv_vol = inv_vol_;
+    // the gradient pass of the iterations: persistent CTAs streaming their tiles through
+    // shared memory with bulk copies, where each CTA gets two or more tiles
+    // (AERO_BULK_COPY=0 never, =1 always)
+    {
+      const char* env = std::getenv("AERO_BULK_COPY");
+      const int mode = (env && env[0] == '0') ? 0 : ((env && env[0] == '1') ? 1 : -1);
+      grad_smem_ = grad_tma_smem<T>(block_, d_);
+      int dev = 0, sms = 0, per_sm = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (grad_smem_ > 48 * 1024) {
+        AERO_CK(cudaFuncSetAttribute(k_gradient_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(grad_smem_)));
+      }
+      AERO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gradient_tma<T>, block_, grad_smem_));
+      grad_grid_ = std::min(ncb_, std::max(1, per_sm) * std::max(1, sms));
+      // the copies of a CTA's next tile overlap its current one only with two or more tiles
+      // per CTA; below that the plain gather kernel is as fast
+      grad_tma_ = mode == 1 || (mode == -1 && ncb_ >= 2 * grad_grid_);
+      tma_err_ = alloc<int>(1);
+      AERO_CK(cudaMemsetAsync(tma_err_, 0, sizeof(int), st_));
+    }
 
     // ---- per-case constants
     ccs_.resize(K_);
@@ -641,6 +664,11 @@ class EngineT final : public Engine {
     }
     for (const Ctrl& c : host_ctrls_) {
       if (c.nonfinite) status = AERO_ERR_NONFINITE;
+    }
+    {
+      int terr = 0;
+      AERO_CK(cudaMemcpy(&terr, tma_err_, sizeof(int), cudaMemcpyDeviceToHost));
+      if (terr) status = AERO_ERR_TIMEOUT;
     }
     if (err_ != cudaSuccess) status = AERO_ERR_CUDA;
     if (n_done) {
@@ -1637,7 +1665,15 @@ class EngineT final : public Engine {
         });
         AERO_CK(cudaEventRecord(ev_join_, side_));
       }
-      if (second) wrap(0, [&] { k_gradient<T><<<ncb_, block_, 0, st_>>>(dm_, W_, gx_, gy_, cell_cases_); });
+      if (second) {
+        wrap(0, [&] {
+          if (grad_tma_) {
+            k_gradient_tma<T><<<grad_grid_, block_, grad_smem_, st_>>>(dm_, W_, gx_, gy_, cell_cases_, ncb_, tma_err_);
+          } else {
+            k_gradient<T><<<ncb_, block_, 0, st_>>>(dm_, W_, gx_, gy_, cell_cases_);
+          }
+        });
+      }
       ResidualLaunch<T> ra = residual_args(fb, R, SR, global_dt);
       if (defer && lm_defer_) {
         ra.lms = lms_;
@@ -1758,6 +1794,10 @@ class EngineT final : public Engine {
   int* perm_dev_ = nullptr;  // case 0: new -> original cell
   int* perm_all_dev_ = nullptr;  // every case's new -> original cell, at the case's cell offset
   bool host_direct_ = false;     // the GPU reads and writes host state arrays in place
+  bool grad_tma_ = false;        // gradient pass through bulk copies into shared memory
+  size_t grad_smem_ = 0;
+  int grad_grid_ = 0;
+  int* tma_err_ = nullptr;       // set by a kernel whose bounded wait on a copy expired
   int2* cblk_ = nullptr;     // per cell block: (case, end of the case's cells)
   int2* fblk_ = nullptr;     // per face block: (case, end of the case's faces)
   int* srfirst_ = nullptr;   // per case: first per-warp time-step partial, [K + 1]

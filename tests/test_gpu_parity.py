@@ -371,14 +371,18 @@ def test_host_state_exchange_paths_agree(precision, monkeypatch):
 
 @pytest.mark.parametrize("precision", [capi.PRECISION_FP64, capi.PRECISION_FP32])
 @pytest.mark.parametrize("block", [64, 128, 256])
-def test_bulk_copy_gradient_matches_the_gather_kernel(precision, block, monkeypatch):
+@pytest.mark.parametrize("low_mach", [False, True])
+def test_bulk_copy_gradient_matches_the_gather_kernel(precision, block, low_mach, monkeypatch):
     """The gradient pass that streams each cell block's slot table and states into shared
     memory with bulk copies (persistent CTAs, two buffers) gives the same runs as the plain
-    gather kernel, bit for bit, on triangles and quads and every block size."""
+    gather kernel, bit for bit: triangles and quads, every block size, with and without the
+    low-Mach features."""
+    lm = dict(precond_on=1, low_mach_fix=1, all_speed_flux_fix=1, precond_farfield_bc=1, mach=0.2) if low_mach \
+        else dict(mach=0.7)
     for cell_type in (3, 4):
         mesh = aero_gb300.ogrid_synthetic(96, 24, cell_type=cell_type, permute=True, jitter=0.1, seed=21)
-        case = capi.make_case(mach=0.7, flux=1, limiter=1, startup_first_order_iters=3, precision=precision,
-                              block_size=block)
+        case = capi.make_case(flux=1, limiter=1, startup_first_order_iters=3, precision=precision,
+                              block_size=block, **lm)
         outs = []
         for mode in ("0", "1"):
             monkeypatch.setenv("AERO_BULK_COPY", mode)

@@ -18,44 +18,49 @@ namespace aero {
 // flux *f and wave-speed term *mws (per unit length). *fo: first-order fallback taken, *df:
 // diffusive fallback taken. Templated on the real type: the face pass runs it in float or
 // double and the adjoint linearisation in dual numbers.
+//
+// Interior, far-field and wall faces share one face-state setup, one acoustic-scale call and
+// one flux call: a warp holding faces of several kinds runs the flux once, not once per kind.
+// Each face's arithmetic is the reference's, operation for operation.
 template <class T, int FLUX, bool SECOND, bool LM>
 __device__ __forceinline__ void eval_face(const FaceParams<T>& fp, int b, const Prim<T>& wo, const Prim<T>& wn,
                                           const T (&gO)[8], const T (&gN)[8], T nx, T ny, T dox, T doy, T dnx,
                                           T dny, Flux<T>* f, T* mws, bool* fo, bool* df) {
+  Prim<T> L = wo, Rt = wn;
+  if (SECOND && b >= 0) {
+    muscl_var(fp.limiter, wo.r, wn.r, gO[0], gO[4], gN[0], gN[4], dox, doy, dnx, dny, &L.r, &Rt.r);
+    muscl_var(fp.limiter, wo.u, wn.u, gO[1], gO[5], gN[1], gN[5], dox, doy, dnx, dny, &L.u, &Rt.u);
+    muscl_var(fp.limiter, wo.v, wn.v, gO[2], gO[6], gN[2], gN[6], dox, doy, dnx, dny, &L.v, &Rt.v);
+    muscl_var(fp.limiter, wo.p, wn.p, gO[3], gO[7], gN[3], gN[7], dox, doy, dnx, dny, &L.p, &Rt.p);
+    L.r = smax(L.r, Kn<T>::rho_floor);
+    Rt.r = smax(Rt.r, Kn<T>::rho_floor);
+    L.p = smax(L.p, Kn<T>::p_floor);
+    Rt.p = smax(Rt.p, Kn<T>::p_floor);
+    if (!valid_prim(L) || !valid_prim(Rt)) {
+      L = wo;
+      Rt = wn;
+      *fo = true;
+    }
+  }
+  // owner side: the reconstructed state (interior) or the cell state (boundary); the other
+  // side: the neighbour's, the free stream (far field) or the owner's own (slip wall)
+  const Cons<T> cl = prim_to_cons(L, fp.gamma);
+  Cons<T> cr = cl;
   if (b >= 0) {
-    Prim<T> L = wo, Rt = wn;
-    if (SECOND) {
-      muscl_var(fp.limiter, wo.r, wn.r, gO[0], gO[4], gN[0], gN[4], dox, doy, dnx, dny, &L.r, &Rt.r);
-      muscl_var(fp.limiter, wo.u, wn.u, gO[1], gO[5], gN[1], gN[5], dox, doy, dnx, dny, &L.u, &Rt.u);
-      muscl_var(fp.limiter, wo.v, wn.v, gO[2], gO[6], gN[2], gN[6], dox, doy, dnx, dny, &L.v, &Rt.v);
-      muscl_var(fp.limiter, wo.p, wn.p, gO[3], gO[7], gN[3], gN[7], dox, doy, dnx, dny, &L.p, &Rt.p);
-      L.r = smax(L.r, Kn<T>::rho_floor);
-      Rt.r = smax(Rt.r, Kn<T>::rho_floor);
-      L.p = smax(L.p, Kn<T>::p_floor);
-      Rt.p = smax(Rt.p, Kn<T>::p_floor);
-      if (!valid_prim(L) || !valid_prim(Rt)) {
-        L = wo;
-        Rt = wn;
-        *fo = true;
-      }
-    }
-    const Cons<T> cl = prim_to_cons(L, fp.gamma), cr = prim_to_cons(Rt, fp.gamma);
-    const T as = face_acoustic_scale<T, LM>(cl, cr, fp);
-    *f = face_flux<T, FLUX, LM>(cl, cr, nx, ny, fp, as, mws, df);
+    cr = prim_to_cons(Rt, fp.gamma);
+  } else if (b != -2) {
+    cr = fp.farfield;
+  }
+  const T as = face_acoustic_scale<T, LM>(cl, cr, fp);
+  if (b == -2) {  // slip wall: pressure-only flux (boundary_conditions.cpp:97-110)
+    const Prim<T> w = cons_to_prim(cl, fp.gamma);
+    const T un = w.u * nx + w.v * ny;
+    const T a = sound_speed(w, fp.gamma);
+    *f = Flux<T>{T(0), w.p * nx, w.p * ny, T(0)};
+    *mws = precond_speeds(un, a, as).sr;
   } else {
-    const Cons<T> in = prim_to_cons(wo, fp.gamma);
-    if (b == -2) {  // slip wall: pressure-only flux (boundary_conditions.cpp:97-110)
-      const T as = face_acoustic_scale<T, LM>(in, in, fp);
-      const Prim<T> w = cons_to_prim(in, fp.gamma);
-      const T un = w.u * nx + w.v * ny;
-      const T a = sound_speed(w, fp.gamma);
-      *f = Flux<T>{T(0), w.p * nx, w.p * ny, T(0)};
-      *mws = precond_speeds(un, a, as).sr;
-    } else {
-      const T as = face_acoustic_scale<T, LM>(in, fp.farfield, fp);
-      const Cons<T> bs = fp.precond_farfield_bc ? precond_farfield_state(in, nx, ny, fp, as) : fp.farfield;
-      *f = face_flux<T, FLUX, LM>(in, bs, nx, ny, fp, as, mws, df);
-    }
+    if (b < 0 && fp.precond_farfield_bc) cr = precond_farfield_state(cl, nx, ny, fp, as);
+    *f = face_flux<T, FLUX, LM>(cl, cr, nx, ny, fp, as, mws, df);
   }
 }
 

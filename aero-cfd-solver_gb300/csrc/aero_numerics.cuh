@@ -38,6 +38,35 @@ template <class T>
 __host__ __device__ __forceinline__ T sclamp(T v, T lo, T hi) {
   return (v < lo) ? lo : ((hi < v) ? hi : v);
 }
+// Float on the device: the hardware's NaN-propagating max / min (one instruction where the
+// forms above take a compare and a select). Equal to them for every pair of numbers, up to
+// the sign of a zero result; a NaN in either operand gives NaN, where std::max(a, NaN) gives
+// a. A NaN operand only arises from a non-finite state, which the non-finite trap stops
+// either way. sclamp is max-then-min, equal to the form above whenever lo <= hi (every use).
+template <>
+__host__ __device__ __forceinline__ float smax<float>(float a, float b) {
+#ifdef __CUDA_ARCH__
+  float r;
+  asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+#else
+  return (a < b) ? b : a;
+#endif
+}
+template <>
+__host__ __device__ __forceinline__ float smin<float>(float a, float b) {
+#ifdef __CUDA_ARCH__
+  float r;
+  asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+#else
+  return (b < a) ? b : a;
+#endif
+}
+template <>
+__host__ __device__ __forceinline__ float sclamp<float>(float v, float lo, float hi) {
+  return smin<float>(smax<float>(v, lo), hi);
+}
 template <class T>
 __host__ __device__ __forceinline__ T sabs(T x) {
   return fabs(x);

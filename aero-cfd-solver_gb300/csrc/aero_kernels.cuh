@@ -548,7 +548,7 @@ __device__ void block_monitors(bool valid, const Prim<T>& w, int c, const Monito
         }
         if (kind & 2) {  // euler_solver.cpp:976-1006
           v[8] = smax(v[8], fabs(w.u * wnx[j] + w.v * wny[j]));
-          const T cp = gp / q_inf;
+          const T cp = sdiv(gp, q_inf);
           if (isfinite(cp)) {
             v[9] = smax(v[9], cp);
             v[10] = smax(v[10], -cp);
@@ -709,25 +709,152 @@ __device__ __forceinline__ void cell_gradient(const DevMesh<T>& m, const typenam
   oy.x = ay0 * inv; oy.y = ay1 * inv; oy.z = ay2 * inv; oy.w = ay3 * inv;
 }
 
-template <class T>
+// The Green-Gauss gradients of CPT cells per thread (cell_gradient's arithmetic, same order
+// per cell), their slot and neighbour loads issued together. on[j]: cell c[j] is computed.
+template <class T, int CPT>
+__device__ __forceinline__ void cell_gradients(const DevMesh<T>& m, const typename Vec<T>::v4* __restrict__ W,
+                                               const int (&c)[CPT], const bool (&on)[CPT],
+                                               typename Vec<T>::v4 (&gxo)[CPT], typename Vec<T>::v4 (&gyo)[CPT],
+                                               const typename Vec<T>::v4* sW, int base, int nsw) {
+  using V2 = typename Vec<T>::v2;
+  using V4 = typename Vec<T>::v4;
+  V4 wc[CPT];
+  T ax[CPT][4], ay[CPT][4];
+  bool live[CPT];
+#pragma unroll
+  for (int j = 0; j < CPT; ++j) {
+    live[j] = on[j];
+    if (on[j]) wc[j] = sW[c[j] - base];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) ax[j][v] = ay[j][v] = T(0);
+  }
+  constexpr int kU = 4;
+  for (int k0 = 0; k0 < m.d; k0 += kU) {
+    int lk[CPT][kU];
+    V2 nd[CPT][kU];
+    T ar[CPT][kU];
+    V4 wo[CPT][kU];
+#pragma unroll
+    for (int j = 0; j < CPT; ++j)
+#pragma unroll
+      for (int u = 0; u < kU; ++u) lk[j][u] = (live[j] && k0 + u < m.d) ? m.link[(k0 + u) * m.n + c[j]] : kPad;
+#pragma unroll
+    for (int j = 0; j < CPT; ++j)
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        if (live[j] && k0 + u < m.d) {
+          const int s = (k0 + u) * m.n + c[j];
+          nd[j][u] = m.nrm[s];
+          ar[j][u] = m.area[s];
+        }
+      }
+#pragma unroll
+    for (int j = 0; j < CPT; ++j)
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        if (lk[j][u] >= 0) {
+          const int o = lk[j][u] >> 1;
+          const unsigned off = static_cast<unsigned>(o - base);
+          wo[j][u] = off < static_cast<unsigned>(nsw) ? sW[off] : W[o];
+        } else {
+          wo[j][u] = wc[j];
+        }
+      }
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) {
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int link = lk[j][u];
+        if (link == kPad) break;
+        const T nax = nd[j][u].x * ar[j][u], nay = nd[j][u].y * ar[j][u];
+        T q0 = wc[j].x, q1 = wc[j].y, q2 = wc[j].z, q3 = wc[j].w;
+        bool minus = false;
+        if (link >= 0) {
+          q0 = T(0.5) * (q0 + wo[j][u].x);
+          q1 = T(0.5) * (q1 + wo[j][u].y);
+          q2 = T(0.5) * (q2 + wo[j][u].z);
+          q3 = T(0.5) * (q3 + wo[j][u].w);
+          minus = (link & 1) != 0;
+        }
+        if (minus) {
+          ax[j][0] -= q0 * nax; ay[j][0] -= q0 * nay;
+          ax[j][1] -= q1 * nax; ay[j][1] -= q1 * nay;
+          ax[j][2] -= q2 * nax; ay[j][2] -= q2 * nay;
+          ax[j][3] -= q3 * nax; ay[j][3] -= q3 * nay;
+        } else {
+          ax[j][0] += q0 * nax; ay[j][0] += q0 * nay;
+          ax[j][1] += q1 * nax; ay[j][1] += q1 * nay;
+          ax[j][2] += q2 * nax; ay[j][2] += q2 * nay;
+          ax[j][3] += q3 * nax; ay[j][3] += q3 * nay;
+        }
+      }
+      if (lk[j][kU - 1] == kPad) live[j] = false;
+    }
+    bool more = false;
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) more = more || live[j];
+    if (!more) break;
+  }
+#pragma unroll
+  for (int j = 0; j < CPT; ++j) {
+    if (!on[j]) continue;
+    const T inv = m.inv_vol[c[j]];
+    gxo[j].x = ax[j][0] * inv; gxo[j].y = ax[j][1] * inv; gxo[j].z = ax[j][2] * inv; gxo[j].w = ax[j][3] * inv;
+    gyo[j].x = ay[j][0] * inv; gyo[j].y = ay[j][1] * inv; gyo[j].z = ay[j][2] * inv; gyo[j].w = ay[j][3] * inv;
+  }
+}
+
+// Gradient pass. CPT (cells per thread, 1 or 2): a block of B threads covers CPT cell blocks
+// (nblk: cell blocks in all, for CPT > 1); thread t computes cells t, t + B, ... of them.
+template <class T, int CPT = 1>
 __global__ void __launch_bounds__(256) k_gradient(DevMesh<T> m, const typename Vec<T>::v4* __restrict__ W,
                                                   typename Vec<T>::v4* __restrict__ gx,
-                                                  typename Vec<T>::v4* __restrict__ gy, Cases<T> cs) {
+                                                  typename Vec<T>::v4* __restrict__ gy, Cases<T> cs, int nblk = 0) {
   // the block's own cells' W staged in shared memory: with the cells in Morton / RCM order
   // most neighbours fall inside the block, and their loads no longer go to L2
-  __shared__ typename Vec<T>::v4 sW[256];
-  const int2 bd = cs.blk[blockIdx.x];
-  const int base = blockIdx.x * blockDim.x;
-  const int c = base + threadIdx.x;
-  if (cs.ctrl[bd.x].done) return;  // uniform over the block (one case per block)
-  const int nsw = min(static_cast<int>(blockDim.x), bd.y - base);
-  if (threadIdx.x < nsw) sW[threadIdx.x] = W[c];
-  __syncthreads();
-  if (c >= bd.y) return;
-  typename Vec<T>::v4 ox, oy;
-  cell_gradient<T>(m, W, c, &ox, &oy, sW, base, nsw);
-  gx[c] = ox;
-  gy[c] = oy;
+  __shared__ typename Vec<T>::v4 sW[256 * CPT];
+  if constexpr (CPT == 1) {
+    const int2 bd = cs.blk[blockIdx.x];
+    const int base = blockIdx.x * blockDim.x;
+    const int c = base + threadIdx.x;
+    if (cs.ctrl[bd.x].done) return;  // uniform over the block (one case per block)
+    const int nsw = min(static_cast<int>(blockDim.x), bd.y - base);
+    if (threadIdx.x < nsw) sW[threadIdx.x] = W[c];
+    __syncthreads();
+    if (c >= bd.y) return;
+    typename Vec<T>::v4 ox, oy;
+    cell_gradient<T>(m, W, c, &ox, &oy, sW, base, nsw);
+    gx[c] = ox;
+    gy[c] = oy;
+  } else {
+    const int B = blockDim.x, lb0 = blockIdx.x * CPT;
+    const int base = lb0 * B;
+    const int nlb = min(CPT, nblk - lb0);
+    // every cell of the covered blocks (padding included: in bounds, never a neighbour)
+    const int nsw = nlb * B;
+    for (int i = threadIdx.x; i < nsw; i += B) sW[i] = W[base + i];
+    __syncthreads();
+    int c[CPT];
+    bool on[CPT];
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) {
+      c[j] = base + j * B + static_cast<int>(threadIdx.x);
+      on[j] = false;
+      if (j < nlb) {
+        const int2 bd = cs.blk[lb0 + j];
+        on[j] = c[j] < bd.y && !cs.ctrl[bd.x].done;
+      }
+    }
+    typename Vec<T>::v4 ox[CPT], oy[CPT];
+    cell_gradients<T, CPT>(m, W, c, on, ox, oy, sW, base, nsw);
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) {
+      if (on[j]) {
+        gx[c[j]] = ox[j];
+        gy[c[j]] = oy[j];
+      }
+    }
+  }
 }
 
 // MUSCL on one variable (reconstruction.cpp:183-193)
@@ -762,7 +889,7 @@ static __global__ void k_srmax(const double* __restrict__ srmax, const int* __re
 // total and above twice the pressure floor, so the double clamp can be skipped. NaN fails.
 __device__ __forceinline__ bool positivity_safe(const Cons<float>& f, float gm1) {
   if (!(f.r > 2.0e-8f)) return false;
-  const float inv = 1.0f / f.r;
+  const float inv = sdiv(1.0f, f.r);
   const float u = f.ru * inv, v = f.rv * inv;
   const float ke = 0.5f * f.r * (u * u + v * v);
   const float e = f.rE - ke;
@@ -852,7 +979,7 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
       fpf.pc_beta_max = pc.beta_max_f;
       const float beta = cell_beta(w, fpf);
       const float b2 = beta * beta;
-      const float inv_rho = 1.0f / smax(w.r, 1.0e-8f);
+      const float inv_rho = sdiv(1.0f, smax(w.r, 1.0e-8f));
       const float ud = fmaf(w.u, float(r1), w.v * float(r2));
       r3 = T(fmaf(b2, float(r3), (b2 - 1.0f) * inv_rho * ud));
     } else if (PRECOND) {  // energy row of the preconditioned residual, in double
@@ -873,10 +1000,10 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
     const T cfl = (sizeof(T) == 4) ? T(ctrl->cfl_f) : T(ctrl->cfl);
     T dt;
     if (global_dt) {
-      dt = cfl / T(ctrl->sr_max);
+      dt = sdiv(cfl, T(ctrl->sr_max));
       if (!sfinite(dt)) dt = T(0);
     } else {
-      dt = cfl / smax(src, Kn<T>::wave_floor);
+      dt = sdiv(cfl, smax(src, Kn<T>::wave_floor));
     }
     if constexpr (sizeof(T) == 4) {
       float d0, d1, d2, d3;

@@ -178,6 +178,7 @@ void aero_case_defaults(aero_case_desc* c) {
   c->block_size = 0;
   c->diagnostics = 0;
   c->density_l2_target = 0.0;
+  c->cells_per_thread = 0;
 }
 
 }  // extern "C"
@@ -397,14 +398,17 @@ int aero_autotune(const aero_mesh_desc* mesh, const aero_case_desc* c, int iters
     return fail(nullptr, AERO_ERR_INVALID, "aero_autotune: bad argument");
   const int orders[2] = {AERO_ORDER_MORTON, AERO_ORDER_RCM};
   const int blocks[3] = {64, 128, 256};
+  const int cpts[2] = {1, 2};
   double best_ms = 0.0;
   int k = 0;
   *best = *c;
   for (int o : orders) {
     for (int b : blocks) {
+     for (int t : cpts) {
       aero_case_desc v = *c;
       v.ordering = o;
       v.block_size = b;
+      v.cells_per_thread = t;
       aero_ctx* ctx = nullptr;
       int rc = create_ctx(1, mesh, &v, &ctx);
       if (rc != AERO_OK) return rc;
@@ -422,8 +426,10 @@ int aero_autotune(const aero_mesh_desc* mesh, const aero_case_desc* c, int iters
         best_ms = ms;
         best->ordering = o;
         best->block_size = b;
+        best->cells_per_thread = t;
       }
       ++k;
+     }
     }
   }
   return AERO_OK;

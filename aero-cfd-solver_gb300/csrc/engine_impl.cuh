@@ -77,15 +77,21 @@ class EngineT final : public Engine {
       *err = "block_size must be 64, 128 or 256";
       return false;
     }
+    cpt_ = c0.cells_per_thread > 0 ? c0.cells_per_thread : 1;
+    if (cpt_ != 1 && cpt_ != 2) {
+      *err = "cells_per_thread must be 1 or 2";
+      return false;
+    }
     lm_ = rs_[0].lm;
     for (int k = 1; k < K_; ++k) {  // settings that select kernel variants are shared
       const aero_case_desc& c = cfg_[k];
       if (c.flux != c0.flux || c.limiter != c0.limiter || c.precision != c0.precision ||
           c.rk_stages != c0.rk_stages || c.local_time_stepping != c0.local_time_stepping ||
           c.startup_first_order_iters != c0.startup_first_order_iters || c.precond_on != c0.precond_on ||
-          rs_[k].lm != lm_ || (c.block_size > 0 ? c.block_size : 128) != block_) {
+          rs_[k].lm != lm_ || (c.block_size > 0 ? c.block_size : 128) != block_ ||
+          (c.cells_per_thread > 0 ? c.cells_per_thread : 1) != cpt_) {
         *err = "cases of one batch must share flux, limiter, precision, RK stages, time-step mode, "
-               "start-up length, low-Mach switches and block size";
+               "start-up length, low-Mach switches, block size and cells per thread";
         return false;
       }
     }
@@ -1669,6 +1675,8 @@ class EngineT final : public Engine {
         wrap(0, [&] {
           if (grad_tma_) {
             k_gradient_tma<T><<<grad_grid_, block_, grad_smem_, st_>>>(dm_, W_, gx_, gy_, cell_cases_, ncb_, tma_err_);
+          } else if (cpt_ == 2) {
+            k_gradient<T, 2><<<(ncb_ + 1) / 2, block_, 0, st_>>>(dm_, W_, gx_, gy_, cell_cases_, ncb_);
           } else {
             k_gradient<T><<<ncb_, block_, 0, st_>>>(dm_, W_, gx_, gy_, cell_cases_);
           }
@@ -1795,6 +1803,7 @@ class EngineT final : public Engine {
   int* perm_all_dev_ = nullptr;  // every case's new -> original cell, at the case's cell offset
   bool host_direct_ = false;     // the GPU reads and writes host state arrays in place
   bool grad_tma_ = false;        // gradient pass through bulk copies into shared memory
+  int cpt_ = 1;                  // cells per thread of the gather gradient pass (1 or 2)
   size_t grad_smem_ = 0;
   int grad_grid_ = 0;
   int* tma_err_ = nullptr;       // set by a kernel whose bounded wait on a copy expired

@@ -251,19 +251,23 @@ def ogrid_synthetic(n_circ: int, n_radial: int, cell_type: int = 3, permute: boo
 
 
 def autotune(mesh: Mesh, case: CaseDesc, iters: int = 20):
-    """Fastest block size and cell ordering for this mesh and case (aero_autotune). Returns
-    (case with them set, {(ordering, block): device ms of `iters` iterations})."""
+    """Fastest cell ordering, block size and cells per thread for this mesh and case
+    (aero_autotune). Returns (case with them set, {(ordering, block, cells_per_thread): device
+    ms of `iters` iterations})."""
     lib = load()
     md = mesh.desc()
     best = CaseDesc()
-    ms = (C.c_double * 6)()
+    ms = (C.c_double * 12)()
     rc = lib.aero_autotune(C.byref(md), C.byref(case), iters, C.byref(best), ms)
     if rc != 0:
         raise AeroError(rc, lib.aero_last_error(None).decode())
     table = {}
-    for i, o in enumerate((capi.ORDER_MORTON, capi.ORDER_RCM)):
-        for j, b in enumerate((64, 128, 256)):
-            table[(o, b)] = ms[3 * i + j]
+    k = 0
+    for o in (capi.ORDER_MORTON, capi.ORDER_RCM):
+        for b in (64, 128, 256):
+            for t in (1, 2):
+                table[(o, b, t)] = ms[k]
+                k += 1
     return best, table
 
 

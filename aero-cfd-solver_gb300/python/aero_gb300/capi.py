@@ -98,6 +98,7 @@ _CASE_FIELDS = [
     ("block_size", C.c_int),
     ("diagnostics", C.c_int),
     ("density_l2_target", C.c_double),
+    ("cells_per_thread", C.c_int),
 ]
 
 
@@ -160,7 +161,7 @@ CASE_DEFAULTS = dict(
     all_speed_cfl_min_scale=_F(0.1),
     aoa0_symmetry_enforce=0, aoa0_symmetry_enforce_interval=0,
     precision=PRECISION_FP64, ordering=ORDER_MORTON, block_size=0, diagnostics=0,
-    density_l2_target=0.0,
+    density_l2_target=0.0, cells_per_thread=0,
 )
 
 

@@ -284,10 +284,11 @@ def c4_draw(rank: int):
 def c4_sweep(args, aero_gb300, capi, rank):
     """96 FP32 cases, mesh sizes drawn from the four O-grids, alpha ~ U[-4, 8] deg, M ~
     U[0.3, 0.85], HLLC + MUSCL venkat, per-case CFL ramp to 0.8 and a density-residual stop
-    mask at 1e-8 relative; seeded synthetic inputs. Block size and cell ordering come from
-    the autotuner (aero_autotune on the largest mesh of the draw with the first case's flow).
-    Returns device ms of `steps` iterations (L2 flushed before each), the batch's cell count,
-    its launches per iteration and the tuned (ordering, block size)."""
+    mask at 1e-8 relative; seeded synthetic inputs. Block size, cell ordering and cells per
+    thread come from the autotuner (aero_autotune on the largest mesh of the draw with the
+    first case's flow). Returns device ms of `steps` iterations (L2 flushed before each), the
+    batch's cell count, its launches per iteration and the tuned (ordering, block size, cells
+    per thread)."""
     base = {sz: aero_gb300.ogrid_synthetic(sz[0], sz[1], cell_type=3, permute=True, jitter=0.1, seed=100 + i,
                                            wall_spacing=0.005, farfield_radius=20.0)
             for i, sz in enumerate(C4_SIZES)}
@@ -305,13 +306,14 @@ def c4_sweep(args, aero_gb300, capi, rank):
     for c in cases:
         c.block_size = tuned.block_size
         c.ordering = tuned.ordering
+        c.cells_per_thread = tuned.cells_per_thread
     with aero_gb300.Batch(meshes, cases) as b:
         cells = b.info()["cells"]
         b.run(STARTUP)
         b.time_iterations(args.warmup, use_graph=True, flush_l2=True)
         ms = b.time_iterations(args.steps, use_graph=True, flush_l2=not args.no_flush)
         launches = b.info()["launches_per_iteration"]
-    return ms, int(cells), int(launches), (int(tuned.ordering), int(tuned.block_size))
+    return ms, int(cells), int(launches), (int(tuned.ordering), int(tuned.block_size), int(tuned.cells_per_thread))
 
 
 def c3_low_mach(args, aero_gb300, capi, peak):
@@ -544,7 +546,7 @@ def run_gpu_arm(args):
               "fp32_batched_mcell_iter_s": world * c4_cells * args.steps / (c4_ms / 1e3) / 1e6,
               "launches_per_step": c4_launch,
               "autotuned": {"ordering": {1: "morton", 2: "rcm"}.get(c4_tuned[0], c4_tuned[0]),
-                            "block_size": c4_tuned[1]},
+                            "block_size": c4_tuned[1], "cells_per_thread": c4_tuned[2]},
               "inputs": "96 seeded cases per GPU: sizes from {64x16,128x32,256x64,512x128} triangulated "
                         "O-grids, alpha~U[-4,8], M~U[0.3,0.85], HLLC+MUSCL venkat, CFL ramp to 0.8, "
                         "density-residual stop mask 1e-8; one batched context, L2 flushed per step"}

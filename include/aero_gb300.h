@@ -119,6 +119,11 @@ typedef struct aero_case_desc {
    * residual's L2 norm has fallen to this fraction of its first value (the per-case mask of
    * a batched sweep); 0: the reference's stop rule only. No reference counterpart. */
   double density_l2_target;
+  /* cells per thread of the gradient pass's gather kernel (1 or 2; 0 = 1): with 2, each thread
+   * computes two cells of adjacent blocks and issues their loads together. Results are the
+   * same bit for bit. The bulk-copy gradient keeps one cell per thread. No reference
+   * counterpart (picked by aero_autotune). */
+  int cells_per_thread;
 } aero_case_desc;
 
 /* One record per pseudo-time iteration: the rows of residuals.csv and forces.csv
@@ -252,10 +257,12 @@ AERO_API int aero_residual_noalloc(aero_ctx* ctx, const double* conserved_dev, i
 AERO_API int aero_get_info(aero_ctx* ctx, long long* info, int n_info);
 
 /* Autotuner (no reference counterpart): times `iters` second-order iterations of the case on
- * this mesh for every block size (64, 128, 256) and cell ordering (Morton, RCM), each in its
- * own context after the case's first-order start-up, and writes the case with the fastest
- * pair into *best (all other fields copied from *c). ms_out (may be NULL) receives the 6
- * device times in ms, ordering-major: [Morton 64, 128, 256, RCM 64, 128, 256]. */
+ * this mesh for every cell ordering (Morton, RCM), block size (64, 128, 256) and number of
+ * cells per thread of the gradient pass (1, 2), each in its own context after the case's
+ * first-order start-up, and writes the case with the fastest combination into *best (all
+ * other fields copied from *c). ms_out (may be NULL) receives the 12 device times in ms,
+ * ordering-major, then block size, then cells per thread: [Morton 64/1, 64/2, 128/1, 128/2,
+ * 256/1, 256/2, RCM 64/1, ...]. */
 AERO_API int aero_autotune(const aero_mesh_desc* mesh, const aero_case_desc* c, int iters, aero_case_desc* best,
                            double* ms_out);
 

@@ -91,8 +91,8 @@ def test_autotune_picks_the_fastest_measured_variant():
     case = capi.make_case(mach=0.6, flux=capi.FLUX_HLLC, limiter=capi.LIMITER_VENKAT, startup_first_order_iters=3,
                           precision=capi.PRECISION_FP32)
     best, table = aero_gb300.autotune(mesh, case, iters=10)
-    assert len(table) == 6 and all(v > 0 for v in table.values())
-    assert (best.ordering, best.block_size) == min(table, key=table.get)
+    assert len(table) == 12 and all(v > 0 for v in table.values())
+    assert (best.ordering, best.block_size, best.cells_per_thread) == min(table, key=table.get)
     assert best.mach == case.mach and best.flux == case.flux
     with aero_gb300.Solver(mesh, best) as s:  # the tuned case runs and matches the default's results
         _, rec = s.run(8)

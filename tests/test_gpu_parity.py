@@ -391,3 +391,51 @@ def test_bulk_copy_gradient_matches_the_gather_kernel(precision, block, low_mach
                 outs.append((s.get_state(), rec["residual_l2"], rec["cl"]))
         for a, b in zip(outs[0], outs[1]):
             np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("precision", [capi.PRECISION_FP64, capi.PRECISION_FP32])
+@pytest.mark.parametrize("block", [64, 128, 256])
+def test_two_cells_per_thread_match_one(precision, block, monkeypatch):
+    """The gather gradient pass with two cells per thread (a block covers two cell blocks)
+    gives the same runs as one cell per thread, bit for bit: triangles and quads, odd block
+    counts with a partial last block."""
+    monkeypatch.setenv("AERO_BULK_COPY", "0")
+    for cell_type in (3, 4):
+        mesh = aero_gb300.ogrid_synthetic(90, 22, cell_type=cell_type, permute=True, jitter=0.1, seed=23)
+        outs = []
+        for cpt in (1, 2):
+            case = capi.make_case(flux=1, limiter=1, mach=0.7, startup_first_order_iters=3, precision=precision,
+                                  block_size=block, cells_per_thread=cpt)
+            with aero_gb300.Solver(mesh, case) as s:
+                _, rec = s.run(15)
+                outs.append((s.get_state(), rec["residual_l2"], rec["cl"]))
+        for a, b in zip(outs[0], outs[1]):
+            np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("precision", [capi.PRECISION_FP64, capi.PRECISION_FP32])
+def test_two_cells_per_thread_in_a_batch(precision, monkeypatch):
+    """Two cells per thread in a batch, where one block covers the last cell block of one case
+    and the first of the next (and a case that has stopped), reproduces one cell per thread."""
+    monkeypatch.setenv("AERO_BULK_COPY", "0")
+    meshes = [aero_gb300.ogrid_synthetic(nc, nr, cell_type=3, permute=True, jitter=0.1, seed=41 + i)
+              for i, (nc, nr) in enumerate([(90, 22), (34, 9), (56, 14)])]
+    states = []
+    for cpt in (1, 2):
+        cases = [capi.make_case(mach=m, aoa_deg=a, flux=capi.FLUX_HLLC, limiter=capi.LIMITER_VENKAT,
+                                startup_first_order_iters=3, precision=precision, block_size=64,
+                                cells_per_thread=cpt, iterations=n)
+                 for m, a, n in ((0.5, 2.0, 40), (0.7, -1.0, 12), (0.3, 4.0, 40))]
+        with aero_gb300.Batch(meshes, cases) as b:
+            _, recs = b.run(20)
+            states.append(([b.get_state(k) for k in range(3)], [r["residual_l2"] for r in recs]))
+    for k in range(3):
+        np.testing.assert_array_equal(states[0][0][k], states[1][0][k])
+        np.testing.assert_array_equal(states[0][1][k], states[1][1][k])
+
+
+def test_cells_per_thread_is_checked():
+    mesh = aero_gb300.ogrid_synthetic(32, 8, cell_type=3)
+    case = capi.make_case(cells_per_thread=3)
+    with pytest.raises(aero_gb300.AeroError):
+        aero_gb300.Solver(mesh, case)

@@ -104,6 +104,11 @@ template <class T>
 __host__ __device__ __forceinline__ bool sfinite(T x) {
   return isfinite(x);
 }
+// float: |x| < inf is false exactly for the infinities and NaN (one compare)
+template <>
+__host__ __device__ __forceinline__ bool sfinite<float>(float x) {
+  return fabsf(x) < INFINITY;
+}
 
 template <class T>
 struct Prim {

@@ -460,24 +460,18 @@ __device__ void block_norms(T (&q)[kNorm], Partials part) {
     for (int k = 0; k < kNorm; ++k) shn[k][wid] = q[k];
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    T a = T(0), b = T(0), mx = T(0), rr = T(0);
-    for (int i = 0; i < nw; ++i) {
-      a += shn[0][i];
-      b += shn[1][i];
-      mx = smax(mx, shn[2][i]);
-      rr += shn[3][i];
-    }
+  // one term per thread, each over the warps in order
+  if (threadIdx.x < kNorm) {
+    const int k = threadIdx.x;
+    T a = T(0);
+    for (int i = 0; i < nw; ++i) a = (k == 2) ? smax(a, shn[2][i]) : a + shn[k][i];
     T* out;
     if constexpr (sizeof(T) == 4) {
       out = part.norms_f;
     } else {
       out = part.norms;
     }
-    out[blockIdx.x] = a;
-    out[part.nb + blockIdx.x] = b;
-    out[2 * part.nb + blockIdx.x] = mx;
-    out[3 * part.nb + blockIdx.x] = rr;
+    out[k * part.nb + blockIdx.x] = a;
   }
 }
 
@@ -571,29 +565,29 @@ __device__ void block_monitors(bool valid, const Prim<T>& w, int c, const Monito
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int k = 0; k < kMon; ++k) {
-      T m = T(0);
-      for (int i = 0; i < nw; ++i) m = smax(m, shf[k][i]);
-      if constexpr (kF) {
-        part.mon[k * part.nb + blockIdx.x] = static_cast<long long>(__float_as_uint(m));
-      } else {
-        part.mon[k * part.nb + blockIdx.x] = __double_as_longlong(m);
-      }
+  // one quantity per thread, each over the warps in order: the maxima on threads
+  // 0..kMon-1, the wall sums and maxima on threads 32..32+kWall-1
+  const int t = threadIdx.x;
+  if (t < kMon) {
+    T m = T(0);
+    for (int i = 0; i < nw; ++i) m = smax(m, shf[t][i]);
+    if constexpr (kF) {
+      part.mon[t * part.nb + blockIdx.x] = static_cast<long long>(__float_as_uint(m));
+    } else {
+      part.mon[t * part.nb + blockIdx.x] = __double_as_longlong(m);
     }
-    if (slot >= 0) {
-      T* out;
-      if constexpr (kF) {
-        out = part.wall_f;
-      } else {
-        out = part.wall;
-      }
-      for (int k = 0; k < kWall; ++k) {
-        T a = (k == 9 || k == 10) ? kLow : T(0);
-        for (int i = 0; i < nw; ++i) a = (k >= 8 && k <= 10) ? smax(a, shd[k][i]) : a + shd[k][i];
-        out[k * part.nwb + slot] = a;
-      }
+  }
+  const int k = t - 32;
+  if (slot >= 0 && k >= 0 && k < kWall) {
+    T* out;
+    if constexpr (kF) {
+      out = part.wall_f;
+    } else {
+      out = part.wall;
     }
+    T a = (k == 9 || k == 10) ? kLow : T(0);
+    for (int i = 0; i < nw; ++i) a = (k >= 8 && k <= 10) ? smax(a, shd[k][i]) : a + shd[k][i];
+    out[k * part.nwb + slot] = a;
   }
 }
 

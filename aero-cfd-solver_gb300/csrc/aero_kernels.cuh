@@ -1168,9 +1168,10 @@ struct Record {
   double rho_ratio;
 };
 
-// The controller's serial work, split over lane 0 of the four warps (each warp on its own SM
+// The controller's serial work, split over the four warps (each warp on its own SM
 // sub-partition, so their double arithmetic proceeds side by side) in two phases:
-//   phase 1  ctl_forces    force coefficients and their stability window
+//   phase 1  ctl_forces_lane  force coefficients and their stability window (lanes 0-2 of
+//                          warp 0, one coefficient each)
 //            ctl_residual  residual monitor, adaptive CFL, the iteration-only part of the
 //                          next schedule
 //            ctl_side      density-residual ratio, wall pressure-jump energy
@@ -1256,73 +1257,94 @@ __device__ inline void ctl_residual(const CtrlConfig& cc, const CtlIn& in, Ctrl&
   s.prev_l2 = l2;
 }
 
-__device__ inline void ctl_forces(const CtrlConfig& cc, const CtlIn& in, Ctrl& s, Record& r, bool* stable_out,
-                                  bool* dstable_out) {
+// Forces and the force-window tests on lanes k = 0, 1, 2 of one warp (CL, CD, CM): each lane
+// forms its coefficient, its column of the history ring and its window tests, every
+// quantity with the operations, in the order, of the one-lane form; the three stability and
+// drift tests are combined across the lanes. A GB300 SM runs double arithmetic at a small
+// fraction of its float rate, so the three coefficients' chains run side by side.
+__device__ inline void ctl_forces_lane(const CtrlConfig& cc, const CtlIn& in, Ctrl& s, Record& r, int k,
+                                       bool* stable_out, bool* dstable_out) {
+  constexpr unsigned kLanes = 0x7u;
   const double* fsum = in.wv;
   // integrate_pressure_forces (gauge -> reported)
   const double qs = cc.q_inf * cc.s_ref;
   const double fxg = fsum[4], fyg = fsum[5];
-  r.drag = fxg * cc.cos_a + fyg * cc.sin_a;
-  r.lift = -fxg * cc.sin_a + fyg * cc.cos_a;
-  r.moment = fsum[7];
-  r.cd = r.drag / qs;
-  r.cl = r.lift / qs;
-  r.cm = fsum[7] / (qs * cc.chord);
-  // ConvergenceMonitor::update_forces
-  r.dcl = r.dcd = r.dcm = 0.0;
-  if (s.has_prev) {
-    r.dcl = fabs(r.cl - s.prev_cl);
-    r.dcd = fabs(r.cd - s.prev_cd);
-    r.dcm = fabs(r.cm - s.prev_cm);
+  double coef, prev;
+  if (k == 0) {
+    r.lift = -fxg * cc.sin_a + fyg * cc.cos_a;
+    coef = r.lift / qs;
+    r.cl = coef;
+    prev = s.prev_cl;
+  } else if (k == 1) {
+    r.drag = fxg * cc.cos_a + fyg * cc.sin_a;
+    coef = r.drag / qs;
+    r.cd = coef;
+    prev = s.prev_cd;
+  } else {
+    r.moment = fsum[7];
+    coef = fsum[7] / (qs * cc.chord);
+    r.cm = coef;
+    prev = s.prev_cm;
   }
-  s.prev_cl = r.cl; s.prev_cd = r.cd; s.prev_cm = r.cm;
-  s.has_prev = 1;
+  // ConvergenceMonitor::update_forces
+  const double dc = s.has_prev ? fabs(coef - prev) : 0.0;
   const int req = cc.window < 1 ? 1 : cc.window;
   const int cap = 2 * req;
-  {
-    const int slot = (s.hist_head + s.hist_count) % cap;
-    s.hist[3 * slot] = r.cl;
-    s.hist[3 * slot + 1] = r.cd;
-    s.hist[3 * slot + 2] = r.cm;
-    if (s.hist_count < cap) {
-      ++s.hist_count;
-    } else {
-      s.hist_head = (s.hist_head + 1) % cap;
-    }
+  int count = s.hist_count, head = s.hist_head;
+  const int slot = (head + count) % cap;
+  s.hist[3 * slot + k] = coef;  // each lane reads and writes its own column only
+  if (count < cap) {
+    ++count;
+  } else {
+    head = (head + 1) % cap;
   }
-  auto H = [&](int i, int k) {  // entry i of the ring (0 = oldest); head < cap, i < cap
-    const int j = s.hist_head + i;
+  auto H = [&](int i) {  // entry i of the ring (0 = oldest); head < cap, i < cap
+    const int j = head + i;
     return s.hist[3 * (j >= cap ? j - cap : j) + k];
   };
-  bool stable = false;
-  if (s.hist_count >= req) {
-    const int b = s.hist_count - req;
-    double lo[3], hi[3];
-    for (int k = 0; k < 3; ++k) lo[k] = hi[k] = H(b, k);
-    for (int i = b; i < s.hist_count; ++i) {
-      for (int k = 0; k < 3; ++k) {
-        lo[k] = smin(lo[k], H(i, k));
-        hi[k] = smax(hi[k], H(i, k));
-      }
+  bool st = false;
+  if (count >= req) {
+    const int b = count - req;
+    double lo = H(b), hi = lo;
+    for (int i = b; i < count; ++i) {
+      lo = smin(lo, H(i));
+      hi = smax(hi, H(i));
     }
-    stable = (hi[0] - lo[0]) <= cc.stab_tol && (hi[1] - lo[1]) <= cc.stab_tol && (hi[2] - lo[2]) <= cc.stab_tol;
+    st = (hi - lo) <= cc.stab_tol;
   }
-  bool dstable = false;
-  r.mdcl = r.mdcd = r.mdcm = 0.0;
-  if (s.hist_count >= cap) {
-    double pa[3] = {0, 0, 0}, ca[3] = {0, 0, 0};
-    for (int i = 0; i < req; ++i)
-      for (int k = 0; k < 3; ++k) pa[k] += H(i, k);
-    for (int i = req; i < cap; ++i)
-      for (int k = 0; k < 3; ++k) ca[k] += H(i, k);
+  bool dst = false;
+  double mdc = 0.0;
+  if (count >= cap) {
+    double pa = 0, ca = 0;
+    for (int i = 0; i < req; ++i) pa += H(i);
+    for (int i = req; i < cap; ++i) ca += H(i);
     const double inv = 1.0 / double(req);
-    r.mdcl = fabs(ca[0] * inv - pa[0] * inv);
-    r.mdcd = fabs(ca[1] * inv - pa[1] * inv);
-    r.mdcm = fabs(ca[2] * inv - pa[2] * inv);
-    dstable = r.mdcl <= cc.drift_tol && r.mdcd <= cc.drift_tol && r.mdcm <= cc.drift_tol;
+    mdc = fabs(ca * inv - pa * inv);
+    dst = mdc <= cc.drift_tol;
   }
-  *stable_out = stable;
-  *dstable_out = dstable;
+  if (k == 0) {
+    r.dcl = dc;
+    r.mdcl = mdc;
+  } else if (k == 1) {
+    r.dcd = dc;
+    r.mdcd = mdc;
+  } else {
+    r.dcm = dc;
+    r.mdcm = mdc;
+  }
+  *stable_out = __ballot_sync(kLanes, st) == kLanes;
+  *dstable_out = __ballot_sync(kLanes, dst) == kLanes;
+  __syncwarp(kLanes);  // every lane has read the ring's head, count and has_prev
+  if (k == 0) {
+    s.prev_cl = coef;
+    s.has_prev = 1;
+    s.hist_count = count;
+    s.hist_head = head;
+  } else if (k == 1) {
+    s.prev_cd = coef;
+  } else {
+    s.prev_cm = coef;
+  }
 }
 
 __device__ inline void ctl_decide(const CtrlConfig& cc, Ctrl& s, Record& r, bool stable, bool dstable,
@@ -1445,7 +1467,7 @@ static __global__ void __launch_bounds__(kCtlThreads) k_control(const CtrlConfig
   if (cc.bulk_f32) {
     // float block partials summed in float-float, then one conversion per warp
     float h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f, h3 = 0.f, l3 = 0.f;
-#pragma unroll 2
+#pragma unroll 4
     for (int b = bb + tid; b < bb + nb; b += kCtlThreads) {
       ff_add(h1, l1, part.norms_f[b], &h1, &l1);
       ff_add(h2, l2, part.norms_f[st + b], &h2, &l2);
@@ -1505,9 +1527,13 @@ static __global__ void __launch_bounds__(kCtlThreads) k_control(const CtrlConfig
     return cc.bulk_f32 ? double(part.wall_f[i]) : part.wall[i];
   };
   if (nwb <= 32) {
+    // every (quantity, block) value loaded at once, then combined over the blocks in order
+    __shared__ double s_wload[kWall][32];
+    for (int i = tid; i < kWall * nwb; i += kCtlThreads) s_wload[i / nwb][i % nwb] = wall_at(i / nwb, i % nwb);
+    __syncthreads();
     if (tid < kWall) {
       double acc = wall_init(tid);
-      for (int b = 0; b < nwb; ++b) acc = wall_comb(tid, acc, wall_at(tid, b));
+      for (int b = 0; b < nwb; ++b) acc = wall_comb(tid, acc, s_wload[tid][b]);
       s_wall[0][tid] = acc;
     }
   } else {
@@ -1539,38 +1565,38 @@ static __global__ void __launch_bounds__(kCtlThreads) k_control(const CtrlConfig
   __shared__ Record srec;
   __shared__ SchedBase snext;
   __shared__ int s_slot;
-  if (tid == 0) {
-    double a[kNorm] = {0.0, 0.0, 0.0, 0.0}, p4[4] = {0.0, 0.0, 0.0, 0.0};
-    long long m[1 + kMon] = {0, 0, 0, 0, 0, 0, 0};
-    for (int w = 0; w < kWarps; ++w) {
-      a[0] += s_sum[w][0];
-      a[1] += s_sum[w][1];
-      a[3] += s_sum[w][2];
-      for (int k = 0; k < 4; ++k) p4[k] += s_sum[w][3 + k];
-      for (int k = 0; k < 1 + kMon; ++k) m[k] = max_bits(m[k], s_max[w][k]);
+  // the warps' partials combined one quantity per lane of warp 0, each over the warps in
+  // order: sums (lanes 0-6), maxima (7-13), wall quantities (14-25)
+  if (tid < 7) {
+    double v = 0.0;
+    for (int w = 0; w < kWarps; ++w) v += s_sum[w][tid];
+    if (tid == 0) s_in.a[0] = v;
+    else if (tid == 1) s_in.a[1] = v;
+    else if (tid == 2) s_in.a[3] = v;
+    else s_in.pj[tid - 3] = v;
+  } else if (tid < 7 + 1 + kMon) {
+    const int k = tid - 7;
+    long long m = 0;
+    for (int w = 0; w < kWarps; ++w) m = max_bits(m, s_max[w][k]);
+    const double v = cc.bulk_f32 ? double(__uint_as_float(static_cast<unsigned>(m))) : __longlong_as_double(m);
+    if (k == 0) s_in.a[2] = v;
+    else s_in.mon[k - 1] = v;
+  } else if (tid < 8 + kMon + kWall) {
+    const int k = tid - (8 + kMon);
+    double v = s_wall[0][k];
+    if (nwb > 32) {
+      for (int w = 1; w < kWarps; ++w) v = wall_comb(k, v, s_wall[w][k]);
     }
-    auto decode = [&](long long bits) {
-      return cc.bulk_f32 ? double(__uint_as_float(static_cast<unsigned>(bits))) : __longlong_as_double(bits);
-    };
-    a[2] = decode(m[0]);
-    for (int k = 0; k < kNorm; ++k) s_in.a[k] = a[k];
-    for (int k = 0; k < 4; ++k) s_in.pj[k] = p4[k];
-    for (int k = 0; k < kMon; ++k) s_in.mon[k] = decode(m[k + 1]);
-    for (int k = 0; k < kWall; ++k) {
-      double v = s_wall[0][k];
-      if (nwb > 32) {
-        for (int w = 1; w < kWarps; ++w) v = wall_comb(k, v, s_wall[w][k]);
-      }
-      s_in.wv[k] = v;
-    }
+    s_in.wv[k] = v;
+  } else if (tid == 8 + kMon + kWall) {
     s_slot = sc.iter - sc.rec_base;  // the record slot of this iteration
   }
   __syncthreads();
-  // phase 1: four independent chains on lane 0 of warps 0..3
+  // phase 1: independent chains on warps 0..3 (the force coefficients on lanes 0-2 of warp 0)
   static_assert(kCtlThreads >= 128, "the controller's phase 1 uses four warps");
   bool stable = false, dstable = false;
-  if (tid == 0) {
-    ctl_forces(cc, s_in, sc, srec, &stable, &dstable);
+  if (tid < 3) {
+    ctl_forces_lane(cc, s_in, sc, srec, tid, &stable, &dstable);
   } else if (tid == 32) {
     ctl_residual(cc, s_in, sc, srec, &snext);
   } else if (tid == 64) {

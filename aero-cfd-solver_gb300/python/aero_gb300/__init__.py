@@ -114,6 +114,9 @@ def load(build_if_missing: bool = False):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
+    if lib.aero_abi_version() != capi.ABI_VERSION:  # a stale build: its structures differ
+        raise ImportError(f"{path} has ABI {lib.aero_abi_version()}, these bindings ABI {capi.ABI_VERSION}: "
+                          "rebuild with aero-cfd-solver_gb300/build.py")
     _lib = lib
     return lib
 

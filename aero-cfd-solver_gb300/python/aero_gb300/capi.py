@@ -15,6 +15,7 @@ import numpy as np
 PKG_ROOT = Path(__file__).resolve().parents[2]  # .../aero-cfd-solver_gb300
 REPO_ROOT = PKG_ROOT.parent
 LIB_PATH = PKG_ROOT / "lib" / "libaero_gb300.so"
+ABI_VERSION = 3  # AERO_ABI_VERSION of include/aero_gb300.h that these structures mirror
 
 AERO_OK = 0
 AERO_ERR_INVALID = 1

@@ -28,7 +28,8 @@
 extern "C" {
 #endif
 
-#define AERO_ABI_VERSION 2
+/* 3: aero_case_desc gained cells_per_thread; aero_autotune writes 12 timings */
+#define AERO_ABI_VERSION 3
 
 #if defined(__GNUC__)
 #define AERO_API __attribute__((visibility("default")))

@@ -40,7 +40,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_identity(lib):
-    assert lib.aero_abi_version() == 2
+    assert lib.aero_abi_version() == capi.ABI_VERSION == 3
     assert lib.aero_version().decode().endswith("gb300")
 
 

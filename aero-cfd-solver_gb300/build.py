@@ -27,7 +27,10 @@ CU_SOURCES = ["engine_f32.cu", "engine_f64.cu", "noalloc.cu"]
 # Float division and square root by the hardware approximations (at most 2 ulp) in the units
 # holding FP32 kernels: the FP32 residual stays within twice the reference float path's own
 # deviation from FP64 either way, and the correctly rounded sequences cost the face pass
-# about a tenth of its time. Double arithmetic is unaffected by these flags.
+# about a tenth of its time. Float subnormals (below 1.2e-38) flush to zero there: the
+# solver's floored densities, pressures and wave speeds never come near them, and the square
+# roots and quotients then skip their subnormal scaling (face pass 12.7 -> 11.6 us at 131k
+# cells). Double arithmetic is unaffected by these flags.
 FAST_FLOAT_DIV_SQRT = ("engine_f32.cu", "noalloc.cu")
 CPP_SOURCES = ["capi.cpp", "mesh_prep.cpp", "mesh_gen.cpp", "driver.cpp"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
@@ -72,7 +75,7 @@ def build(force: bool = False, ptxas_v: bool = False, verbose: bool = False) -> 
         if ptxas_v:
             cmd.insert(3, "-Xptxas=-v")
         if src in FAST_FLOAT_DIV_SQRT:
-            cmd[3:3] = ["-prec-div=false", "-prec-sqrt=false"]
+            cmd[3:3] = ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
         jobs.append(cmd)
     for src in CPP_SOURCES:
         obj = OBJ / (src + ".o")

@@ -402,35 +402,32 @@ int aero_autotune(const aero_mesh_desc* mesh, const aero_case_desc* c, int iters
   double best_ms = 0.0;
   int k = 0;
   *best = *c;
-  for (int o : orders) {
-    for (int b : blocks) {
-     for (int t : cpts) {
-      aero_case_desc v = *c;
-      v.ordering = o;
-      v.block_size = b;
-      v.cells_per_thread = t;
-      aero_ctx* ctx = nullptr;
-      int rc = create_ctx(1, mesh, &v, &ctx);
-      if (rc != AERO_OK) return rc;
-      double ms = 0.0;
-      const int warm = std::max(c->startup_first_order_iters, 0);
-      if (warm > 0) rc = ctx->engine->time_iterations(warm, 1, 0, &ms);  // first-order start-up
-      if (rc == AERO_OK) rc = ctx->engine->time_iterations(2, 1, 0, &ms);  // graphs instantiated
-      if (rc == AERO_OK) rc = ctx->engine->time_iterations(iters, 1, 0, &ms);
-      const int cs = cuda_status(ctx);
-      aero_destroy(ctx);
-      if (cs != AERO_OK) return cs;
-      if (rc != AERO_OK && rc != AERO_ERR_NONFINITE) return fail(nullptr, rc, "aero_autotune: timing failed");
-      if (ms_out) ms_out[k] = ms;
-      if (k == 0 || ms < best_ms) {
-        best_ms = ms;
-        best->ordering = o;
-        best->block_size = b;
-        best->cells_per_thread = t;
-      }
-      ++k;
-     }
+  for (int n = 0; n < 2 * 3 * 2; ++n) {  // ordering-major, then block size, then cells per thread
+    const int o = orders[n / 6], b = blocks[(n / 2) % 3], t = cpts[n % 2];
+    aero_case_desc v = *c;
+    v.ordering = o;
+    v.block_size = b;
+    v.cells_per_thread = t;
+    aero_ctx* ctx = nullptr;
+    int rc = create_ctx(1, mesh, &v, &ctx);
+    if (rc != AERO_OK) return rc;
+    double ms = 0.0;
+    const int warm = std::max(c->startup_first_order_iters, 0);
+    if (warm > 0) rc = ctx->engine->time_iterations(warm, 1, 0, &ms);  // first-order start-up
+    if (rc == AERO_OK) rc = ctx->engine->time_iterations(2, 1, 0, &ms);  // graphs instantiated
+    if (rc == AERO_OK) rc = ctx->engine->time_iterations(iters, 1, 0, &ms);
+    const int cs = cuda_status(ctx);
+    aero_destroy(ctx);
+    if (cs != AERO_OK) return cs;
+    if (rc != AERO_OK && rc != AERO_ERR_NONFINITE) return fail(nullptr, rc, "aero_autotune: timing failed");
+    if (ms_out) ms_out[k] = ms;
+    if (k == 0 || ms < best_ms) {
+      best_ms = ms;
+      best->ordering = o;
+      best->block_size = b;
+      best->cells_per_thread = t;
     }
+    ++k;
   }
   return AERO_OK;
 }

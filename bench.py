@@ -256,8 +256,9 @@ def run_reference_arm(args):
         "cpu_baseline": {"value": value, "unit": "Mcell-iter/s", "cores": procs_n, "kind": "port",
                          "sample": f"{args.steps} second-order iterations per process after {args.warmup} "
                                    f"warm-up, {procs_n} independent single-thread replicas of the oracle float "
-                                   f"port (bit-identical to the reference CPU path); the reference's sources "
-                                   f"are not on this host, so its own binary cannot be built here"},
+                                   f"port (bit-identical to the reference CPU path, pinned against the "
+                                   f"reference's own library by the oracle tests); the GPU host carries no "
+                                   f"reference sources, so the reference binary itself is not built there"},
         "e2e": {"value": value, "unit": "Mcell-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "elapsed_s": time.perf_counter() - t0,
     }

@@ -1,0 +1,45 @@
+"""bench.py's contract on the CPU: the reference arm's JSON line (the oracle float port timed
+on host cores), the algorithmic-byte model the roofline divides by, and the warm-up rule."""
+
+import json
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+REPO = Path(__file__).resolve().parents[1]
+sys.path.insert(0, str(REPO))
+
+import bench  # noqa: E402
+
+
+def test_face_pass_algorithmic_bytes():
+    # W and gradients of every cell (12 floats) + per face cell ids, normal, length, offsets
+    # (8 B + 7 floats) and the F*A and wave-speed outputs (5 floats)
+    assert bench.algorithmic_bytes("face", 131072, 3, "fp32", 197120) == 131072 * 48 + 197120 * 56 == 17330176
+    assert bench.algorithmic_bytes("face", 131072, 3, "fp64", 197120) == 131072 * 96 + 197120 * 104
+
+
+def test_warmup_below_three_is_refused():
+    r = subprocess.run([sys.executable, str(REPO / "bench.py"), "--impl", "reference", "--warmup", "2"],
+                       capture_output=True, text=True, cwd=REPO)
+    assert r.returncode != 0 and "warmup" in r.stderr
+
+
+def test_reference_arm_prints_the_contract_line():
+    r = subprocess.run([sys.executable, str(REPO / "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "3",
+                        "--cpu-procs", "2"], capture_output=True, text=True, cwd=REPO, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["metric"] == bench.METRIC and line["unit"] == "Mcell-iter/s" and line["higher_is_better"] is True
+    assert line["value"] > 0 and line["steps"] == 1 and line["warmup"] == 3 and line["vs_baseline"] is None
+    assert "workload" in line["config"]
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] == 2 and cb["value"] == line["value"] and cb["sample"]
+    e2e = line["e2e"]
+    assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0

@@ -75,3 +75,31 @@ def test_record_struct_size_matches_header():
     # aero_iter_record: 4 ints + 42 doubles + 2 ints + 1 double
     assert C.sizeof(capi.IterRecord) == 4 * 4 + 42 * 8 + 2 * 4 + 8
     assert np.dtype(capi.RECORD_DTYPE).itemsize == C.sizeof(capi.IterRecord)
+
+
+@pytest.mark.parametrize("c_name,py_struct", [
+    ("aero_case_desc", capi.CaseDesc), ("aero_mesh_desc", capi.MeshDesc), ("aero_iter_record", capi.IterRecord),
+    ("aero_ogrid_spec", aero_gb300.OgridSpec), ("aero_mesh_sizes", aero_gb300.MeshSizes)])
+def test_struct_layouts_match_the_headers(c_name, py_struct, tmp_path):
+    """Every field offset and the size of the ctypes mirrors equal what a C compiler lays out
+    from include/*.h, so a field added on one side only fails here instead of shifting the
+    fields after it."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    fields = [f[0] for f in py_struct._fields_]
+    src = ["#include <stddef.h>", "#include <stdio.h>", '#include "aero_gb300.h"', '#include "aero_mesh.h"',
+           "int main(void) {", f'  printf("size %zu\\n", sizeof({c_name}));']
+    src += [f'  printf("{f} %zu\\n", offsetof({c_name}, {f}));' for f in fields]
+    src += ["  return 0;", "}"]
+    (tmp_path / "layout.c").write_text("\n".join(src) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", str(REPO / "include"), str(tmp_path / "layout.c"), "-o", str(exe)], check=True)
+    out = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                       check=True).stdout.splitlines())
+    assert int(out["size"]) == C.sizeof(py_struct)
+    for f in fields:
+        assert int(out[f]) == getattr(py_struct, f).offset, f

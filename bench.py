@@ -45,8 +45,9 @@ STARTUP = 25  # first-order start-up iterations run untimed before warm-up
 
 # DRAM traffic per launch of the face pass from one ncu capture (dram__bytes_read.sum +
 # dram__bytes_write.sum; the launch's writes stay in L2), keyed by (precision, n_cells);
-# profiles/kernels_c2_512x128.md gives the command.
-NCU_TRAFFIC = {("fp32", 131072): 13413120, ("fp64", 131072): 25307904}
+# profiles/kernels_c2_512x128.md gives the commands (FP32: the capture of the current face
+# pass; FP64: the first capture).
+NCU_TRAFFIC = {("fp32", 131072): 13419264, ("fp64", 131072): 25307904}
 
 
 def algorithmic_bytes(kernel: str, n: int, slots: int, precision: str, faces: int = 0) -> float:

@@ -67,7 +67,8 @@ struct alignas(16) Ctrl {
   double prev_cl, prev_cd, prev_cm;
   double hist[3 * 2 * kMaxForceWindow];
   double stage_b_fmin;
-  int stage_b_progress, pjump_below, freeze, pad0;
+  int stage_b_progress, pjump_below, freeze;
+  int wait_stop;   // set by the updates of an iteration whose gradient pass gave up a wait
   float cfl_f, stab_f, as_fmin_f, as_ramp_f;  // float copies of the schedule values (FP32 kernels)
   double sr_max;  // global max of max(SR, floor) for global time stepping
   double initial_l2rho;  // first density-residual L2 (< 0: not yet seen)
@@ -293,6 +294,9 @@ struct Cases {
   const FaceParams<T>* fp;
   const PrecondD* pc;
   const MonitorConsts* mc;
+  // wait[0]: nonzero once a kernel of the iteration gave up a bounded wait (its outputs are
+  // then incomplete); wait[1]: the poll limit of those waits. Null outside the iterations.
+  const int* wait = nullptr;
 };
 
 // Conserved state of the cells. FP64 holds it as double4; FP32 as a float-float pair: hi is
@@ -919,6 +923,13 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
   const int n = bd.y;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (ctrl->done) return;
+  if (cs.wait != nullptr && cs.wait[0] != 0) {
+    // The gradient pass of this iteration gave up a wait and left gradients unwritten: no
+    // stage of the iteration is applied (the conserved state is written by the last stage
+    // only), and the controller stops the run without recording the iteration.
+    if (threadIdx.x == 0) ctrl->wait_stop = 1;
+    return;
+  }
   bool bad = false;
   Cons<double> s{1.0, 0.0, 0.0, 1.0};
   Prim<T> w{T(1), T(0), T(0), T(1)};
@@ -1452,6 +1463,14 @@ static __global__ void __launch_bounds__(kCtlThreads) k_control(const CtrlConfig
   __shared__ long long s_max[kWarps][1 + kMon];  // linf, monitors (bit patterns)
   __shared__ double s_wall[kWarps][kWall];
   if (ctrl->done) return;
+  if (ctrl->wait_stop) {  // the iteration was not applied: stop without a record
+    if (threadIdx.x == 0) {
+      fb[0] = 0;  // its face passes' fallback counts are dropped with it
+      fb[1] = 0;
+      ctrl->done = 1;
+    }
+    return;
+  }
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   constexpr int kWords = int(sizeof(Ctrl) / 16);
   {

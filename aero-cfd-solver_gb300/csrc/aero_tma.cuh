@@ -96,11 +96,18 @@ inline size_t grad_tma_smem(int B, int D) {
 // Green-Gauss gradients (cell_gradient's arithmetic, same order) over ntiles cell blocks of
 // blockDim.x cells; blockDim.x must be the engine's block size (64, 128 or 256) so that every
 // copied segment is 16-byte aligned and a multiple of 16 bytes.
+//
+// Bounded waits: wait[1] is the poll limit of the wait on each tile's copies (negative: the
+// default kTmaPolls). A CTA whose wait runs out records wait[0] = 1, then waits (bounded by
+// kTmaPolls, whatever the limit) for its copies still in flight into either buffer, so that
+// none lands after it has exited, and returns without computing its remaining tiles. The
+// gradients of those tiles are then missing, so the update kernels discard the iteration
+// (Cases::wait) and the host reports AERO_ERR_TIMEOUT.
 template <class T>
 __global__ void __launch_bounds__(256) k_gradient_tma(DevMesh<T> m, const typename Vec<T>::v4* __restrict__ W,
                                                       typename Vec<T>::v4* __restrict__ gx,
                                                       typename Vec<T>::v4* __restrict__ gy, Cases<T> cs,
-                                                      int ntiles, int* __restrict__ err) {
+                                                      int ntiles, int* __restrict__ wait) {
   using V2 = typename Vec<T>::v2;
   using V4 = typename Vec<T>::v4;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -129,6 +136,7 @@ __global__ void __launch_bounds__(256) k_gradient_tma(DevMesh<T> m, const typena
     bulk_copy_g2s(base + L.w, W + c0, uint32_t(B * sizeof(V4)), &bar[buf]);
     bulk_copy_g2s(base + L.inv, m.inv_vol + c0, uint32_t(B * sizeof(T)), &bar[buf]);
   };
+  const int limit = wait[1] < 0 ? kTmaPolls : wait[1];
   if (threadIdx.x == 0) issue(tile, 0);
   uint32_t phase0 = 0, phase1 = 0;
   for (int i = 0; tile < ntiles; ++i, tile += gridDim.x) {
@@ -139,14 +147,16 @@ __global__ void __launch_bounds__(256) k_gradient_tma(DevMesh<T> m, const typena
         fence_proxy_async_smem();  // the block's reads of that buffer come before the copies
         issue(next, buf ^ 1);
       }
-      s_ok = mbar_wait(&bar[buf], buf ? phase1 : phase0, kTmaPolls) ? 1 : 0;
+      s_ok = mbar_wait(&bar[buf], buf ? phase1 : phase0, limit) ? 1 : 0;
     }
     __syncthreads();
     if (!s_ok) {  // uniform: record the failure, let the copies in flight land, return
       if (threadIdx.x == 0) {
-        atomicExch(err, 1);
+        atomicExch(&wait[0], 1);
+        mbar_wait(&bar[buf], buf ? phase1 : phase0, kTmaPolls);
         if (next < ntiles) mbar_wait(&bar[buf ^ 1], buf ? phase0 : phase1, kTmaPolls);
       }
+      __syncthreads();
       return;
     }
     if (buf) {

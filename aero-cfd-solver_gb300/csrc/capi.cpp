@@ -392,6 +392,13 @@ int aero_get_info(aero_ctx* ctx, long long* info, int n_info) {
   return AERO_OK;
 }
 
+int aero_set_wait_limit(aero_ctx* ctx, int polls) {
+  if (ctx == nullptr) return fail(ctx, AERO_ERR_INVALID, "aero_set_wait_limit: null context");
+  const int rc = ctx->engine->set_wait_limit(polls);
+  const int cs = cuda_status(ctx);
+  return cs != AERO_OK ? cs : rc;
+}
+
 int aero_autotune(const aero_mesh_desc* mesh, const aero_case_desc* c, int iters, aero_case_desc* best,
                   double* ms_out) {
   if (mesh == nullptr || c == nullptr || best == nullptr || iters <= 0)

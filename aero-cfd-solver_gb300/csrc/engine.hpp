@@ -75,6 +75,8 @@ class Engine {
   virtual int profile_kernels(int n, int flush_l2, double* ms, int* launches) = 0;
   virtual void info(long long* out, int n) = 0;
   virtual cudaError_t last_cuda_error() = 0;
+  virtual int set_wait_limit(int polls) = 0;
+  virtual bool uses_bulk_copy_gradient() const = 0;
 
   // Discrete adjoint at the current state (single-case FP64 contexts; others return
   // AERO_ERR_INVALID). Objective J = w_cd CD + w_cl CL; second_order -1: the run's scheme at

@@ -359,20 +359,37 @@ class EngineT final : public Engine {
       const char* env = std::getenv("AERO_BULK_COPY");
       const int mode = (env && env[0] == '0') ? 0 : ((env && env[0] == '1') ? 1 : -1);
       grad_smem_ = grad_tma_smem<T>(block_, d_);
-      int dev = 0, sms = 0, per_sm = 0;
+      int dev = 0, sms = 0, smem_optin = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      if (grad_smem_ > 48 * 1024) {
-        AERO_CK(cudaFuncSetAttribute(k_gradient_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(grad_smem_)));
+      cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+      // two tile buffers of B cells x D slots: cells with many faces (up to 32 per cell) at
+      // block 256 need more shared memory than a CTA can have, and then the plain gather
+      // kernel runs; forcing the bulk-copy pass (AERO_BULK_COPY=1) there is an error
+      const bool fits = grad_smem_ <= static_cast<size_t>(smem_optin);
+      if (mode == 1 && !fits) {
+        *err = "the bulk-copy gradient pass needs " + std::to_string(grad_smem_) +
+               " bytes of shared memory per block, more than the device's " + std::to_string(smem_optin) +
+               " (AERO_BULK_COPY=1 with this block size and faces per cell)";
+        return false;
       }
-      AERO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gradient_tma<T>, block_, grad_smem_));
-      grad_grid_ = std::min(ncb_, std::max(1, per_sm) * std::max(1, sms));
-      // the copies of a CTA's next tile overlap its current one only with two or more tiles
-      // per CTA; below that the plain gather kernel is as fast
-      grad_tma_ = mode == 1 || (mode == -1 && ncb_ >= 2 * grad_grid_);
-      tma_err_ = alloc<int>(1);
-      AERO_CK(cudaMemsetAsync(tma_err_, 0, sizeof(int), st_));
+      if (mode != 0 && fits) {
+        int per_sm = 0;
+        if (grad_smem_ > 48 * 1024) {
+          AERO_CK(cudaFuncSetAttribute(k_gradient_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(grad_smem_)));
+        }
+        AERO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gradient_tma<T>, block_, grad_smem_));
+        grad_grid_ = std::min(ncb_, std::max(1, per_sm) * std::max(1, sms));
+        // the copies of a CTA's next tile overlap its current one only with two or more
+        // tiles per CTA; below that the plain gather kernel is as fast
+        grad_tma_ = mode == 1 || ncb_ >= 2 * grad_grid_;
+      }
+      // [0] wait-expired word, [1] poll limit of the bulk-copy waits (-1: the default)
+      tma_err_ = alloc<int>(2);
+      const int init_words[2] = {0, -1};
+      AERO_CK(cudaMemcpyAsync(tma_err_, init_words, sizeof(init_words), cudaMemcpyHostToDevice, st_));
+      AERO_CK(cudaStreamSynchronize(st_));
     }
 
     // ---- per-case constants
@@ -391,8 +408,8 @@ class EngineT final : public Engine {
     AERO_CK(cudaMemcpyAsync(fps_dev_, fps_.data(), sizeof(FaceParams<T>) * K_, cudaMemcpyHostToDevice, st_));
     AERO_CK(cudaMemcpyAsync(pcs_dev_, pcs_.data(), sizeof(PrecondD) * K_, cudaMemcpyHostToDevice, st_));
     AERO_CK(cudaMemcpyAsync(mcs_dev_, mcs_.data(), sizeof(MonitorConsts) * K_, cudaMemcpyHostToDevice, st_));
-    cell_cases_ = Cases<T>{cblk_, ctrls_, fps_dev_, pcs_dev_, mcs_dev_};
-    face_cases_ = Cases<T>{fblk_, ctrls_, fps_dev_, pcs_dev_, mcs_dev_};
+    cell_cases_ = Cases<T>{cblk_, ctrls_, fps_dev_, pcs_dev_, mcs_dev_, tma_err_};
+    face_cases_ = Cases<T>{fblk_, ctrls_, fps_dev_, pcs_dev_, mcs_dev_, tma_err_};
 
     // the controller of iteration i runs beside the gradient and first face pass of
     // iteration i+1 (which need none of its outputs) for RK3 runs; with low-Mach weights in
@@ -671,11 +688,7 @@ class EngineT final : public Engine {
     for (const Ctrl& c : host_ctrls_) {
       if (c.nonfinite) status = AERO_ERR_NONFINITE;
     }
-    {
-      int terr = 0;
-      AERO_CK(cudaMemcpy(&terr, tma_err_, sizeof(int), cudaMemcpyDeviceToHost));
-      if (terr) status = AERO_ERR_TIMEOUT;
-    }
+    if (recover_from_expired_wait()) status = AERO_ERR_TIMEOUT;
     if (err_ != cudaSuccess) status = AERO_ERR_CUDA;
     if (n_done) {
       for (int k = 0; k < K_; ++k) n_done[k] = executed[k];
@@ -1088,9 +1101,10 @@ class EngineT final : public Engine {
   // info[0] cells, [1] faces, [2] slots per cell, [3] launches per iteration, [4] device
   // bytes, [5] precision, [6] block size, [7] cell blocks, [8] cases
   void info(long long* out, int n) override {
-    long long v[9] = {ncells_, nfaces_, d_, launches_per_iteration(true), static_cast<long long>(bytes_),
-                      sizeof(T) == 4 ? AERO_PRECISION_FP32 : AERO_PRECISION_FP64, block_, ncb_, K_};
-    for (int i = 0; i < n && i < 9; ++i) out[i] = v[i];
+    long long v[10] = {ncells_, nfaces_, d_, launches_per_iteration(true), static_cast<long long>(bytes_),
+                       sizeof(T) == 4 ? AERO_PRECISION_FP32 : AERO_PRECISION_FP64, block_, ncb_, K_,
+                       grad_tma_ ? 1 : 0};
+    for (int i = 0; i < n && i < 10; ++i) out[i] = v[i];
   }
 
  private:
@@ -1513,6 +1527,40 @@ class EngineT final : public Engine {
     return p;
   }
 
+  // After a kernel gave up a bounded wait: the iteration it belonged to was not applied
+  // (the updates skipped it and its controller stopped the run without a record). Clear the
+  // word, let the stopped cases run again from their last applied iteration, and rebuild
+  // the primitive state from the conserved state, which that iteration did not touch.
+  // Returns whether a wait had expired.
+  bool recover_from_expired_wait() {
+    int expired = 0;
+    AERO_CK(cudaMemcpy(&expired, tma_err_, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!expired || err_ != cudaSuccess) return expired != 0;
+    download_ctrls();
+    for (Ctrl& c : host_ctrls_) {
+      if (c.wait_stop) {
+        c.wait_stop = 0;
+        c.done = 0;
+      }
+    }
+    AERO_CK(cudaMemcpyAsync(ctrls_, host_ctrls_.data(), sizeof(Ctrl) * K_, cudaMemcpyHostToDevice, st_));
+    AERO_CK(cudaMemsetAsync(tma_err_, 0, sizeof(int), st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+    w_valid_ = false;
+    return true;
+  }
+
+ public:
+  // Poll limit of the bounded waits on bulk copies (< 0: the default, about a second).
+  int set_wait_limit(int polls) override {
+    const int v = polls < 0 ? -1 : polls;
+    AERO_CK(cudaMemcpyAsync(tma_err_ + 1, &v, sizeof(int), cudaMemcpyHostToDevice, st_));
+    AERO_CK(cudaStreamSynchronize(st_));
+    return err_ == cudaSuccess ? AERO_OK : AERO_ERR_CUDA;
+  }
+  bool uses_bulk_copy_gradient() const override { return grad_tma_; }
+
+ private:
   void download_ctrls() {
     host_ctrls_.resize(K_);
     AERO_CK(cudaMemcpyAsync(host_ctrls_.data(), ctrls_, sizeof(Ctrl) * K_, cudaMemcpyDeviceToHost, st_));
@@ -1531,8 +1579,10 @@ class EngineT final : public Engine {
     return it0;
   }
   int end_untracked() {
+    const bool expired = recover_from_expired_wait();
     download_ctrls();
     if (err_ != cudaSuccess) return AERO_ERR_CUDA;
+    if (expired) return AERO_ERR_TIMEOUT;
     for (const Ctrl& c : host_ctrls_) {
       if (c.nonfinite) return AERO_ERR_NONFINITE;
     }

@@ -2,24 +2,27 @@
 // that allocates nothing. Its working arrays live in a file-scope __device__ array of fixed
 // size instead of memory obtained from cudaMalloc.
 //
-// Who needs this: code that runs the residual where device allocation is not allowed or not
-// wanted -- inside a CUDA stream capture that is later replayed, under another framework's
-// memory pool that owns all device memory, or in a time-stepping loop whose memory budget is
-// fixed up front (cudaMalloc/cudaFree can synchronise the device and fragment memory).
+// Who needs this: code that evaluates the residual where device allocation is not allowed or
+// not wanted -- under another framework's memory pool that owns all device memory, or in a
+// time-stepping loop whose memory budget is fixed up front (cudaMalloc/cudaFree can
+// synchronise the device and fragment memory).
 //
 // Limits and sharing: the scratch array is sized for kNoallocMaxCells cells and
-// kNoallocMaxFaces faces (about 16.8 MB) and every GPU that loads this library holds it
-// until the process exits. All calls on a
-// device share it and it keeps the last call's contents; the kernels clear what must start
-// at zero. Two calls whose work overlaps on the same GPU (different streams, or different
-// contexts on one device) race on the shared array and must be serialised by the caller.
+// kNoallocMaxFaces faces (about 16.8 MB); every CUDA context that loads this library (one per
+// GPU for the runtime's primary context) holds its own copy until the process exits. All
+// calls made in one context share that copy and it keeps the last call's contents; the
+// kernels clear what must start at zero. Two calls whose work overlaps on the GPU in the
+// same context (different streams) race on the shared array and must be ordered by the caller.
 #include "aero_face_kernels.cuh"
 #include "ctx.hpp"
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
 #include <string>
+#include <utility>
+#include <vector>
 
 namespace aero {
 namespace {
@@ -36,22 +39,69 @@ constexpr size_t kScratchBytes = kCtrlBytes + 4 * align_up(size_t(kNoallocMaxCel
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mu;
-void* g_scratch_addr[kMaxDevices] = {};
+// The array's device address is looked up once per CUDA context, at the first call made in
+// that context, and cached under the context's ID (unique for the life of the process, so a
+// context created after cudaDeviceReset, or another context on the same device, gets its own
+// lookup). The driver calls that name the current context are fetched through the runtime,
+// so the library needs no link to the driver library.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
 
-// Device address of the scratch array on `device`, which must be current. The host-side
-// name g_noalloc_scratch is only a stand-in; kernels must be given this address.
-cudaError_t scratch_address(int device, void** out) {
-  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+struct DriverCalls {
+  CtxGetCurrentFn get_current = nullptr;
+  CtxGetIdFn get_id = nullptr;
+};
+
+const DriverCalls& driver_calls() {
+  static const DriverCalls calls = [] {
+    DriverCalls d;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      d.get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      d.get_id = reinterpret_cast<CtxGetIdFn>(f);
+    cudaGetLastError();
+    return d;
+  }();
+  return calls;
+}
+
+// ID of the context the runtime uses on this thread (0 when none is current).
+unsigned long long current_context_id() {
+  const DriverCalls& d = driver_calls();
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (d.get_current == nullptr || d.get_id == nullptr || d.get_current(&c) != CUDA_SUCCESS || c == nullptr) return 0;
+  return d.get_id(c, &id) == CUDA_SUCCESS ? id : 0;
+}
+
+std::mutex g_scratch_mu;
+std::vector<std::pair<unsigned long long, void*>> g_scratch_addr;  // (context ID, address)
+
+// Device address of the scratch array in the current context (the context's device must be
+// current). The host-side name g_noalloc_scratch is only a stand-in; kernels must be given
+// this address.
+cudaError_t scratch_address(void** out) {
+  unsigned long long id = current_context_id();
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (g_scratch_addr[device] == nullptr) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_scratch_addr[device] = p;
+  if (id != 0) {
+    for (const auto& e : g_scratch_addr) {
+      if (e.first == id) {
+        *out = e.second;
+        return cudaSuccess;
+      }
+    }
   }
-  *out = g_scratch_addr[device];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return e;
+  if (id == 0) id = current_context_id();  // the lookup above made the runtime's context current
+  if (id != 0) g_scratch_addr.emplace_back(id, p);
+  *out = p;
   return cudaSuccess;
 }
 
@@ -181,7 +231,7 @@ int aero_residual_noalloc(aero_ctx* ctx, const double* conserved_dev, int second
     return AERO_ERR_CUDA;
   }
   void* base = nullptr;
-  cudaError_t e = aero::scratch_address(ctx->device, &base);
+  cudaError_t e = aero::scratch_address(&base);
   if (e == cudaSuccess) {
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : v.stream;
     unsigned char* b = static_cast<unsigned char*>(base);

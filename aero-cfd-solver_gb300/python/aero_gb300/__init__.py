@@ -80,6 +80,7 @@ def load(build_if_missing: bool = False):
         "aero_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip]),
         "aero_select_device": (C.c_int, [C.c_int]),
         "aero_get_info": (C.c_int, [C.c_void_p, _llp, C.c_int]),
+        "aero_set_wait_limit": (C.c_int, [C.c_void_p, C.c_int]),
         "aero_batch_create": (C.c_int, [C.c_int, C.POINTER(MeshDesc), C.POINTER(CaseDesc), C.POINTER(C.c_void_p)]),
         "aero_autotune": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(CaseDesc), C.c_int, C.POINTER(CaseDesc), _dp]),
         "aero_batch_size": (C.c_int, [C.c_void_p]),
@@ -345,7 +346,7 @@ class Solver:
         done = C.c_int(0)
         rc = self.lib.aero_run(self.h, n, recs, C.byref(done))
         out = capi.records_to_array(recs, done.value)
-        if rc == capi.AERO_ERR_NONFINITE and not raise_on_nonfinite:
+        if rc in (capi.AERO_ERR_NONFINITE, capi.AERO_ERR_TIMEOUT) and not raise_on_nonfinite:
             return rc, out
         self._check(rc)
         return rc, out
@@ -377,11 +378,15 @@ class Solver:
         return {k: (ms[i], launches[i]) for i, k in enumerate(self.KERNEL_CLASSES)}
 
     def info(self) -> dict:
-        v = (C.c_longlong * 9)()
-        self._check(self.lib.aero_get_info(self.h, v, 9))
+        v = (C.c_longlong * 10)()
+        self._check(self.lib.aero_get_info(self.h, v, 10))
         keys = ("cells", "faces", "slots_per_cell", "launches_per_iteration", "device_bytes", "precision",
-                "block_size", "blocks", "cases")
+                "block_size", "blocks", "cases", "bulk_copy_gradient")
         return dict(zip(keys, list(v)))
+
+    def set_wait_limit(self, polls: int) -> None:
+        """Poll limit of the iterations' bounded waits on bulk copies (< 0: the default)."""
+        self._check(self.lib.aero_set_wait_limit(self.h, int(polls)))
 
     # ---- discrete adjoint (include/aero_adjoint.h; FP64 contexts)
     def adjoint_linearize(self, w_cd: float = 1.0, w_cl: float = 0.0, second_order: int = -1):
@@ -479,7 +484,7 @@ class Batch(Solver):
         base = capi.records_to_array(recs, n * self.k) if n > 0 else None
         out = [base[k * n: k * n + done[k]].copy() if n > 0 else capi.records_to_array(recs, 0)
                for k in range(self.k)]
-        if rc == capi.AERO_ERR_NONFINITE and not raise_on_nonfinite:
+        if rc in (capi.AERO_ERR_NONFINITE, capi.AERO_ERR_TIMEOUT) and not raise_on_nonfinite:
             return rc, out
         self._check(rc)
         return rc, out

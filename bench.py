@@ -72,6 +72,16 @@ def algorithmic_bytes(kernel: str, n: int, slots: int, precision: str, faces: in
     raise KeyError(kernel)
 
 
+def workload_config(args, cells: int, faces: int) -> dict:
+    """The workload keys both arms report under `config`."""
+    if args.mesh:
+        name = f"NACA0012 {args.mesh[0]}x{args.mesh[1]} O-grid (small profiling case)"
+    else:
+        name = ("NACA0012 512x128 O-grid, 131072 triangles, jitter 10%, permuted; M=0.8, alpha=1.25, "
+                "HLLC+MUSCL venkat, RK3 local dt, CFL 0.8")
+    return {"workload": name, "cells": cells, "faces": faces}
+
+
 def measured_peak():
     p = REPO / "MEASURED_PEAKS.json"
     if p.exists():
@@ -176,28 +186,20 @@ def make_mesh(args):
 # ------------------------------------------------------------------------------------------
 # CPU arms (the oracle port of the reference, bit-identical to it in float mode)
 # ------------------------------------------------------------------------------------------
-def _cpu_worker(mesh_arrays, case_kw, warmup, steps, barrier_, out_q, state=None):
+def _cpu_worker(mesh_kw, case_kw, warmup, steps, barrier_, out_q):
+    """One single-thread oracle replica (spawned process): builds the workload mesh with the
+    oracle's own generator, so that no process of the reference arm loads the product."""
     sys.path.insert(0, str(REPO))
-    sys.path.insert(0, str(REPO / "aero-cfd-solver_gb300" / "python"))
-    from aero_gb300 import capi
     from oracle import oracle_py as op
 
-    mesh = capi.Mesh(**mesh_arrays)
-    case = capi.make_case(**case_kw)
-    sol = op.OracleSolver(op.MODE_FLOAT, mesh, case)
-    if state is not None:
-        sol.set_state(state)
+    mesh = op.ogrid_synthetic(**mesh_kw)
+    sol = op.OracleSolver(op.MODE_FLOAT, mesh, op.make_case(**case_kw))
     sol.run(warmup)
     if barrier_ is not None:
         barrier_.wait()
     t0 = time.perf_counter()
     sol.run(steps)
     out_q.put(time.perf_counter() - t0)
-
-
-def _mesh_arrays(mesh):
-    return dict(owner=mesh.owner, neighbor=mesh.neighbor, bc=mesh.bc, normal=mesh.normal, center=mesh.center,
-                area=mesh.area, volume=mesh.volume, cell_center=mesh.cell_center, wall_faces=mesh.wall_faces)
 
 
 def cpu_sample(mesh, state, target_s=12.0, max_iters=40):
@@ -223,6 +225,10 @@ def cpu_sample(mesh, state, target_s=12.0, max_iters=40):
 
 
 def run_reference_arm(args):
+    """The reference's CPU implementation of the path (the oracle's float mode, bit-identical
+    to the compiled reference) on every host core: one single-thread replica per core, each
+    running the workload case from its first-order start-up state. Nothing from the product
+    package is imported or loaded in any process of this arm."""
     world, rank, local, dist = dist_setup(args)
     if rank != 0:
         return
@@ -231,14 +237,18 @@ def run_reference_arm(args):
     from oracle import oracle_py as op
 
     op.build()
-    mesh = make_mesh(args)
+    mesh_kw = dict(WORKLOAD)
+    if args.mesh:
+        mesh_kw["n_circ"], mesh_kw["n_radial"] = args.mesh
+    n = 2 * mesh_kw["n_circ"] * mesh_kw["n_radial"]
+    faces = mesh_kw["n_circ"] * (3 * mesh_kw["n_radial"] + 1)
     procs_n = args.cpu_procs if args.cpu_procs > 0 else max(1, os.cpu_count() or 1)
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     bar = ctx.Barrier(procs_n)
     kw = dict(CASE, startup_first_order_iters=0)
-    arrays = _mesh_arrays(mesh)
-    procs = [ctx.Process(target=_cpu_worker, args=(arrays, kw, args.warmup, args.steps, bar, q)) for _ in range(procs_n)]
+    procs = [ctx.Process(target=_cpu_worker, args=(mesh_kw, kw, args.warmup, args.steps, bar, q))
+             for _ in range(procs_n)]
     t0 = time.perf_counter()
     for p in procs:
         p.start()
@@ -246,20 +256,19 @@ def run_reference_arm(args):
     for p in procs:
         p.join()
     wall = max(times)
-    value = procs_n * mesh.num_cells * args.steps / wall / 1e6
+    value = procs_n * n * args.steps / wall / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mcell-iter/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "NACA0012 512x128 O-grid, 131072 triangles, jitter 10%, permuted; M=0.8, "
-                               "alpha=1.25, HLLC+MUSCL venkat, RK3 local dt, CFL 0.8",
-                   "cells": mesh.num_cells, "replicas": procs_n},
+        "config": workload_config(args, n, faces),
         "cpu_baseline": {"value": value, "unit": "Mcell-iter/s", "cores": procs_n, "kind": "port",
                          "sample": f"{args.steps} second-order iterations per process after {args.warmup} "
-                                   f"warm-up, {procs_n} independent single-thread replicas of the oracle float "
-                                   f"port (bit-identical to the reference CPU path, pinned against the "
-                                   f"reference's own library by the oracle tests); the GPU host carries no "
-                                   f"reference sources, so the reference binary itself is not built there"},
+                                   f"warm-up, {procs_n} independent single-thread replicas (one per host core) "
+                                   f"of the oracle's float mode, which reproduces the reference CPU path bit for "
+                                   f"bit (pinned by the oracle tests against the compiled reference); the "
+                                   f"GPU host carries no reference sources, so the reference binary itself "
+                                   f"is not built there"},
         "e2e": {"value": value, "unit": "Mcell-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "elapsed_s": time.perf_counter() - t0,
     }

@@ -233,19 +233,20 @@ AERO_API int aero_profile_kernels(aero_ctx* ctx, int n, int flush_l2, double* ms
 AERO_API int aero_select_device(int device);
 
 /* Allocation-free residual. No counterpart in the reference: an addition for callers that
- * cannot allocate device memory while they evaluate the residual -- code being captured into
- * a CUDA graph, code running under another framework's memory pool, or solver loops whose
- * memory is fixed up front (cudaMalloc/cudaFree may synchronise the device).
+ * cannot allocate device memory while they evaluate the residual -- code running under
+ * another framework's memory pool, which owns all device memory, or solver loops whose memory
+ * is fixed up front (cudaMalloc/cudaFree may synchronise the device).
  * Computes what aero_residual computes (gradients only internally), but takes DEVICE
  * pointers owned by the caller: conserved_dev [N][5] and residual_dev [N][5] double in the
  * original cell order, spectral_radius_dev [N] double. It allocates nothing: its working
- * arrays live in one fixed device array of the library (about 16.8 MB, held by every GPU that
- * loads the library until exit), so meshes above 65,536 cells or 196,608 faces are rejected
- * with AERO_ERR_INVALID. The work is queued on `stream` (null: the context's stream) and the call
- * returns without waiting. The first call on each device looks up that array's address;
- * make it before any stream capture. All calls on a device share the array and it keeps
- * the last call's contents: calls whose work overlaps on the GPU race and must be ordered
- * by the caller (one stream, or events). */
+ * arrays live in one fixed device array of the library (about 16.8 MB, held by every CUDA
+ * context that loads the library -- one per GPU for the runtime's primary context -- until
+ * exit), so meshes above 65,536 cells or 196,608 faces are rejected with AERO_ERR_INVALID.
+ * The work is queued on `stream` (null: the context's stream) and the call returns without
+ * waiting. The first call in each CUDA context looks up that array's address; make it before
+ * any stream capture. All calls in one CUDA context share the array and it keeps the last
+ * call's contents: calls whose work overlaps on the GPU race and must be ordered by the
+ * caller (one stream, or events). */
 AERO_API int aero_residual_noalloc(aero_ctx* ctx, const double* conserved_dev, int second_order,
                                    double stab_mach_floor, int all_speed_flux_fix,
                                    double all_speed_f_min, double all_speed_ramp_weight,
@@ -254,8 +255,18 @@ AERO_API int aero_residual_noalloc(aero_ctx* ctx, const double* conserved_dev, i
 /* Sizes and kernel-launch counts of the context, for roofline accounting:
  * info[0] cells, [1] faces, [2] slots per cell (padded), [3] kernel launches per
  * iteration, [4] bytes of device memory held, [5] precision, [6] block size, [7] cell
- * blocks, [8] cases. */
+ * blocks, [8] cases, [9] 1 when the iterations' gradient pass streams its tiles through
+ * shared memory with bulk copies (bounded waits), 0 for the plain gather kernel. */
 AERO_API int aero_get_info(aero_ctx* ctx, long long* info, int n_info);
+
+/* Poll limit of the bounded waits the iterations' kernels make on their bulk copies (no
+ * reference counterpart; the reference has no device waits). polls < 0 restores the default,
+ * about one second. A wait that runs out makes its kernel stop issuing copies, wait for the
+ * copies it has in flight and return; the iteration it belonged to is then not applied (the
+ * conserved state keeps its previous value, no record is written for it), aero_run and the
+ * timing calls return AERO_ERR_TIMEOUT, and the next aero_run continues from the last applied
+ * iteration. */
+AERO_API int aero_set_wait_limit(aero_ctx* ctx, int polls);
 
 /* Autotuner (no reference counterpart): times `iters` second-order iterations of the case on
  * this mesh for every cell ordering (Morton, RCM), block size (64, 128, 256) and number of

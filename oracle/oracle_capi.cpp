@@ -4,6 +4,7 @@
 // bench.py's CPU-baseline leg through ctypes. mode: 0 = float (the reference's
 // arithmetic), 1 = double (FP64 oracle), 2 = float bulk with double accumulation.
 #include "aero_oracle_driver.hpp"
+#include "oracle_mesh.hpp"
 
 #include <memory>
 #include <new>
@@ -91,5 +92,42 @@ int oracle_solver_residual(void* h, const double* u, int second_order, double st
     return 0;
   });
 }
+
+// Synthetic benchmark O-grid (oracle_mesh.hpp). Returns a handle (null on a bad spec) whose
+// sizes oracle_mesh_sizes gives as {cells, faces, wall faces} and whose arrays
+// oracle_mesh_copy writes into caller buffers of those sizes.
+void* oracle_mesh_ogrid(int n_circ, int n_radial, int cell_type, int permute, double chord, double thickness,
+                        double wall_spacing, double farfield_radius, double jitter, unsigned long long seed) {
+  try {
+    return new oracle_mesh::Ogrid(oracle_mesh::ogrid_synthetic(n_circ, n_radial, cell_type, permute != 0, chord,
+                                                               thickness, wall_spacing, farfield_radius, jitter,
+                                                               seed));
+  } catch (...) {
+    return nullptr;
+  }
+}
+
+void oracle_mesh_sizes(const void* h, int* sizes) {
+  const auto* g = static_cast<const oracle_mesh::Ogrid*>(h);
+  sizes[0] = g->num_cells;
+  sizes[1] = g->num_faces;
+  sizes[2] = static_cast<int>(g->wall_faces.size());
+}
+
+void oracle_mesh_copy(const void* h, int* owner, int* neighbor, int* bc, double* normal, double* center,
+                      double* area, double* volume, double* cell_center, int* wall_faces) {
+  const auto* g = static_cast<const oracle_mesh::Ogrid*>(h);
+  std::copy(g->owner.begin(), g->owner.end(), owner);
+  std::copy(g->neighbor.begin(), g->neighbor.end(), neighbor);
+  std::copy(g->bc.begin(), g->bc.end(), bc);
+  std::copy(g->normal.begin(), g->normal.end(), normal);
+  std::copy(g->center.begin(), g->center.end(), center);
+  std::copy(g->area.begin(), g->area.end(), area);
+  std::copy(g->volume.begin(), g->volume.end(), volume);
+  std::copy(g->cell_center.begin(), g->cell_center.end(), cell_center);
+  std::copy(g->wall_faces.begin(), g->wall_faces.end(), wall_faces);
+}
+
+void oracle_mesh_free(void* h) { delete static_cast<oracle_mesh::Ogrid*>(h); }
 
 }  // extern "C"

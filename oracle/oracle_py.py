@@ -1,7 +1,9 @@
 """TEST INFRASTRUCTURE ONLY: ctypes loaders for the CPU oracle (oracle/_build/liboracle.so)
 and, where it was built, the compiled reference (oracle/_ref/libaero_ref.so).
 
-Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module.
+Only tests/, __graft_entry__.smoke() and bench.py's CPU arms import this module. It needs
+nothing from the product package: structures come from oracle_types (read from the C
+header), and the benchmark's synthetic meshes from the oracle's own generator.
 """
 
 from __future__ import annotations
@@ -11,6 +13,9 @@ import subprocess
 from pathlib import Path
 
 import numpy as np
+
+from . import oracle_types as ot
+from .oracle_types import OracleMesh, make_case  # noqa: F401
 
 HERE = Path(__file__).resolve().parent
 ORACLE_LIB = HERE / "_build" / "liboracle.so"
@@ -29,32 +34,28 @@ def build(ref: bool = False) -> None:
     subprocess.run(["make", "-s", "-C", str(HERE), *targets], check=True)
 
 
-def _capi():
-    import sys
-    pkg = HERE.parent / "aero-cfd-solver_gb300" / "python"
-    if str(pkg) not in sys.path:
-        sys.path.insert(0, str(pkg))
-    from aero_gb300 import capi  # noqa: WPS433
-    return capi
-
-
 def oracle_lib():
     global _oracle
     if _oracle is None:
         if not ORACLE_LIB.exists():
             build()
         lib = C.CDLL(str(ORACLE_LIB))
-        capi = _capi()
         lib.oracle_solver_create.restype = C.c_void_p
-        lib.oracle_solver_create.argtypes = [C.c_int, C.POINTER(capi.MeshDesc), C.POINTER(capi.CaseDesc)]
+        lib.oracle_solver_create.argtypes = [C.c_int, C.POINTER(ot.MeshDesc), C.POINTER(ot.CaseDesc)]
         lib.oracle_solver_destroy.argtypes = [C.c_void_p]
         lib.oracle_solver_set_state.argtypes = [C.c_void_p, _dp]
         lib.oracle_solver_get_state.argtypes = [C.c_void_p, _dp]
         lib.oracle_solver_last_residual.argtypes = [C.c_void_p, _dp, _dp]
         lib.oracle_solver_reset_run.argtypes = [C.c_void_p]
-        lib.oracle_solver_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(capi.IterRecord), _ip]
+        lib.oracle_solver_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(ot.IterRecord), _ip]
         lib.oracle_solver_residual.argtypes = [C.c_void_p, _dp, C.c_int, C.c_double, C.c_int,
                                                C.c_double, C.c_double, _dp, _dp, _dp, _ip, _dp]
+        lib.oracle_mesh_ogrid.restype = C.c_void_p
+        lib.oracle_mesh_ogrid.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                          C.c_double, C.c_double, C.c_ulonglong]
+        lib.oracle_mesh_sizes.argtypes = [C.c_void_p, _ip]
+        lib.oracle_mesh_copy.argtypes = [C.c_void_p, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _ip]
+        lib.oracle_mesh_free.argtypes = [C.c_void_p]
         _oracle = lib
     return _oracle
 
@@ -67,15 +68,14 @@ def ref_lib():
         if not REF_LIB.exists():
             return None
         lib = C.CDLL(str(REF_LIB))
-        capi = _capi()
         lib.ref_last_error.restype = C.c_char_p
         lib.ref_ogrid_build.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double]
         lib.ref_mesh_sizes.argtypes = [_ip]
         fp = C.POINTER(C.c_float)
         lib.ref_mesh_get.argtypes = [_ip, _ip, _ip, _ip, fp, fp, fp, fp, fp, fp, _ip, _ip]
-        lib.ref_residual.argtypes = [C.POINTER(capi.MeshDesc), C.POINTER(capi.CaseDesc), _dp, C.c_int,
+        lib.ref_residual.argtypes = [C.POINTER(ot.MeshDesc), C.POINTER(ot.CaseDesc), _dp, C.c_int,
                                      C.c_double, C.c_int, C.c_double, C.c_double, _dp, _dp, _dp, _ip]
-        lib.ref_run_case.argtypes = [C.POINTER(capi.CaseDesc), C.c_char_p, C.c_int, C.c_int, C.c_double,
+        lib.ref_run_case.argtypes = [C.POINTER(ot.CaseDesc), C.c_char_p, C.c_int, C.c_int, C.c_double,
                                      C.c_double, C.c_char_p, _dp, C.c_int, _ip, _dp, _dp, _dp, _dp]
         _ref = lib
     return _ref
@@ -85,16 +85,14 @@ class OracleSolver:
     """One oracle solver instance on an injected mesh."""
 
     def __init__(self, mode: int, mesh, case):
-        capi = _capi()
         self.lib = oracle_lib()
-        self.mesh = mesh
-        self._mdesc = mesh.desc()
-        self._case = case
-        self.h = self.lib.oracle_solver_create(mode, C.byref(self._mdesc), C.byref(case))
+        self.mesh = OracleMesh.of(mesh)
+        self._mdesc = self.mesh.desc()
+        self._case = ot.case_desc(case)
+        self.h = self.lib.oracle_solver_create(mode, C.byref(self._mdesc), C.byref(self._case))
         if not self.h:
             raise RuntimeError("oracle_solver_create failed")
-        self.n = mesh.num_cells
-        self._capi = capi
+        self.n = self.mesh.num_cells
 
     def close(self):
         if self.h:
@@ -123,10 +121,10 @@ class OracleSolver:
         self.lib.oracle_solver_reset_run(self.h)
 
     def run(self, n: int):
-        recs = (self._capi.IterRecord * max(n, 1))()
+        recs = (ot.IterRecord * max(n, 1))()
         done = C.c_int(0)
         status = self.lib.oracle_solver_run(self.h, n, recs, C.byref(done))
-        return status, self._capi.records_to_array(recs, done.value)
+        return status, ot.records_to_array(recs, done.value)
 
     def residual(self, u, second_order=True, stab=0.0, as_fix=False, as_fmin=0.05, as_ramp=1.0,
                  with_scale=False):
@@ -154,8 +152,9 @@ def ref_residual(mesh, case, u, second_order=True, stab=0.0, as_fix=False, as_fm
     s = np.empty(n, np.float64)
     g = np.empty(n * 10, np.float64)
     diag = (C.c_int * 3)()
-    md = mesh.desc()
-    rc = lib.ref_residual(C.byref(md), C.byref(case), u.ctypes.data_as(_dp), int(second_order),
+    md = OracleMesh.of(mesh).desc()
+    cd = ot.case_desc(case)
+    rc = lib.ref_residual(C.byref(md), C.byref(cd), u.ctypes.data_as(_dp), int(second_order),
                           float(stab), int(as_fix), float(as_fmin), float(as_ramp),
                           r.ctypes.data_as(_dp), s.ctypes.data_as(_dp), g.ctypes.data_as(_dp), diag)
     if rc != 0:
@@ -194,3 +193,28 @@ def ref_current_mesh():
     return dict(owner=owner, neighbor=nb, bc=bc, face_vertices=fv, normal=normal, center=center,
                 area=area, volume=vol, cell_center=cc, points=pts, cell_conn=conn,
                 patches=patches, wall_faces=np.array(wall, np.int32))
+
+
+def ogrid_synthetic(n_circ: int, n_radial: int, cell_type: int = 3, permute: bool = True, chord: float = 1.0,
+                    thickness: float = 0.12, wall_spacing: float = 0.005, farfield_radius: float = 20.0,
+                    jitter: float = 0.0, seed: int = 1) -> OracleMesh:
+    """The benchmark's synthetic O-grid from the oracle's own generator (oracle_mesh.hpp),
+    the same mesh as the product generator builds from the same arguments."""
+    lib = oracle_lib()
+    h = lib.oracle_mesh_ogrid(n_circ, n_radial, cell_type, int(permute), chord, thickness, wall_spacing,
+                              farfield_radius, jitter, seed)
+    if not h:
+        raise ValueError("oracle_mesh_ogrid: invalid O-grid specification")
+    try:
+        sizes = (C.c_int * 3)()
+        lib.oracle_mesh_sizes(h, sizes)
+        nc, nf, nw = list(sizes)
+        a = dict(owner=np.empty(nf, np.int32), neighbor=np.empty(nf, np.int32), bc=np.empty(nf, np.int32),
+                 normal=np.empty(3 * nf), center=np.empty(3 * nf), area=np.empty(nf), volume=np.empty(nc),
+                 cell_center=np.empty(3 * nc), wall_faces=np.empty(nw, np.int32))
+        ptr = {k: v.ctypes.data_as(_ip if v.dtype == np.int32 else _dp) for k, v in a.items()}
+        lib.oracle_mesh_copy(h, ptr["owner"], ptr["neighbor"], ptr["bc"], ptr["normal"], ptr["center"],
+                             ptr["area"], ptr["volume"], ptr["cell_center"], ptr["wall_faces"])
+    finally:
+        lib.oracle_mesh_free(h)
+    return OracleMesh(**a)

@@ -4,7 +4,7 @@ The reference is compiled from its own sources by `make -C oracle ref` (into
 oracle/_ref/, never committed) and driven through oracle/ref_shim.cpp. Run from the
 repository root on a machine where the reference sources are mounted:
 
-    python tests/golden/make_golden.py [--ref-root /path/to/reference]
+    python tests/golden/make_golden.py --ref-root <AeroCFD source root>
 
 Outputs (all values exactly as the reference computed them, in float32):
   meshes.npz     reference meshes: demo 2x2 (src/cfd_core/mesh/mesh.cpp:44) and
@@ -35,6 +35,7 @@ sys.path.insert(0, str(REPO / "aero-cfd-solver_gb300" / "python"))
 
 from aero_gb300 import capi  # noqa: E402
 from oracle import oracle_py as op  # noqa: E402
+from oracle import oracle_types as ot  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
 _dp = C.POINTER(C.c_double)
@@ -155,7 +156,7 @@ def seeded_state(mesh: capi.Mesh, case, seed: int, stress: bool) -> np.ndarray:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default="/root/reference")
+    ap.add_argument("--ref-root", required=True, help="root of the AeroCFD sources to compile")
     args = ap.parse_args()
     os.environ["REF_ROOT"] = args.ref_root
     op.build(ref=True)
@@ -211,7 +212,7 @@ def main() -> None:
         else:
             os.environ.pop("AERO_ENABLE_EXPERIMENTAL_PRECOND", None)
         with tempfile.TemporaryDirectory() as d:
-            rc = ref.ref_run_case(C.byref(case), b"0012", nc, nr, radius, stretch, d.encode(),
+            rc = ref.ref_run_case(C.byref(ot.case_desc(case)), b"0012", nc, nr, radius, stretch, d.encode(),
                                   h.ctypes.data_as(_dp), maxh, C.byref(nd), consv.ctypes.data_as(_dp),
                                   lr.ctypes.data_as(_dp), ls.ctypes.data_as(_dp), C.byref(mw))
         os.environ.pop("AERO_ENABLE_EXPERIMENTAL_PRECOND", None)

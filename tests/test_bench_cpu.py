@@ -43,3 +43,39 @@ def test_reference_arm_prints_the_contract_line():
     assert cb["kind"] == "port" and cb["cores"] == 2 and cb["value"] == line["value"] and cb["sample"]
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+_PROBE = r"""
+import sys, queue
+sys.path.insert(0, {repo!r})
+import bench
+from oracle import oracle_py as op
+q = queue.Queue()
+bench._cpu_worker(dict(bench.WORKLOAD, n_circ=32, n_radial=8), dict(bench.CASE, startup_first_order_iters=0),
+                  1, 1, None, q)
+assert q.get() > 0
+maps = open("/proc/self/maps").read()
+print("PRODUCT_IMPORTED" if any(m.startswith("aero_gb300") for m in sys.modules) else "NO_PRODUCT_IMPORT")
+print("PRODUCT_MAPPED" if "libaero_gb300" in maps else "NO_PRODUCT_MAPPED")
+print("ORACLE_MAPPED" if "liboracle" in maps else "NO_ORACLE")
+"""
+
+
+def test_reference_arm_worker_neither_imports_nor_maps_the_product():
+    """The reference arm's replicas build their mesh with the oracle's own generator and run
+    the oracle: no module of the product package is imported and libaero_gb300.so is never
+    mapped into the process."""
+    r = subprocess.run([sys.executable, "-c", _PROBE.format(repo=str(REPO))], capture_output=True, text=True,
+                       cwd=REPO, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = r.stdout.split()
+    assert "NO_PRODUCT_IMPORT" in out and "NO_PRODUCT_MAPPED" in out and "ORACLE_MAPPED" in out
+
+
+def test_reference_arm_reports_the_gpu_arm_workload():
+    class A:
+        mesh = None
+
+    cfg = bench.workload_config(A(), 131072, 197120)
+    assert cfg == {"workload": cfg["workload"], "cells": 131072, "faces": 197120}
+    assert "512x128" in cfg["workload"] and "HLLC+MUSCL venkat" in cfg["workload"]

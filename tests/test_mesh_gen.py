@@ -99,3 +99,18 @@ def test_synthetic_ogrid_deterministic_and_seeded():
     # the far field is a circle of radius 20 chords around mid-chord
     p = a.points.reshape(-1, 3)[-48:]
     assert np.allclose(np.hypot(p[:, 0] - 0.5, p[:, 1]), 20.0, atol=1e-9)
+
+
+@pytest.mark.parametrize("spec", [(512, 128, 3, True, 0.1, 2), (128, 32, 4, False, 0.0, 1), (64, 16, 3, True, 0.1, 100),
+                                  (96, 24, 4, True, 0.1, 11)])
+def test_oracle_generator_builds_the_same_mesh(spec):
+    """The oracle's own synthetic O-grid generator (used by the reference arm of the benchmark,
+    which must not load the product) builds the product generator's mesh bit for bit."""
+    from oracle import oracle_py as op
+
+    nc, nr, ct, perm, jit, seed = spec
+    kw = dict(cell_type=ct, permute=perm, jitter=jit, seed=seed, wall_spacing=0.005, farfield_radius=20.0)
+    a = aero_gb300.ogrid_synthetic(nc, nr, **kw)
+    b = op.ogrid_synthetic(nc, nr, **kw)
+    for key in ("owner", "neighbor", "bc", "normal", "center", "area", "volume", "cell_center", "wall_faces"):
+        np.testing.assert_array_equal(getattr(a, key), getattr(b, key), err_msg=key)

@@ -1,15 +1,15 @@
 """The allocation-free residual entry point, aero_residual_noalloc.
 
 It exists for callers that cannot allocate device memory while they evaluate the
-residual: code being captured into a CUDA graph, code running under another framework's
-memory pool, or solver loops whose device memory is fixed up front. Such a caller owns the
-input and output buffers; the library supplies its working arrays from one fixed device
-array. This test allocates the buffers with PyTorch (standing in for such a caller), calls
-the entry point through the C ABI, and checks it against the existing aero_residual entry
-point on two calls in a row (different states), plus a repeat of the first state, with the
-tolerance of the other parity tests: |dR| <= 1e-12 (FP64) or 2e-5 (FP32) times the
-per-cell sum over faces of |F_k A|. It also checks that meshes above the array's limit are
-refused. It runs on its own in a fresh process as well as after the other tests.
+residual: code running under another framework's memory pool, or solver loops whose device
+memory is fixed up front. Such a caller owns the input and output buffers; the library
+supplies its working arrays from one fixed device array. This test allocates the buffers with
+PyTorch (standing in for such a caller), calls the entry point through the C ABI, and checks
+it against the existing aero_residual entry point on two calls in a row (different states),
+plus a repeat of the first state, with the tolerance of the other parity tests: |dR| <= 1e-12
+(FP64) or 2e-5 (FP32) times the per-cell sum over faces of |F_k A|; the FP64 results are also
+checked against the FP64 oracle at 1e-12. It also checks that meshes above the array's limit
+are refused. It runs on its own in a fresh process as well as after the other tests.
 """
 
 import ctypes as C
@@ -80,9 +80,11 @@ def test_noalloc_matches_existing_entry_point(lib, precision, tol, numerics):
         for u in (u1, u2, u1):  # two calls in a row on different states, then the first again
             r, s = _noalloc(lib, solver, u, args)
             r_ref, s_ref, _ = solver.residual(u, *args)
-            fscale = oracle.residual(u, *args, with_scale=True)[4]
+            r_or, _, _, _, fscale = oracle.residual(u, *args, with_scale=True)
             assert np.all(np.isfinite(r)) and np.all(np.isfinite(s))
             assert np.max(np.abs(r - r_ref) / (fscale + 1e-300)) <= tol
+            if precision == capi.PRECISION_FP64:
+                assert np.max(np.abs(r - r_or) / (fscale + 1e-300)) <= 1e-12
             np.testing.assert_allclose(s, s_ref, rtol=tol)
             results.append(r)
         # the shared array keeps the previous call's contents; results must not depend on it

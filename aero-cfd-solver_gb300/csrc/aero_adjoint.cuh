@@ -539,4 +539,108 @@ __global__ void k_adj_geo_face(DevFaces<double> f, const double2* __restrict__ d
            a.z * (fl.fy.d[0] * A + fl.fy.v * dA) + a.w * (fl.e.d[0] * A + fl.e.v * dA);
 }
 
+// Reverse products of the geometry: the transposes of k_adj_geo_face and k_adj_geo_grad, so
+// that dJ/d(every face normal, length and centre, cell volume and centre) comes from one pass
+// instead of one tangent per geometry perturbation.
+//
+// Per face i, with a = lam_o - lam_n (lam_o at a boundary face): the derivatives of a . (F A)
+// at fixed primitives and gradients with respect to the face's unit normal (x, y), its length,
+// and the MUSCL offsets of the face centre from the owner's and the neighbour's centres:
+// out[7 i + 0..6] = (nx, ny, length, dox, doy, dnx, dny). One pass in six-way dual numbers.
+template <int FLUX, bool SECOND, bool LM>
+__global__ void k_adj_geo_face_vjp(DevFaces<double> f, const int2* __restrict__ fblk,
+                                   const FaceParams<double>* __restrict__ fps, const Ctrl* __restrict__ ctrl,
+                                   const d4* __restrict__ W, const d4* __restrict__ gx, const d4* __restrict__ gy,
+                                   const d4* __restrict__ lam, double* __restrict__ out) {
+  using D = ad::Dual<6>;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int2 bd = fblk[blockIdx.x];
+  if (i >= bd.y) return;
+  const FaceParams<D> fp = dual_params<6>(scheduled_params(fps[bd.x], ctrl, LM));
+  const int2 oc = f.cells[i];
+  const int o = oc.x, b = oc.y;
+  const d4 w0 = W[o];
+  const d4 w1 = b >= 0 ? W[b] : w0;
+  D gO[8], gN[8];
+  for (int k = 0; k < 8; ++k) gO[k] = gN[k] = D(0.0);
+  D dox(0.0), doy(0.0), dnx(0.0), dny(0.0);
+  if (b >= 0 && SECOND) {
+    const d4 a = gx[o], c = gy[o], e = gx[b], h = gy[b];
+    const double g0[8] = {a.x, a.y, a.z, a.w, c.x, c.y, c.z, c.w};
+    const double g1[8] = {e.x, e.y, e.z, e.w, h.x, h.y, h.z, h.w};
+    for (int k = 0; k < 8; ++k) {
+      gO[k] = D(g0[k]);
+      gN[k] = D(g1[k]);
+    }
+    dox = ad::seed<6>(f.doff[i].x, 2);
+    doy = ad::seed<6>(f.doff[i].y, 3);
+    dnx = ad::seed<6>(f.noff[i].x, 4);
+    dny = ad::seed<6>(f.noff[i].y, 5);
+  }
+  const double2 nd = f.nrm[i];
+  Flux<D> fl;
+  D mws;
+  bool fo = false, df = false;
+  eval_face<D, FLUX, SECOND, LM>(fp, b, Prim<D>{D(w0.x), D(w0.y), D(w0.z), D(w0.w)},
+                                 Prim<D>{D(w1.x), D(w1.y), D(w1.z), D(w1.w)}, gO, gN, ad::seed<6>(nd.x, 0),
+                                 ad::seed<6>(nd.y, 1), dox, doy, dnx, dny, &fl, &mws, &fo, &df);
+  const d4 lo = lam[o];
+  d4 a = lo;
+  if (b >= 0) {
+    const d4 ln = lam[b];
+    a = d4{lo.x - ln.x, lo.y - ln.y, lo.z - ln.z, lo.w - ln.w};
+  }
+  const double A = f.area[i];
+  double dk[6];
+  for (int k = 0; k < 6; ++k) dk[k] = A * (a.x * fl.m.d[k] + a.y * fl.fx.d[k] + a.z * fl.fy.d[k] + a.w * fl.e.d[k]);
+  double* r = out + 7 * static_cast<size_t>(i);
+  r[0] = dk[0];
+  r[1] = dk[1];
+  r[2] = a.x * fl.m.v + a.y * fl.fx.v + a.z * fl.fy.v + a.w * fl.e.v;
+  r[3] = dk[2];
+  r[4] = dk[3];
+  r[5] = dk[4];
+  r[6] = dk[5];
+}
+
+// With (mgx, mgy) the adjoint of the Green-Gauss gradients (cell_gradient: G_c = (1/V_c)
+// sum_s sgn_s q_s n_s A_s), per slot s = k * n + c the derivatives of mg . G with respect to
+// the slot's unit normal (x, y) and length, out_slot[3 s + 0..2], and per cell the derivative
+// with respect to 1 / V_c, out_inv[c], at fixed primitives.
+static __global__ void k_adj_geo_grad_vjp(DevMesh<double> m, const int2* __restrict__ cblk, const d4* __restrict__ W,
+                                          const d4* __restrict__ mgx, const d4* __restrict__ mgy,
+                                          double* __restrict__ out_slot, double* __restrict__ out_inv) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cblk[blockIdx.x].y) return;
+  const d4 wc = W[c], bx = mgx[c], by = mgy[c];
+  const double inv = m.inv_vol[c];
+  double binv = 0.0;
+  for (int k = 0; k < m.d; ++k) {
+    const int s = k * m.n + c;
+    const int link = m.link[s];
+    if (link == kPad) break;
+    const double2 nd = m.nrm[s];
+    const double a = m.area[s];
+    double q[4] = {wc.x, wc.y, wc.z, wc.w};
+    double sgn = 1.0;
+    if (link >= 0) {
+      const d4 wo = W[link >> 1];
+      q[0] = 0.5 * (q[0] + wo.x);
+      q[1] = 0.5 * (q[1] + wo.y);
+      q[2] = 0.5 * (q[2] + wo.z);
+      q[3] = 0.5 * (q[3] + wo.w);
+      if (link & 1) sgn = -1.0;
+    }
+    const double px = bx.x * q[0] + bx.y * q[1] + bx.z * q[2] + bx.w * q[3];
+    const double py = by.x * q[0] + by.y * q[1] + by.z * q[2] + by.w * q[3];
+    const double bnax = inv * sgn * px, bnay = inv * sgn * py;  // d/d(n_x A), d/d(n_y A)
+    double* r = out_slot + 3 * static_cast<size_t>(s);
+    r[0] = bnax * a;
+    r[1] = bnay * a;
+    r[2] = bnax * nd.x + bnay * nd.y;
+    binv += sgn * (px * nd.x * a + py * nd.y * a);
+  }
+  out_inv[c] = binv;
+}
+
 }  // namespace aero

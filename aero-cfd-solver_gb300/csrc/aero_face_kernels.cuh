@@ -51,16 +51,24 @@ __device__ __forceinline__ void eval_face(const FaceParams<T>& fp, int b, const 
   } else if (b != -2) {
     cr = fp.farfield;
   }
-  const T as = face_acoustic_scale<T, LM>(cl, cr, fp);
+  // both sides in primitive form, converted once for the acoustic scale and the flux
+  FaceSides<T> sd = face_sides(cl, cr, nx, ny, fp.gamma);
+  SideMach<T> sm{};
+  if (LM) sm = side_mach(sd);
+  const T as = face_acoustic_scale<T, LM>(sd, sm, fp);
   if (b == -2) {  // slip wall: pressure-only flux (boundary_conditions.cpp:97-110)
-    const Prim<T> w = cons_to_prim(cl, fp.gamma);
-    const T un = w.u * nx + w.v * ny;
-    const T a = sound_speed(w, fp.gamma);
+    const Prim<T>& w = sd.pl;
     *f = Flux<T>{T(0), w.p * nx, w.p * ny, T(0)};
-    *mws = precond_speeds(un, a, as).sr;
+    *mws = face_speeds<T, LM>(sd.unl, sd.al, as).sr;
   } else {
-    if (b < 0 && fp.precond_farfield_bc) cr = precond_farfield_state(cl, nx, ny, fp, as);
-    *f = face_flux<T, FLUX, LM>(cl, cr, nx, ny, fp, as, mws, df);
+    if (b < 0 && fp.precond_farfield_bc) {  // the characteristic state replaces the free stream
+      cr = precond_farfield_state(cl, nx, ny, fp, as);
+      sd.pr = cons_to_prim(cr, fp.gamma);
+      sd.unr = sd.pr.u * nx + sd.pr.v * ny;
+      sd.ar = sound_speed(sd.pr, fp.gamma);
+      if (LM) sm = side_mach(sd);
+    }
+    *f = face_flux<T, FLUX, LM>(cl, cr, sd, sm, nx, ny, fp, as, mws, df);
   }
 }
 

@@ -218,6 +218,28 @@ __device__ __forceinline__ Speeds<T> precond_speeds(T un, T a, T acoustic_scale)
   return s;
 }
 
+// precond_speeds at acoustic scale 1 (no low-Mach scaling), with the same results: beta = 1,
+// so ut = un exactly and ct = sqrt(4 a^2) / 2 = a exactly (the correctly rounded square root of
+// a rounded square returns the operand, and scaling by 4 is exact), and the largest of |un|,
+// |un - a|, |un + a| (a >= 0) is the rounded |un| + a.
+template <class T>
+__device__ __forceinline__ Speeds<T> unit_speeds(T un, T a) {
+  Speeds<T> s;
+  s.lm = un - a;
+  s.lp = un + a;
+  s.sr = smax(sabs(un) + a, Kn<T>::wave_floor);
+  return s;
+}
+// the speeds at the face's acoustic scale: LM false means the scale is exactly 1
+template <class T, bool LM>
+__device__ __forceinline__ Speeds<T> face_speeds(T un, T a, T as) {
+  if constexpr (LM) {
+    return precond_speeds(un, a, as);
+  } else {
+    return unit_speeds(un, a);
+  }
+}
+
 // Settings of one residual evaluation that do not change within a launch
 // (residual_assembly.hpp:12-31, preconditioning.hpp:9-15).
 template <class T>
@@ -235,16 +257,48 @@ struct FaceParams {
   T as_cutoff, as_fmin, as_ramp;
 };
 
+// The two sides of a face in primitive form with the quantities the acoustic scale, the
+// all-speed pressure scale and the flux all use, formed once per face: the reference's helpers
+// each convert and derive them again from the conservative states, with identical results.
+template <class T>
+struct FaceSides {
+  Prim<T> pl, pr;
+  T unl, unr;  // normal velocities
+  T al, ar;    // sound speeds
+};
+template <class T>
+__device__ __forceinline__ FaceSides<T> face_sides(const Cons<T>& l, const Cons<T>& r, T nx, T ny, T gamma) {
+  FaceSides<T> f;
+  f.pl = cons_to_prim(l, gamma);
+  f.pr = cons_to_prim(r, gamma);
+  f.unl = f.pl.u * nx + f.pl.v * ny;
+  f.unr = f.pr.u * nx + f.pr.v * ny;
+  f.al = sound_speed(f.pl, gamma);
+  f.ar = sound_speed(f.pr, gamma);
+  return f;
+}
+// local Mach numbers |u| / max(a, floor) of both sides (preconditioning.cpp:17-22, the
+// euler_flux.cpp:159-163 and :189-191 forms are the same expression)
+template <class T>
+struct SideMach {
+  T al, ar;  // max(a, floor)
+  T ml, mr;
+};
+template <class T>
+__device__ __forceinline__ SideMach<T> side_mach(const FaceSides<T>& f) {
+  SideMach<T> m;
+  m.al = smax(f.al, Kn<T>::wave_floor);
+  m.ar = smax(f.ar, Kn<T>::wave_floor);
+  m.ml = sdiv(vmag(f.pl), m.al);
+  m.mr = sdiv(vmag(f.pr), m.ar);
+  return m;
+}
+
 // euler_flux.cpp:154-175 (prims already converted by the caller)
 template <class T>
-__device__ __forceinline__ T low_mach_dissipation_scale(const Prim<T>& pl, const Prim<T>& pr,
-                                                        T gamma, T cutoff, T mach_ref) {
+__device__ __forceinline__ T low_mach_dissipation_scale(const SideMach<T>& sm, T cutoff, T mach_ref) {
   if (cutoff <= T(0)) return T(1);
-  const T al = smax(sound_speed(pl, gamma), Kn<T>::wave_floor);
-  const T ar = smax(sound_speed(pr, gamma), Kn<T>::wave_floor);
-  const T ml = sdiv(vmag(pl), al);
-  const T mr = sdiv(vmag(pr), ar);
-  const T fm = T(0.5) * (ml + mr);
+  const T fm = T(0.5) * (sm.ml + sm.mr);
   const T mstar = smax(fm, smax(mach_ref, Kn<T>::wave_floor));
   const T ratio = sdiv(mstar, smax(cutoff, Kn<T>::wave_floor));
   return sclamp(ratio, Kn<T>::low_mach_min, T(1));
@@ -252,13 +306,10 @@ __device__ __forceinline__ T low_mach_dissipation_scale(const Prim<T>& pl, const
 
 // euler_flux.cpp:81-98 + 177-201
 template <class T>
-__device__ __forceinline__ T all_speed_pressure_scale(const Prim<T>& pl, const Prim<T>& pr, T nx,
-                                                      T ny, const FaceParams<T>& fp) {
-  const T unl = pl.u * nx + pl.v * ny, unr = pr.u * nx + pr.v * ny;
-  const T al = smax(sound_speed(pl, fp.gamma), Kn<T>::wave_floor);
-  const T ar = smax(sound_speed(pr, fp.gamma), Kn<T>::wave_floor);
-  const T mach = smax(T(0.5) * (sdiv(vmag(pl), al) + sdiv(vmag(pr), ar)), Kn<T>::all_speed_floor);
-  T mn = smax(T(0.5) * (sdiv(sabs(unl), al) + sdiv(sabs(unr), ar)), Kn<T>::all_speed_floor);
+__device__ __forceinline__ T all_speed_pressure_scale(const FaceSides<T>& f, const SideMach<T>& sm,
+                                                      const FaceParams<T>& fp) {
+  const T mach = smax(T(0.5) * (sm.ml + sm.mr), Kn<T>::all_speed_floor);
+  T mn = smax(T(0.5) * (sdiv(sabs(f.unl), sm.al) + sdiv(sabs(f.unr), sm.ar)), Kn<T>::all_speed_floor);
   mn = smin(mn, mach);
   mn = smax(mn, Kn<T>::all_speed_floor);
   const T cut = smax(fp.as_cutoff, Kn<T>::all_speed_floor);
@@ -272,15 +323,15 @@ __device__ __forceinline__ T all_speed_pressure_scale(const Prim<T>& pl, const P
   return sclamp(te, tfloor, T(1));
 }
 
-// euler_flux.cpp:203-239. ul/ur conservative, pl/pr = cons_to_prim(ul/ur).
-template <class T>
-__device__ __forceinline__ Flux<T> rusanov(const Cons<T>& ul, const Cons<T>& ur, const Prim<T>& pl,
-                                           const Prim<T>& pr, T nx, T ny, T gamma, T as,
-                                           T* mws) {
-  const T unl = pl.u * nx + pl.v * ny, unr = pr.u * nx + pr.v * ny;
-  const T al = sound_speed(pl, gamma), ar = sound_speed(pr, gamma);
+// euler_flux.cpp:203-239. ul/ur conservative, f their primitive sides.
+template <class T, bool LM>
+__device__ __forceinline__ Flux<T> rusanov(const Cons<T>& ul, const Cons<T>& ur, const FaceSides<T>& f, T nx,
+                                           T ny, T as, T* mws) {
+  const T unl = f.unl, unr = f.unr, al = f.al, ar = f.ar;
+  const Prim<T>& pl = f.pl;
+  const Prim<T>& pr = f.pr;
   const T smax_phys = smax(sabs(unl) + al, sabs(unr) + ar);
-  const T sdiss = smax(precond_speeds(unl, al, as).sr, precond_speeds(unr, ar, as).sr);
+  const T sdiss = smax(face_speeds<T, LM>(unl, al, as).sr, face_speeds<T, LM>(unr, ar, as).sr);
   *mws = smax(smax_phys, Kn<T>::wave_floor);
   const Flux<T> fl = physical_flux(ul, pl, nx, ny), fr = physical_flux(ur, pr, nx, ny);
   const T hs = T(0.5) * sdiss;
@@ -296,21 +347,21 @@ __device__ __forceinline__ bool finite4(T a, T b, T c, T d) {
 // euler_flux.cpp:241-364. LM selects the all-speed pressure correction; with LM false the
 // pressure scale is the constant 1 the reference uses when the fix is off.
 template <class T, bool LM>
-__device__ __forceinline__ Flux<T> hllc(const Cons<T>& ul, const Cons<T>& ur, T nx, T ny,
-                                        const FaceParams<T>& fp, T as, T* mws, bool* fallback) {
-  const T gamma = fp.gamma;
-  const Prim<T> pl = cons_to_prim(ul, gamma), pr = cons_to_prim(ur, gamma);
-  const T unl = pl.u * nx + pl.v * ny, unr = pr.u * nx + pr.v * ny;
-  const T al = sound_speed(pl, gamma), ar = sound_speed(pr, gamma);
+__device__ __forceinline__ Flux<T> hllc(const Cons<T>& ul, const Cons<T>& ur, const FaceSides<T>& f,
+                                        const SideMach<T>& sm, T nx, T ny, const FaceParams<T>& fp, T as,
+                                        T* mws, bool* fallback) {
+  const Prim<T>& pl = f.pl;
+  const Prim<T>& pr = f.pr;
+  const T unl = f.unl, unr = f.unr, al = f.al, ar = f.ar;
   T ps = T(1);
   if (LM) {
-    if (fp.as_fix) ps = all_speed_pressure_scale(pl, pr, nx, ny, fp);
+    if (fp.as_fix) ps = all_speed_pressure_scale(f, sm, fp);
   }
   const T pavg = T(0.5) * (pl.p + pr.p);
   const T plc = pavg + ps * (pl.p - pavg);
   const T prc = pavg + ps * (pr.p - pavg);
-  const Speeds<T> spl = precond_speeds(unl, al, as);
-  const Speeds<T> spr = precond_speeds(unr, ar, as);
+  const Speeds<T> spl = face_speeds<T, LM>(unl, al, as);
+  const Speeds<T> spr = face_speeds<T, LM>(unr, ar, as);
   const T s_l = smin(spl.lm, spr.lm);
   const T s_r = smax(spl.lp, spr.lp);
   const T slp = smin(unl - al, unr - ar);
@@ -319,7 +370,7 @@ __device__ __forceinline__ Flux<T> hllc(const Cons<T>& ul, const Cons<T>& ur, T 
   *fallback = false;
 
   bool diffusive = sabs(s_r - s_l) < Kn<T>::wave_floor;
-  Flux<T> f;
+  Flux<T> fx;
   if (!diffusive) {
     const Flux<T> fl = physical_flux(ul, pl, nx, ny);
     const Flux<T> fr = physical_flux(ur, pr, nx, ny);
@@ -365,21 +416,21 @@ __device__ __forceinline__ Flux<T> hllc(const Cons<T>& ul, const Cons<T>& ur, T 
                   stl.r <= T(0) || str.r <= T(0);
       if (!diffusive) {
         if (s_m >= T(0)) {
-          f = {fl.m + s_l * (stl.r - ul.r), fl.fx + s_l * (stl.ru - ul.ru), fl.fy + s_l * (stl.rv - ul.rv),
+          fx = {fl.m + s_l * (stl.r - ul.r), fl.fx + s_l * (stl.ru - ul.ru), fl.fy + s_l * (stl.rv - ul.rv),
                fl.e + s_l * (stl.rE - ul.rE)};
         } else {
-          f = {fr.m + s_r * (str.r - ur.r), fr.fx + s_r * (str.ru - ur.ru), fr.fy + s_r * (str.rv - ur.rv),
+          fx = {fr.m + s_r * (str.r - ur.r), fr.fx + s_r * (str.ru - ur.ru), fr.fy + s_r * (str.rv - ur.rv),
                fr.e + s_r * (str.rE - ur.rE)};
         }
-        diffusive = !finite4(f.m, f.fx, f.fy, f.e);
+        diffusive = !finite4(fx.m, fx.fx, fx.fy, fx.e);
       }
     }
   }
   if (diffusive) {
     *fallback = true;
-    f = rusanov(ul, ur, pl, pr, nx, ny, gamma, as, mws);
+    fx = rusanov<T, LM>(ul, ur, f, nx, ny, as, mws);
   }
-  return f;
+  return fx;
 }
 
 // preconditioning.cpp:9-15 + 24-32 on a primitive state
@@ -405,21 +456,20 @@ __device__ __forceinline__ T smooth_max(T a, T b) {
 // preconditioning.cpp:34-49 (face beta) and residual_assembly.cpp:31-51 (acoustic scale),
 // from the two conservative face states. Without LM the scale is exactly 1.
 template <class T, bool LM>
-__device__ __forceinline__ T face_acoustic_scale(const Cons<T>& l, const Cons<T>& r,
+__device__ __forceinline__ T face_acoustic_scale(const FaceSides<T>& f, const SideMach<T>& sm,
                                                  const FaceParams<T>& fp) {
   if (!LM) return T(1);
-  const Prim<T> pl = cons_to_prim(l, fp.gamma), pr = cons_to_prim(r, fp.gamma);
+  const Prim<T>& pl = f.pl;
+  const Prim<T>& pr = f.pr;
   T s = T(1);
   if (fp.precond) {
     const Prim<T> avg{T(0.5) * (pl.r + pr.r), T(0.5) * (pl.u + pr.u), T(0.5) * (pl.v + pr.v),
                       T(0.5) * (pl.p + pr.p)};
     s = sclamp(cell_beta(avg, fp), Kn<T>::low_mach_min, T(1));
   }
-  if (fp.low_mach_fix) {
-    s = smin(s, low_mach_dissipation_scale(pl, pr, fp.gamma, fp.mach_cutoff, fp.pc_mach_ref));
-  }
+  if (fp.low_mach_fix) s = smin(s, low_mach_dissipation_scale(sm, fp.mach_cutoff, fp.pc_mach_ref));
   s = sclamp(s, Kn<T>::low_mach_min, T(1));
-  const T fm = T(0.5) * (local_mach(pl, fp.gamma) + local_mach(pr, fp.gamma));
+  const T fm = T(0.5) * (sm.ml + sm.mr);
   const T fl = sclamp(fp.stab_floor, T(0), T(1));
   const T stab = sclamp(smooth_max(fm, fl), Kn<T>::low_mach_min, T(1));
   return smax(s, stab);
@@ -458,12 +508,12 @@ __device__ __forceinline__ Cons<T> precond_farfield_state(const Cons<T>& in, T n
 
 // euler_flux.cpp:366-395
 template <class T, int FLUX, bool LM>
-__device__ __forceinline__ Flux<T> face_flux(const Cons<T>& l, const Cons<T>& r, T nx, T ny,
-                                             const FaceParams<T>& fp, T as, T* mws, bool* fallback) {
-  if (FLUX == 1) return hllc<T, LM>(l, r, nx, ny, fp, as, mws, fallback);
+__device__ __forceinline__ Flux<T> face_flux(const Cons<T>& l, const Cons<T>& r, const FaceSides<T>& f,
+                                             const SideMach<T>& sm, T nx, T ny, const FaceParams<T>& fp, T as,
+                                             T* mws, bool* fallback) {
+  if (FLUX == 1) return hllc<T, LM>(l, r, f, sm, nx, ny, fp, as, mws, fallback);
   *fallback = false;
-  const Prim<T> pl = cons_to_prim(l, fp.gamma), pr = cons_to_prim(r, fp.gamma);
-  return rusanov(l, r, pl, pr, nx, ny, fp.gamma, as, mws);
+  return rusanov<T, LM>(l, r, f, nx, ny, as, mws);
 }
 
 // reconstruction.cpp:121-146

@@ -2,6 +2,7 @@
 #include "../../include/aero_adjoint.h"
 #include "../../include/aero_batch.h"
 #include "../../include/aero_gb300.h"
+#include "../../include/aero_mesh.h"
 #include "engine.hpp"
 #include "mesh_prep.hpp"
 
@@ -377,6 +378,16 @@ int aero_profile_kernels(aero_ctx* ctx, int n, int flush_l2, double* ms, int* la
   return cs != AERO_OK ? cs : rc;
 }
 
+int aero_profile_graph(aero_ctx* ctx, int n, int flush_l2, double* ms, int* launches, double* iteration_ms) {
+  if (ctx == nullptr || n <= 0 || ms == nullptr || launches == nullptr || iteration_ms == nullptr)
+    return fail(ctx, AERO_ERR_INVALID, "aero_profile_graph: bad argument");
+  const int rc = ctx->engine->profile_graph(n, flush_l2, ms, launches, iteration_ms);
+  const int cs = cuda_status(ctx);
+  if (cs != AERO_OK) return cs;
+  if (rc == AERO_ERR_STATE) return fail(ctx, rc, "aero_profile_graph: event nodes in the graph carry no timing");
+  return rc;
+}
+
 int aero_select_device(int device) {
   if (!device_ok(device)) return fail(nullptr, AERO_ERR_CUDA, "device is not a usable compute capability 10.3 GPU");
   if (cudaSetDevice(device) != cudaSuccess) {
@@ -512,6 +523,33 @@ int aero_adjoint_geometry(aero_ctx* ctx, const aero_mesh_desc* tangent, double* 
   if (ctx == nullptr || tangent == nullptr || dj == nullptr)
     return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_geometry: null argument");
   return adjoint_status(ctx, ctx->engine->adjoint_geometry(*tangent, dj), "aero_adjoint_geometry");
+}
+
+int aero_adjoint_geometry_vjp(aero_ctx* ctx, double* d_normal, double* d_center, double* d_area, double* d_volume,
+                              double* d_cell_center) {
+  if (ctx == nullptr || !d_normal || !d_center || !d_area || !d_volume || !d_cell_center)
+    return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_geometry_vjp: null argument");
+  return adjoint_status(ctx, ctx->engine->adjoint_geometry_vjp(d_normal, d_center, d_area, d_volume, d_cell_center),
+                        "aero_adjoint_geometry_vjp");
+}
+
+int aero_adjoint_node_vjp(aero_ctx* ctx, const aero_mesh* mesh, double* dj_dpoints) {
+  if (ctx == nullptr || mesh == nullptr || dj_dpoints == nullptr)
+    return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_node_vjp: null argument");
+  aero_mesh_sizes sz{};
+  if (aero_mesh_get_sizes(mesh, &sz) != AERO_OK)
+    return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_node_vjp: bad mesh");
+  long long info[2] = {0, 0};
+  ctx->engine->info(info, 2);
+  if (info[0] != sz.num_cells || info[1] != sz.num_faces)
+    return fail(ctx, AERO_ERR_INVALID, "aero_adjoint_node_vjp: the mesh is not the context's");
+  std::vector<double> bn(3 * static_cast<size_t>(sz.num_faces)), bc(bn.size()), ba(sz.num_faces),
+      bv(sz.num_cells), bcc(3 * static_cast<size_t>(sz.num_cells));
+  const int rc = aero_adjoint_geometry_vjp(ctx, bn.data(), bc.data(), ba.data(), bv.data(), bcc.data());
+  if (rc != AERO_OK) return rc;
+  if (aero_mesh_geometry_vjp(mesh, bn.data(), bc.data(), ba.data(), bv.data(), bcc.data(), dj_dpoints) != AERO_OK)
+    return fail(ctx, AERO_ERR_INVALID, std::string("aero_adjoint_node_vjp: ") + aero_mesh_last_error());
+  return AERO_OK;
 }
 
 }  // extern "C"

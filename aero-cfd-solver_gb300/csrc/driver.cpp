@@ -1,5 +1,6 @@
 // driver.cpp -- case-level driver of the device path (include/aero_driver.h): the "cuda"
 // branch of run_case / run_euler_airfoil_case with the reference's outputs.
+#include "../../include/aero_batch.h"
 #include "../../include/aero_driver.h"
 #include "../../include/aero_gb300.h"
 #include "../../include/aero_mesh.h"
@@ -402,19 +403,25 @@ void check(int rc, aero_ctx* ctx, const char* what) {
   throw std::runtime_error(std::string(what) + ": " + aero_last_error(ctx));
 }
 
-// run_euler_airfoil_case (euler_solver.cpp:463-1487) on the device.
-void run_euler(const aero_case_desc& cfg_in, const aero_airfoil_mesh_cfg& mc, const fs::path& out_dir,
-               const DriverOpts& opts, aero_run_summary* summary) {
-  if (cfg_in.iterations <= 0) throw std::invalid_argument("Euler iterations must be positive.");
-  if (cfg_in.rk_stages != 1 && cfg_in.rk_stages != 3)
-    throw std::invalid_argument("Euler pseudo-time rk_stages must be 1 or 3.");
+// The reference O-grid of a run with the auxiliary arrays its outputs use (euler_solver.cpp:474).
+struct EulerMesh {
   MeshHolder mh;
-  if (aero_mesh_ogrid_reference(mc.naca_code, mc.num_circumferential, mc.num_radial, mc.farfield_radius,
-                                mc.radial_stretch, mc.chord, &mh.m) != AERO_OK)
-    throw std::invalid_argument(aero_mesh_last_error());
   aero_mesh_sizes sz{};
-  aero_mesh_get_sizes(mh.m, &sz);
   aero_mesh_desc md{};
+  std::vector<double> pts;
+  std::vector<int> fv, conn, offs, ff, wall;
+  std::vector<unsigned char> types;
+  int N = 0, F = 0;
+};
+
+void build_mesh(const aero_airfoil_mesh_cfg& mc, EulerMesh* em) {
+  if (aero_mesh_ogrid_reference(mc.naca_code, mc.num_circumferential, mc.num_radial, mc.farfield_radius,
+                                mc.radial_stretch, mc.chord, &em->mh.m) != AERO_OK)
+    throw std::invalid_argument(aero_mesh_last_error());
+  MeshHolder& mh = em->mh;
+  aero_mesh_sizes& sz = em->sz;
+  aero_mesh_get_sizes(mh.m, &sz);
+  aero_mesh_desc& md = em->md;
   aero_mesh_describe(mh.m, &md);
   std::vector<double> pts(3 * static_cast<size_t>(sz.num_points));
   std::vector<int> fv(2 * static_cast<size_t>(sz.num_faces)), conn(sz.conn_length), offs(sz.num_cells),
@@ -425,7 +432,41 @@ void run_euler(const aero_case_desc& cfg_in, const aero_airfoil_mesh_cfg& mc, co
   const int N = sz.num_cells, F = sz.num_faces;
   const std::vector<int> wall(md.wall_faces, md.wall_faces + md.num_wall_faces);
   if (wall.empty()) throw std::runtime_error("Wall patch face set is empty.");
+  em->pts = std::move(pts);
+  em->fv = std::move(fv);
+  em->conn = std::move(conn);
+  em->offs = std::move(offs);
+  em->ff = std::move(ff);
+  em->types = std::move(types);
+  em->wall = wall;
+  em->N = N;
+  em->F = F;
+}
 
+// One run's settings as run_euler_airfoil_case resolves them (euler_solver.cpp:463-566), its
+// output directory and driver options.
+struct EulerCase {
+  aero_case_desc cfg{};
+  bool pc_req = false, pc_env = false, pc_forced_off = false;
+  double g = 0, rho_inf = 0, alpha = 0, a_inf = 0, v_inf = 0, u_inf_x = 0, u_inf_y = 0, q_inf = 0;
+  double chord = 0, s_ref = 0, pressure_ref = 0;
+  PcCfg pc{};
+  double ks = 0, kt = 0, stab_start = 0, stab_target = 0;
+  fs::path out_dir;
+  DriverOpts opts;
+};
+
+// Resolves the case and writes the outputs known before the iterations:
+// boundary_faces_debug.txt and effective_config_snapshot.txt.
+EulerCase prepare_case(const aero_case_desc& cfg_in, const aero_airfoil_mesh_cfg& mc, const EulerMesh& em,
+                       const fs::path& out_dir, const DriverOpts& opts) {
+  if (cfg_in.iterations <= 0) throw std::invalid_argument("Euler iterations must be positive.");
+  if (cfg_in.rk_stages != 1 && cfg_in.rk_stages != 3)
+    throw std::invalid_argument("Euler pseudo-time rk_stages must be 1 or 3.");
+  const aero_mesh_desc& md = em.md;
+  const int F = em.F;
+  const std::vector<int>& wall = em.wall;
+  const std::vector<int>& ff = em.ff;
   aero_case_desc cfg = cfg_in;
   const bool pc_req = cfg.precond_on != 0;
   const bool pc_env = env_flag_on("AERO_ENABLE_EXPERIMENTAL_PRECOND");
@@ -531,16 +572,42 @@ void run_euler(const aero_case_desc& cfg_in, const aero_airfoil_mesh_cfg& mc, co
       << "\nstabilization_ramp_iters_effective=" << std::max(cfg.stab_ramp_iters, 0)
       << "\nprecision=" << (cfg.precision == AERO_PRECISION_FP64 ? "fp64" : "fp32") << "\n";
   }
+  EulerCase ec;
+  ec.cfg = cfg;
+  ec.pc_req = pc_req;
+  ec.pc_env = pc_env;
+  ec.pc_forced_off = pc_forced_off;
+  ec.g = g;
+  ec.rho_inf = rho_inf;
+  ec.alpha = alpha;
+  ec.a_inf = a_inf;
+  ec.v_inf = v_inf;
+  ec.u_inf_x = u_inf_x;
+  ec.u_inf_y = u_inf_y;
+  ec.q_inf = q_inf;
+  ec.chord = chord;
+  ec.s_ref = s_ref;
+  ec.pressure_ref = pressure_ref;
+  ec.pc = pc;
+  ec.ks = ks;
+  ec.kt = kt;
+  ec.stab_start = stab_start;
+  ec.stab_target = stab_target;
+  ec.out_dir = out_dir;
+  ec.opts = opts;
+  return ec;
+}
 
-  CtxHolder ch;
-  check(aero_create(&md, &cfg, &ch.c), nullptr, "aero_create");
-  if (!opts.restart_in.empty()) {  // start from a dumped state instead of the free stream
-    std::vector<double> u0(5 * static_cast<size_t>(N));
-    if (aero_state_read(opts.restart_in.c_str(), N, u0.data()) != AERO_OK)
-      throw std::invalid_argument(std::string("restart_in: ") + aero_driver_last_error());
-    check(aero_set_state(ch.c, u0.data()), ch.c, "aero_set_state");
-  }
-
+// residuals.csv, forces.csv and euler_diagnostics.csv of the executed iterations
+// (euler_solver.cpp:723-738, 1161-1203).
+void write_history(const EulerCase& ec, const EulerMesh& em, const std::vector<aero_iter_record>& hist) {
+  const aero_mesh_desc& md = em.md;
+  const std::vector<int>& wall = em.wall;
+  const fs::path& out_dir = ec.out_dir;
+  const aero_case_desc& cfg = ec.cfg;
+  const double q_inf = ec.q_inf, rho_inf = ec.rho_inf, v_inf = ec.v_inf, s_ref = ec.s_ref, chord = ec.chord;
+  const double pressure_ref = ec.pressure_ref;
+  auto fl = [](double x) { return static_cast<float>(x); };
   std::ofstream rcsv(out_dir / "residuals.csv", std::ios::trunc);
   std::ofstream fcsv(out_dir / "forces.csv", std::ios::trunc);
   std::ofstream dcsv(out_dir / "euler_diagnostics.csv", std::ios::trunc);
@@ -562,62 +629,77 @@ void run_euler(const aero_case_desc& cfg_in, const aero_airfoil_mesh_cfg& mc, co
           "first_failure_owner,first_failure_neighbor\n";
   double sum_wall_ds = 0.0;
   for (int f : wall) sum_wall_ds += md.face_area[f];
-
-  auto fl = [](double x) { return static_cast<float>(x); };
-  std::vector<aero_iter_record> recs(512);
-  std::vector<aero_iter_record> hist;
-  int remaining = cfg.iterations;
-  bool stop = false, nonfinite = false;
-  while (remaining > 0 && !stop) {
-    const int chunk = std::min(remaining, static_cast<int>(recs.size()));
-    int done = 0;
-    const int rc = aero_run(ch.c, chunk, recs.data(), &done);
-    if (rc == AERO_ERR_NONFINITE) nonfinite = true;
-    else check(rc, ch.c, "aero_run");
-    for (int k = 0; k < done; ++k) {
-      const aero_iter_record& r = recs[k];
-      if (r.flags & AERO_REC_NONFINITE) {
-        std::cerr << "non_finite_trap iter=" << r.iter << " location=conserved\n";
-        break;
-      }
-      const bool ws = r.flags & AERO_REC_FORCE_WINDOW_STABLE, ds = r.flags & AERO_REC_FORCE_DRIFT_STABLE;
-      const bool flip = !hist.empty() && ((hist.back().cd >= 0.0) != (r.cd >= 0.0));
-      rcsv << r.iter << "," << fl(r.residual_l1) << "," << fl(r.residual_l2) << "," << fl(r.residual_linf) << ","
-           << fl(r.residual_ratio) << "\n";
-      fcsv << r.iter << "," << fl(r.cl) << "," << fl(r.cd) << "," << fl(r.cm) << "," << fl(r.lift) << ","
-           << fl(r.drag) << "," << fl(r.moment) << "," << fl(r.dcl) << "," << fl(r.dcd) << "," << fl(r.dcm) << ","
-           << fl(r.mean_dcl) << "," << fl(r.mean_dcd) << "," << fl(r.mean_dcm) << "," << ws << "," << ds << ","
-           << (ws && ds) << "\n";
-      const char* stage = (r.flags & AERO_REC_STAGE_A) ? "A" : ((r.flags & AERO_REC_STAGE_B) ? "B" : "single");
-      dcsv << r.iter << "," << fl(r.residual_ratio) << "," << ws << "," << wall.size() << "," << wall.size() << ",0,"
-           << fl(sum_wall_ds) << "," << fl(r.sum_nax) << "," << fl(r.sum_nay) << ","
-           << fl(std::sqrt(r.sum_nax * r.sum_nax + r.sum_nay * r.sum_nay)) << "," << fl(r.max_wall_un) << ","
-           << fl(r.max_wall_mass_flux) << "," << fl(r.max_farfield_abs_dp) << "," << fl(r.max_farfield_abs_drho) << ","
-           << fl(r.max_farfield_abs_du) << "," << fl(r.max_farfield_abs_dv) << ",0," << fl(r.wall_cp_min) << ","
-           << fl(r.wall_cp_max) << "," << r.wall_cp_nonfinite << "," << fl(q_inf) << "," << fl(rho_inf) << ","
-           << fl(v_inf) << "," << fl(s_ref) << "," << fl(chord) << "," << fl(r.fx_gauge) << "," << fl(r.fy_gauge)
-           << "," << fl(r.fx_abs) << "," << fl(r.fy_abs) << "," << fl(r.lift) << "," << fl(r.drag) << ","
-           << fl(r.cl) << "," << fl(r.cd) << "," << fl(r.cm) << "," << fl(r.cl_abs) << "," << fl(r.cd_abs) << ","
-           << fl(r.cm_abs) << "," << fl(r.dcl) << "," << fl(r.dcd) << "," << fl(r.dcm) << "," << ds << ","
-           << (ws && ds) << "," << fl(r.mean_dcl) << "," << fl(r.mean_dcd) << "," << fl(r.mean_dcm) << ","
-           << flip << "," << fl(r.p_jump_energy_nd) << "," << fl(r.p_jump_energy_wall_nd) << "," << stage << ","
-           << ((r.flags & AERO_REC_ALL_SPEED_FIX) ? 1 : 0) << "," << fl(r.all_speed_f_min) << ","
-           << fl(r.all_speed_ramp_weight) << ",0," << r.controller_action << "," << fl(r.cfl_scale) << ","
-           << fl(r.cd * std::max(cfg.mach, 0.0)) << "," << fl(r.max_abs_dp_domain / pressure_ref) << ","
-           << fl(r.max_abs_dp_wall / pressure_ref) << "," << fl(r.max_farfield_abs_dp / pressure_ref) << ","
-           << r.first_order_fallback_faces << "," << r.diffusive_fallback_faces << ",-1,-1,-1\n";
-      hist.push_back(r);
-      if (r.flags & AERO_REC_CONVERGED) stop = true;
-    }
-    if (nonfinite || done < chunk) stop = true;
-    remaining -= done;
+  for (size_t k = 0; k < hist.size(); ++k) {
+    const aero_iter_record& r = hist[k];
+    const bool ws = r.flags & AERO_REC_FORCE_WINDOW_STABLE, ds = r.flags & AERO_REC_FORCE_DRIFT_STABLE;
+    const bool flip = k > 0 && ((hist[k - 1].cd >= 0.0) != (r.cd >= 0.0));
+    rcsv << r.iter << "," << fl(r.residual_l1) << "," << fl(r.residual_l2) << "," << fl(r.residual_linf) << ","
+         << fl(r.residual_ratio) << "\n";
+    fcsv << r.iter << "," << fl(r.cl) << "," << fl(r.cd) << "," << fl(r.cm) << "," << fl(r.lift) << ","
+         << fl(r.drag) << "," << fl(r.moment) << "," << fl(r.dcl) << "," << fl(r.dcd) << "," << fl(r.dcm) << ","
+         << fl(r.mean_dcl) << "," << fl(r.mean_dcd) << "," << fl(r.mean_dcm) << "," << ws << "," << ds << ","
+         << (ws && ds) << "\n";
+    const char* stage = (r.flags & AERO_REC_STAGE_A) ? "A" : ((r.flags & AERO_REC_STAGE_B) ? "B" : "single");
+    dcsv << r.iter << "," << fl(r.residual_ratio) << "," << ws << "," << wall.size() << "," << wall.size() << ",0,"
+         << fl(sum_wall_ds) << "," << fl(r.sum_nax) << "," << fl(r.sum_nay) << ","
+         << fl(std::sqrt(r.sum_nax * r.sum_nax + r.sum_nay * r.sum_nay)) << "," << fl(r.max_wall_un) << ","
+         << fl(r.max_wall_mass_flux) << "," << fl(r.max_farfield_abs_dp) << "," << fl(r.max_farfield_abs_drho) << ","
+         << fl(r.max_farfield_abs_du) << "," << fl(r.max_farfield_abs_dv) << ",0," << fl(r.wall_cp_min) << ","
+         << fl(r.wall_cp_max) << "," << r.wall_cp_nonfinite << "," << fl(q_inf) << "," << fl(rho_inf) << ","
+         << fl(v_inf) << "," << fl(s_ref) << "," << fl(chord) << "," << fl(r.fx_gauge) << "," << fl(r.fy_gauge)
+         << "," << fl(r.fx_abs) << "," << fl(r.fy_abs) << "," << fl(r.lift) << "," << fl(r.drag) << ","
+         << fl(r.cl) << "," << fl(r.cd) << "," << fl(r.cm) << "," << fl(r.cl_abs) << "," << fl(r.cd_abs) << ","
+         << fl(r.cm_abs) << "," << fl(r.dcl) << "," << fl(r.dcd) << "," << fl(r.dcm) << "," << ds << ","
+         << (ws && ds) << "," << fl(r.mean_dcl) << "," << fl(r.mean_dcd) << "," << fl(r.mean_dcm) << ","
+         << flip << "," << fl(r.p_jump_energy_nd) << "," << fl(r.p_jump_energy_wall_nd) << "," << stage << ","
+         << ((r.flags & AERO_REC_ALL_SPEED_FIX) ? 1 : 0) << "," << fl(r.all_speed_f_min) << ","
+         << fl(r.all_speed_ramp_weight) << ",0," << r.controller_action << "," << fl(r.cfl_scale) << ","
+         << fl(r.cd * std::max(cfg.mach, 0.0)) << "," << fl(r.max_abs_dp_domain / pressure_ref) << ","
+         << fl(r.max_abs_dp_wall / pressure_ref) << "," << fl(r.max_farfield_abs_dp / pressure_ref) << ","
+         << r.first_order_fallback_faces << "," << r.diffusive_fallback_faces << ",-1,-1,-1\n";
   }
-  if (hist.empty()) throw std::runtime_error("Euler run produced no iterations.");
+}
 
-  // final fields (euler_solver.cpp:1217-1260)
-  std::vector<double> U(5 * static_cast<size_t>(N)), R(5 * static_cast<size_t>(N)), SR(N);
-  check(aero_get_state(ch.c, U.data()), ch.c, "aero_get_state");
-  check(aero_get_last_residual(ch.c, R.data(), SR.data()), ch.c, "aero_get_last_residual");
+// Appends a chunk of records to a run's history; the record of a non-finite trap is not kept
+// (the reference stops before writing it). Returns whether the run stopped.
+bool take_records(const aero_iter_record* recs, int done, int chunk, std::vector<aero_iter_record>* hist,
+                  bool* nonfinite) {
+  for (int k = 0; k < done; ++k) {
+    const aero_iter_record& r = recs[k];
+    if (r.flags & AERO_REC_NONFINITE) {
+      std::cerr << "non_finite_trap iter=" << r.iter << " location=conserved\n";
+      *nonfinite = true;
+      return true;
+    }
+    hist->push_back(r);
+    if (r.flags & AERO_REC_CONVERGED) return true;
+  }
+  return done < chunk;
+}
+
+// The outputs of the final state (euler_solver.cpp:1217-1477): fields, acoustic-scale
+// statistics, wall_flux.csv, dissipation_debug.csv, cp_wall.csv, the state dump, the VTU
+// file and run.log, and the summary dict's values.
+void write_final(const EulerCase& ec, const EulerMesh& em, const std::vector<double>& U, const std::vector<double>& R,
+                 const std::vector<aero_iter_record>& hist, bool nonfinite, aero_run_summary* summary) {
+  const aero_mesh_desc& md = em.md;
+  const int N = em.N, F = em.F;
+  const std::vector<int>& wall = em.wall;
+  const std::vector<int>& fv = em.fv;
+  const std::vector<int>& conn = em.conn;
+  const std::vector<int>& offs = em.offs;
+  const std::vector<unsigned char>& types = em.types;
+  const std::vector<double>& pts = em.pts;
+  const aero_mesh_sizes& sz = em.sz;
+  const fs::path& out_dir = ec.out_dir;
+  const DriverOpts& opts = ec.opts;
+  const aero_case_desc& cfg = ec.cfg;
+  const double g = ec.g, rho_inf = ec.rho_inf, alpha = ec.alpha, u_inf_x = ec.u_inf_x, u_inf_y = ec.u_inf_y;
+  const double q_inf = ec.q_inf, v_inf = ec.v_inf, s_ref = ec.s_ref, chord = ec.chord, pressure_ref = ec.pressure_ref;
+  const double ks = ec.ks, kt = ec.kt, stab_start = ec.stab_start, stab_target = ec.stab_target;
+  const bool pc_req = ec.pc_req;
+  const PcCfg& pc = ec.pc;
+  auto fl = [](double x) { return static_cast<float>(x); };
   std::vector<float> rho(N), uu(N), vv(N), pp(N), mach(N), rmag(N);
   double bmin = 1e300, bmax = -1e300, bsum = 0, mmin = 1e300, mmax = -1e300, msum = 0;
   std::vector<P> prim(N);
@@ -887,6 +969,114 @@ void run_euler(const aero_case_desc& cfg_in, const aero_airfoil_mesh_cfg& mc, co
   summary->cm = fl(last.cm);
 }
 
+// run_euler_airfoil_case (euler_solver.cpp:463-1487) on the device.
+void run_euler(const aero_case_desc& cfg_in, const aero_airfoil_mesh_cfg& mc, const fs::path& out_dir,
+               const DriverOpts& opts, aero_run_summary* summary) {
+  if (cfg_in.iterations <= 0) throw std::invalid_argument("Euler iterations must be positive.");
+  if (cfg_in.rk_stages != 1 && cfg_in.rk_stages != 3)
+    throw std::invalid_argument("Euler pseudo-time rk_stages must be 1 or 3.");
+  EulerMesh em;
+  build_mesh(mc, &em);
+  const EulerCase ec = prepare_case(cfg_in, mc, em, out_dir, opts);
+  const int N = em.N;
+  CtxHolder ch;
+  check(aero_create(&em.md, &ec.cfg, &ch.c), nullptr, "aero_create");
+  if (!opts.restart_in.empty()) {  // start from a dumped state instead of the free stream
+    std::vector<double> u0(5 * static_cast<size_t>(N));
+    if (aero_state_read(opts.restart_in.c_str(), N, u0.data()) != AERO_OK)
+      throw std::invalid_argument(std::string("restart_in: ") + aero_driver_last_error());
+    check(aero_set_state(ch.c, u0.data()), ch.c, "aero_set_state");
+  }
+  std::vector<aero_iter_record> recs(512), hist;
+  int remaining = ec.cfg.iterations;
+  bool stop = false, nonfinite = false;
+  while (remaining > 0 && !stop) {
+    const int chunk = std::min(remaining, static_cast<int>(recs.size()));
+    int done = 0;
+    const int rc = aero_run(ch.c, chunk, recs.data(), &done);
+    if (rc != AERO_ERR_NONFINITE) check(rc, ch.c, "aero_run");
+    stop = take_records(recs.data(), done, chunk, &hist, &nonfinite);
+    remaining -= done;
+  }
+  if (hist.empty()) throw std::runtime_error("Euler run produced no iterations.");
+  write_history(ec, em, hist);
+  std::vector<double> U(5 * static_cast<size_t>(N)), R(5 * static_cast<size_t>(N)), SR(N);
+  check(aero_get_state(ch.c, U.data()), ch.c, "aero_get_state");
+  check(aero_get_last_residual(ch.c, R.data(), SR.data()), ch.c, "aero_get_last_residual");
+  write_final(ec, em, U, R, hist, nonfinite, summary);
+}
+
+// A sweep of the base case over angles of attack (and Mach numbers): every case runs in one
+// batched context on the base case's mesh, and each writes the outputs of a single run into
+// out_root/run_NNN (python/cfd/sweep.py:41-56 runs them one after another). The cases'
+// results are those of single runs: a batch reproduces them bit for bit.
+void run_sweep(const aero_case_desc& base, const aero_airfoil_mesh_cfg& mc, int n, const double* aoa,
+               const double* mach, const fs::path& out_root, const DriverOpts& opts, const std::string& case_path,
+               aero_run_summary* summaries) {
+  if (n <= 0) throw std::invalid_argument("a sweep needs at least one case");
+  EulerMesh em;
+  build_mesh(mc, &em);
+  const int N = em.N;
+  fs::create_directories(out_root);
+  std::vector<EulerCase> cases;
+  std::vector<aero_case_desc> cds;
+  for (int k = 0; k < n; ++k) {
+    aero_case_desc c = base;
+    c.aoa_deg = static_cast<double>(static_cast<float>(aoa[k]));  // case values are floats
+    if (mach) c.mach = static_cast<double>(static_cast<float>(mach[k]));
+    char name[32];
+    std::snprintf(name, sizeof(name), "run_%03d", k);
+    cases.push_back(prepare_case(c, mc, em, out_root / name, opts));
+    cds.push_back(cases.back().cfg);
+  }
+  std::vector<aero_mesh_desc> mds(static_cast<size_t>(n), em.md);
+  CtxHolder ch;
+  check(aero_batch_create(n, mds.data(), cds.data(), &ch.c), nullptr, "aero_batch_create");
+  if (!opts.restart_in.empty()) {
+    std::vector<double> u0(5 * static_cast<size_t>(N));
+    if (aero_state_read(opts.restart_in.c_str(), N, u0.data()) != AERO_OK)
+      throw std::invalid_argument(std::string("restart_in: ") + aero_driver_last_error());
+    for (int k = 0; k < n; ++k) check(aero_batch_set_state(ch.c, k, u0.data()), ch.c, "aero_batch_set_state");
+  }
+  const int cap = 512;
+  std::vector<aero_iter_record> recs(static_cast<size_t>(n) * cap);
+  std::vector<int> done(n);
+  std::vector<std::vector<aero_iter_record>> hist(n);
+  std::vector<char> stopped(n, 0), nonfinite(n, 0);
+  int remaining = base.iterations;
+  auto running = [&] { return std::count(stopped.begin(), stopped.end(), 0) > 0; };
+  while (remaining > 0 && running()) {
+    const int chunk = std::min(remaining, cap);
+    const int rc = aero_batch_run(ch.c, chunk, recs.data(), done.data());
+    if (rc != AERO_ERR_NONFINITE) check(rc, ch.c, "aero_batch_run");
+    for (int k = 0; k < n; ++k) {
+      if (stopped[k]) continue;
+      bool nf = false;
+      stopped[k] = take_records(recs.data() + static_cast<size_t>(k) * chunk, done[k], chunk, &hist[k], &nf);
+      nonfinite[k] = nf;
+    }
+    remaining -= chunk;
+  }
+  std::ofstream sweep_csv(out_root / "sweep_summary.csv", std::ios::trunc);
+  sweep_csv << "run,aoa_deg,mach,iterations,residual_l2,cl,cd,cm,status\n";
+  for (int k = 0; k < n; ++k) {
+    if (hist[k].empty()) throw std::runtime_error("sweep case " + std::to_string(k) + " produced no iterations.");
+    write_history(cases[k], em, hist[k]);
+    std::vector<double> U(5 * static_cast<size_t>(N)), R(5 * static_cast<size_t>(N)), SR(N);
+    check(aero_batch_get_state(ch.c, k, U.data()), ch.c, "aero_batch_get_state");
+    check(aero_batch_get_last_residual(ch.c, k, R.data(), SR.data()), ch.c, "aero_batch_get_last_residual");
+    aero_run_summary& sm = summaries[k];
+    std::memset(&sm, 0, sizeof(sm));
+    std::snprintf(sm.run_log, sizeof(sm.run_log), "%s", case_path.c_str());  // case_path for run.log
+    write_final(cases[k], em, U, R, hist[k], nonfinite[k] != 0, &sm);
+    const aero_iter_record& last = hist[k].back();
+    sweep_csv << k << "," << static_cast<float>(cases[k].cfg.aoa_deg) << "," << static_cast<float>(cases[k].cfg.mach)
+              << "," << hist[k].size() << "," << static_cast<float>(last.residual_l2) << ","
+              << static_cast<float>(last.cl) << "," << static_cast<float>(last.cd) << ","
+              << static_cast<float>(last.cm) << "," << (nonfinite[k] ? "nonfinite" : "ok") << "\n";
+  }
+}
+
 template <class Fn>
 int guard(Fn&& fn) {
   try {
@@ -1016,6 +1206,28 @@ int aero_run_case(const char* case_path, const char* out_dir, const char* backen
     std::memset(out, 0, sizeof(*out));
     std::snprintf(out->run_log, sizeof(out->run_log), "%s", case_path);  // case_path for run.log
     run_euler(c, m, out_dir, opts, out);
+  });
+}
+
+int aero_run_sweep(const char* case_path, int n_cases, const double* aoa_deg, const double* mach,
+                   const char* out_root, const char* backend, aero_run_summary* summaries) {
+  if (!case_path || !out_root || !aoa_deg || !summaries || n_cases <= 0) {
+    g_driver_error = "aero_run_sweep: bad argument";
+    return AERO_ERR_INVALID;
+  }
+  char nb[16];
+  const int rc = aero_normalize_backend(backend, nb, sizeof(nb));
+  if (rc != AERO_OK) return rc;
+  return guard([&] {
+    const KV kv = parse_kv(case_path);
+    const std::string case_type = get_s(kv, "case_type", "scalar_advect_demo");
+    if (case_type != "euler_airfoil_2d")
+      throw std::invalid_argument("case_type '" + case_type + "' is not served by the device Euler path");
+    aero_case_desc c;
+    aero_airfoil_mesh_cfg m;
+    map_case(kv, &c, &m);
+    const DriverOpts opts = map_opts(kv, fs::path(case_path).parent_path());
+    run_sweep(c, m, n_cases, aoa_deg, mach, out_root, opts, case_path, summaries);
   });
 }
 

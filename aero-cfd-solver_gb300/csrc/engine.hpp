@@ -73,6 +73,7 @@ class Engine {
   virtual void last_residual(int cs, double* res, double* sr) = 0;
   virtual int time_iterations(int n, int use_graph, int flush_l2, double* ms) = 0;
   virtual int profile_kernels(int n, int flush_l2, double* ms, int* launches) = 0;
+  virtual int profile_graph(int n, int flush_l2, double* ms, int* launches, double* iter_ms) = 0;
   virtual void info(long long* out, int n) = 0;
   virtual cudaError_t last_cuda_error() = 0;
   virtual int set_wait_limit(int polls) = 0;
@@ -91,6 +92,8 @@ class Engine {
                                    double* history, int* done) = 0;
   virtual int adjoint_dalpha(double* dj_dalpha_deg) = 0;
   virtual int adjoint_geometry(const aero_mesh_desc& tangent, double* dj) = 0;
+  virtual int adjoint_geometry_vjp(double* d_normal, double* d_center, double* d_area, double* d_volume,
+                                   double* d_cell_center) = 0;
 };
 
 Engine* make_engine_f32(const std::vector<HostSlots>& hs, const std::vector<aero_case_desc>& cfg,

@@ -785,6 +785,99 @@ class EngineT final : public Engine {
     return end_untracked();
   }
 
+  // In-graph attribution of n iterations: each iteration runs as a CUDA graph with the
+  // same kernel nodes and dependencies as the iteration graphs of time_iterations, plus an
+  // event-record node before and after every kernel node (on the stream the kernel is
+  // launched on), so each kernel's time is measured where it runs in the graph. ms[cls] /
+  // launches[cls] as in profile_kernels (class 5, the controller, runs beside the next
+  // iteration's first kernels on a side stream and overlaps them); *iter_ms: summed time
+  // from the first to the last event node of each iteration's graph.
+  int profile_graph(int n, int flush_l2, double* ms, int* launches, double* iter_ms) override {
+    const int it0 = begin_untracked();
+    if (flush_l2 && !ensure_flush_buffer()) return AERO_ERR_NOMEM;
+    for (int k = 0; k < 6; ++k) {
+      ms[k] = 0.0;
+      launches[k] = 0;
+    }
+    *iter_ms = 0.0;
+    struct Marked {
+      cudaGraphExec_t exec = nullptr;
+      std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+      cudaEvent_t first = nullptr, last = nullptr;
+    };
+    std::vector<Marked> cache(16);
+    std::vector<cudaEvent_t> events;
+    auto event = [&]() {
+      cudaEvent_t e = nullptr;
+      AERO_CK(cudaEventCreate(&e));
+      events.push_back(e);
+      return e;
+    };
+    auto marked = [&](bool second, int parity, bool defer, bool pending) -> Marked& {
+      Marked& m = cache[graph_index(second, parity, defer, pending)];
+      if (m.exec != nullptr || err_ != cudaSuccess) return m;
+      m.first = event();
+      m.last = event();
+      // recorded as event-record nodes of the graph (an event recorded during capture
+      // without the external flag only orders the captured work and is never recorded)
+      auto mark = [&](cudaEvent_t e, cudaStream_t s) {
+        AERO_CK(cudaEventRecordWithFlags(e, s, cudaEventRecordExternal));
+      };
+      cudaGraph_t g = nullptr;
+      AERO_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+      mark(m.first, st_);
+      launch_iteration(second, parity, defer, pending, [&](int cls, auto&& launch) {
+        // the previous iteration's controller is the one launch on the side stream
+        cudaStream_t s = (cls == 5 && pending) ? side_ : st_;
+        cudaEvent_t a = event(), b = event();
+        mark(a, s);
+        launch();
+        mark(b, s);
+        m.marks.push_back({cls, {a, b}});
+      });
+      mark(m.last, st_);
+      AERO_CK(cudaStreamEndCapture(st_, &g));
+      if (g) {
+        AERO_CK(cudaGraphInstantiate(&m.exec, g, 0));
+        cudaGraphDestroy(g);
+      }
+      return m;
+    };
+    int rc = AERO_OK;
+    for (int j = 0; j < n && rc == AERO_OK && err_ == cudaSuccess; ++j) {
+      const int it = it0 + j;
+      if (flush_l2) AERO_CK(cudaMemsetAsync(flush_, j & 0xff, flush_bytes_, st_));
+      Marked& m = marked(second_at(it), it & 1, defer_control_, defer_control_ && j > 0);
+      if (m.exec == nullptr) break;
+      AERO_CK(cudaGraphLaunch(m.exec, st_));
+      if (defer_control_ && j == n - 1) launch_control(it & 1, Direct{});
+      AERO_CK(cudaStreamSynchronize(st_));
+      float f = 0.0f;
+      if (cudaEventElapsedTime(&f, m.first, m.last) != cudaSuccess) {
+        cudaGetLastError();
+        rc = AERO_ERR_STATE;  // event nodes of this graph carry no timing
+        break;
+      }
+      *iter_ms += f;
+      for (auto& mk : m.marks) {
+        float g = 0.0f;
+        if (cudaEventElapsedTime(&g, mk.second.first, mk.second.second) != cudaSuccess) {
+          cudaGetLastError();
+          rc = AERO_ERR_STATE;
+          break;
+        }
+        ms[mk.first] += g;
+        ++launches[mk.first];
+      }
+    }
+    for (auto& m : cache) {
+      if (m.exec) cudaGraphExecDestroy(m.exec);
+    }
+    for (auto e : events) cudaEventDestroy(e);
+    const int end = end_untracked();
+    return end != AERO_OK ? end : rc;
+  }
+
   // ---- discrete adjoint (FP64, one case) -------------------------------------------------
   int adjoint_linearize(double w_cd, double w_cl, int second_order) override {
     if constexpr (sizeof(T) != 8) {
@@ -1095,6 +1188,122 @@ class EngineT final : public Engine {
       const CtrlConfig& cc = ccs_[0];
       *dj = s / (cc.q_inf * cc.s_ref) + lam_dr;
       return err_ == cudaSuccess ? AERO_OK : AERO_ERR_CUDA;
+    }
+  }
+
+  // Transpose of adjoint_geometry with the current lam: dJ/d(geometry) for every face normal
+  // [3F], face centre [3F], face length [F], cell volume [N] and cell centre [3N] of the
+  // original numbering (z components 0), so that for every geometry tangent t,
+  // adjoint_geometry(t) = sum of these times t.
+  int adjoint_geometry_vjp(double* bn, double* bc, double* ba, double* bv, double* bcc) override {
+    if constexpr (sizeof(T) != 8) {
+      return AERO_ERR_INVALID;
+    } else {
+      if (!adj_ready_ || !bn || !bc || !ba || !bv || !bcc) return AERO_ERR_INVALID;
+      const HostSlots& hs = hs_[0];
+      const Pack& pk = pk_[0];
+      std::fill(bn, bn + 3 * static_cast<size_t>(hs.nf), 0.0);
+      std::fill(bc, bc + 3 * static_cast<size_t>(hs.nf), 0.0);
+      std::fill(ba, ba + hs.nf, 0.0);
+      std::fill(bv, bv + hs.n, 0.0);
+      std::fill(bcc, bcc + 3 * static_cast<size_t>(hs.n), 0.0);
+      const size_t ns = static_cast<size_t>(ntot_) * d_;
+      if (!geo_vjp_alloc_) {
+        geo_face_vjp_ = alloc<double>(7 * static_cast<size_t>(ftot_));
+        geo_slot_vjp_ = alloc<double>(3 * ns);
+        geo_inv_vjp_ = alloc<double>(ntot_);
+        geo_vjp_alloc_ = true;
+        if (err_ != cudaSuccess) return AERO_ERR_NOMEM;
+      }
+      const bool sec = adj_second_;
+      if (sec) {  // the gradients' adjoint under lam, then its geometric part
+        k_adj_face_vjp<kJac><<<nfb_, block_, 0, st_>>>(df_, fblk_, Jf_, lam_, adj_face_);
+        k_adj_gather<kJac><<<ncb_, block_, 0, st_>>>(dg_, cblk_, adj_face_, mw_, mgx_, mgy_);
+        AERO_CK(cudaMemsetAsync(geo_slot_vjp_, 0, sizeof(double) * 3 * ns, st_));
+        k_adj_geo_grad_vjp<<<ncb_, block_, 0, st_>>>(dm_, cblk_, Wlin_, mgx_, mgy_, geo_slot_vjp_, geo_inv_vjp_);
+      }
+      auto go = [&](auto kern) {
+        kern<<<nfb_, block_, 0, st_>>>(df_, fblk_, fps_dev_, ctrl_lin_, Wlin_, gxlin_, gylin_, lam_, geo_face_vjp_);
+      };
+      const bool hllc = cfg_[0].flux == AERO_FLUX_HLLC, lm = lm_ != 0;
+      if (hllc) {
+        if (sec) {
+          if (lm) go(k_adj_geo_face_vjp<1, true, true>);
+          else go(k_adj_geo_face_vjp<1, true, false>);
+        } else {
+          if (lm) go(k_adj_geo_face_vjp<1, false, true>);
+          else go(k_adj_geo_face_vjp<1, false, false>);
+        }
+      } else {
+        if (sec) {
+          if (lm) go(k_adj_geo_face_vjp<0, true, true>);
+          else go(k_adj_geo_face_vjp<0, true, false>);
+        } else {
+          if (lm) go(k_adj_geo_face_vjp<0, false, true>);
+          else go(k_adj_geo_face_vjp<0, false, false>);
+        }
+      }
+      AERO_CK(cudaGetLastError());
+      std::vector<double> fv(7 * static_cast<size_t>(pk.nf)), sv, iv;
+      AERO_CK(cudaMemcpyAsync(fv.data(), geo_face_vjp_, sizeof(double) * fv.size(), cudaMemcpyDeviceToHost, st_));
+      if (sec) {
+        sv.resize(3 * ns);
+        iv.resize(static_cast<size_t>(ntot_));
+        AERO_CK(cudaMemcpyAsync(sv.data(), geo_slot_vjp_, sizeof(double) * sv.size(), cudaMemcpyDeviceToHost, st_));
+        AERO_CK(cudaMemcpyAsync(iv.data(), geo_inv_vjp_, sizeof(double) * iv.size(), cudaMemcpyDeviceToHost, st_));
+      }
+      AERO_CK(cudaStreamSynchronize(st_));
+      if (err_ != cudaSuccess) return AERO_ERR_CUDA;
+      // face pass: normal, length, and the MUSCL offsets dO = c_f - c_owner, dN = c_f - c_nb
+      for (int i = 0; i < pk.nf; ++i) {
+        const double* r = fv.data() + 7 * static_cast<size_t>(i);
+        const int f = hs.f_orig[i];
+        bn[3 * f] += r[0];
+        bn[3 * f + 1] += r[1];
+        ba[f] += r[2];
+        if (sec && hs.f_nb[i] >= 0) {
+          const int o = hs.f_own_old[i], b = hs.f_nb_old[i];
+          bc[3 * f] += r[3] + r[5];
+          bc[3 * f + 1] += r[4] + r[6];
+          bcc[3 * o] -= r[3];
+          bcc[3 * o + 1] -= r[4];
+          bcc[3 * b] -= r[5];
+          bcc[3 * b + 1] -= r[6];
+        }
+      }
+      if (sec) {  // gradient pass: slot normals and lengths are the faces'; 1/V = 1/max(V, 1e-12)
+        for (int j = 0; j < hs.d; ++j) {
+          for (int c = 0; c < hs.n; ++c) {
+            const int f = hs.slot_face[static_cast<size_t>(j) * hs.n + c];
+            if (f < 0) continue;
+            const double* r = sv.data() + 3 * (static_cast<size_t>(j) * ntot_ + c);
+            bn[3 * f] += r[0];
+            bn[3 * f + 1] += r[1];
+            ba[f] += r[2];
+          }
+        }
+        for (int c = 0; c < hs.n; ++c) {
+          const double v = hs.vol[c];
+          if (v > 1.0e-12) bv[hs.perm[c]] += -iv[c] / (v * v);
+        }
+      }
+      // the objective's own dependence on the force patch's normals and lengths
+      const std::vector<double> pw = wall_pressures();
+      const double pinf = rs_[0].p_inf;
+      const CtrlConfig& cc = ccs_[0];
+      const double scale = 1.0 / (cc.q_inf * cc.s_ref);
+      for (int c = 0; c < pk.n; ++c) {
+        const int cnt = hs.flags[c] >> 2;
+        for (int j = hs.wall_first[c]; j < hs.wall_first[c] + cnt; ++j) {
+          if (!(hs.wkind[j] & 1)) continue;
+          const int f = hs.w_face[j];
+          const double coef = (pw[c] - pinf) * scale;
+          bn[3 * f] += coef * adj_ex_ * hs.warea[j];
+          bn[3 * f + 1] += coef * adj_ey_ * hs.warea[j];
+          ba[f] += coef * (adj_ex_ * hs.wnx[j] + adj_ey_ * hs.wny[j]);
+        }
+      }
+      return AERO_OK;
     }
   }
 
@@ -1898,6 +2107,8 @@ class EngineT final : public Engine {
   double* Jf_ = nullptr;        // per face: 4 x kJac local Jacobian
   double* adj_face_ = nullptr;  // per face: kJac transpose-product contributions
   double* adj_face_out_ = nullptr;
+  bool geo_vjp_alloc_ = false;
+  double *geo_face_vjp_ = nullptr, *geo_slot_vjp_ = nullptr, *geo_inv_vjp_ = nullptr;
   d4 *mw_ = nullptr, *mgx_ = nullptr, *mgy_ = nullptr, *adj_r_ = nullptr, *adj_g_ = nullptr;
   d4 *lam_ = nullptr, *lam_n_ = nullptr, *adj_v_ = nullptr;
   double* adj_rn_ = nullptr;     // per cell block: sum of the squared adjoint residual

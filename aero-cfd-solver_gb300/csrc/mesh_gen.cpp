@@ -596,6 +596,62 @@ void node_geometry(const aero_mesh& m, const std::vector<S>& px, const std::vect
   }
 }
 
+// Transpose of node_geometry's derivative: from the derivatives of a scalar with respect to
+// the face normals [3F], face centres [3F], face lengths [F], cell volumes [N] and cell centres
+// [3N], its derivatives with respect to the node coordinates bp [3P] (z entries 0). Reverse
+// mode of the same formulas, one pass over cells and faces.
+void node_geometry_vjp(const aero_mesh& m, const double* bn, const double* bc, const double* ba, const double* bv,
+                       const double* bcc, double* bp) {
+  const std::vector<double>& P = m.points;
+  std::fill(bp, bp + 3 * static_cast<size_t>(m.np), 0.0);
+  for (int k = 0; k < m.nc; ++k) {
+    const int b = k == 0 ? 0 : m.offsets[k - 1], e = m.offsets[k], nv = e - b;
+    double a2 = 0.0, sx = 0.0, sy = 0.0;
+    for (int j = 0; j < nv; ++j) {
+      const int p = m.conn[b + j], q = m.conn[b + (j + 1) % nv];
+      const double cr = P[3 * p] * P[3 * q + 1] - P[3 * q] * P[3 * p + 1];
+      a2 += cr;
+      sx += (P[3 * p] + P[3 * q]) * cr;
+      sy += (P[3 * p + 1] + P[3 * q + 1]) * cr;
+    }
+    double ba2 = 0.5 * bv[k], bsx = 0.0, bsy = 0.0;  // volume = a2 / 2
+    if (nv == 3) {  // centre = vertex mean
+      for (int j = 0; j < 3; ++j) {
+        const int v = m.conn[b + j];
+        bp[3 * v] += bcc[3 * k] / 3.0;
+        bp[3 * v + 1] += bcc[3 * k + 1] / 3.0;
+      }
+    } else {  // centre = (sx, sy) / (3 a2)
+      bsx = bcc[3 * k] / (3.0 * a2);
+      bsy = bcc[3 * k + 1] / (3.0 * a2);
+      ba2 -= (bcc[3 * k] * sx + bcc[3 * k + 1] * sy) / (3.0 * a2 * a2);
+    }
+    for (int j = 0; j < nv; ++j) {
+      const int p = m.conn[b + j], q = m.conn[b + (j + 1) % nv];
+      const double xp = P[3 * p], yp = P[3 * p + 1], xq = P[3 * q], yq = P[3 * q + 1];
+      const double cr = xp * yq - xq * yp;
+      const double bcr = ba2 + bsx * (xp + xq) + bsy * (yp + yq);
+      bp[3 * p] += bsx * cr + bcr * yq;
+      bp[3 * q] += bsx * cr - bcr * yp;
+      bp[3 * p + 1] += bsy * cr - bcr * xq;
+      bp[3 * q + 1] += bsy * cr + bcr * xp;
+    }
+  }
+  for (int f = 0; f < m.nf; ++f) {
+    const int v0 = m.face_vertices[2 * f], v1 = m.face_vertices[2 * f + 1];
+    const double dx = P[3 * v1] - P[3 * v0], dy = P[3 * v1 + 1] - P[3 * v0 + 1];
+    const double len = std::hypot(dx, dy), l3 = len * len * len;
+    // normal = (dy, -dx) / len, length = len, centre = (p0 + p1) / 2
+    const double bnx = bn[3 * f], bny = bn[3 * f + 1];
+    const double bdx = bnx * (-dy * dx / l3) + bny * (-dy * dy / l3) + ba[f] * dx / len;
+    const double bdy = bnx * (dx * dx / l3) + bny * (dx * dy / l3) + ba[f] * dy / len;
+    bp[3 * v1] += bdx + 0.5 * bc[3 * f];
+    bp[3 * v0] += -bdx + 0.5 * bc[3 * f];
+    bp[3 * v1 + 1] += bdy + 0.5 * bc[3 * f + 1];
+    bp[3 * v0 + 1] += -bdy + 0.5 * bc[3 * f + 1];
+  }
+}
+
 // Hicks-Henne bump on [0, 1]: sin(pi x^(ln 0.5 / ln peak))^width, 0 at both ends.
 double hicks_henne(double x, double peak, double width) {
   if (!(x > 0.0) || !(x < 1.0)) return 0.0;
@@ -806,6 +862,15 @@ int aero_mesh_geometry_tangent(const aero_mesh* m, const double* dpoints, double
     for (size_t i = 0; i < volume.size(); ++i) d_volume[i] = volume[i].d;
     for (size_t i = 0; i < cc.size(); ++i) d_cell_center[i] = cc[i].d;
   });
+}
+
+int aero_mesh_geometry_vjp(const aero_mesh* m, const double* b_normal, const double* b_center, const double* b_area,
+                           const double* b_volume, const double* b_cell_center, double* b_points) {
+  if (m == nullptr || !b_normal || !b_center || !b_area || !b_volume || !b_cell_center || !b_points) {
+    g_mesh_error = "null argument";
+    return AERO_ERR_INVALID;
+  }
+  return guarded([&] { node_geometry_vjp(*m, b_normal, b_center, b_area, b_volume, b_cell_center, b_points); });
 }
 
 int aero_mesh_hicks_henne_modes(const aero_mesh* m, int n_bumps, const double* peak_x, const int* upper,

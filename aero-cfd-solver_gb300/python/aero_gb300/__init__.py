@@ -78,6 +78,7 @@ def load(build_if_missing: bool = False):
         "aero_get_last_residual": (C.c_int, [C.c_void_p, _dp, _dp]),
         "aero_time_iterations": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp]),
         "aero_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip]),
+        "aero_profile_graph": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip, _dp]),
         "aero_select_device": (C.c_int, [C.c_int]),
         "aero_get_info": (C.c_int, [C.c_void_p, _llp, C.c_int]),
         "aero_set_wait_limit": (C.c_int, [C.c_void_p, C.c_int]),
@@ -110,6 +111,9 @@ def load(build_if_missing: bool = False):
                                                 _ip]),
         "aero_adjoint_dalpha": (C.c_int, [C.c_void_p, _dp]),
         "aero_adjoint_geometry": (C.c_int, [C.c_void_p, C.POINTER(MeshDesc), _dp]),
+        "aero_adjoint_geometry_vjp": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp]),
+        "aero_adjoint_node_vjp": (C.c_int, [C.c_void_p, C.c_void_p, _dp]),
+        "aero_mesh_geometry_vjp": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -209,6 +213,20 @@ def geometry_tangent(mesh: Mesh, dpoints: np.ndarray) -> Mesh:
     if rc != 0:
         raise AeroError(rc, lib.aero_mesh_last_error().decode())
     return Mesh(mesh.owner, mesh.neighbor, mesh.bc, dn, dc, da, dv, dcc, mesh.wall_faces)
+
+
+def geometry_vjp(mesh: Mesh, bars: Mesh) -> np.ndarray:
+    """The transpose of geometry_tangent: `bars` carries, in its geometry arrays, derivatives of
+    a scalar with respect to the mesh geometry (Solver.adjoint_geometry_vjp); returns the
+    derivatives with respect to the node coordinates [P, 3]."""
+    lib = load()
+    out = np.empty(mesh.points.size, np.float64)
+    arrays = [np.ascontiguousarray(a, dtype=np.float64) for a in
+              (bars.normal, bars.center, bars.area, bars.volume, bars.cell_center)]
+    rc = lib.aero_mesh_geometry_vjp(_handle(mesh), *[a.ctypes.data_as(_dp) for a in arrays], out.ctypes.data_as(_dp))
+    if rc != 0:
+        raise AeroError(rc, lib.aero_mesh_last_error().decode())
+    return out.reshape(-1, 3)
 
 
 def hicks_henne_modes(mesh: Mesh, peaks, upper, width: float = 3.0) -> np.ndarray:
@@ -377,6 +395,16 @@ class Solver:
         self._check(self.lib.aero_profile_kernels(self.h, n, int(flush_l2), ms, launches))
         return {k: (ms[i], launches[i]) for i, k in enumerate(self.KERNEL_CLASSES)}
 
+    def profile_graph(self, n: int, flush_l2: bool = False) -> tuple[dict, float]:
+        """In-graph kernel times of n iterations: ({class: (ms, launches)}, summed ms from
+        each iteration graph's first event node to its last)."""
+        ms = (C.c_double * 6)()
+        launches = (C.c_int * 6)()
+        total = C.c_double(0.0)
+        self._check(self.lib.aero_profile_graph(self.h, n, int(flush_l2), ms, launches, C.byref(total)))
+        names = ("gradient", "face_pass", "update", "global_dt", "symmetry_pjump", "control")
+        return {names[k]: (ms[k], launches[k]) for k in range(6)}, total.value
+
     def info(self) -> dict:
         v = (C.c_longlong * 10)()
         self._check(self.lib.aero_get_info(self.h, v, 10))
@@ -444,6 +472,23 @@ class Solver:
         out = C.c_double(0.0)
         self._check(self.lib.aero_adjoint_geometry(self.h, C.byref(d), C.byref(out)))
         return out.value
+
+    def adjoint_geometry_vjp(self) -> Mesh:
+        """dJ/d(geometry) with the current lam, as a Mesh with this solver's connectivity whose
+        geometry arrays hold the derivatives (the transpose of adjoint_geometry)."""
+        m = self.mesh
+        nf, nc = m.num_faces, m.num_cells
+        dn, dc, da, dv, dcc = np.empty(3 * nf), np.empty(3 * nf), np.empty(nf), np.empty(nc), np.empty(3 * nc)
+        self._check(self.lib.aero_adjoint_geometry_vjp(self.h, dn.ctypes.data_as(_dp), dc.ctypes.data_as(_dp),
+                                                       da.ctypes.data_as(_dp), dv.ctypes.data_as(_dp),
+                                                       dcc.ctypes.data_as(_dp)))
+        return Mesh(m.owner, m.neighbor, m.bc, dn, dc, da, dv, dcc, m.wall_faces)
+
+    def adjoint_node_vjp(self) -> np.ndarray:
+        """dJ/dX for every node of this solver's (generated) mesh [P, 3], one reverse pass."""
+        out = np.empty(self.mesh.points.size, np.float64)
+        self._check(self.lib.aero_adjoint_node_vjp(self.h, _handle(self.mesh), out.ctypes.data_as(_dp)))
+        return out.reshape(-1, 3)
 
 
 class Batch(Solver):

@@ -7,7 +7,8 @@ primal's pseudo-time smoother (or GMRES preconditioned by it), and
     dJ/d(alpha) = dJ/d(alpha)|_U + lam^T dR/d(alpha)          (far-field state)
     dJ/d(a_k)   = dJ/dX . m_k   + lam^T (dR/dX . m_k)          (m_k: Hicks-Henne mode k)
 
-with the geometry tangents of each mode from aero_mesh_geometry_tangent. AirfoilForces is
+with the geometry tangents of each mode from aero_mesh_geometry_tangent, or with dJ/dX for
+every node from one reverse pass (aero_adjoint_node_vjp) contracted with the modes. AirfoilForces is
 the torch.autograd.Function over (amplitudes, alpha) -> (CD, CL). There is no reference
 counterpart: AeroCFD has no shape parameterisation and no adjoint.
 """
@@ -73,6 +74,10 @@ class ShapeProblem:
     krylov_restart: int = 40
     krylov_smooth: int = 10
     primal_precision: int = capi.PRECISION_FP64
+    # "tangent": lam^T dR/dX . m_k from one forward geometry tangent per mode; "reverse":
+    # dJ/dX for every node in one reverse pass, then dJ/da_k = dJ/dX . m_k (any number of modes
+    # at the cost of one)
+    geometry_product: str = "tangent"
     modes: np.ndarray = field(init=False)
     last_adjoint_seconds: float = field(init=False, default=0.0)
     last_adjoint_iterations: int = field(init=False, default=0)
@@ -144,9 +149,13 @@ class ShapeProblem:
                 if not np.isfinite(ratio) or ratio < self.adjoint_tol:
                     break
         dalpha = s.adjoint_dalpha()
-        da = np.empty(self.peaks.size)
-        for k in range(self.peaks.size):
-            da[k] = s.adjoint_geometry(geometry_tangent(primal.mesh, self.modes[k]))
+        if self.geometry_product == "reverse":
+            dj_dx = s.adjoint_node_vjp()
+            da = np.tensordot(self.modes, dj_dx, axes=([1, 2], [0, 1]))
+        else:
+            da = np.empty(self.peaks.size)
+            for k in range(self.peaks.size):
+                da[k] = s.adjoint_geometry(geometry_tangent(primal.mesh, self.modes[k]))
         self.last_adjoint_seconds = time.perf_counter() - t0
         self.last_adjoint_iterations = done
         self.last_adjoint_ratio = float(ratio)

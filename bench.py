@@ -43,11 +43,38 @@ CASE = dict(mach=0.8, aoa_deg=1.25, flux=1, limiter=1, precond_farfield_bc=1, cf
             residual_reduction_target=0.0)
 STARTUP = 25  # first-order start-up iterations run untimed before warm-up
 
-# DRAM traffic per launch of the face pass from one ncu capture (dram__bytes_read.sum +
-# dram__bytes_write.sum; the launch's writes stay in L2), keyed by (precision, n_cells);
-# profiles/kernels_c2_512x128.md gives the commands (FP32: the capture of the current face
-# pass; FP64: the first capture).
-NCU_TRAFFIC = {("fp32", 131072): 13419264, ("fp64", 131072): 25307904}
+# DRAM traffic of the face pass (dram__bytes_read.sum + dram__bytes_write.sum per launch) comes
+# from an ncu capture recorded in profiles/dram_traffic.txt together with a hash of the kernel
+# sources it was captured from; a capture of other sources is not reported (traffic null).
+TRAFFIC_FILE = REPO / "profiles" / "dram_traffic.txt"
+KERNEL_SOURCES = ("aero_face_kernels.cuh", "aero_numerics.cuh", "aero_kernels.cuh")
+
+
+def kernel_source_hash() -> str:
+    import hashlib
+
+    h = hashlib.sha256()
+    for name in KERNEL_SOURCES:
+        h.update((REPO / "aero-cfd-solver_gb300" / "csrc" / name).read_bytes())
+    return h.hexdigest()[:16]
+
+
+def measured_traffic(kernel: str, precision: str, cells: int):
+    """(bytes per launch, note) from the recorded capture of the current sources, else (None, why)."""
+    if not TRAFFIC_FILE.exists():
+        return None, "no capture recorded"
+    want = kernel_source_hash()
+    stale = False
+    for line in TRAFFIC_FILE.read_text().splitlines():
+        parts = line.split()
+        if len(parts) < 5 or line.startswith("#"):
+            continue
+        k, prec, n, sha, nbytes = parts[:5]
+        if k == kernel and prec == precision and int(n) == cells:
+            if sha == want:
+                return int(nbytes), f"ncu capture of sources {sha}"
+            stale = True
+    return None, ("recorded capture is of other kernel sources" if stale else "no capture of this workload")
 
 
 def algorithmic_bytes(kernel: str, n: int, slots: int, precision: str, faces: int = 0) -> float:
@@ -205,12 +232,11 @@ def _cpu_worker(mesh_kw, case_kw, warmup, steps, barrier_, out_q):
 def cpu_sample(mesh, state, target_s=12.0, max_iters=40):
     """Single-core oracle port on a bounded sample: second-order iterations from the
     device state after start-up, until about target_s seconds of CPU work."""
-    from aero_gb300 import capi
     from oracle import oracle_py as op
 
     op.build()
     kw = dict(CASE, startup_first_order_iters=0)
-    sol = op.OracleSolver(op.MODE_FLOAT, mesh, capi.make_case(**kw))
+    sol = op.OracleSolver(op.MODE_FLOAT, mesh, op.make_case(**kw))
     sol.set_state(state)
     t0 = time.perf_counter()
     sol.run(1)
@@ -292,14 +318,8 @@ def c4_draw(rank: int):
     return pick, alphas, machs
 
 
-def c4_sweep(args, aero_gb300, capi, rank):
-    """96 FP32 cases, mesh sizes drawn from the four O-grids, alpha ~ U[-4, 8] deg, M ~
-    U[0.3, 0.85], HLLC + MUSCL venkat, per-case CFL ramp to 0.8 and a density-residual stop
-    mask at 1e-8 relative; seeded synthetic inputs. Block size, cell ordering and cells per
-    thread come from the autotuner (aero_autotune on the largest mesh of the draw with the
-    first case's flow). Returns device ms of `steps` iterations (L2 flushed before each), the
-    batch's cell count, its launches per iteration and the tuned (ordering, block size, cells
-    per thread)."""
+def c4_cases(aero_gb300, capi, rank, precision):
+    """The sweep's meshes and cases on one rank (C4_CASES of them)."""
     base = {sz: aero_gb300.ogrid_synthetic(sz[0], sz[1], cell_type=3, permute=True, jitter=0.1, seed=100 + i,
                                            wall_spacing=0.005, farfield_radius=20.0)
             for i, sz in enumerate(C4_SIZES)}
@@ -309,9 +329,21 @@ def c4_sweep(args, aero_gb300, capi, rank):
     for k in range(C4_CASES):
         kw = dict(CASE)
         kw.update(mach=float(machs[k]), aoa_deg=float(alphas[k]))
-        c = capi.make_case(**kw, precision=capi.PRECISION_FP32)
+        c = capi.make_case(**kw, precision=precision)
         c.density_l2_target = 1e-8
         cases.append(c)
+    return meshes, cases
+
+
+def c4_sweep(args, aero_gb300, capi, rank):
+    """96 FP32 cases, mesh sizes drawn from the four O-grids, alpha ~ U[-4, 8] deg, M ~
+    U[0.3, 0.85], HLLC + MUSCL venkat, per-case CFL ramp to 0.8 and a density-residual stop
+    mask at 1e-8 relative; seeded synthetic inputs. Block size, cell ordering and cells per
+    thread come from the autotuner (aero_autotune on the largest mesh of the draw with the
+    first case's flow). Returns device ms of `steps` iterations (L2 flushed before each), the
+    batch's cell count, its launches per iteration and the tuned (ordering, block size, cells
+    per thread)."""
+    meshes, cases = c4_cases(aero_gb300, capi, rank, capi.PRECISION_FP32)
     largest = max(range(C4_CASES), key=lambda k: meshes[k].num_cells)
     tuned, _ = aero_gb300.autotune(meshes[largest], cases[0], iters=10)
     for c in cases:
@@ -345,13 +377,13 @@ def c3_low_mach(args, aero_gb300, capi, peak):
             p = s.get_primitive()[3]  # the wall pressures after the same 400 iterations as CL, CD
             s.time_iterations(args.warmup, use_graph=True, flush_l2=True)
             ms = s.time_iterations(args.steps, use_graph=True, flush_l2=not args.no_flush)
-            prof = s.profile_kernels(max(2, min(args.steps, 10)), flush_l2=not args.no_flush)
+            prof, graph_ms = s.profile_graph(max(3, min(args.steps, 10)), flush_l2=not args.no_flush)
         f_ms, f_n = prof["face_pass"]
         avg = f_ms / max(f_n, 1)
         nbytes = algorithmic_bytes("face", mesh.num_cells, info["slots_per_cell"], prec, int(info["faces"]))
         res[prec] = dict(mcell=mesh.num_cells * args.steps / (ms / 1e3) / 1e6, cl=float(rec["cl"][-1]),
                          cd=float(rec["cd"][-1]), pw=p[mesh.owner[wall]], face_ms=avg, face_gbs=nbytes / (avg / 1e3) / 1e9,
-                         kernels={k: (v[0] / v[1] if v[1] else 0.0) for k, v in prof.items()})
+                         kernels=kernel_times(prof))
     q = 0.5 * 1.4 * 101325.0 * mach * mach
     m01 = {}
     for prec, code in (("fp32", capi.PRECISION_FP32), ("fp64", capi.PRECISION_FP64)):
@@ -362,7 +394,10 @@ def c3_low_mach(args, aero_gb300, capi, peak):
     q01 = 0.5 * 1.4 * 101325.0 * 0.01 * 0.01
     mach01 = {"abs_dcl_400": abs(m01["fp32"][0] - m01["fp64"][0]), "abs_dcd_400": abs(m01["fp32"][1] - m01["fp64"][1]),
               "max_abs_dcp_wall_400": float(np.max(np.abs(m01["fp32"][2] - m01["fp64"][2])) / q01),
-              "residual_ratio_fp64_400": m01["fp64"][3]}
+              "residual_ratio_fp64_400": m01["fp64"][3],
+              "note": "a comparison of two unconverged transients, not a gate result: neither precision "
+                      "converges on this case, and float pressure resolves p ~ 1/(gamma M^2) only to ~4e-4 "
+                      "of the free-stream dynamic pressure's scale"}
     return {"cells": mesh.num_cells, "mach": mach, "fp32_mcell_iter_s": res["fp32"]["mcell"],
             "mach_0.01": mach01,
             "fp64_mcell_iter_s": res["fp64"]["mcell"], "fp32_over_fp64": res["fp32"]["mcell"] / res["fp64"]["mcell"],
@@ -373,7 +408,7 @@ def c3_low_mach(args, aero_gb300, capi, peak):
                                         "frac": res["fp32"]["face_gbs"] / peak, "avg_launch_ms": res["fp32"]["face_ms"]},
             "roofline_face_pass_fp64": {"achieved": res["fp64"]["face_gbs"], "frac": res["fp64"]["face_gbs"] / peak,
                                         "avg_launch_ms": res["fp64"]["face_ms"]},
-            "kernel_ms_per_launch_fp32": res["fp32"]["kernels"]}
+            "in_graph_kernel_us_per_launch_fp32": res["fp32"]["kernels"]}
 
 
 def c3_case(capi, precision, mach=0.05):
@@ -383,19 +418,25 @@ def c3_case(capi, precision, mach=0.05):
                           startup_first_order_iters=25, precision=precision)
 
 
-def c3_profile_run(args):
-    """The C3 case with direct (non-graph) launches, for kernel profilers: 30 iterations
-    (25 first-order start-up, 5 second-order), then 5 timed second-order iterations."""
+def profile_run(args):
+    """One of the measured cases with direct (non-graph) launches, for kernel profilers: 30
+    iterations (25 first-order start-up, 5 second-order), then 5 timed second-order iterations.
+    workload: the 512x128 single-case workload (FP32); c3: the 1024x256 low-Mach case (FP32)."""
     import aero_gb300
     from aero_gb300 import capi
 
     aero_gb300.load()
-    mesh = aero_gb300.ogrid_synthetic(1024, 256, cell_type=3, permute=True, jitter=0.1, seed=3)
-    with aero_gb300.Solver(mesh, c3_case(capi, capi.PRECISION_FP32)) as s:
+    if args.profile_run == "c3":
+        mesh = aero_gb300.ogrid_synthetic(1024, 256, cell_type=3, permute=True, jitter=0.1, seed=3)
+        case = c3_case(capi, capi.PRECISION_FP32)
+    else:
+        mesh = make_mesh(args)
+        case = capi.make_case(**CASE, precision=capi.PRECISION_FP32)
+    with aero_gb300.Solver(mesh, case) as s:
         s.time_iterations(30, use_graph=False, flush_l2=False)
         ms = s.time_iterations(5, use_graph=False, flush_l2=True)
-    print(json.dumps({"c3_profile_run": {"cells": mesh.num_cells, "ms_5_iters": ms,
-                                         "mcell_iter_s": mesh.num_cells * 5 / ms / 1e3}}))
+    print(json.dumps({"profile_run": {"case": args.profile_run, "cells": mesh.num_cells, "ms_5_iters": ms,
+                                      "mcell_iter_s": mesh.num_cells * 5 / ms / 1e3}}))
 
 
 def c5_adjoint(args, aero_gb300, capi):
@@ -464,13 +505,194 @@ def c5_adjoint(args, aero_gb300, capi):
 
 
 # ------------------------------------------------------------------------------------------
+# Checks against the FP64 oracle, run in spawned processes on host cores while the GPU legs run
+# ------------------------------------------------------------------------------------------
+C1_MESH = dict(n_circ=128, n_radial=32, cell_type=4, permute=False, jitter=0.0, seed=1, wall_spacing=0.005,
+               farfield_radius=20.0)
+C1_CASE = dict(mach=0.5, aoa_deg=2.0, flux=0, limiter=0, cfl_start=0.8, cfl_max=0.8, startup_first_order_iters=10 ** 9,
+               iterations=2000, min_iterations=2000, residual_reduction_target=0.0)
+C1_ITERS = 2000
+C2_ORACLE_ITERS = 30  # 25 first-order start-up iterations and 5 second-order ones
+
+
+def _oracle_history(tag, mesh_kw, case_kw, iters, out_q):
+    """The FP64 oracle's run of a case (spawned process): its CL / CD / CM / residual history
+    and wall seconds on one host core."""
+    sys.path.insert(0, str(REPO))
+    from oracle import oracle_py as op
+
+    mesh = op.ogrid_synthetic(**mesh_kw)
+    sol = op.OracleSolver(op.MODE_DOUBLE, mesh, op.make_case(**case_kw))
+    t0 = time.perf_counter()
+    _, rec = sol.run(iters)
+    dt = time.perf_counter() - t0
+    out_q.put((tag, {k: rec[k].tolist() for k in ("cl", "cd", "cm", "residual_l2")}, dt, mesh.num_cells))
+
+
+def start_oracle_checks(enabled: bool):
+    """Spawned before the first GPU call: the C1 case (plain FP64 quads, 2,000 iterations) and
+    the first 30 iterations of the workload case, both in the FP64 oracle."""
+    if not enabled:
+        return None
+    import multiprocessing as mp
+
+    from oracle import oracle_py as op
+
+    op.build()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    jobs = [("c1", C1_MESH, dict(C1_CASE), C1_ITERS),
+            ("c2", dict(WORKLOAD), dict(CASE), C2_ORACLE_ITERS)]
+    procs = [ctx.Process(target=_oracle_history, args=(tag, m, c, n, q)) for tag, m, c, n in jobs]
+    for p in procs:
+        p.start()
+    return q, procs
+
+
+def collect_oracle_checks(handle) -> dict:
+    if handle is None:
+        return {}
+    q, procs = handle
+    out = {}
+    for _ in procs:
+        tag, hist, dt, cells = q.get(timeout=1800)
+        out[tag] = (hist, dt, cells)
+    for p in procs:
+        p.join()
+    return out
+
+
+def history_diff(rec, hist, n) -> dict:
+    return {f"max_abs_d{k}": float(np.max(np.abs(np.asarray(rec[k][:n]) - np.asarray(hist[k][:n]))))
+            for k in ("cl", "cd", "cm")}
+
+
+# ------------------------------------------------------------------------------------------
+# GPU legs
+# ------------------------------------------------------------------------------------------
+def c1_quad(aero_gb300, capi):
+    """Plain-FP64 configuration: NACA 0012 on a 128x32 quad O-grid (4,096 cells, cosine
+    clustering at the leading and trailing edges, first wall spacing 0.005 c, geometric growth
+    to a far field at 20 c), M=0.5, alpha=2 deg, first-order Rusanov, local time stepping at
+    CFL 0.8, 2,000 iterations: the records of the run and its device time (graphs, no flush:
+    the 1 MB working set lives in L2)."""
+    mesh = aero_gb300.ogrid_synthetic(**C1_MESH)
+    case = capi.make_case(**C1_CASE, precision=capi.PRECISION_FP64)
+    with aero_gb300.Solver(mesh, case) as s:
+        t0 = time.perf_counter()
+        _, rec = s.run(C1_ITERS)
+        wall = time.perf_counter() - t0
+    with aero_gb300.Solver(mesh, case) as s:
+        ms = s.time_iterations(C1_ITERS, use_graph=True, flush_l2=False)
+    return {"cells": mesh.num_cells, "faces": mesh.num_faces, "iterations": C1_ITERS,
+            "gpu_fp64_mcell_iter_s": mesh.num_cells * C1_ITERS / (ms / 1e3) / 1e6,
+            "gpu_run_with_records_s": wall, "cl": float(rec["cl"][-1]), "cd": float(rec["cd"][-1]),
+            "residual_ratio": float(rec["residual_ratio"][-1])}, rec
+
+
+def wall_cp(mesh, s, case):
+    """Cp at the wall faces' owner cells from the primitive state (p - p_inf) / q_inf."""
+    p = s.get_primitive()[3][mesh.owner[mesh.wall_faces]]
+    q = 0.5 * case.gamma * case.p_inf * case.mach * case.mach
+    return (p - case.p_inf) / q
+
+
+def c2_gate(mesh, aero_gb300, capi):
+    """The workload case run for its configured 5,000 iterations from free stream in FP32 and
+    FP64: |dCL|, |dCD| and the largest wall |dCp| between them at the end."""
+    out = {}
+    for prec, code in (("fp32", capi.PRECISION_FP32), ("fp64", capi.PRECISION_FP64)):
+        case = capi.make_case(**CASE, precision=code)
+        with aero_gb300.Solver(mesh, case) as s:
+            t0 = time.perf_counter()
+            _, rec = s.run(CASE["iterations"])
+            wall = time.perf_counter() - t0
+            out[prec] = (rec, wall_cp(mesh, s, case), wall)
+    r32, r64 = out["fp32"][0], out["fp64"][0]
+    return {"iterations": int(len(r64)), "abs_dcl": abs(float(r32["cl"][-1] - r64["cl"][-1])),
+            "abs_dcd": abs(float(r32["cd"][-1] - r64["cd"][-1])),
+            "max_abs_dcp_wall": float(np.max(np.abs(out["fp32"][1] - out["fp64"][1]))),
+            "cl_fp64": float(r64["cl"][-1]), "cd_fp64": float(r64["cd"][-1]),
+            "residual_ratio_fp64": float(r64["residual_ratio"][-1]),
+            "residual_ratio_fp32": float(r32["residual_ratio"][-1]),
+            "run_s_fp32": out["fp32"][2], "run_s_fp64": out["fp64"][2]}, r64
+
+
+def c4_accuracy(args, aero_gb300, capi, rank, n_check=8, iters=1000):
+    """FP32 batch against FP64 single runs: the sweep's 96 cases run as one FP32 batch for
+    `iters` iterations from free stream, and the first n_check of them again, one FP64 context
+    each; |dCL| and |dCD| at the end of each case's run (a case stops early at its mask)."""
+    meshes, cases = c4_cases(aero_gb300, capi, rank, capi.PRECISION_FP32)
+    with aero_gb300.Batch(meshes, cases) as b:
+        _, recs = b.run(iters)
+    per = []
+    for k in range(n_check):
+        c64 = capi.make_case(**dict(capi.case_to_dict(cases[k]), precision=capi.PRECISION_FP64))
+        with aero_gb300.Solver(meshes[k], c64) as s:
+            _, r = s.run(iters)
+        per.append({"cells": meshes[k].num_cells, "mach": round(float(cases[k].mach), 4),
+                    "alpha": round(float(cases[k].aoa_deg), 4), "iterations_fp32": int(len(recs[k])),
+                    "iterations_fp64": int(len(r)), "abs_dcl": abs(float(recs[k]["cl"][-1] - r["cl"][-1])),
+                    "abs_dcd": abs(float(recs[k]["cd"][-1] - r["cd"][-1]))})
+    return {"iterations": iters, "cases_checked": n_check, "max_abs_dcl": max(p["abs_dcl"] for p in per),
+            "max_abs_dcd": max(p["abs_dcd"] for p in per), "per_case": per}
+
+
+def c5_bounded(aero_gb300, capi):
+    """The adjoint configuration's family at a bounded size: 128x32 triangulated O-grid (8,192
+    cells), M=0.75, alpha=2, HLLC first order, 16 seeded Hicks-Henne bumps, J = CD. FP64 primal
+    to a density-residual ratio of 1e-8, adjoint by the same RK3 smoother to 1e-8, and the
+    gradient again from an FP32 primal (ratio 1e-6) whose state seeds the FP64 adjoint."""
+    from aero_gb300.adjoint import ShapeProblem
+
+    rng = np.random.default_rng(5)
+    peaks = rng.uniform(0.05, 0.95, 16)
+    upper = np.array([1] * 8 + [0] * 8)
+    amps = rng.normal(0.0, 1e-3, 16)
+    kw = dict(CASE)
+    kw.update(mach=0.75, aoa_deg=2.0, startup_first_order_iters=10 ** 9)
+    case = capi.make_case(**kw, precision=capi.PRECISION_FP64)
+    mesh = aero_gb300.ogrid_synthetic(128, 32, cell_type=3, permute=True, jitter=0.1, seed=55)
+
+    def problem(rho, prec):
+        return ShapeProblem(mesh, case, peaks=peaks, upper=upper, width=3.0, max_iters=200000, rho_target=rho,
+                            chunk=20000, adjoint_max_iters=400000, adjoint_tol=1e-8, adjoint_method="smoother",
+                            primal_precision=prec)
+
+    prob = problem(1e-8, capi.PRECISION_FP64)
+    base = prob.solve(amps, 2.0)
+    da, dal = prob.gradient(base, 1.0, 0.0)
+    base.solver.close()
+    out = {"cells": mesh.num_cells, "bumps": 16, "scheme": "HLLC first order", "primal_fp64_s": base.seconds,
+           "primal_iters": base.iterations, "primal_rho_ratio": base.rho_ratio, "cd": base.cd, "cl": base.cl,
+           "adjoint_s": prob.last_adjoint_seconds, "adjoint_iters": prob.last_adjoint_iterations,
+           "adjoint_residual_ratio": prob.last_adjoint_ratio,
+           "adjoint_over_primal": prob.last_adjoint_seconds / base.seconds,
+           "dcd_dalpha_per_deg": dal, "dcd_damp_norm": float(np.linalg.norm(da))}
+    p32 = problem(1e-6, capi.PRECISION_FP32)
+    b32 = p32.solve(amps, 2.0)
+    da32, dal32 = p32.gradient(b32, 1.0, 0.0)
+    b32.solver.close()
+    ref = np.append(da, dal)
+    out.update({"primal_fp32_s": b32.seconds, "primal_fp32_iters": b32.iterations,
+                "fp32_primal_gradient_rel_diff": float(np.linalg.norm(np.append(da32, dal32) - ref) /
+                                                       np.linalg.norm(ref))})
+    return out
+
+
+def kernel_times(prof: dict) -> dict:
+    return {k: (v[0] / v[1] * 1e3 if v[1] else 0.0) for k, v in prof.items()}
+
+
+# ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
 def run_gpu_arm(args):
+    world, rank, local, dist = dist_setup(args)
+    checks = start_oracle_checks(rank == 0 and world == 1 and not args.no_cpu and not args.mesh)
     import aero_gb300
     from aero_gb300 import capi
 
-    world, rank, local, dist = dist_setup(args)
     aero_gb300.load()
     aero_gb300.select_device(local)
     mesh = make_mesh(args)
@@ -478,6 +700,7 @@ def run_gpu_arm(args):
     precisions = ["fp32", "fp64"] if args.precision == "both" else [args.precision]
     results = {}
     peak, peak_kind = measured_peak()
+    nprof = max(3, min(args.steps, 10))
     for prec in precisions:
         pcode = capi.PRECISION_FP32 if prec == "fp32" else capi.PRECISION_FP64
         case = capi.make_case(**CASE, precision=pcode)
@@ -495,31 +718,29 @@ def run_gpu_arm(args):
             barrier(dist)
             ms_max = reduce_max(dist, ms)
             warm_ms = s.time_iterations(args.steps, use_graph=True, flush_l2=False)
-            prof = s.profile_kernels(max(2, min(args.steps, 10)), flush_l2=not args.no_flush)
+            graph_prof, graph_ms = s.profile_graph(nprof, flush_l2=not args.no_flush)
+            plain_ms = s.time_iterations(nprof, use_graph=True, flush_l2=not args.no_flush)
+            prof = s.profile_kernels(nprof, flush_l2=not args.no_flush)
             state = s.get_state() if prec == "fp32" else None
             finite = bool(np.all(np.isfinite(s.get_state())))
         value = world * n * args.steps / (ms_max / 1e3) / 1e6
-        res_ms, res_n = prof["face_pass"]
-        avg_res = res_ms / max(res_n, 1)
-        bytes_res = algorithmic_bytes("face", n, info["slots_per_cell"], prec, int(info["faces"]))
-        achieved = bytes_res / (avg_res / 1e3) / 1e9
-        total_prof = sum(v[0] for v in prof.values())
-        results[prec] = dict(value=value, ms=ms_max, warm_ms=warm_ms, info=info, prof=prof, state=state,
-                             finite=finite, achieved=achieved, avg_res_ms=avg_res, bytes_res=bytes_res,
-                             share=res_ms / total_prof if total_prof else None, clocks=sampler.summary() if sampler else None)
+        f_ms, f_n = graph_prof["face_pass"]
+        avg_face = f_ms / max(f_n, 1)
+        bytes_face = algorithmic_bytes("face", n, info["slots_per_cell"], prec, int(info["faces"]))
+        main_ms = sum(v[0] for k, v in graph_prof.items() if k != "control")
+        in_graph = {"us_per_launch": kernel_times(graph_prof),
+                    "launches_per_iteration": {k: v[1] / nprof for k, v in graph_prof.items()},
+                    "us_per_iteration": {k: v[0] / nprof * 1e3 for k, v in graph_prof.items()},
+                    "kernels_on_main_stream_us_per_iteration": main_ms / nprof * 1e3,
+                    "marked_graph_us_per_iteration": graph_ms / nprof * 1e3,
+                    "plain_graph_us_per_iteration": plain_ms / nprof * 1e3,
+                    "note": "each kernel between event nodes inside the iteration graph; the controller "
+                            "runs on a side stream beside the next iteration's first kernels"}
+        results[prec] = dict(value=value, ms=ms_max, warm_ms=warm_ms, info=info, state=state, finite=finite,
+                             achieved=bytes_face / (avg_face / 1e3) / 1e9, avg_face_ms=avg_face, bytes_face=bytes_face,
+                             share=f_ms / main_ms if main_ms else None, in_graph=in_graph,
+                             isolated=kernel_times(prof), clocks=sampler.summary() if sampler else None)
     head = results[precisions[0]]
-
-    # |dCL| between FP32 and FP64 after a common number of iterations from freestream
-    dcl = None
-    if args.precision == "both" and args.dcl_iters > 0:
-        cls = {}
-        for prec, pcode in (("fp32", capi.PRECISION_FP32), ("fp64", capi.PRECISION_FP64)):
-            with aero_gb300.Solver(mesh, capi.make_case(**CASE, precision=pcode)) as s:
-                _, rec = s.run(args.dcl_iters)
-                cls[prec] = (rec["cl"][-1], rec["cd"][-1], rec["residual_l2"][-1] / rec["residual_l2"][0])
-        dcl = dict(iters=args.dcl_iters, abs_dcl=abs(cls["fp32"][0] - cls["fp64"][0]),
-                   abs_dcd=abs(cls["fp32"][1] - cls["fp64"][1]), cl_fp64=cls["fp64"][0], cd_fp64=cls["fp64"][1],
-                   l2_ratio_fp64=cls["fp64"][2])
 
     # end to end through the C ABI with host buffers: upload the state, run K iterations
     # with every iteration's record copied to the host, download the state
@@ -561,9 +782,31 @@ def run_gpu_arm(args):
               "inputs": "96 seeded cases per GPU: sizes from {64x16,128x32,256x64,512x128} triangulated "
                         "O-grids, alpha~U[-4,8], M~U[0.3,0.85], HLLC+MUSCL venkat, CFL ramp to 0.8, "
                         "density-residual stop mask 1e-8; one batched context, L2 flushed per step"}
+        if rank == 0 and not args.mesh:
+            c4["fp32_batch_vs_fp64_single"] = c4_accuracy(args, aero_gb300, capi, rank)
 
-    c3 = c3_low_mach(args, aero_gb300, capi, peak) if not args.no_c3 and rank == 0 else None
-    c5 = c5_adjoint(args, aero_gb300, capi) if (args.c5 or args.c5_fd) and rank == 0 else None
+    gate = c1 = c3 = c5 = None
+    gate_rec64 = c1_rec = None
+    if rank == 0 and not args.mesh:
+        if "fp32" in precisions and "fp64" in precisions:
+            gate, gate_rec64 = c2_gate(mesh, aero_gb300, capi)
+        c1, c1_rec = c1_quad(aero_gb300, capi)
+        if not args.no_c3:
+            c3 = c3_low_mach(args, aero_gb300, capi, peak)
+        if not args.no_c5:
+            c5 = c5_adjoint(args, aero_gb300, capi) if args.c5 or args.c5_fd else c5_bounded(aero_gb300, capi)
+
+    oracle = collect_oracle_checks(checks)
+    if "c1" in oracle and c1 is not None:
+        hist, dt, cells = oracle["c1"]
+        c1.update(history_diff(c1_rec, hist, C1_ITERS))
+        c1.update({"cpu_oracle_fp64_mcell_iter_s": cells * C1_ITERS / dt / 1e6, "cpu_oracle_cores": 1,
+                   "cpu_oracle_s": dt})
+    if "c2" in oracle and gate is not None:
+        hist, dt, cells = oracle["c2"]
+        gate["fp64_gpu_vs_fp64_cpu_oracle"] = dict(iterations=C2_ORACLE_ITERS,
+                                                   **history_diff(gate_rec64, hist, C2_ORACLE_ITERS),
+                                                   cpu_oracle_fp64_mcell_iter_s=cells * C2_ORACLE_ITERS / dt / 1e6)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu and head["state"] is not None:
@@ -573,34 +816,37 @@ def run_gpu_arm(args):
         return
     r32 = results.get("fp32")
     r64 = results.get("fp64")
+    traffic, traffic_note = measured_traffic("face_pass", precisions[0], n)
+    config = workload_config(args, n, int(head["info"]["faces"]))
+    config.update({
+        "precision_headline": precisions[0],
+        "l2": "flushed before every timed iteration (256 MiB write)" if not args.no_flush else "not flushed",
+        "parallelism": f"replicas x{world}", "timing": "CUDA events on the library stream, CUDA graph per iteration",
+        "fp32_mcell_iter_s": r32["value"] if r32 else None,
+        "fp64_mcell_iter_s": r64["value"] if r64 else None,
+        "fp32_over_fp64": (r32["value"] / r64["value"]) if (r32 and r64) else None,
+        "fp32_l2_warm_mcell_iter_s": world * n * args.steps / (r32["warm_ms"] / 1e3) / 1e6 if r32 else None,
+        "fp64_l2_warm_mcell_iter_s": world * n * args.steps / (r64["warm_ms"] / 1e3) / 1e6 if r64 else None,
+        "in_graph_kernels": {p: results[p]["in_graph"] for p in precisions},
+        "isolated_kernel_us_per_launch": {p: results[p]["isolated"] for p in precisions},
+        "c2_gate": gate,
+        "c1": c1,
+        "c4_batched_sweep": c4,
+        "c3_low_mach": c3,
+        "c5_adjoint": c5,
+        "state_finite": head["finite"],
+    })
     line = {
         "metric": METRIC, "value": head["value"], "unit": "Mcell-iter/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms"] / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if precisions[0] == "fp32" else "f64", "data": "synthetic",
-        "config": {
-            "workload": "NACA0012 512x128 O-grid, 131072 triangles, jitter 10%, permuted; M=0.8, alpha=1.25, "
-                        "HLLC+MUSCL venkat, RK3 local dt, CFL 0.8" if not args.mesh else
-                        f"NACA0012 {args.mesh[0]}x{args.mesh[1]} O-grid (small profiling case)",
-            "cells": n, "faces": int(head["info"]["faces"]), "precision_headline": precisions[0],
-            "l2": "flushed before every timed iteration (256 MiB write)" if not args.no_flush else "not flushed",
-            "parallelism": f"replicas x{world}", "timing": "CUDA events on the library stream, CUDA graph per iteration",
-            "fp32_mcell_iter_s": r32["value"] if r32 else None,
-            "fp64_mcell_iter_s": r64["value"] if r64 else None,
-            "fp32_over_fp64": (r32["value"] / r64["value"]) if (r32 and r64) else None,
-            "fp32_l2_warm_mcell_iter_s": world * n * args.steps / (r32["warm_ms"] / 1e3) / 1e6 if r32 else None,
-            "fp64_l2_warm_mcell_iter_s": world * n * args.steps / (r64["warm_ms"] / 1e3) / 1e6 if r64 else None,
-            "dcl": dcl,
-            "c4_batched_sweep": c4,
-            "c3_low_mach": c3,
-            "c5_adjoint": c5,
-            "kernel_profile_ms_per_launch": {k: (v[0] / v[1] if v[1] else 0.0) for k, v in head["prof"].items()},
-            "state_finite": head["finite"],
-        },
+        "config": config,
         "roofline": {"bound": "hbm", "kernel": "k_face_flux (MUSCL reconstruction + HLLC flux, one thread per face)",
                      "achieved": head["achieved"], "peak": peak, "unit": "GB/s", "frac": head["achieved"] / peak,
-                     "peak_kind": peak_kind, "traffic": NCU_TRAFFIC.get((precisions[0], n)),
-                     "algorithmic_bytes_per_launch": head["bytes_res"], "avg_launch_ms": head["avg_res_ms"],
+                     "peak_kind": peak_kind, "traffic": traffic, "traffic_source": traffic_note,
+                     "algorithmic_bytes_per_launch": head["bytes_face"], "avg_launch_ms": head["avg_face_ms"],
+                     "launch_time": "in the iteration graph, between event nodes",
                      "time_share": head["share"]},
         "cpu_baseline": cpu,
         "e2e": e2e,
@@ -609,7 +855,7 @@ def run_gpu_arm(args):
     }
     if r64 and precisions[0] == "fp32":
         line["roofline_fp64"] = {"achieved": r64["achieved"], "frac": r64["achieved"] / peak,
-                                 "avg_launch_ms": r64["avg_res_ms"]}
+                                 "avg_launch_ms": r64["avg_face_ms"]}
     print(json.dumps(line))
 
 
@@ -621,22 +867,23 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--precision", choices=["fp32", "fp64", "both"], default="both")
     ap.add_argument("--mesh", type=int, nargs=2, default=None, help="n_circ n_radial of a smaller mesh")
-    ap.add_argument("--dcl-iters", type=int, default=300)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-flush", action="store_true")
     ap.add_argument("--no-clocks", action="store_true")
     ap.add_argument("--no-c4", action="store_true", help="skip the 96-case batched sweep measurement")
     ap.add_argument("--cpu-procs", type=int, default=0, help="processes of the reference arm (0: all cores)")
     ap.add_argument("--no-c3", action="store_true", help="skip the 524k-cell low-Mach measurement")
-    ap.add_argument("--c3-profile", action="store_true",
-                    help="only run the 524k-cell low-Mach case with direct launches (for ncu)")
-    ap.add_argument("--c5", action="store_true", help="also time the adjoint gradient case (primal + adjoint)")
+    ap.add_argument("--profile-run", choices=["workload", "c3"], default=None,
+                    help="only run one case with direct launches (for kernel profilers)")
+    ap.add_argument("--no-c5", action="store_true", help="skip the adjoint leg")
+    ap.add_argument("--c5", action="store_true",
+                    help="the adjoint leg on the configured 512x128 grid instead of the bounded 128x32 one")
     ap.add_argument("--c5-fd", action="store_true", help="--c5 plus central differences for alpha and two bumps")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
-    if args.c3_profile:
-        c3_profile_run(args)
+    if args.profile_run:
+        profile_run(args)
     elif args.impl == "reference":
         run_reference_arm(args)
     else:

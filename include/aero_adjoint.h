@@ -67,6 +67,22 @@ AERO_API int aero_adjoint_dalpha(aero_ctx* ctx, double* dj_dalpha_deg);
  * free stream and the reference length are held fixed. */
 AERO_API int aero_adjoint_geometry(aero_ctx* ctx, const aero_mesh_desc* tangent, double* dj);
 
+/* Reverse product with respect to the geometry, the transpose of aero_adjoint_geometry (no
+ * reference counterpart): with the current lam, dJ/d(geometry) for every face normal
+ * d_normal [3F], face centre d_center [3F], face length d_area [F], cell volume d_volume [N]
+ * and cell centre d_cell_center [3N] in the mesh's original numbering (z entries 0), the
+ * objective's own dependence through the force patch included. For every geometry tangent
+ * t, aero_adjoint_geometry(t) equals the sum of these arrays times t's. */
+AERO_API int aero_adjoint_geometry_vjp(aero_ctx* ctx, double* d_normal, double* d_center, double* d_area,
+                                       double* d_volume, double* d_cell_center);
+
+/* dJ/dX for every node of the generator mesh the context's mesh was described from
+ * (aero_mesh_describe of `mesh`): aero_adjoint_geometry_vjp followed by
+ * aero_mesh_geometry_vjp, dj_dpoints [3P] (z entries 0). One reverse pass whatever the
+ * number of nodes: dJ/d(any shape parameter p) = sum of dj_dpoints * dX/dp. */
+struct aero_mesh;
+AERO_API int aero_adjoint_node_vjp(aero_ctx* ctx, const struct aero_mesh* mesh, double* dj_dpoints);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,7 +60,17 @@ AERO_API int aero_run_euler_airfoil_case(const aero_case_desc* cfg, const aero_a
 AERO_API int aero_run_case(const char* case_path, const char* out_dir, const char* backend,
                            aero_run_summary* out);
 
-/* Message of the last failed driver call on this thread. */
+/* Sweep of a base case over angles of attack, replacing the serial loop of the reference's
+ * run_sweep (python/cfd/sweep.py:14-59, one run_case per angle, each into
+ * <output root>/run_NNN). Reads the base case file, sets case k's aoa_deg = aoa_deg[k] (and
+ * mach = mach[k] when mach is not NULL; no reference counterpart), runs all n_cases cases as
+ * one batch on the base case's mesh, and writes each case's run_case outputs into
+ * out_root/run_000, run_001, ... plus out_root/sweep_summary.csv (run, aoa_deg, mach,
+ * iterations, residual_l2, cl, cd, cm, status). summaries[k] receives case k's run_case dict
+ * values. Every case's results equal those of run_case on the modified case file. */
+AERO_API int aero_run_sweep(const char* case_path, int n_cases, const double* aoa_deg, const double* mach,
+                            const char* out_root, const char* backend, aero_run_summary* summaries);
+
 /* State dump for continuation (no reference counterpart; the reference has no restart):
  * a 16-byte magic, int64 cell count, int64 component count (5), then the conserved state
  * [N][5] double in the reference's cell order and AoS layout, host byte order. Read checks
@@ -72,6 +82,7 @@ AERO_API int aero_run_case(const char* case_path, const char* out_dir, const cha
 AERO_API int aero_state_write(const char* path, int num_cells, const double* conserved);
 AERO_API int aero_state_read(const char* path, int num_cells, double* conserved);
 
+/* Message of the last failed driver call on this thread. */
 AERO_API const char* aero_driver_last_error(void);
 
 #ifdef __cplusplus

@@ -228,6 +228,16 @@ AERO_API int aero_time_iterations(aero_ctx* ctx, int n, int use_graph, int flush
  * 3 global-time-step reduction, 4 symmetry/pressure-jump, 5 controller. */
 AERO_API int aero_profile_kernels(aero_ctx* ctx, int n, int flush_l2, double* ms, int* launches);
 
+/* In-graph attribution of n iterations (no reference counterpart): every iteration runs as a
+ * CUDA graph with the kernel nodes and dependencies of the timed iteration graphs plus an
+ * event-record node before and after each kernel node, on the kernel's own stream. ms[6] /
+ * launches[6] as in aero_profile_kernels, each kernel timed where it runs in the graph (class 5,
+ * the controller, runs on a side stream beside the next iteration's first kernels, so its time
+ * overlaps theirs); *iteration_ms: summed time from each iteration graph's first event node to
+ * its last. With flush_l2 = 1 the L2 is overwritten before every iteration. */
+AERO_API int aero_profile_graph(aero_ctx* ctx, int n, int flush_l2, double* ms, int* launches,
+                                double* iteration_ms);
+
 /* Make `device` the current device of the library's CUDA runtime for this host thread
  * (contexts created afterwards on this thread live there). */
 AERO_API int aero_select_device(int device);

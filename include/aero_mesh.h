@@ -75,6 +75,15 @@ AERO_API int aero_mesh_geometry_tangent(const aero_mesh* m, const double* dpoint
                                         double* d_center, double* d_area, double* d_volume,
                                         double* d_cell_center);
 
+/* Transpose of aero_mesh_geometry_tangent (no reference counterpart): from the derivatives of a
+ * scalar with respect to face_normal [3F], face_center [3F], face_area [F], cell_volume [N] and
+ * cell_center [3N], its derivatives with respect to the node coordinates, b_points [3P] (z
+ * entries 0), in one reverse pass; for every node displacement dX, the sum of b_points * dX
+ * equals the sum of the given derivatives times aero_mesh_geometry_tangent(dX). */
+AERO_API int aero_mesh_geometry_vjp(const aero_mesh* m, const double* b_normal, const double* b_center,
+                                    const double* b_area, const double* b_volume, const double* b_cell_center,
+                                    double* b_points);
+
 /* Shape modes of n Hicks-Henne bumps, modes [n][3P]: mode k moves the wall-patch nodes of
  * the upper (upper[k] != 0, y > 0) or lower (y < 0) surface in y by
  * sin(pi xi^(ln 0.5 / ln peak_x[k]))^width_exponent, xi the chordwise position in [0, 1]

@@ -29,8 +29,9 @@ _oracle = None
 _ref = None
 
 
-def build(ref: bool = False) -> None:
-    targets = ["all"] + (["ref"] if ref else [])
+def build(ref_root: str | None = None) -> None:
+    """Compile the oracle; with ref_root (the AeroCFD source root) also the reference library."""
+    targets = ["all"] + (["ref", f"REF_ROOT={ref_root}"] if ref_root else [])
     subprocess.run(["make", "-s", "-C", str(HERE), *targets], check=True)
 
 

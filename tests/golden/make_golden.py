@@ -158,8 +158,7 @@ def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-root", required=True, help="root of the AeroCFD sources to compile")
     args = ap.parse_args()
-    os.environ["REF_ROOT"] = args.ref_root
-    op.build(ref=True)
+    op.build(ref_root=args.ref_root)
 
     meshes = {"demo_2x2": export_mesh("demo_2x2")}
     for name in OGRIDS:

@@ -15,6 +15,7 @@ import pytest
 import aero_gb300
 from aero_gb300 import capi
 from aero_gb300.adjoint import ShapeProblem
+from oracle import oracle_py as op
 
 pytestmark = pytest.mark.gpu
 
@@ -282,3 +283,111 @@ def test_autograd_function_returns_the_adjoint_gradient():
     da, dal = prob.gradient(base, 1.0, 2.0)
     np.testing.assert_allclose(a.grad.numpy(), da, rtol=1e-9, atol=1e-12)
     assert abs(alpha.grad.item() - dal) <= 1e-9 * abs(dal)
+
+
+def _oracle_cd(prim, alpha_deg, iters=60):
+    """CD of a converged device state as the FP64 oracle computes it on the same deformed mesh
+    after `iters` further iterations started from that state, with the oracle's own density
+    residual over them (the state must already be the oracle's steady state)."""
+    from aero_gb300.adjoint import converged_case
+
+    case = converged_case(prim.solver.case, alpha_deg, capi.PRECISION_FP64, iters, 0.0)
+    o = op.OracleSolver(op.MODE_DOUBLE, prim.mesh, case)
+    o.set_state(prim.solver.get_state())
+    _, rec = o.run(iters)
+    return float(rec["cd"][-1]), rec
+
+
+def test_gradients_against_oracle_central_differences():
+    """The adjoint configuration's numerics (HLLC, M = 0.75, alpha = 2 deg, 16 Hicks-Henne bumps
+    with the configuration's seeded draw, J = CD, first order: the second-order primal has no
+    steady state on these meshes) on the 64x16 grid of its family. dCD/dalpha and dCD/da_0 from
+    the discrete adjoint against central differences (step 1e-6) of CD from the FP64 CPU oracle:
+    each perturbed state is converged on the device to a density-residual ratio of 1e-13, then
+    handed to the oracle, which must keep it (its own residual stays at round-off) and
+    integrates CD from it. Agreement within 1e-4 relative."""
+    op.build()
+    rng = np.random.default_rng(5)
+    peaks = rng.uniform(0.05, 0.95, 16)
+    upper = np.array([1] * 8 + [0] * 8)
+    amps = rng.normal(0.0, 1e-3, 16)
+    mesh = aero_gb300.ogrid_synthetic(64, 16, cell_type=3, permute=True, jitter=0.1, seed=55)
+    case = capi.make_case(mach=0.75, aoa_deg=2.0, flux=capi.FLUX_HLLC, limiter=capi.LIMITER_VENKAT,
+                          startup_first_order_iters=10 ** 9, cfl_start=0.2, cfl_max=0.8, cfl_ramp_iters=120,
+                          precision=capi.PRECISION_FP64)
+    prob = ShapeProblem(mesh, case, peaks=peaks, upper=upper, width=3.0, max_iters=200000, rho_target=1e-13,
+                        chunk=20000, adjoint_max_iters=400000, adjoint_tol=1e-12, adjoint_method="smoother")
+    base = prob.solve(amps, 2.0)
+    assert base.rho_ratio <= 1e-13
+    da, dal = prob.gradient(base, 1.0, 0.0)
+    assert prob.last_adjoint_ratio <= 1e-12
+    cd0, _ = _oracle_cd(base, 2.0)
+    assert abs(cd0 - base.cd) <= 1e-12 * abs(base.cd)  # the oracle agrees on the base state's CD
+    # the oracle's residual at the free stream, the scale its residual at a steady state is read against
+    _, fs = op.OracleSolver(op.MODE_DOUBLE, base.mesh, case).run(1)
+    l2_free = float(fs["residual_l2"][0])
+    h = 1e-6
+    for name, e, al in (("alpha", np.zeros(16), h), ("a0", np.eye(16)[0] * h, 0.0)):
+        cds = []
+        for sgn in (1.0, -1.0):
+            prim = prob.solve(amps + sgn * e, 2.0 + sgn * al)
+            assert prim.rho_ratio <= 1e-13
+            cd, rec = _oracle_cd(prim, 2.0 + sgn * al)
+            # the device state is the oracle's steady state: its residual stays at round-off
+            assert rec["residual_l2"][-1] <= 1e-11 * l2_free
+            cds.append(cd)
+            prim.solver.close()
+        fd = (cds[0] - cds[1]) / (2 * h)
+        adj = dal if name == "alpha" else float(da[0])
+        assert abs(adj - fd) <= 1e-4 * abs(fd), (name, adj, fd)
+
+
+@pytest.mark.parametrize("scheme", sorted(SCHEMES))
+@pytest.mark.parametrize("low_mach", [False, True])
+def test_geometry_vjp_is_the_transpose_of_the_geometry_product(scheme, low_mach):
+    """The reverse geometry product (one pass for every face normal, length and centre and
+    every cell volume and centre) against the forward one: for random lam and random node
+    displacements dX, sum(vjp * tangent(dX)) = lam^T dR/dX dX + dJ/dX|_U dX from
+    aero_adjoint_geometry, and the node-level product sum(dJ/dX * dX) gives the same number."""
+    sc = SCHEMES[scheme]
+    mesh = _mesh(48, 12, seed=9)
+    kw = dict(mach=0.6, aoa_deg=2.0, flux=sc["flux"], limiter=sc["limiter"], startup_first_order_iters=5,
+              cfl_max=0.8, iterations=100000, precision=capi.PRECISION_FP64)
+    if low_mach:
+        kw.update(mach=0.2, precond_on=1, low_mach_fix=1, all_speed_flux_fix=1, precond_farfield_bc=1)
+    case = capi.make_case(**kw)
+    rng = np.random.default_rng(11)
+    with aero_gb300.Solver(mesh, case) as s:
+        s.run(60)
+        s.adjoint_linearize(0.7, 0.3, sc["second"])
+        lam = rng.standard_normal((mesh.num_cells, 5))
+        lam[:, 3] = 0.0
+        s.adjoint_set_lambda(lam)
+        bars = s.adjoint_geometry_vjp()
+        nodes = s.adjoint_node_vjp()
+        pts = mesh.points.reshape(-1, 3)
+        for trial in range(3):
+            dp = np.zeros_like(pts)
+            dp[:, :2] = rng.standard_normal((pts.shape[0], 2)) * 1e-3
+            t = aero_gb300.geometry_tangent(mesh, dp)
+            want = s.adjoint_geometry(t)
+            got = sum(float(np.dot(getattr(bars, k), getattr(t, k)))
+                      for k in ("normal", "center", "area", "volume", "cell_center"))
+            assert abs(got - want) <= 1e-10 * abs(want), (trial, got, want)
+            assert abs(float(np.sum(nodes * dp)) - want) <= 1e-10 * abs(want), trial
+
+
+def test_shape_gradient_by_the_node_reverse_product():
+    """ShapeProblem's gradient through dJ/dX (one reverse pass, then the modes) equals the one
+    through one geometry tangent per bump."""
+    mesh = _mesh(64, 16, seed=11)
+    case = capi.make_case(mach=0.5, aoa_deg=2.0, flux=capi.FLUX_HLLC, startup_first_order_iters=10 ** 9,
+                          cfl_max=0.8, precision=capi.PRECISION_FP64)
+    prob = ShapeProblem(mesh, case, peaks=[0.2, 0.4, 0.6, 0.8], upper=[1, 0, 1, 0], width=3.0, max_iters=100000,
+                        rho_target=1e-12, adjoint_max_iters=200000, adjoint_tol=1e-11, adjoint_method="smoother")
+    base = prob.solve(np.full(4, 1e-3), 2.0)
+    da_t, dal_t = prob.gradient(base, 1.0, 0.5)
+    prob.geometry_product = "reverse"
+    da_r, dal_r = prob.gradient(base, 1.0, 0.5)
+    np.testing.assert_allclose(da_r, da_t, rtol=1e-9, atol=1e-12 * np.abs(da_t).max())
+    assert dal_r == dal_t

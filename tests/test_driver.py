@@ -189,3 +189,100 @@ def test_restart_dump_and_binary_vtu(tmp_path):
     assert set(va) == set(vb) and len(va) == 10
     for k in va:
         np.testing.assert_allclose(vb[k].astype(np.float64), va[k], rtol=1e-5, atol=1e-12, err_msg=k)
+
+
+SMALL = dict(naca_code="0012", num_circumferential=48, num_radial=12, farfield_radius=12, radial_stretch=1.35,
+             min_iterations=40, residual_reduction_target=1e-9, flux="hllc", limiter="venkat", precond="off",
+             startup_first_order_iters=10, cfl_ramp_iters=20, cfl_start=0.3, cfl_max=0.8, mach=0.5)
+
+
+def _csv_text(path):
+    return path.read_text()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_sweep_writes_each_case_like_run_case(tmp_path, precision):
+    """The batched sweep entry (python/cfd/sweep.py:14-59 as one batch) writes, for each angle,
+    the files run_case writes for the case file at that angle: forces, residuals, diagnostics
+    and Cp identical to the byte."""
+    base = write_cfg(tmp_path / "base.cfg", iterations=40, aoa_deg=0.0, precision=precision, **SMALL)
+    sweep = tmp_path / "sweep.cfg"
+    sweep.write_text("base_case = base.cfg\naoa_deg = -2, 1.5, 4\n")
+    res = cfd_core.run_sweep(str(sweep), jobs=3, backend="cuda", out_dir=str(tmp_path / "sw"))
+    assert res["status"] == "ok" and res["jobs_requested"] == 3 and len(res["runs"]) == 3
+    summary = list(csv.DictReader(open(tmp_path / "sw" / "sweep_summary.csv")))
+    assert [float(r["aoa_deg"]) for r in summary] == [-2.0, 1.5, 4.0]
+    for k, aoa in enumerate((-2.0, 1.5, 4.0)):
+        single = write_cfg(tmp_path / f"single{k}.cfg", iterations=40, aoa_deg=aoa, precision=precision, **SMALL)
+        one = cfd_core.run_case(str(single), str(tmp_path / f"one{k}"), "cuda")
+        run = res["runs"][k]
+        assert run["aoa_deg"] == aoa and run["iterations"] == one["iterations"]
+        for key in ("cl", "cd", "cm", "residual_l2"):
+            assert run[key] == one[key], key
+        for f in ("forces.csv", "residuals.csv", "euler_diagnostics.csv", "cp_wall.csv", "wall_flux.csv"):
+            assert _csv_text(tmp_path / "sw" / f"run_{k:03d}" / f) == _csv_text(tmp_path / f"one{k}" / f), f
+        assert float(summary[k]["cl"]) == pytest.approx(one["cl"], rel=1e-6)
+    # lift grows with incidence across the sweep
+    assert res["runs"][0]["cl"] < res["runs"][1]["cl"] < res["runs"][2]["cl"]
+
+
+@pytest.mark.gpu
+def test_sweep_over_mach_numbers(tmp_path):
+    base = write_cfg(tmp_path / "base.cfg", iterations=20, aoa_deg=2.0, precision="fp64", **SMALL)
+    runs = cfd_core.run_case_sweep(str(base), str(tmp_path / "sw"), [2.0, 2.0], "cuda", mach=[0.3, 0.6])
+    assert [r["mach"] for r in runs] == [0.3, 0.6]
+    snap = dict(line.split("=", 1) for line in
+                open(tmp_path / "sw" / "run_001" / "effective_config_snapshot.txt").read().split())
+    assert float(snap["mach_inf"]) == pytest.approx(0.6)
+    with pytest.raises(ValueError):
+        cfd_core.run_case_sweep(str(base), str(tmp_path / "x"), [1.0, 2.0], "cuda", mach=[0.3])
+
+
+@pytest.mark.gpu
+def test_run_case_outputs_match_the_oracle(tmp_path):
+    """forces.csv, residuals.csv and cp_wall.csv of an FP64 run_case against the FP64 oracle's
+    run of the same case on the same mesh (run_euler_airfoil_case, euler_solver.cpp:1161-1175,
+    and extract_wall_cp, forces.cpp:177-206). The files hold the reference writer's float
+    values at its default 6 significant digits."""
+    from oracle import oracle_py as op
+
+    op.build()
+    p = write_cfg(tmp_path / "c.cfg", iterations=60, aoa_deg=2.0, precision="fp64", **SMALL)
+    out = tmp_path / "out"
+    cfd_core.run_case(str(p), str(out), "cuda")
+    case, mcfg, _ = parse(p)
+    case.diagnostics = 1
+    mesh = aero_gb300.ogrid_reference(mcfg.naca_code.decode(), mcfg.num_circumferential, mcfg.num_radial,
+                                      mcfg.farfield_radius, mcfg.radial_stretch, mcfg.chord)
+    o = op.OracleSolver(op.MODE_DOUBLE, mesh, case)
+    _, orec = o.run(case.iterations)
+    frows = list(csv.DictReader(open(out / "forces.csv")))
+    rrows = list(csv.DictReader(open(out / "residuals.csv")))
+    assert len(frows) == len(rrows) == len(orec)
+    for key in ("cl", "cd", "cm"):
+        got = np.array([float(r[key]) for r in frows])
+        np.testing.assert_allclose(got, orec[key], rtol=1e-5, atol=1e-7, err_msg=key)
+    for key in ("residual_l1", "residual_l2", "residual_linf"):
+        got = np.array([float(r[key]) for r in rrows])
+        np.testing.assert_allclose(got, orec[key], rtol=1e-5, err_msg=key)
+    # wall Cp of the final state, matched to the wall faces by their centres
+    u = o.get_state()
+    g = case.gamma
+    rho = u[:, 0]
+    pres = (g - 1.0) * (u[:, 4] - 0.5 * (u[:, 1] ** 2 + u[:, 2] ** 2) / rho)
+    rho_inf = case.p_inf / (case.gas_constant * case.t_inf)
+    v_inf = case.mach * np.sqrt(g * case.p_inf / rho_inf)
+    q_inf = 0.5 * rho_inf * v_inf * v_inf + 1e-12
+    wall = mesh.wall_faces
+    centres = mesh.center.reshape(-1, 3)[wall, :2]
+    want = (pres[mesh.owner[wall]] - case.p_inf) / q_inf
+    cp = list(csv.DictReader(open(out / "cp_wall.csv")))
+    assert len(cp) == len(wall)
+    seen = set()
+    for r in cp:  # the file's centres carry 6 significant digits: take the nearest wall face
+        d = np.hypot(centres[:, 0] - float(r["x"]), centres[:, 1] - float(r["y"]))
+        k = int(np.argmin(d))
+        assert d[k] < 1e-5 and k not in seen
+        seen.add(k)
+        assert float(r["Cp"]) == pytest.approx(want[k], rel=1e-5, abs=1e-6)

@@ -439,3 +439,27 @@ def test_cells_per_thread_is_checked():
     case = capi.make_case(cells_per_thread=3)
     with pytest.raises(aero_gb300.AeroError):
         aero_gb300.Solver(mesh, case)
+
+
+@pytest.mark.parametrize("precision", [capi.PRECISION_FP64, capi.PRECISION_FP32])
+def test_in_graph_kernel_attribution(precision):
+    """aero_profile_graph times every kernel between event nodes inside the iteration graph:
+    per RK3 second-order iteration 3 gradient, 3 face and 3 update launches and one controller;
+    the main-stream kernels fit inside the iteration's span, which is close to the plain
+    graph's time; and the iterations it runs are real ones (the state moves on exactly as
+    in a run of the same length)."""
+    mesh = aero_gb300.ogrid_synthetic(128, 32, cell_type=3, permute=True, jitter=0.1, seed=5)
+    case = capi.make_case(mach=0.7, flux=1, limiter=1, startup_first_order_iters=2, precision=precision)
+    with aero_gb300.Solver(mesh, case) as s:
+        s.run(4)
+        prof, span = s.profile_graph(6)
+        after = s.get_state()
+    with aero_gb300.Solver(mesh, case) as s:
+        s.run(10)
+        ref = s.get_state()
+    np.testing.assert_array_equal(after, ref)
+    assert prof["gradient"][1] == prof["face_pass"][1] == prof["update"][1] == 18
+    assert prof["control"][1] == 6
+    main = sum(v[0] for k, v in prof.items() if k != "control")
+    assert 0.0 < main <= span * 1.0001
+    assert all(v[0] > 0.0 for k, v in prof.items() if v[1] > 0)

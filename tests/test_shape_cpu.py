@@ -78,3 +78,29 @@ def test_set_points_refuses_inverted_cells(mesh):
     pts[:, 0] *= -1.0  # mirror: every cell turns clockwise
     with pytest.raises(aero_gb300.AeroError):
         aero_gb300.deform(mesh, pts)
+
+
+@pytest.mark.parametrize("name", ["mesh", "quad_mesh"])
+def test_geometry_vjp_is_the_transpose_of_the_tangent(name, request):
+    """Dot-product test of the reverse geometry pass: for random node displacements dX and
+    random geometry derivatives b, sum(b * tangent(dX)) = sum(vjp(b) * dX)."""
+    m = request.getfixturevalue(name)
+    rng = np.random.default_rng(7)
+    pts = m.points.reshape(-1, 3)
+    nf, nc = m.num_faces, m.num_cells
+    for trial in range(3):
+        dp = np.zeros_like(pts)
+        dp[:, :2] = rng.standard_normal((pts.shape[0], 2))
+        t = aero_gb300.geometry_tangent(m, dp)
+        b = {k: rng.standard_normal(n) for k, n in (("normal", 3 * nf), ("center", 3 * nf), ("area", nf),
+                                                     ("volume", nc), ("cell_center", 3 * nc))}
+        for k in ("normal", "center"):
+            b[k].reshape(-1, 3)[:, 2] = 0.0
+        b["cell_center"].reshape(-1, 3)[:, 2] = 0.0
+        bars = aero_gb300.capi.Mesh(m.owner, m.neighbor, m.bc, b["normal"], b["center"], b["area"], b["volume"],
+                                    b["cell_center"], m.wall_faces)
+        bp = aero_gb300.geometry_vjp(m, bars)
+        lhs = sum(float(np.dot(b[k], getattr(t, k))) for k in b)
+        rhs = float(np.sum(bp * dp))
+        assert abs(lhs - rhs) <= 1e-11 * (abs(lhs) + abs(rhs)), (trial, lhs, rhs)
+        assert not bp[:, 2].any()

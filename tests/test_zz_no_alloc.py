@@ -8,8 +8,9 @@ PyTorch (standing in for such a caller), calls the entry point through the C ABI
 it against the existing aero_residual entry point on two calls in a row (different states),
 plus a repeat of the first state, with the tolerance of the other parity tests: |dR| <= 1e-12
 (FP64) or 2e-5 (FP32) times the per-cell sum over faces of |F_k A|; the FP64 results are also
-checked against the FP64 oracle at 1e-12. It also checks that meshes above the array's limit
-are refused. It runs on its own in a fresh process as well as after the other tests.
+checked against the FP64 oracle at 1e-12. The device's free memory is the same just before
+and just after every call once the first has loaded the kernels. It also checks that meshes
+above the array's limit are refused. It runs on its own in a fresh process as well as after the other tests.
 """
 
 import ctypes as C
@@ -52,16 +53,20 @@ def _states(mesh, case, seeds):
 
 
 def _noalloc(lib, solver, u, args):
+    """One call on caller-owned device buffers; returns the residual, the spectral radius and
+    the device's free memory just before and just after the call."""
     torch = pytest.importorskip("torch")
     n = solver.n
     u_dev = torch.from_numpy(np.ascontiguousarray(u)).to("cuda")
     r_dev = torch.full((n, 5), float("nan"), dtype=torch.float64, device="cuda")
     s_dev = torch.full((n,), float("nan"), dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()  # inputs written before the library's stream reads them
+    free_before = torch.cuda.mem_get_info()[0]
     rc = lib.aero_residual_noalloc(solver.h, u_dev.data_ptr(), *args, r_dev.data_ptr(), s_dev.data_ptr(), None)
     assert rc == 0, lib.aero_last_error(solver.h).decode()
     torch.cuda.synchronize()  # device-wide: also waits for the library's own stream
-    return r_dev.cpu().numpy(), s_dev.cpu().numpy()
+    free_after = torch.cuda.mem_get_info()[0]
+    return r_dev.cpu().numpy(), s_dev.cpu().numpy(), (free_before, free_after)
 
 
 @pytest.mark.parametrize("precision,tol", [(capi.PRECISION_FP64, 1e-12), (capi.PRECISION_FP32, 2e-5)])
@@ -77,8 +82,10 @@ def test_noalloc_matches_existing_entry_point(lib, precision, tol, numerics):
     oracle = op.OracleSolver(op.MODE_DOUBLE, mesh, case)
     with aero_gb300.Solver(mesh, case) as solver:
         results = []
-        for u in (u1, u2, u1):  # two calls in a row on different states, then the first again
-            r, s = _noalloc(lib, solver, u, args)
+        for call, u in enumerate((u1, u2, u1)):  # two calls in a row on different states, then the first again
+            r, s, (free_before, free_after) = _noalloc(lib, solver, u, args)
+            if call > 0:  # after the first call has loaded the kernels, no call takes device memory
+                assert free_after == free_before, (call, free_before - free_after)
             r_ref, s_ref, _ = solver.residual(u, *args)
             r_or, _, _, _, fscale = oracle.residual(u, *args, with_scale=True)
             assert np.all(np.isfinite(r)) and np.all(np.isfinite(s))

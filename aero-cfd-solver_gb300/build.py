@@ -32,7 +32,7 @@ CU_SOURCES = ["engine_f32.cu", "engine_f64.cu", "noalloc.cu"]
 # roots and quotients then skip their subnormal scaling (face pass 12.7 -> 11.6 us at 131k
 # cells). Double arithmetic is unaffected by these flags.
 FAST_FLOAT_DIV_SQRT = ("engine_f32.cu", "noalloc.cu")
-CPP_SOURCES = ["capi.cpp", "mesh_prep.cpp", "mesh_gen.cpp", "driver.cpp"]
+CPP_SOURCES = ["capi.cpp", "mesh_prep.cpp", "mesh_gen.cpp", "driver.cpp", "graph_profile.cpp"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -76,6 +76,7 @@ def build(force: bool = False, ptxas_v: bool = False, verbose: bool = False) -> 
             cmd.insert(3, "-Xptxas=-v")
         if src in FAST_FLOAT_DIV_SQRT:
             cmd[3:3] = ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
+        cmd[3:3] = os.environ.get("AERO_NVCC_FLAGS", "").split()  # extra nvcc flags (experiments)
         jobs.append(cmd)
     for src in CPP_SOURCES:
         obj = OBJ / (src + ".o")
@@ -94,7 +95,7 @@ def build(force: bool = False, ptxas_v: bool = False, verbose: bool = False) -> 
     if failed:
         raise RuntimeError("libaero_gb300 compilation failed")
     tmp = LIB.with_suffix(".so.tmp")
-    link = [nvcc, GENCODE, "-shared", "-o", str(tmp), *map(str, objs), "-Xcompiler", "-fPIC"]
+    link = [nvcc, GENCODE, "-shared", "-o", str(tmp), *map(str, objs), "-Xcompiler", "-fPIC", "-ldl"]
     _, res = _run(link)
     if res.returncode != 0:
         sys.stderr.write(res.stdout + res.stderr)

@@ -218,10 +218,10 @@ __device__ __forceinline__ Speeds<T> precond_speeds(T un, T a, T acoustic_scale)
   return s;
 }
 
-// precond_speeds at acoustic scale 1 (no low-Mach scaling), with the same results: beta = 1,
-// so ut = un exactly and ct = sqrt(4 a^2) / 2 = a exactly (the correctly rounded square root of
-// a rounded square returns the operand, and scaling by 4 is exact), and the largest of |un|,
-// |un - a|, |un + a| (a >= 0) is the rounded |un| + a.
+// precond_speeds at acoustic scale 1 (no low-Mach scaling): beta = 1, so ut = un exactly and
+// ct = sqrt(4 a^2) / 2 = a exactly in the reference's arithmetic (the correctly rounded square
+// root of a rounded square returns the operand, and scaling by 4 is exact), and the largest of
+// |un|, |un - a|, |un + a| (a >= 0) is the rounded |un| + a.
 template <class T>
 __device__ __forceinline__ Speeds<T> unit_speeds(T un, T a) {
   Speeds<T> s;
@@ -259,7 +259,8 @@ struct FaceParams {
 
 // The two sides of a face in primitive form with the quantities the acoustic scale, the
 // all-speed pressure scale and the flux all use, formed once per face: the reference's helpers
-// each convert and derive them again from the conservative states, with identical results.
+// each convert and derive them again from the conservative states by the same formulas (the
+// values agree up to where the compiler contracts a multiply-add).
 template <class T>
 struct FaceSides {
   Prim<T> pl, pr;

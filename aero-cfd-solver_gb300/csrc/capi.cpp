@@ -378,16 +378,6 @@ int aero_profile_kernels(aero_ctx* ctx, int n, int flush_l2, double* ms, int* la
   return cs != AERO_OK ? cs : rc;
 }
 
-int aero_profile_graph(aero_ctx* ctx, int n, int flush_l2, double* ms, int* launches, double* iteration_ms) {
-  if (ctx == nullptr || n <= 0 || ms == nullptr || launches == nullptr || iteration_ms == nullptr)
-    return fail(ctx, AERO_ERR_INVALID, "aero_profile_graph: bad argument");
-  const int rc = ctx->engine->profile_graph(n, flush_l2, ms, launches, iteration_ms);
-  const int cs = cuda_status(ctx);
-  if (cs != AERO_OK) return cs;
-  if (rc == AERO_ERR_STATE) return fail(ctx, rc, "aero_profile_graph: event nodes in the graph carry no timing");
-  return rc;
-}
-
 int aero_select_device(int device) {
   if (!device_ok(device)) return fail(nullptr, AERO_ERR_CUDA, "device is not a usable compute capability 10.3 GPU");
   if (cudaSetDevice(device) != cudaSuccess) {

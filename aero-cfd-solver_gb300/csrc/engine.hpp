@@ -73,7 +73,6 @@ class Engine {
   virtual void last_residual(int cs, double* res, double* sr) = 0;
   virtual int time_iterations(int n, int use_graph, int flush_l2, double* ms) = 0;
   virtual int profile_kernels(int n, int flush_l2, double* ms, int* launches) = 0;
-  virtual int profile_graph(int n, int flush_l2, double* ms, int* launches, double* iter_ms) = 0;
   virtual void info(long long* out, int n) = 0;
   virtual cudaError_t last_cuda_error() = 0;
   virtual int set_wait_limit(int polls) = 0;

@@ -785,99 +785,6 @@ class EngineT final : public Engine {
     return end_untracked();
   }
 
-  // In-graph attribution of n iterations: each iteration runs as a CUDA graph with the
-  // same kernel nodes and dependencies as the iteration graphs of time_iterations, plus an
-  // event-record node before and after every kernel node (on the stream the kernel is
-  // launched on), so each kernel's time is measured where it runs in the graph. ms[cls] /
-  // launches[cls] as in profile_kernels (class 5, the controller, runs beside the next
-  // iteration's first kernels on a side stream and overlaps them); *iter_ms: summed time
-  // from the first to the last event node of each iteration's graph.
-  int profile_graph(int n, int flush_l2, double* ms, int* launches, double* iter_ms) override {
-    const int it0 = begin_untracked();
-    if (flush_l2 && !ensure_flush_buffer()) return AERO_ERR_NOMEM;
-    for (int k = 0; k < 6; ++k) {
-      ms[k] = 0.0;
-      launches[k] = 0;
-    }
-    *iter_ms = 0.0;
-    struct Marked {
-      cudaGraphExec_t exec = nullptr;
-      std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
-      cudaEvent_t first = nullptr, last = nullptr;
-    };
-    std::vector<Marked> cache(16);
-    std::vector<cudaEvent_t> events;
-    auto event = [&]() {
-      cudaEvent_t e = nullptr;
-      AERO_CK(cudaEventCreate(&e));
-      events.push_back(e);
-      return e;
-    };
-    auto marked = [&](bool second, int parity, bool defer, bool pending) -> Marked& {
-      Marked& m = cache[graph_index(second, parity, defer, pending)];
-      if (m.exec != nullptr || err_ != cudaSuccess) return m;
-      m.first = event();
-      m.last = event();
-      // recorded as event-record nodes of the graph (an event recorded during capture
-      // without the external flag only orders the captured work and is never recorded)
-      auto mark = [&](cudaEvent_t e, cudaStream_t s) {
-        AERO_CK(cudaEventRecordWithFlags(e, s, cudaEventRecordExternal));
-      };
-      cudaGraph_t g = nullptr;
-      AERO_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
-      mark(m.first, st_);
-      launch_iteration(second, parity, defer, pending, [&](int cls, auto&& launch) {
-        // the previous iteration's controller is the one launch on the side stream
-        cudaStream_t s = (cls == 5 && pending) ? side_ : st_;
-        cudaEvent_t a = event(), b = event();
-        mark(a, s);
-        launch();
-        mark(b, s);
-        m.marks.push_back({cls, {a, b}});
-      });
-      mark(m.last, st_);
-      AERO_CK(cudaStreamEndCapture(st_, &g));
-      if (g) {
-        AERO_CK(cudaGraphInstantiate(&m.exec, g, 0));
-        cudaGraphDestroy(g);
-      }
-      return m;
-    };
-    int rc = AERO_OK;
-    for (int j = 0; j < n && rc == AERO_OK && err_ == cudaSuccess; ++j) {
-      const int it = it0 + j;
-      if (flush_l2) AERO_CK(cudaMemsetAsync(flush_, j & 0xff, flush_bytes_, st_));
-      Marked& m = marked(second_at(it), it & 1, defer_control_, defer_control_ && j > 0);
-      if (m.exec == nullptr) break;
-      AERO_CK(cudaGraphLaunch(m.exec, st_));
-      if (defer_control_ && j == n - 1) launch_control(it & 1, Direct{});
-      AERO_CK(cudaStreamSynchronize(st_));
-      float f = 0.0f;
-      if (cudaEventElapsedTime(&f, m.first, m.last) != cudaSuccess) {
-        cudaGetLastError();
-        rc = AERO_ERR_STATE;  // event nodes of this graph carry no timing
-        break;
-      }
-      *iter_ms += f;
-      for (auto& mk : m.marks) {
-        float g = 0.0f;
-        if (cudaEventElapsedTime(&g, mk.second.first, mk.second.second) != cudaSuccess) {
-          cudaGetLastError();
-          rc = AERO_ERR_STATE;
-          break;
-        }
-        ms[mk.first] += g;
-        ++launches[mk.first];
-      }
-    }
-    for (auto& m : cache) {
-      if (m.exec) cudaGraphExecDestroy(m.exec);
-    }
-    for (auto e : events) cudaEventDestroy(e);
-    const int end = end_untracked();
-    return end != AERO_OK ? end : rc;
-  }
-
   // ---- discrete adjoint (FP64, one case) -------------------------------------------------
   int adjoint_linearize(double w_cd, double w_cl, int second_order) override {
     if constexpr (sizeof(T) != 8) {

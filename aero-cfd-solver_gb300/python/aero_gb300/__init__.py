@@ -396,8 +396,8 @@ class Solver:
         return {k: (ms[i], launches[i]) for i, k in enumerate(self.KERNEL_CLASSES)}
 
     def profile_graph(self, n: int, flush_l2: bool = False) -> tuple[dict, float]:
-        """In-graph kernel times of n iterations: ({class: (ms, launches)}, summed ms from
-        each iteration graph's first event node to its last)."""
+        """Kernel times of n iterations inside the timed iteration graphs (recorded through
+        CUPTI): ({class: (ms, launches)}, device ms of the n iterations)."""
         ms = (C.c_double * 6)()
         launches = (C.c_int * 6)()
         total = C.c_double(0.0)

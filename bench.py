@@ -719,7 +719,6 @@ def run_gpu_arm(args):
             ms_max = reduce_max(dist, ms)
             warm_ms = s.time_iterations(args.steps, use_graph=True, flush_l2=False)
             graph_prof, graph_ms = s.profile_graph(nprof, flush_l2=not args.no_flush)
-            plain_ms = s.time_iterations(nprof, use_graph=True, flush_l2=not args.no_flush)
             prof = s.profile_kernels(nprof, flush_l2=not args.no_flush)
             state = s.get_state() if prec == "fp32" else None
             finite = bool(np.all(np.isfinite(s.get_state())))
@@ -732,10 +731,13 @@ def run_gpu_arm(args):
                     "launches_per_iteration": {k: v[1] / nprof for k, v in graph_prof.items()},
                     "us_per_iteration": {k: v[0] / nprof * 1e3 for k, v in graph_prof.items()},
                     "kernels_on_main_stream_us_per_iteration": main_ms / nprof * 1e3,
-                    "marked_graph_us_per_iteration": graph_ms / nprof * 1e3,
-                    "plain_graph_us_per_iteration": plain_ms / nprof * 1e3,
-                    "note": "each kernel between event nodes inside the iteration graph; the controller "
-                            "runs on a side stream beside the next iteration's first kernels"}
+                    "iteration_us_while_traced": graph_ms / nprof * 1e3,
+                    "untraced_step_us": ms_max / args.steps * 1e3,
+                    "launch_gaps_us_per_iteration": ms_max / args.steps * 1e3 - main_ms / nprof * 1e3,
+                    "note": "kernel start/end recorded by CUPTI inside the timed iteration graphs (L2 flushed "
+                            "before each iteration as in the timed run); the main-stream kernels run one after "
+                            "another, the controller on a side stream beside the next iteration's first "
+                            "kernels; the untraced step time minus the main-stream kernels is the launch gaps"}
         results[prec] = dict(value=value, ms=ms_max, warm_ms=warm_ms, info=info, state=state, finite=finite,
                              achieved=bytes_face / (avg_face / 1e3) / 1e9, avg_face_ms=avg_face, bytes_face=bytes_face,
                              share=f_ms / main_ms if main_ms else None, in_graph=in_graph,
@@ -846,7 +848,7 @@ def run_gpu_arm(args):
                      "achieved": head["achieved"], "peak": peak, "unit": "GB/s", "frac": head["achieved"] / peak,
                      "peak_kind": peak_kind, "traffic": traffic, "traffic_source": traffic_note,
                      "algorithmic_bytes_per_launch": head["bytes_face"], "avg_launch_ms": head["avg_face_ms"],
-                     "launch_time": "in the iteration graph, between event nodes",
+                     "launch_time": "kernel duration inside the timed iteration graphs (CUPTI)",
                      "time_share": head["share"]},
         "cpu_baseline": cpu,
         "e2e": e2e,

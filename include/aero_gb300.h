@@ -228,13 +228,14 @@ AERO_API int aero_time_iterations(aero_ctx* ctx, int n, int use_graph, int flush
  * 3 global-time-step reduction, 4 symmetry/pressure-jump, 5 controller. */
 AERO_API int aero_profile_kernels(aero_ctx* ctx, int n, int flush_l2, double* ms, int* launches);
 
-/* In-graph attribution of n iterations (no reference counterpart): every iteration runs as a
- * CUDA graph with the kernel nodes and dependencies of the timed iteration graphs plus an
- * event-record node before and after each kernel node, on the kernel's own stream. ms[6] /
- * launches[6] as in aero_profile_kernels, each kernel timed where it runs in the graph (class 5,
- * the controller, runs on a side stream beside the next iteration's first kernels, so its time
- * overlaps theirs); *iteration_ms: summed time from each iteration graph's first event node to
- * its last. With flush_l2 = 1 the L2 is overwritten before every iteration. */
+/* In-graph attribution of n iterations (no reference counterpart): the iterations run exactly
+ * as aero_time_iterations runs them with use_graph = 1 (the same CUDA graphs; the controller
+ * on its side stream beside the next iteration's first kernels) while the CUPTI activity API
+ * records every kernel's start and end on the GPU, without serialising them. ms[6] /
+ * launches[6]: summed kernel time and launches per class as in aero_profile_kernels (class 5,
+ * the controller, overlaps other kernels); *iteration_ms: the device time of the n
+ * iterations between CUDA events. CUPTI is loaded at run time; without it the call returns
+ * AERO_ERR_STATE. One profiling session runs at a time in a process. */
 AERO_API int aero_profile_graph(aero_ctx* ctx, int n, int flush_l2, double* ms, int* launches,
                                 double* iteration_ms);
 

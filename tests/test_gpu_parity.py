@@ -443,11 +443,11 @@ def test_cells_per_thread_is_checked():
 
 @pytest.mark.parametrize("precision", [capi.PRECISION_FP64, capi.PRECISION_FP32])
 def test_in_graph_kernel_attribution(precision):
-    """aero_profile_graph times every kernel between event nodes inside the iteration graph:
-    per RK3 second-order iteration 3 gradient, 3 face and 3 update launches and one controller;
-    the main-stream kernels fit inside the iteration's span, which is close to the plain
-    graph's time; and the iterations it runs are real ones (the state moves on exactly as
-    in a run of the same length)."""
+    """aero_profile_graph records every kernel of the timed iteration graphs through CUPTI:
+    per RK3 second-order iteration 3 gradient, 3 face and 3 update launches and one
+    controller; the main-stream kernels, which run one after another, fit inside the
+    iterations' device time; and the iterations it runs are real ones (the state moves on
+    exactly as in a run of the same length)."""
     mesh = aero_gb300.ogrid_synthetic(128, 32, cell_type=3, permute=True, jitter=0.1, seed=5)
     case = capi.make_case(mach=0.7, flux=1, limiter=1, startup_first_order_iters=2, precision=precision)
     with aero_gb300.Solver(mesh, case) as s:

@@ -81,7 +81,18 @@ __global__ void __launch_bounds__(256) k_face_flux(DevFaces<T> f, Cases<T> cs,
                                                    const typename Vec<T>::v4* __restrict__ gy,
                                                    typename Vec<T>::v4* __restrict__ F, T* __restrict__ FS,
                                                    int* __restrict__ fb_all, const LmSched* __restrict__ lms,
-                                                   int parity) {
+                                                   int parity, int pf) {
+  if (pf > 0 && threadIdx.x < 5 && blockIdx.x + pf < gridDim.x) {
+    // the face table of the block pf blocks ahead (every block's range is inside the
+    // block-padded table): one array per thread
+    const size_t f0 = static_cast<size_t>(blockIdx.x + pf) * blockDim.x;
+    const unsigned nb = blockDim.x;
+    if (threadIdx.x == 0) l2_prefetch(f.cells + f0, nb * sizeof(int2));
+    if (threadIdx.x == 1) l2_prefetch(f.nrm + f0, nb * sizeof(f.nrm[0]));
+    if (threadIdx.x == 2) l2_prefetch(f.area + f0, nb * sizeof(T));
+    if (SECOND && threadIdx.x == 3) l2_prefetch(f.doff + f0, nb * sizeof(f.doff[0]));
+    if (SECOND && threadIdx.x == 4) l2_prefetch(f.noff + f0, nb * sizeof(f.noff[0]));
+  }
   const int2 bd = cs.blk[blockIdx.x];  // face blocks: (case, end of the case's faces)
   const Ctrl* ctrl = cs.ctrl + bd.x;
   int* fb = fb_all + 4 * bd.x;
@@ -222,8 +233,9 @@ struct ResidualLaunch {
 template <class T, int FLUX, bool SECOND, bool LM>
 void launch_face_flux_t(const ResidualLaunch<T>& a) {
   const int grid = (a.faces.nf + a.block - 1) / a.block;
-  k_face_flux<T, FLUX, SECOND, LM>
-      <<<grid, a.block, 0, a.st>>>(a.faces, a.face_cases, a.W, a.gx, a.gy, a.F, a.FS, a.fb, a.lms, a.parity);
+  auto kern = k_face_flux<T, FLUX, SECOND, LM>;
+  const int pf = resident_blocks(kern, a.block);
+  kern<<<grid, a.block, 0, a.st>>>(a.faces, a.face_cases, a.W, a.gx, a.gy, a.F, a.FS, a.fb, a.lms, a.parity, pf);
 }
 
 // Face pass, dispatched on the flux, order and low-Mach switches.

@@ -23,6 +23,8 @@
 #include "aero_numerics.cuh"
 
 #include <cstdint>
+#include <mutex>
+#include <vector>
 
 namespace aero {
 
@@ -49,6 +51,49 @@ struct Vec<double> {
 template <class T>
 __device__ __forceinline__ typename Vec<T>::v4 ld4(const typename Vec<T>::v4* p) {
   return *p;
+}
+
+// Hint to bring [p, p + bytes) into L2: one bulk prefetch with no completion to wait for
+// (p 16-byte aligned, bytes a multiple of 16). The streaming kernels issue it for the block
+// that will run `pf` blocks later, the blocks resident on the whole GPU at once, so that the
+// block's coalesced loads, issued before its gathers can start, hit L2 instead of DRAM.
+__device__ __forceinline__ void l2_prefetch(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "r"(bytes)
+               : "memory");
+}
+
+// Blocks of `kernel` at `block` threads resident on the whole device at once (occupancy x
+// SM count): the prefetch distance of the streaming kernels. Host side; the answer is kept
+// per kernel, block size and device, so a launch queries the runtime once.
+template <class K>
+inline int resident_blocks(K kernel, int block) {
+  struct Entry {
+    const void* k;
+    int block, dev, blocks;
+  };
+  static std::mutex mu;
+  static std::vector<Entry> seen;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  const void* key = reinterpret_cast<const void*>(kernel);
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    for (const Entry& e : seen) {
+      if (e.k == key && e.block == block && e.dev == dev) return e.blocks;
+    }
+  }
+  int per_sm = 0, sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  seen.push_back(Entry{key, block, dev, per_sm * sms});
+  return per_sm * sms;
 }
 
 // Controller and per-iteration state (device memory, one per context).
@@ -97,6 +142,7 @@ struct CtrlConfig {
 // Precondition constants in double for the residual preconditioner (preconditioning.cpp:51-76).
 struct PrecondD {
   int enabled;
+  int fp64;  // FP32 contexts: the preconditioned energy row in double (FP64 contexts: always)
   double gamma, mach_ref, mach_min, beta_min, beta_max;
   float gamma_f, gm1_f;  // float(gamma), float(gamma - 1)
   float mach_ref_f, mach_min_f, beta_min_f, beta_max_f;  // float copies (FP32 update)
@@ -916,7 +962,23 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
                                                 const typename Vec<T>::v4* __restrict__ F, const T* __restrict__ FS,
                                                 typename Vec<T>::v4* __restrict__ W, StateRef U,
                                                 typename Vec<T>::v4* __restrict__ Us, MonitorSet ms, Partials part,
-                                                int global_dt) {
+                                                int global_dt, int pf) {
+  if (pf > 0 && blockIdx.x + pf < gridDim.x) {
+    // the cell streams of the block pf blocks ahead (inside the block-padded arrays): the
+    // state, the stage increment, the primitive state and the gather slots, one per thread
+    const size_t c0 = static_cast<size_t>(blockIdx.x + pf) * blockDim.x;
+    const unsigned nb = blockDim.x;
+    const int t = threadIdx.x;
+    if constexpr (sizeof(T) == 4) {
+      if (t == 0) l2_prefetch(U.hi + c0, nb * sizeof(float4));
+      if (LAST && t == 1) l2_prefetch(U.lo + c0, nb * sizeof(float4));
+    } else {
+      if (t == 0) l2_prefetch(U.un + c0, nb * sizeof(d4));
+    }
+    if (stage > 0 && t == 2) l2_prefetch(Us + c0, nb * sizeof(Us[0]));
+    if (PRECOND && t == 3) l2_prefetch(W + c0, nb * sizeof(W[0]));
+    if (GATHER && t >= 4 && t < 4 + g.d) l2_prefetch(g.slot + static_cast<size_t>(t - 4) * g.n + c0, nb * sizeof(int));
+  }
   const int2 bd = cs.blk[blockIdx.x];
   Ctrl* ctrl = cs.ctrl + bd.x;
   const PrecondD& pc = cs.pc[bd.x];
@@ -970,10 +1032,10 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
       r3 = r4.w;
       if (!global_dt) src = SR[c];
     }
-    if (PRECOND && sizeof(T) == 4) {
-      // energy row of the preconditioned residual in float: the scaling changes the
-      // pseudo-time path only, not the steady state, and the float-bulk path's reference
-      // arithmetic is float (GB300 runs double at a small fraction of the float rate)
+    if (PRECOND && sizeof(T) == 4 && !pc.fp64) {
+      // energy row of the preconditioned residual in float (FP32 contexts above Mach 0.1 by
+      // default): the scaling changes the pseudo-time path only, not the steady state, and
+      // the reference's own arithmetic is float
       const auto w4 = st_w;
       const Prim<float> w{float(w4.x), float(w4.y), float(w4.z), float(w4.w)};
       FaceParams<float> fpf;
@@ -987,7 +1049,10 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
       const float inv_rho = sdiv(1.0f, smax(w.r, 1.0e-8f));
       const float ud = fmaf(w.u, float(r1), w.v * float(r2));
       r3 = T(fmaf(b2, float(r3), (b2 - 1.0f) * inv_rho * ud));
-    } else if (PRECOND) {  // energy row of the preconditioned residual, in double
+    } else if (PRECOND) {
+      // energy row of the preconditioned residual in double: FP64 contexts, and FP32 contexts
+      // below Mach 0.1 by default, where beta^2 ~ M^2 scales the energy residual against the
+      // momentum term (GB300 runs double at a small fraction of the float rate)
       const auto w4 = st_w;
       const Prim<double> w{double(w4.x), double(w4.y), double(w4.z), double(w4.w)};
       FaceParams<double> fpd;

@@ -180,6 +180,7 @@ void aero_case_defaults(aero_case_desc* c) {
   c->diagnostics = 0;
   c->density_l2_target = 0.0;
   c->cells_per_thread = 0;
+  c->precond_fp64 = 0;
 }
 
 }  // extern "C"
@@ -195,6 +196,8 @@ int check_case(const aero_case_desc* cfg) {
     return fail(nullptr, AERO_ERR_INVALID, "unknown limiter");
   if (cfg->precision != AERO_PRECISION_FP64 && cfg->precision != AERO_PRECISION_FP32)
     return fail(nullptr, AERO_ERR_INVALID, "unknown precision");
+  if (cfg->precond_fp64 < -1 || cfg->precond_fp64 > 1)
+    return fail(nullptr, AERO_ERR_INVALID, "precond_fp64 must be -1, 0 or 1");
   double rho_inf = cfg->rho_inf;
   if (rho_inf <= 0.0) rho_inf = cfg->p_inf / (cfg->gas_constant * cfg->t_inf);
   if (!(rho_inf > 0.0))

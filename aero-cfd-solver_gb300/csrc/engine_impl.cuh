@@ -1275,6 +1275,7 @@ class EngineT final : public Engine {
 
     PrecondD& pc = pcs_[k];
     pc.enabled = cfg.precond_on;
+    pc.fp64 = cfg.precond_fp64 > 0 || (cfg.precond_fp64 == 0 && cfg.mach < 0.1);
     pc.gamma = rs.gamma;
     pc.mach_ref = double(fp.pc_mach_ref);
     pc.mach_min = double(fp.pc_mach_min);
@@ -1792,8 +1793,9 @@ class EngineT final : public Engine {
 
   template <bool PRECOND, bool LAST, bool GATHER>
   void update_t(int stage, int global_dt, V4* R, T* SR) {
-    k_update<T, PRECOND, LAST, GATHER><<<ncb_, block_, 0, st_>>>(stage, cell_cases_, R, SR, dg_, F_, FS_, W_, sref_,
-                                                                 Us_, ms_, part_, global_dt);
+    auto kern = k_update<T, PRECOND, LAST, GATHER>;
+    const int pf = resident_blocks(kern, block_);
+    kern<<<ncb_, block_, 0, st_>>>(stage, cell_cases_, R, SR, dg_, F_, FS_, W_, sref_, Us_, ms_, part_, global_dt, pf);
   }
   template <bool PRECOND>
   void update_p(int stage, bool last, int global_dt, V4* R, T* SR) {

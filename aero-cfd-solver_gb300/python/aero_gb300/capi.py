@@ -15,7 +15,7 @@ import numpy as np
 PKG_ROOT = Path(__file__).resolve().parents[2]  # .../aero-cfd-solver_gb300
 REPO_ROOT = PKG_ROOT.parent
 LIB_PATH = PKG_ROOT / "lib" / "libaero_gb300.so"
-ABI_VERSION = 3  # AERO_ABI_VERSION of include/aero_gb300.h that these structures mirror
+ABI_VERSION = 4  # AERO_ABI_VERSION of include/aero_gb300.h that these structures mirror
 
 AERO_OK = 0
 AERO_ERR_INVALID = 1
@@ -100,6 +100,7 @@ _CASE_FIELDS = [
     ("diagnostics", C.c_int),
     ("density_l2_target", C.c_double),
     ("cells_per_thread", C.c_int),
+    ("precond_fp64", C.c_int),
 ]
 
 
@@ -162,7 +163,7 @@ CASE_DEFAULTS = dict(
     all_speed_cfl_min_scale=_F(0.1),
     aoa0_symmetry_enforce=0, aoa0_symmetry_enforce_interval=0,
     precision=PRECISION_FP64, ordering=ORDER_MORTON, block_size=0, diagnostics=0,
-    density_l2_target=0.0, cells_per_thread=0,
+    density_l2_target=0.0, cells_per_thread=0, precond_fp64=0,
 )
 
 

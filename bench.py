@@ -367,13 +367,19 @@ def c3_low_mach(args, aero_gb300, capi, peak):
     field, HLLC + minmod, alpha=3. At M=0.05: throughput of FP32 and FP64 (L2 flushed before
     each timed iteration) and the face pass's roofline at this size (its working set no longer
     fits in L2). At M=0.05 and M=0.01: |dCL|, |dCD|, max |dCp| at the wall between FP32 and
-    FP64 after 400 iterations from free stream."""
+    FP64 after 400 iterations from free stream. FP32 forms the preconditioned energy row in
+    double below Mach 0.1 (the default); the same figures with it in float are reported beside
+    them."""
     mesh = aero_gb300.ogrid_synthetic(1024, 256, cell_type=3, permute=True, jitter=0.1, seed=3)
     wall = mesh.wall_faces
     mach = 0.05
     res = {}
-    for prec, code in (("fp32", capi.PRECISION_FP32), ("fp64", capi.PRECISION_FP64)):
-        with aero_gb300.Solver(mesh, c3_case(capi, code)) as s:
+    legs = (("fp32", capi.PRECISION_FP32, 0), ("fp32_float_precond", capi.PRECISION_FP32, -1),
+            ("fp64", capi.PRECISION_FP64, 0))
+    for prec, code, pfp in legs:
+        case = c3_case(capi, code)
+        case.precond_fp64 = pfp
+        with aero_gb300.Solver(mesh, case) as s:
             info = s.info()
             _, rec = s.run(400)
             p = s.get_primitive()[3]  # the wall pressures after the same 400 iterations as CL, CD
@@ -382,14 +388,16 @@ def c3_low_mach(args, aero_gb300, capi, peak):
             prof, graph_ms = s.profile_graph(max(3, min(args.steps, 10)), flush_l2=not args.no_flush)
         f_ms, f_n = prof["face_pass"]
         avg = f_ms / max(f_n, 1)
-        nbytes = algorithmic_bytes("face", mesh.num_cells, info["slots_per_cell"], prec, int(info["faces"]))
+        nbytes = algorithmic_bytes("face", mesh.num_cells, info["slots_per_cell"], prec[:4], int(info["faces"]))
         res[prec] = dict(mcell=mesh.num_cells * args.steps / (ms / 1e3) / 1e6, cl=float(rec["cl"][-1]),
                          cd=float(rec["cd"][-1]), pw=p[mesh.owner[wall]], face_ms=avg, face_gbs=nbytes / (avg / 1e3) / 1e9,
                          kernels=kernel_times(prof))
     q = 0.5 * 1.4 * 101325.0 * mach * mach
     m01 = {}
-    for prec, code in (("fp32", capi.PRECISION_FP32), ("fp64", capi.PRECISION_FP64)):
-        with aero_gb300.Solver(mesh, c3_case(capi, code, 0.01)) as s:
+    for prec, code, pfp in legs:
+        case = c3_case(capi, code, 0.01)
+        case.precond_fp64 = pfp
+        with aero_gb300.Solver(mesh, case) as s:
             _, rec = s.run(400)
             m01[prec] = (float(rec["cl"][-1]), float(rec["cd"][-1]), s.get_primitive()[3][mesh.owner[wall]],
                          float(rec["residual_ratio"][-1]))
@@ -397,6 +405,8 @@ def c3_low_mach(args, aero_gb300, capi, peak):
     mach01 = {"abs_dcl_400": abs(m01["fp32"][0] - m01["fp64"][0]), "abs_dcd_400": abs(m01["fp32"][1] - m01["fp64"][1]),
               "max_abs_dcp_wall_400": float(np.max(np.abs(m01["fp32"][2] - m01["fp64"][2])) / q01),
               "residual_ratio_fp64_400": m01["fp64"][3],
+              "float_precond": {"abs_dcl_400": abs(m01["fp32_float_precond"][0] - m01["fp64"][0]),
+                                "abs_dcd_400": abs(m01["fp32_float_precond"][1] - m01["fp64"][1])},
               "note": "a comparison of two unconverged transients, not a gate result: neither precision "
                       "converges on this case, and float pressure resolves p ~ 1/(gamma M^2) only to ~4e-4 "
                       "of the free-stream dynamic pressure's scale"}
@@ -406,6 +416,13 @@ def c3_low_mach(args, aero_gb300, capi, peak):
             "abs_dcl_400": abs(res["fp32"]["cl"] - res["fp64"]["cl"]),
             "abs_dcd_400": abs(res["fp32"]["cd"] - res["fp64"]["cd"]),
             "max_abs_dcp_wall_400": float(np.max(np.abs(res["fp32"]["pw"] - res["fp64"]["pw"])) / q),
+            "fp32_float_precond": {
+                "mcell_iter_s": res["fp32_float_precond"]["mcell"],
+                "abs_dcl_400": abs(res["fp32_float_precond"]["cl"] - res["fp64"]["cl"]),
+                "abs_dcd_400": abs(res["fp32_float_precond"]["cd"] - res["fp64"]["cd"]),
+                "max_abs_dcp_wall_400": float(np.max(np.abs(res["fp32_float_precond"]["pw"] - res["fp64"]["pw"])) / q),
+                "face_pass_frac": res["fp32_float_precond"]["face_gbs"] / peak,
+                "in_graph_kernel_us_per_launch": res["fp32_float_precond"]["kernels"]},
             "roofline_face_pass_fp32": {"achieved": res["fp32"]["face_gbs"], "peak": peak, "unit": "GB/s",
                                         "frac": res["fp32"]["face_gbs"] / peak, "avg_launch_ms": res["fp32"]["face_ms"]},
             "roofline_face_pass_fp64": {"achieved": res["fp64"]["face_gbs"], "frac": res["fp64"]["face_gbs"] / peak,

@@ -29,7 +29,7 @@ extern "C" {
 #endif
 
 /* 3: aero_case_desc gained cells_per_thread; aero_autotune writes 12 timings */
-#define AERO_ABI_VERSION 3
+#define AERO_ABI_VERSION 4
 
 #if defined(__GNUC__)
 #define AERO_API __attribute__((visibility("default")))
@@ -125,6 +125,11 @@ typedef struct aero_case_desc {
    * same bit for bit. The bulk-copy gradient keeps one cell per thread. No reference
    * counterpart (picked by aero_autotune). */
   int cells_per_thread;
+  /* FP32-bulk contexts with the residual preconditioner on: arithmetic of the preconditioned
+   * energy row (preconditioning.cpp:51-76, the cell beta of :9-32). 0 = double when the
+   * free-stream Mach number is below 0.1, float above; 1 = double; -1 = float. FP64 contexts
+   * always form it in double. No reference counterpart (the reference computes it in float). */
+  int precond_fp64;
 } aero_case_desc;
 
 /* One record per pseudo-time iteration: the rows of residuals.csv and forces.csv

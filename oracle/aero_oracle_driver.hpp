@@ -283,7 +283,14 @@ class Solver {
         itd.diffusive_fallback += dg.diffusive_fallback;
         std::vector<A> rp(res.begin(), res.end());
         if constexpr (kMixed) {
-          precondition_residual_fma(w, nm, &rp);
+          // the FP32 mode's energy row: in double below Mach 0.1 by default (the case's
+          // precond_fp64 setting), else in float with fused multiply-adds
+          const bool pc64 = cfg_.precond_fp64 > 0 || (cfg_.precond_fp64 == 0 && cfg_.mach < 0.1);
+          if (pc64) {
+            precondition_residual<R, A>(w, nm, &rp);
+          } else {
+            precondition_residual_fma(w, nm, &rp);
+          }
         } else {
           precondition_residual<R, A>(w, nm, &rp);
         }

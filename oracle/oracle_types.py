@@ -154,7 +154,7 @@ REFERENCE_DEFAULTS = dict(
     all_speed_pjump_hold_iters=120, all_speed_freeze_iters=120, all_speed_cfl_drop_factor=_f32(0.8),
     all_speed_cfl_restore_factor=_f32(1.02), all_speed_cfl_min_scale=_f32(0.1), aoa0_symmetry_enforce=0,
     aoa0_symmetry_enforce_interval=0, precision=0, ordering=0, block_size=0, diagnostics=0, density_l2_target=0.0,
-    cells_per_thread=0,
+    cells_per_thread=0, precond_fp64=0,
 )
 
 

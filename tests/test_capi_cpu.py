@@ -40,7 +40,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_identity(lib):
-    assert lib.aero_abi_version() == capi.ABI_VERSION == 3
+    assert lib.aero_abi_version() == capi.ABI_VERSION == 4
     assert lib.aero_version().decode().endswith("gb300")
 
 
@@ -68,6 +68,9 @@ def test_invalid_arguments_are_rejected(lib):
     assert exc.value.code == capi.AERO_ERR_INVALID
     with pytest.raises(aero_gb300.AeroError) as exc:
         aero_gb300.Solver(mesh, capi.make_case(rho_inf=-1.0, p_inf=-1.0))
+    assert exc.value.code == capi.AERO_ERR_INVALID
+    with pytest.raises(aero_gb300.AeroError) as exc:
+        aero_gb300.Solver(mesh, capi.make_case(precond_fp64=2))
     assert exc.value.code == capi.AERO_ERR_INVALID
 
 

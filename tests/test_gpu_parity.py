@@ -246,6 +246,35 @@ def test_run_fp32_vs_mixed_oracle_and_reference(name, golden_meshes, golden_hist
         assert abs(rec["cd"][-1] - ref[-1, 5]) < 1e-3
 
 
+def test_fp32_preconditioner_precision():
+    """FP32 contexts form the preconditioned energy row (preconditioning.cpp:51-76) in double
+    below Mach 0.1 by default (precond_fp64 = 0) and in float above; 1 and -1 force either.
+    The default follows the free-stream Mach number, the switch takes effect, and both forms
+    follow the mixed-precision oracle, which applies the same rule."""
+    mesh = aero_gb300.ogrid_synthetic(96, 24, cell_type=3, permute=True, jitter=0.1, seed=11)
+    n = 40
+
+    def run(mach, pfp):
+        case = capi.make_case(mach=mach, aoa_deg=3.0, flux=capi.FLUX_HLLC, limiter=capi.LIMITER_MINMOD, precond_on=1,
+                              low_mach_fix=1, all_speed_flux_fix=1, precond_farfield_bc=1, iterations=n,
+                              min_iterations=n, startup_first_order_iters=5, precision=capi.PRECISION_FP32,
+                              precond_fp64=pfp)
+        with aero_gb300.Solver(mesh, case) as s:
+            _, rec = s.run(n)
+            return case, rec, s.get_state()
+
+    case, rec, u_auto = run(0.05, 0)
+    _, _, u_double = run(0.05, 1)
+    case_f, rec_f, u_float = run(0.05, -1)
+    np.testing.assert_array_equal(u_auto, u_double)
+    assert not np.array_equal(u_auto, u_float)
+    np.testing.assert_array_equal(run(0.3, 0)[2], run(0.3, -1)[2])
+    for c, r in ((case, rec), (case_f, rec_f)):
+        _, orec = op.OracleSolver(op.MODE_MIXED, mesh, c).run(n)
+        assert np.max(np.abs(r["cl"] - orec["cl"])) < 1e-4
+        assert np.max(np.abs(r["residual_l2"] - orec["residual_l2"]) / orec["residual_l2"]) < 1e-2
+
+
 def test_reference_test_assertions_hold_on_device(golden_meshes, golden_histories):
     """The reference's C++ test thresholds, run on the device in both precisions
     (test_euler_regression.cpp:40-61, test_euler_aoa0_regression.cpp:78-83,

@@ -142,7 +142,7 @@ struct CtrlConfig {
 // Precondition constants in double for the residual preconditioner (preconditioning.cpp:51-76).
 struct PrecondD {
   int enabled;
-  int fp64;  // FP32 contexts: the preconditioned energy row in double (FP64 contexts: always)
+  int fp64;  // FP32 contexts: energy row 0 float, 1 IEEE double (beta too), 2 double-float
   double gamma, mach_ref, mach_min, beta_min, beta_max;
   float gamma_f, gm1_f;  // float(gamma), float(gamma - 1)
   float mach_ref_f, mach_min_f, beta_min_f, beta_max_f;  // float copies (FP32 update)
@@ -220,7 +220,7 @@ __host__ __device__ inline void apply_schedule(const CtrlConfig& cc, Ctrl* sp) {
 // controller (they then depend on the iteration index alone): the values apply_schedule
 // gives, kept per iteration parity so that an iteration's face passes can read them while
 // the previous iteration's controller is still running.
-struct LmSched {
+struct alignas(16) LmSched {
   int as_fix, pad;
   double stab_floor, as_fmin, as_ramp;
   float stab_f, as_fmin_f, as_ramp_f, pad_f;
@@ -1032,10 +1032,13 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
       r3 = r4.w;
       if (!global_dt) src = SR[c];
     }
-    if (PRECOND && sizeof(T) == 4 && !pc.fp64) {
-      // energy row of the preconditioned residual in float (FP32 contexts above Mach 0.1 by
-      // default): the scaling changes the pseudo-time path only, not the steady state, and
-      // the reference's own arithmetic is float
+    if (PRECOND && sizeof(T) == 4 && pc.fp64 != 1) {
+      // FP32 contexts: beta from the float state (preconditioning.cpp:9-32 in float); the
+      // energy row (:51-76) in float, or with fp64 == 2 (by default below Mach 0.1) as the
+      // double-float sum N = b2 (r3 rho) + (b2 - 1)(u r1 + v r2): every product split
+      // error-free with a fused multiply-add, every sum with two-sum (Knuth), so N carries
+      // about 44 significant bits on the float pipe, where the float row loses digits to the
+      // cancellation between its two terms at low Mach. r3 = N / rho in float.
       const auto w4 = st_w;
       const Prim<float> w{float(w4.x), float(w4.y), float(w4.z), float(w4.w)};
       FaceParams<float> fpf;
@@ -1045,14 +1048,37 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
       fpf.pc_beta_min = pc.beta_min_f;
       fpf.pc_beta_max = pc.beta_max_f;
       const float beta = cell_beta(w, fpf);
-      const float b2 = beta * beta;
-      const float inv_rho = sdiv(1.0f, smax(w.r, 1.0e-8f));
-      const float ud = fmaf(w.u, float(r1), w.v * float(r2));
-      r3 = T(fmaf(b2, float(r3), (b2 - 1.0f) * inv_rho * ud));
+      if (pc.fp64 == 0) {
+        const float b2 = beta * beta;
+        const float inv_rho = sdiv(1.0f, smax(w.r, 1.0e-8f));
+        const float ud = fmaf(w.u, float(r1), w.v * float(r2));
+        r3 = T(fmaf(b2, float(r3), (b2 - 1.0f) * inv_rho * ud));
+      } else {
+        const float rho = smax(w.r, 1.0e-8f);
+        float bh, bl, dh, dl, ph, pl, qh, ql, uh, ul, th, tl, mh, ml, gh, gl, nh, nl, e;
+        bh = __fmul_rn(beta, beta);  // b2 = bh + bl exactly
+        bl = __fmaf_rn(beta, beta, -bh);
+        two_sum(bh, -1.0f, &dh, &e);  // b2 - 1
+        dl = __fadd_rn(e, bl);
+        ph = __fmul_rn(w.u, float(r1));  // u r1 + v r2
+        pl = __fmaf_rn(w.u, float(r1), -ph);
+        qh = __fmul_rn(w.v, float(r2));
+        ql = __fmaf_rn(w.v, float(r2), -qh);
+        two_sum(ph, qh, &uh, &e);
+        ul = __fadd_rn(e, __fadd_rn(pl, ql));
+        th = __fmul_rn(dh, uh);  // (b2 - 1)(u r1 + v r2)
+        tl = __fadd_rn(__fmaf_rn(dh, uh, -th), __fmaf_rn(dh, ul, __fmul_rn(dl, uh)));
+        mh = __fmul_rn(float(r3), rho);  // r3 rho
+        ml = __fmaf_rn(float(r3), rho, -mh);
+        gh = __fmul_rn(bh, mh);  // b2 (r3 rho)
+        gl = __fadd_rn(__fmaf_rn(bh, mh, -gh), __fmaf_rn(bh, ml, __fmul_rn(bl, mh)));
+        two_sum(gh, th, &nh, &e);
+        nl = __fadd_rn(e, __fadd_rn(gl, tl));
+        r3 = T(sdiv(__fadd_rn(nh, nl), rho));
+      }
     } else if (PRECOND) {
-      // energy row of the preconditioned residual in double: FP64 contexts, and FP32 contexts
-      // below Mach 0.1 by default, where beta^2 ~ M^2 scales the energy residual against the
-      // momentum term (GB300 runs double at a small fraction of the float rate)
+      // the preconditioned energy row in double, beta included: FP64 contexts, and FP32
+      // contexts with fp64 == 1 (GB300 runs double at a small fraction of the float rate)
       const auto w4 = st_w;
       const Prim<double> w{double(w4.x), double(w4.y), double(w4.z), double(w4.w)};
       FaceParams<double> fpd;

@@ -242,10 +242,11 @@ __device__ __forceinline__ Speeds<T> face_speeds(T un, T a, T as) {
 
 // Settings of one residual evaluation that do not change within a launch
 // (residual_assembly.hpp:12-31, preconditioning.hpp:9-15).
+// 16-byte aligned, so that a kernel loads the fields it uses in vector loads.
 template <class T>
-struct FaceParams {
-  T gamma;
+struct alignas(16) FaceParams {
   Cons<T> farfield;
+  T gamma;
   int limiter;  // 0 minmod, 1 venkat
   int precond;
   int low_mach_fix;

@@ -196,8 +196,8 @@ int check_case(const aero_case_desc* cfg) {
     return fail(nullptr, AERO_ERR_INVALID, "unknown limiter");
   if (cfg->precision != AERO_PRECISION_FP64 && cfg->precision != AERO_PRECISION_FP32)
     return fail(nullptr, AERO_ERR_INVALID, "unknown precision");
-  if (cfg->precond_fp64 < -1 || cfg->precond_fp64 > 1)
-    return fail(nullptr, AERO_ERR_INVALID, "precond_fp64 must be -1, 0 or 1");
+  if (cfg->precond_fp64 < -1 || cfg->precond_fp64 > 2)
+    return fail(nullptr, AERO_ERR_INVALID, "precond_fp64 must be -1, 0, 1 or 2");
   double rho_inf = cfg->rho_inf;
   if (rho_inf <= 0.0) rho_inf = cfg->p_inf / (cfg->gas_constant * cfg->t_inf);
   if (!(rho_inf > 0.0))

@@ -183,7 +183,10 @@ void map_case(const KV& kv, aero_case_desc* c, aero_airfoil_mesh_cfg* m) {
   const std::string ord = lower(trim(get_s(kv, "ordering", "morton")));
   c->ordering = ord == "none" ? AERO_ORDER_NONE : (ord == "rcm" ? AERO_ORDER_RCM : AERO_ORDER_MORTON);
   const std::string pp = lower(trim(get_s(kv, "precond_precision", "auto")));
-  c->precond_fp64 = (pp == "fp64" || pp == "double") ? 1 : ((pp == "fp32" || pp == "float") ? -1 : 0);
+  c->precond_fp64 = (pp == "fp64" || pp == "double")      ? 1
+                    : (pp == "fp32" || pp == "float")       ? -1
+                    : (pp == "ff" || pp == "double-float") ? 2
+                                                            : 0;
 
   std::memset(m, 0, sizeof(*m));
   const std::string src = get_s(kv, "airfoil_source", "naca4");

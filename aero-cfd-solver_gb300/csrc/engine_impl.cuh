@@ -1275,7 +1275,10 @@ class EngineT final : public Engine {
 
     PrecondD& pc = pcs_[k];
     pc.enabled = cfg.precond_on;
-    pc.fp64 = cfg.precond_fp64 > 0 || (cfg.precond_fp64 == 0 && cfg.mach < 0.1);
+    // energy row of FP32 contexts: -1 float, 1 IEEE double, 2 double-float, 0 double-float
+    // below Mach 0.1 and float above
+    pc.fp64 = cfg.precond_fp64 == 1 ? 1
+              : (cfg.precond_fp64 == 2 || (cfg.precond_fp64 == 0 && cfg.mach < 0.1)) ? 2 : 0;
     pc.gamma = rs.gamma;
     pc.mach_ref = double(fp.pc_mach_ref);
     pc.mach_min = double(fp.pc_mach_min);

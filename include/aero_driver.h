@@ -8,7 +8,7 @@
  * outputs: residuals.csv, forces.csv, euler_diagnostics.csv, cp_wall.csv, wall_flux.csv,
  * dissipation_debug.csv, boundary_faces_debug.txt, effective_config_snapshot.txt,
  * field_0000.vtu and run.log. Added keys: precision=fp32|fp64 (default fp32), ordering,
- * precond_precision=auto|fp64|fp32 (aero_case_desc.precond_fp64 0|1|-1, default auto).
+ * precond_precision=auto|fp64|fp32|ff (aero_case_desc.precond_fp64 0|1|-1|2, default auto).
  */
 #ifndef AERO_DRIVER_H
 #define AERO_DRIVER_H

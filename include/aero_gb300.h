@@ -126,9 +126,14 @@ typedef struct aero_case_desc {
    * counterpart (picked by aero_autotune). */
   int cells_per_thread;
   /* FP32-bulk contexts with the residual preconditioner on: arithmetic of the preconditioned
-   * energy row (preconditioning.cpp:51-76, the cell beta of :9-32). 0 = double when the
-   * free-stream Mach number is below 0.1, float above; 1 = double; -1 = float. FP64 contexts
-   * always form it in double. No reference counterpart (the reference computes it in float). */
+   * energy row (preconditioning.cpp:51-76, the cell beta of :9-32).
+   *  -1: float;
+   *   1: IEEE double, beta included (the FP64 contexts' arithmetic);
+   *   2: beta in float, the row in double-float arithmetic (error-free products and sums on
+   *      the float pipe, about 44 significant bits);
+   *   0: 2 when the free-stream Mach number is below 0.1, else -1 (default).
+   * FP64 contexts always form it in double. No reference counterpart (the reference computes
+   * it in float). */
   int precond_fp64;
 } aero_case_desc;
 

@@ -664,6 +664,26 @@ void precondition_residual_fma(const std::vector<Prim<float>>& w, const Numerics
   }
 }
 
+// The FP32-bulk mode's low-Mach energy row (preconditioning.cpp:51-76): beta from the float
+// state, N = b2 (r4 rho) + (b2 - 1)(u r1 + v r2) formed in double with one fused
+// multiply-add (the device forms the same sum in double-float arithmetic), then
+// r4 = float(N) / rho in float.
+template <class A>
+void precondition_residual_row64(const std::vector<Prim<float>>& w, const Numerics<float>& nm,
+                                 std::vector<A>* res) {
+  if (!nm.precond) return;
+  for (size_t c = 0; c < w.size(); ++c) {
+    const float beta = cell_beta(w[c], nm);
+    const float rho = std::max(w[c].rho, K<float>::rho_floor);
+    A* r = res->data() + 5 * c;
+    const double b2 = double(beta) * double(beta);
+    const double rr = double(float(r[4])) * double(rho);
+    const double ud = double(w[c].u) * double(float(r[1])) + double(w[c].v) * double(float(r[2]));
+    const double n = std::fma(b2, rr, (b2 - 1.0) * ud);
+    r[4] = A(float(n) / rho);
+  }
+}
+
 // time_integrator.cpp:31-59
 template <class R>
 std::vector<R> dt_over_volume(const std::vector<R>& sr, R cfl, bool local) {

@@ -283,11 +283,13 @@ class Solver {
         itd.diffusive_fallback += dg.diffusive_fallback;
         std::vector<A> rp(res.begin(), res.end());
         if constexpr (kMixed) {
-          // the FP32 mode's energy row: in double below Mach 0.1 by default (the case's
-          // precond_fp64 setting), else in float with fused multiply-adds
-          const bool pc64 = cfg_.precond_fp64 > 0 || (cfg_.precond_fp64 == 0 && cfg_.mach < 0.1);
-          if (pc64) {
+          // the FP32 mode's energy row (the case's precond_fp64): 1 all in double; 2, and by
+          // default below Mach 0.1, the row in double from a float beta; else float
+          const int pm = cfg_.precond_fp64;
+          if (pm == 1) {
             precondition_residual<R, A>(w, nm, &rp);
+          } else if (pm == 2 || (pm == 0 && cfg_.mach < 0.1)) {
+            precondition_residual_row64(w, nm, &rp);
           } else {
             precondition_residual_fma(w, nm, &rp);
           }

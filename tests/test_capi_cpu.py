@@ -70,7 +70,7 @@ def test_invalid_arguments_are_rejected(lib):
         aero_gb300.Solver(mesh, capi.make_case(rho_inf=-1.0, p_inf=-1.0))
     assert exc.value.code == capi.AERO_ERR_INVALID
     with pytest.raises(aero_gb300.AeroError) as exc:
-        aero_gb300.Solver(mesh, capi.make_case(precond_fp64=2))
+        aero_gb300.Solver(mesh, capi.make_case(precond_fp64=3))
     assert exc.value.code == capi.AERO_ERR_INVALID
 
 

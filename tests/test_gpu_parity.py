@@ -247,10 +247,11 @@ def test_run_fp32_vs_mixed_oracle_and_reference(name, golden_meshes, golden_hist
 
 
 def test_fp32_preconditioner_precision():
-    """FP32 contexts form the preconditioned energy row (preconditioning.cpp:51-76) in double
-    below Mach 0.1 by default (precond_fp64 = 0) and in float above; 1 and -1 force either.
-    The default follows the free-stream Mach number, the switch takes effect, and both forms
-    follow the mixed-precision oracle, which applies the same rule."""
+    """FP32 contexts form the preconditioned energy row (preconditioning.cpp:51-76) by the
+    case's precond_fp64: -1 float; 1 IEEE double, beta included; 2 beta in float and the row in
+    double-float arithmetic; 0 (default) 2 below Mach 0.1 and -1 above. The default follows the
+    free-stream Mach number, the forms differ, and each follows the mixed-precision oracle,
+    which restates the same three forms."""
     mesh = aero_gb300.ogrid_synthetic(96, 24, cell_type=3, permute=True, jitter=0.1, seed=11)
     n = 40
 
@@ -263,16 +264,16 @@ def test_fp32_preconditioner_precision():
             _, rec = s.run(n)
             return case, rec, s.get_state()
 
-    case, rec, u_auto = run(0.05, 0)
-    _, _, u_double = run(0.05, 1)
-    case_f, rec_f, u_float = run(0.05, -1)
-    np.testing.assert_array_equal(u_auto, u_double)
-    assert not np.array_equal(u_auto, u_float)
+    runs = {pfp: run(0.05, pfp) for pfp in (0, -1, 1, 2)}
+    np.testing.assert_array_equal(runs[0][2], runs[2][2])
+    assert not np.array_equal(runs[2][2], runs[-1][2])
+    assert not np.array_equal(runs[2][2], runs[1][2])
     np.testing.assert_array_equal(run(0.3, 0)[2], run(0.3, -1)[2])
-    for c, r in ((case, rec), (case_f, rec_f)):
+    for pfp in (-1, 1, 2):
+        c, r, _ = runs[pfp]
         _, orec = op.OracleSolver(op.MODE_MIXED, mesh, c).run(n)
-        assert np.max(np.abs(r["cl"] - orec["cl"])) < 1e-4
-        assert np.max(np.abs(r["residual_l2"] - orec["residual_l2"]) / orec["residual_l2"]) < 1e-2
+        assert np.max(np.abs(r["cl"] - orec["cl"])) < 1e-4, pfp
+        assert np.max(np.abs(r["residual_l2"] - orec["residual_l2"]) / orec["residual_l2"]) < 1e-2, pfp
 
 
 def test_reference_test_assertions_hold_on_device(golden_meshes, golden_histories):

@@ -343,8 +343,8 @@ def c4_sweep(args, aero_gb300, capi, rank):
     mask at 1e-8 relative; seeded synthetic inputs. Block size, cell ordering and cells per
     thread come from the autotuner (aero_autotune on the largest mesh of the draw with the
     first case's flow). Returns device ms of `steps` iterations (L2 flushed before each), the
-    batch's cell count, its launches per iteration and the tuned (ordering, block size, cells
-    per thread)."""
+    batch's cell count, its launches per iteration, the tuned (ordering, block size, cells
+    per thread), the in-graph kernel profile and the context's info."""
     meshes, cases = c4_cases(aero_gb300, capi, rank, capi.PRECISION_FP32)
     largest = max(range(C4_CASES), key=lambda k: meshes[k].num_cells)
     tuned, _ = aero_gb300.autotune(meshes[largest], cases[0], iters=10)
@@ -357,8 +357,27 @@ def c4_sweep(args, aero_gb300, capi, rank):
         b.run(STARTUP)
         b.time_iterations(args.warmup, use_graph=True, flush_l2=True)
         ms = b.time_iterations(args.steps, use_graph=True, flush_l2=not args.no_flush)
-        launches = b.info()["launches_per_iteration"]
-    return ms, int(cells), int(launches), (int(tuned.ordering), int(tuned.block_size), int(tuned.cells_per_thread))
+        info = b.info()
+        prof, _ = b.profile_graph(max(3, min(args.steps, 10)), flush_l2=not args.no_flush)
+    tuned_t = (int(tuned.ordering), int(tuned.block_size), int(tuned.cells_per_thread))
+    return ms, int(cells), int(info["launches_per_iteration"]), tuned_t, prof, info
+
+
+def batch_roofline(ms_per_step: float, prof: dict, info: dict, peak: float) -> dict:
+    """HBM fractions of the batched sweep: its packed working set (4.8 M cells) is far larger
+    than L2. The face pass's algorithmic bytes per launch over its in-graph launch time, and
+    the algorithmic bytes of a whole iteration (3 gradient passes, 3 face passes, 3 updates)
+    over the timed iteration."""
+    n, f, d = int(info["cells"]), int(info["faces"]), int(info["slots_per_cell"])
+    face = algorithmic_bytes("face", n, d, "fp32", f)
+    step = 3 * (algorithmic_bytes("gradient", n, d, "fp32") + face + algorithmic_bytes("update", n, d, "fp32"))
+    f_ms, f_n = prof["face_pass"]
+    face_ms = f_ms / max(f_n, 1)
+    return {"face_pass": {"achieved": face / (face_ms / 1e3) / 1e9, "frac": face / (face_ms / 1e3) / 1e9 / peak,
+                          "algorithmic_bytes_per_launch": face, "avg_launch_ms": face_ms},
+            "iteration": {"achieved": step / (ms_per_step / 1e3) / 1e9, "frac": step / (ms_per_step / 1e3) / 1e9 / peak,
+                          "algorithmic_bytes": step},
+            "peak": peak, "unit": "GB/s"}
 
 
 def c3_low_mach(args, aero_gb300, capi, peak):
@@ -795,12 +814,14 @@ def run_gpu_arm(args):
     c4 = None
     if not args.no_c4 and "fp32" in precisions:
         barrier(dist)
-        c4_ms, c4_cells, c4_launch, c4_tuned = c4_sweep(args, aero_gb300, capi, rank)
+        c4_ms, c4_cells, c4_launch, c4_tuned, c4_prof, c4_info = c4_sweep(args, aero_gb300, capi, rank)
         c4_ms = reduce_max(dist, c4_ms)
         c4 = {"cases_per_gpu": C4_CASES, "cells_per_gpu": c4_cells, "steps": args.steps,
               "ms_per_step": c4_ms / args.steps,
               "fp32_batched_mcell_iter_s": world * c4_cells * args.steps / (c4_ms / 1e3) / 1e6,
               "launches_per_step": c4_launch,
+              "in_graph_kernel_us_per_launch": kernel_times(c4_prof),
+              "roofline": batch_roofline(c4_ms / args.steps, c4_prof, c4_info, peak),
               "autotuned": {"ordering": {1: "morton", 2: "rcm"}.get(c4_tuned[0], c4_tuned[0]),
                             "block_size": c4_tuned[1], "cells_per_thread": c4_tuned[2]},
               "inputs": "96 seeded cases per GPU: sizes from {64x16,128x32,256x64,512x128} triangulated "

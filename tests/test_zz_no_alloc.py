@@ -7,8 +7,8 @@ supplies its working arrays from one fixed device array. This test allocates the
 PyTorch (standing in for such a caller), calls the entry point through the C ABI, and checks
 it against the existing aero_residual entry point on two calls in a row (different states),
 plus a repeat of the first state, with the tolerance of the other parity tests: |dR| <= 1e-12
-(FP64) or 2e-5 (FP32) times the per-cell sum over faces of |F_k A|; the FP64 results are also
-checked against the FP64 oracle at 1e-12. The device's free memory is the same just before
+(FP64) or 2e-5 (FP32) times the per-cell sum over faces of |F_k A|; every result is also
+checked against the FP64 oracle, at 1e-12 (FP64) or 5e-5 (FP32) of the same scale. The device's free memory is the same just before
 and just after every call once the first has loaded the kernels. It also checks that meshes
 above the array's limit are refused. It runs on its own in a fresh process as well as after the other tests.
 """
@@ -90,8 +90,9 @@ def test_noalloc_matches_existing_entry_point(lib, precision, tol, numerics):
             r_or, _, _, _, fscale = oracle.residual(u, *args, with_scale=True)
             assert np.all(np.isfinite(r)) and np.all(np.isfinite(s))
             assert np.max(np.abs(r - r_ref) / (fscale + 1e-300)) <= tol
-            if precision == capi.PRECISION_FP64:
-                assert np.max(np.abs(r - r_or) / (fscale + 1e-300)) <= 1e-12
+            # against the FP64 oracle: 1e-12 in FP64, float-class (the bound of the FP32 parity
+            # tests, which the reference's own float residual meets) in FP32
+            assert np.max(np.abs(r - r_or) / (fscale + 1e-300)) <= (1e-12 if precision == capi.PRECISION_FP64 else 5e-5)
             np.testing.assert_allclose(s, s_ref, rtol=tol)
             results.append(r)
         # the shared array keeps the previous call's contents; results must not depend on it

@@ -93,10 +93,21 @@ __global__ void __launch_bounds__(256) k_face_flux(DevFaces<T> f, Cases<T> cs,
     if (SECOND && threadIdx.x == 3) l2_prefetch(f.doff + f0, nb * sizeof(f.doff[0]));
     if (SECOND && threadIdx.x == 4) l2_prefetch(f.noff + f0, nb * sizeof(f.noff[0]));
   }
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  // The face's table entries before the case lookup, so that their latency overlaps it
+  // (every block lies inside the block-padded table; padding entries go unused). The MUSCL
+  // offsets do not depend on the cell ids: loaded with them, not after.
+  const int2 oc = f.cells[i];
+  const auto nd = f.nrm[i];
+  const T area = f.area[i];
+  typename Vec<T>::v2 dO{}, dN{};
+  if (SECOND) {
+    dO = f.doff[i];
+    dN = f.noff[i];
+  }
   const int2 bd = cs.blk[blockIdx.x];  // face blocks: (case, end of the case's faces)
   const Ctrl* ctrl = cs.ctrl + bd.x;
   int* fb = fb_all + 4 * bd.x;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (ctrl->done) return;
   FaceParams<T> fp = cs.fp[bd.x];
   if (LM && lms) {  // the parity slot of this iteration's low-Mach weights
@@ -125,15 +136,6 @@ __global__ void __launch_bounds__(256) k_face_flux(DevFaces<T> f, Cases<T> cs,
   }
   int fo = 0, df = 0;
   if (i < bd.y) {
-    const int2 oc = f.cells[i];
-    const auto nd = f.nrm[i];
-    const T area = f.area[i];
-    // the MUSCL offsets do not depend on the cell ids: loaded with them, not after
-    typename Vec<T>::v2 dO{}, dN{};
-    if (SECOND) {
-      dO = f.doff[i];
-      dN = f.noff[i];
-    }
     const int o = oc.x, b = oc.y;
     const T nx = nd.x, ny = nd.y;
     const auto wo4 = W[o];
@@ -186,14 +188,17 @@ template <class T, bool NORMS>
 __global__ void __launch_bounds__(256) k_gather(DevGather<T> g, const typename Vec<T>::v4* __restrict__ F,
                                                 const T* __restrict__ FS, typename Vec<T>::v4* __restrict__ R,
                                                 T* __restrict__ SR, Partials part, Cases<T> cs, int global_dt) {
-  const int2 bd = cs.blk[blockIdx.x];  // cell blocks
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  // the cell's first slots before the case lookup (every block lies inside the padded table)
+  int first[kGatherBatch];
+  gather_slots(g, c, 0, first);
+  const int2 bd = cs.blk[blockIdx.x];  // cell blocks
   if (cs.ctrl[bd.x].done) return;
   T nq[kNorm] = {T(0), T(0), T(0), T(0)};
   double srm = 0.0;
   if (c < bd.y) {
     T r[4], sr;
-    gather_cell<T>(g, F, FS, c, r, &sr);
+    gather_cell<T>(g, F, FS, c, first, r, &sr);
     typename Vec<T>::v4 out;
     out.x = r[0]; out.y = r[1]; out.z = r[2]; out.w = r[3];
     R[c] = out;

@@ -447,19 +447,32 @@ __device__ __forceinline__ T warp_max_nonneg(T x) {
   }
 }
 
+// The first kGatherBatch gather slots of cell c (kPad beyond the table's d).
+constexpr int kGatherBatch = 4;
+template <class T>
+__device__ __forceinline__ void gather_slots(const DevGather<T>& g, int c, int k0, int (&sl)[kGatherBatch]) {
+#pragma unroll
+  for (int u = 0; u < kGatherBatch; ++u) sl[u] = (k0 + u < g.d) ? g.slot[(k0 + u) * g.n + c] : kPad;
+}
+
 // Residual of cell c from the per-face fluxes: +-F*A over its faces in ascending original
 // face order, and the sum of the faces' wave-speed terms. The slots are read first so the
-// flux loads of one cell are in flight together.
+// flux loads of one cell are in flight together; `first`, when given, holds the first batch
+// of slots, loaded by the caller (gather_slots(g, c, 0, first)) ahead of its other work.
 template <class T>
 __device__ __forceinline__ void gather_cell(const DevGather<T>& g, const typename Vec<T>::v4* __restrict__ F,
-                                            const T* __restrict__ FS, int c, T (&r)[4], T* sr) {
-  constexpr int kU = 4;
+                                            const T* __restrict__ FS, int c, const int* first, T (&r)[4], T* sr) {
+  constexpr int kU = kGatherBatch;
   r[0] = r[1] = r[2] = r[3] = T(0);
   *sr = T(0);
   for (int k0 = 0; k0 < g.d; k0 += kU) {
     int sl[kU];
+    if (k0 == 0 && first != nullptr) {
 #pragma unroll
-    for (int u = 0; u < kU; ++u) sl[u] = (k0 + u < g.d) ? g.slot[(k0 + u) * g.n + c] : kPad;
+      for (int u = 0; u < kU; ++u) sl[u] = first[u];
+    } else {
+      gather_slots(g, c, k0, sl);
+    }
     typename Vec<T>::v4 fv[kU];
     T fs[kU];
 #pragma unroll
@@ -682,6 +695,32 @@ __device__ __forceinline__ double block_max(double v, double* shm) {
 // Green-Gauss gradient of cell c (reconstruction.cpp:73-119): the face averages of the
 // primitive state times the outward face vectors, over 1/V. sW (may be null) holds W of the
 // cells [base, base + nsw): neighbours in that range are read from shared memory.
+// One batch of a cell's gradient slots: links, normals and lengths of slots k0 .. k0 + 3.
+// The slot geometry does not depend on the links (padding slots hold zeros), so its loads go
+// out with the links' and only the neighbour states wait for them.
+constexpr int kGradBatch = 4;
+template <class T>
+struct GradSlots {
+  int lk[kGradBatch];
+  typename Vec<T>::v2 nd[kGradBatch];
+  T ar[kGradBatch];
+};
+template <class T>
+__device__ __forceinline__ void grad_slots(const DevMesh<T>& m, int c, int k0, GradSlots<T>* sb) {
+#pragma unroll
+  for (int u = 0; u < kGradBatch; ++u) {
+    sb->lk[u] = kPad;
+    sb->nd[u] = typename Vec<T>::v2{};
+    sb->ar[u] = T(0);
+    if (k0 + u < m.d) {
+      const int s = (k0 + u) * m.n + c;
+      sb->lk[u] = m.link[s];
+      sb->nd[u] = m.nrm[s];
+      sb->ar[u] = m.area[s];
+    }
+  }
+}
+
 template <class T>
 __device__ __forceinline__ void cell_gradient(const DevMesh<T>& m, const typename Vec<T>::v4* __restrict__ W, int c,
                                               typename Vec<T>::v4* gxo, typename Vec<T>::v4* gyo,
@@ -690,24 +729,14 @@ __device__ __forceinline__ void cell_gradient(const DevMesh<T>& m, const typenam
   T ax0 = 0, ax1 = 0, ax2 = 0, ax3 = 0, ay0 = 0, ay1 = 0, ay2 = 0, ay3 = 0;
   // slots in batches of kU: the links first, then every load of the batch, then the sums in
   // slot order, so the neighbour loads of one cell are in flight together
-  constexpr int kU = 4;
+  constexpr int kU = kGradBatch;
   for (int k0 = 0; k0 < m.d; k0 += kU) {
-    int lk[kU];
-#pragma unroll
-    for (int u = 0; u < kU; ++u) lk[u] = (k0 + u < m.d) ? m.link[(k0 + u) * m.n + c] : kPad;
-    typename Vec<T>::v2 nd[kU];
-    T ar[kU];
+    GradSlots<T> sb;
+    grad_slots(m, c, k0, &sb);
+    const int(&lk)[kU] = sb.lk;
+    const typename Vec<T>::v2(&nd)[kU] = sb.nd;
+    const T(&ar)[kU] = sb.ar;
     typename Vec<T>::v4 wo[kU];
-    // the slot geometry does not depend on the links (padding slots hold zeros), so its loads
-    // go out with the links' and only the neighbour states wait for them
-#pragma unroll
-    for (int u = 0; u < kU; ++u) {
-      if (k0 + u < m.d) {
-        const int s = (k0 + u) * m.n + c;
-        nd[u] = m.nrm[s];
-        ar[u] = m.area[s];
-      }
-    }
 #pragma unroll
     for (int u = 0; u < kU; ++u) {
       if (lk[u] >= 0) {
@@ -858,12 +887,16 @@ __global__ void __launch_bounds__(256) k_gradient(DevMesh<T> m, const typename V
   // most neighbours fall inside the block, and their loads no longer go to L2
   __shared__ typename Vec<T>::v4 sW[256 * CPT];
   if constexpr (CPT == 1) {
-    const int2 bd = cs.blk[blockIdx.x];
     const int base = blockIdx.x * blockDim.x;
     const int c = base + threadIdx.x;
+    // the cell's own state before the case lookup, so that its latency overlaps it (every
+    // block lies inside the block-padded arrays). Its slots are loaded after: held across the
+    // barrier they cost 9 registers per thread and a slower pass.
+    const auto w_own = W[c];
+    const int2 bd = cs.blk[blockIdx.x];
     if (cs.ctrl[bd.x].done) return;  // uniform over the block (one case per block)
     const int nsw = min(static_cast<int>(blockDim.x), bd.y - base);
-    if (threadIdx.x < nsw) sW[threadIdx.x] = W[c];
+    if (threadIdx.x < nsw) sW[threadIdx.x] = w_own;
     __syncthreads();
     if (c >= bd.y) return;
     typename Vec<T>::v4 ox, oy;
@@ -979,11 +1012,32 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
     if (PRECOND && t == 3) l2_prefetch(W + c0, nb * sizeof(W[0]));
     if (GATHER && t >= 4 && t < 4 + g.d) l2_prefetch(g.slot + static_cast<size_t>(t - 4) * g.n + c0, nb * sizeof(int));
   }
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  // The cell's own state and first gather slots, loaded before the case lookup so that their
+  // latency overlaps it (every block lies inside the block-padded arrays; padding cells'
+  // values go unused). The preconditioned last stage, and the FP64 kernels, load them after
+  // the checks: held across them, they take the float stage from 64 to 80 registers per
+  // thread and the FP64 kernels from 80 to 100.
+  constexpr bool kEarly = sizeof(T) == 4 && !(PRECOND && LAST);
+  typename Vec<T>::v4 st_hi{}, st_lo{}, st_us{}, st_w{};
+  d4 st_un{};
+  int first[kGatherBatch];
+  auto load_own = [&] {
+    if constexpr (sizeof(T) == 4) {
+      st_hi = U.hi[c];
+      if (LAST) st_lo = U.lo[c];
+    } else {
+      st_un = U.un[c];
+    }
+    if (stage > 0) st_us = Us[c];
+    if (PRECOND) st_w = W[c];
+    if (GATHER && kEarly) gather_slots(g, c, 0, first);
+  };
+  if (kEarly) load_own();
   const int2 bd = cs.blk[blockIdx.x];
   Ctrl* ctrl = cs.ctrl + bd.x;
   const PrecondD& pc = cs.pc[bd.x];
   const int n = bd.y;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (ctrl->done) return;
   if (cs.wait != nullptr && cs.wait[0] != 0) {
     // The gradient pass of this iteration gave up a wait and left gradients unwritten: no
@@ -997,22 +1051,11 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
   Prim<T> w{T(1), T(0), T(0), T(1)};
   T nq[kNorm] = {T(0), T(0), T(0), T(0)};
   if (c < n) {
-    // the cell's own state first, so these loads overlap the gather's
-    typename Vec<T>::v4 st_hi{}, st_lo{}, st_us{};
-    d4 st_un{};
-    if constexpr (sizeof(T) == 4) {
-      st_hi = U.hi[c];
-      if (LAST) st_lo = U.lo[c];
-    } else {
-      st_un = U.un[c];
-    }
-    if (stage > 0) st_us = Us[c];
-    typename Vec<T>::v4 st_w{};
-    if (PRECOND) st_w = W[c];
+    if (!kEarly) load_own();
     T r0, r1, r2, r3, src;
     if (GATHER) {
       T rr[4];
-      gather_cell<T>(g, F, FS, c, rr, &src);
+      gather_cell<T>(g, F, FS, c, kEarly ? first : nullptr, rr, &src);
       r0 = rr[0];
       r1 = rr[1];
       r2 = rr[2];

@@ -106,6 +106,8 @@ __global__ void __launch_bounds__(256) k_face_flux(DevFaces<T> f, Cases<T> cs,
     dN = f.noff[i];
   }
   const int2 bd = cs.blk[blockIdx.x];  // face blocks: (case, end of the case's faces)
+  pdl_trigger();
+  pdl_wait();  // the cells' states and gradients, the controller's flags
   const Ctrl* ctrl = cs.ctrl + bd.x;
   int* fb = fb_all + 4 * bd.x;
   if (ctrl->done) return;
@@ -233,6 +235,7 @@ struct ResidualLaunch {
   int global_dt;
   const LmSched* lms = nullptr;  // parity slots of the low-Mach weights (null: read the controller)
   int parity = 0;
+  bool pdl = false;  // launch the face pass with programmatic stream serialization
 };
 
 template <class T, int FLUX, bool SECOND, bool LM>
@@ -240,7 +243,8 @@ void launch_face_flux_t(const ResidualLaunch<T>& a) {
   const int grid = (a.faces.nf + a.block - 1) / a.block;
   auto kern = k_face_flux<T, FLUX, SECOND, LM>;
   const int pf = resident_blocks(kern, a.block);
-  kern<<<grid, a.block, 0, a.st>>>(a.faces, a.face_cases, a.W, a.gx, a.gy, a.F, a.FS, a.fb, a.lms, a.parity, pf);
+  launch_kernel(kern, grid, a.block, 0, a.st, a.pdl, a.faces, a.face_cases, a.W, a.gx, a.gy, a.F, a.FS, a.fb, a.lms,
+                a.parity, pf);
 }
 
 // Face pass, dispatched on the flux, order and low-Mach switches.

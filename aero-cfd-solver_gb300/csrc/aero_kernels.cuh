@@ -24,6 +24,7 @@
 
 #include <cstdint>
 #include <mutex>
+#include <utility>
 #include <vector>
 
 namespace aero {
@@ -60,6 +61,38 @@ __device__ __forceinline__ typename Vec<T>::v4 ld4(const typename Vec<T>::v4* p)
 __device__ __forceinline__ void l2_prefetch(const void* p, unsigned bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "r"(bytes)
                : "memory");
+}
+
+// Programmatic dependent launch (opt-in per context: AERO_PDL=1). The iteration's gradient,
+// face and update kernels may be launched with programmatic stream serialization: such a
+// kernel starts while its
+// predecessor in the stream is still running, once every block of the predecessor has
+// called pdl_trigger() (each does so on entry, so the successor's blocks take the SM slots
+// the predecessor's last wave frees). Before pdl_wait() a kernel reads only tables no kernel
+// writes (face and slot tables, geometry, case blocks); pdl_wait() returns once the
+// predecessor grids have completed and their writes are visible. Both are no-ops in a kernel
+// launched without the attribute.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Launches kernel<<<grid, block, smem, st>>>(args...), with programmatic stream serialization
+// when `pdl` is set.
+template <class... P, class... A>
+inline cudaError_t launch_kernel(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool pdl,
+                                 A&&... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  if (pdl) {
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+  }
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
 }
 
 // Blocks of `kernel` at `block` threads resident on the whole device at once (occupancy x
@@ -887,6 +920,8 @@ __global__ void __launch_bounds__(256) k_gradient(DevMesh<T> m, const typename V
   // most neighbours fall inside the block, and their loads no longer go to L2
   __shared__ typename Vec<T>::v4 sW[256 * CPT];
   if constexpr (CPT == 1) {
+    pdl_trigger();
+    pdl_wait();
     const int base = blockIdx.x * blockDim.x;
     const int c = base + threadIdx.x;
     // the cell's own state before the case lookup, so that its latency overlaps it (every
@@ -904,6 +939,8 @@ __global__ void __launch_bounds__(256) k_gradient(DevMesh<T> m, const typename V
     gx[c] = ox;
     gy[c] = oy;
   } else {
+    pdl_trigger();
+    pdl_wait();
     const int B = blockDim.x, lb0 = blockIdx.x * CPT;
     const int base = lb0 * B;
     const int nlb = min(CPT, nblk - lb0);
@@ -1012,6 +1049,8 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
     if (PRECOND && t == 3) l2_prefetch(W + c0, nb * sizeof(W[0]));
     if (GATHER && t >= 4 && t < 4 + g.d) l2_prefetch(g.slot + static_cast<size_t>(t - 4) * g.n + c0, nb * sizeof(int));
   }
+  pdl_trigger();
+  pdl_wait();
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   // The cell's own state and first gather slots, loaded before the case lookup so that their
   // latency overlaps it (every block lies inside the block-padded arrays; padding cells'

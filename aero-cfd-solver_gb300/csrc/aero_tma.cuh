@@ -136,6 +136,8 @@ __global__ void __launch_bounds__(256) k_gradient_tma(DevMesh<T> m, const typena
     bulk_copy_g2s(base + L.w, W + c0, uint32_t(B * sizeof(V4)), &bar[buf]);
     bulk_copy_g2s(base + L.inv, m.inv_vol + c0, uint32_t(B * sizeof(T)), &bar[buf]);
   };
+  pdl_trigger();
+  pdl_wait();  // the copies read W
   const int limit = wait[1] < 0 ? kTmaPolls : wait[1];
   if (threadIdx.x == 0) issue(tile, 0);
   uint32_t phase0 = 0, phase1 = 0;

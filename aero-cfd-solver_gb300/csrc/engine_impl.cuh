@@ -352,6 +352,13 @@ class EngineT final : public Engine {
     dg_.n = ntot_;
     dg_.d = d_;
     dg_.inv_vol = inv_vol_;
+    {
+      // programmatic dependent launch of the iteration's kernels (AERO_PDL=1; off by
+      // default: 1.7% off the 131k-cell step, 0.5% onto the 524k-cell one, and each kernel's
+      // recorded span then includes its wait for the predecessor)
+      const char* env = std::getenv("AERO_PDL");
+      pdl_ = env && env[0] == '1';
+    }
     // the gradient pass of the iterations: persistent CTAs streaming their tiles through
     // shared memory with bulk copies, where each CTA gets two or more tiles
     // (AERO_BULK_COPY=0 never, =1 always)
@@ -1795,19 +1802,20 @@ class EngineT final : public Engine {
   }
 
   template <bool PRECOND, bool LAST, bool GATHER>
-  void update_t(int stage, int global_dt, V4* R, T* SR) {
+  void update_t(int stage, int global_dt, V4* R, T* SR, bool pdl) {
     auto kern = k_update<T, PRECOND, LAST, GATHER>;
     const int pf = resident_blocks(kern, block_);
-    kern<<<ncb_, block_, 0, st_>>>(stage, cell_cases_, R, SR, dg_, F_, FS_, W_, sref_, Us_, ms_, part_, global_dt, pf);
+    AERO_CK(launch_kernel(kern, ncb_, block_, 0, st_, pdl, stage, cell_cases_, R, SR, dg_, F_, FS_, W_, sref_, Us_,
+                          ms_, part_, global_dt, pf));
   }
   template <bool PRECOND>
-  void update_p(int stage, bool last, int global_dt, V4* R, T* SR) {
+  void update_p(int stage, bool last, int global_dt, V4* R, T* SR, bool pdl = false) {
     if (global_dt) {  // residual already gathered (the global time step needs all of SR first)
-      if (last) update_t<PRECOND, true, false>(stage, global_dt, R, SR);
-      else update_t<PRECOND, false, false>(stage, global_dt, R, SR);
+      if (last) update_t<PRECOND, true, false>(stage, global_dt, R, SR, pdl);
+      else update_t<PRECOND, false, false>(stage, global_dt, R, SR, pdl);
     } else {
-      if (last) update_t<PRECOND, true, true>(stage, global_dt, R, SR);
-      else update_t<PRECOND, false, true>(stage, global_dt, R, SR);
+      if (last) update_t<PRECOND, true, true>(stage, global_dt, R, SR, pdl);
+      else update_t<PRECOND, false, true>(stage, global_dt, R, SR, pdl);
     }
   }
 
@@ -1842,18 +1850,24 @@ class EngineT final : public Engine {
         });
         AERO_CK(cudaEventRecord(ev_join_, side_));
       }
+      // programmatic dependent launch of the gradient, face and update kernels (not of the
+      // update that also waits for the controller on the side stream)
+      const bool pdl = pdl_ && !global_dt;
       if (second) {
         wrap(0, [&] {
           if (grad_tma_) {
-            k_gradient_tma<T><<<grad_grid_, block_, grad_smem_, st_>>>(dm_, W_, gx_, gy_, cell_cases_, ncb_, tma_err_);
+            AERO_CK(launch_kernel(k_gradient_tma<T>, grad_grid_, block_, grad_smem_, st_, pdl, dm_, W_, gx_, gy_,
+                                  cell_cases_, ncb_, tma_err_));
           } else if (cpt_ == 2) {
-            k_gradient<T, 2><<<(ncb_ + 1) / 2, block_, 0, st_>>>(dm_, W_, gx_, gy_, cell_cases_, ncb_);
+            AERO_CK(launch_kernel(k_gradient<T, 2>, (ncb_ + 1) / 2, block_, 0, st_, pdl, dm_, W_, gx_, gy_, cell_cases_,
+                                  ncb_));
           } else {
-            k_gradient<T><<<ncb_, block_, 0, st_>>>(dm_, W_, gx_, gy_, cell_cases_);
+            AERO_CK(launch_kernel(k_gradient<T, 1>, ncb_, block_, 0, st_, pdl, dm_, W_, gx_, gy_, cell_cases_, 0));
           }
         });
       }
       ResidualLaunch<T> ra = residual_args(fb, R, SR, global_dt);
+      ra.pdl = pdl;
       if (defer && lm_defer_) {
         ra.lms = lms_;
         ra.parity = parity;
@@ -1864,11 +1878,12 @@ class EngineT final : public Engine {
       if (global_dt) {
         wrap(3, [&] { k_srmax<<<K_, 1024, 0, st_>>>(part_.srmax, srfirst_, ctrls_); });
       }
+      const bool pdl_update = pdl && !(stage == 0 && pending);
       wrap(2, [&] {
         if (cfg_[0].precond_on) {
-          update_p<true>(stage, last, global_dt, R, SR);
+          update_p<true>(stage, last, global_dt, R, SR, pdl_update);
         } else {
-          update_p<false>(stage, last, global_dt, R, SR);
+          update_p<false>(stage, last, global_dt, R, SR, pdl_update);
         }
       });
     }
@@ -1974,6 +1989,7 @@ class EngineT final : public Engine {
   int* perm_all_dev_ = nullptr;  // every case's new -> original cell, at the case's cell offset
   bool host_direct_ = false;     // the GPU reads and writes host state arrays in place
   bool grad_tma_ = false;        // gradient pass through bulk copies into shared memory
+  bool pdl_ = false;             // programmatic dependent launch of the iteration's kernels
   int cpt_ = 1;                  // cells per thread of the gather gradient pass (1 or 2)
   size_t grad_smem_ = 0;
   int grad_grid_ = 0;

@@ -172,6 +172,29 @@ def test_ordering_and_block_size_do_not_change_results(precision):
                 np.testing.assert_array_equal(sr, ref[1])
 
 
+@pytest.mark.parametrize("bulk_copy", ["0", "1"])
+def test_programmatic_launch_is_bit_identical(bulk_copy, monkeypatch):
+    """The opt-in programmatic dependent launch (AERO_PDL=1) lets each kernel of the iteration
+    start before its predecessor ends, its reads of the predecessor's outputs behind
+    griddepcontrol.wait: records and states are bit-identical to ordinary launches, with the
+    controller overlapping the next iteration, through the gather and the bulk-copy gradient
+    passes, in both precisions."""
+    monkeypatch.setenv("AERO_BULK_COPY", bulk_copy)
+    mesh = aero_gb300.ogrid_synthetic(128, 32, cell_type=3, permute=True, jitter=0.1, seed=6)
+    for precision in (capi.PRECISION_FP32, capi.PRECISION_FP64):
+        case = capi.make_case(mach=0.7, aoa_deg=1.5, flux=capi.FLUX_HLLC, limiter=capi.LIMITER_VENKAT,
+                              startup_first_order_iters=4, precision=precision)
+        out = {}
+        for pdl in ("0", "1"):
+            monkeypatch.setenv("AERO_PDL", pdl)
+            with aero_gb300.Solver(mesh, case) as s:
+                _, rec = s.run(12)
+                out[pdl] = (rec, s.get_state())
+        for key in ("residual_l2", "cl", "cd", "first_order_fallback_faces"):
+            np.testing.assert_array_equal(out["0"][0][key], out["1"][0][key])
+        np.testing.assert_array_equal(out["0"][1], out["1"][1])
+
+
 # ------------------------------------------------------------------------------------------
 # whole runs
 # ------------------------------------------------------------------------------------------

@@ -229,6 +229,68 @@ def _cpu_worker(mesh_kw, case_kw, warmup, steps, barrier_, out_q):
     out_q.put(time.perf_counter() - t0)
 
 
+def _cpu_sweep_worker(tasks, warmup, steps, barrier_, out_q):
+    """One single-thread oracle process of the sweep's CPU baseline (spawned): its share of the
+    96 cases, each built with the oracle's own generator, `warmup` untimed and `steps` timed
+    second-order iterations from the free stream. Returns (cell-iterations, seconds)."""
+    sys.path.insert(0, str(REPO))
+    from oracle import oracle_py as op
+
+    meshes = {}
+    sols = []
+    for (nc, nr, seed), case_kw in tasks:
+        if (nc, nr, seed) not in meshes:
+            meshes[(nc, nr, seed)] = op.ogrid_synthetic(nc, nr, cell_type=3, permute=True, jitter=0.1, seed=seed,
+                                                        wall_spacing=0.005, farfield_radius=20.0)
+        sol = op.OracleSolver(op.MODE_FLOAT, meshes[(nc, nr, seed)], op.make_case(**case_kw))
+        sol.run(warmup)
+        sols.append((sol, 2 * nc * nr))
+    if barrier_ is not None:
+        barrier_.wait()
+    t0 = time.perf_counter()
+    work = 0
+    for sol, cells in sols:
+        sol.run(steps)
+        work += cells * steps
+    out_q.put((work, time.perf_counter() - t0))
+
+
+def c4_cpu_sweep(rank: int, warmup: int = 1, steps: int = 2) -> dict:
+    """CPU baseline of the batched sweep: the same 96 cases (sizes, alpha, Mach) in the oracle's
+    float mode, bit-identical to the reference CPU path, one single-thread process per host core
+    with the cases dealt round-robin; a bounded sample of each case's iterations."""
+    import multiprocessing as mp
+
+    from oracle import oracle_py as op
+
+    op.build()
+    pick, alphas, machs = c4_draw(rank)
+    tasks = []
+    for k in range(C4_CASES):
+        kw = dict(CASE)
+        kw.update(mach=float(machs[k]), aoa_deg=float(alphas[k]), startup_first_order_iters=0)
+        nc, nr = C4_SIZES[pick[k]]
+        tasks.append(((nc, nr, 100 + int(pick[k])), kw))
+    procs_n = max(1, min(os.cpu_count() or 1, C4_CASES))
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    bar = ctx.Barrier(procs_n)
+    procs = [ctx.Process(target=_cpu_sweep_worker, args=(tasks[i::procs_n], warmup, steps, bar, q))
+             for i in range(procs_n)]
+    for p in procs:
+        p.start()
+    res = [q.get() for _ in procs]
+    for p in procs:
+        p.join()
+    work = sum(w for w, _ in res)
+    wall = max(t for _, t in res)
+    return {"value": work / wall / 1e6, "unit": "Mcell-iter/s", "cores": procs_n, "kind": "port",
+            "sample": f"the 96 cases' second-order iterations from the free stream ({warmup} untimed, {steps} "
+                      f"timed per case) in the oracle's float mode, bit-identical to the reference CPU path; "
+                      f"{procs_n} single-thread processes, cases dealt round-robin; value = all cell-iterations "
+                      f"/ the slowest process's time"}
+
+
 def cpu_sample(mesh, target_s=12.0, max_iters=40, warmup=3):
     """Single-core oracle port on a bounded sample of the workload, the same iterations as each
     replica of the reference arm runs: second-order iterations from the free stream, `warmup`
@@ -829,6 +891,8 @@ def run_gpu_arm(args):
                         "density-residual stop mask 1e-8; one batched context, L2 flushed per step"}
         if rank == 0 and not args.mesh:
             c4["fp32_batch_vs_fp64_single"] = c4_accuracy(args, aero_gb300, capi, rank)
+        if rank == 0 and world == 1 and not args.no_cpu and not args.mesh:
+            c4["cpu_baseline"] = c4_cpu_sweep(rank)
 
     gate = c1 = c3 = c5 = None
     gate_rec64 = c1_rec = None

@@ -425,6 +425,23 @@ def c4_sweep(args, aero_gb300, capi, rank):
     return ms, int(cells), int(info["launches_per_iteration"]), tuned_t, prof, info
 
 
+def kernel_fractions(prof: dict, info: dict, precision: str, peak: float) -> dict:
+    """Per kernel class (gradient, face pass, update): algorithmic bytes per launch, the mean
+    in-graph launch time, the achieved GB/s and its fraction of the measured HBM peak."""
+    n, f, d = int(info["cells"]), int(info["faces"]), int(info["slots_per_cell"])
+    out = {}
+    for name, kernel in (("gradient", "gradient"), ("face_pass", "face"), ("update", "update")):
+        t_ms, cnt = prof[name]
+        if not cnt:
+            continue
+        nbytes = algorithmic_bytes(kernel, n, d, precision, f)
+        avg = t_ms / cnt
+        gbs = nbytes / (avg / 1e3) / 1e9
+        out[name] = {"algorithmic_bytes_per_launch": nbytes, "avg_launch_us": avg * 1e3, "achieved_gbs": gbs,
+                     "frac": gbs / peak}
+    return out
+
+
 def batch_roofline(ms_per_step: float, prof: dict, info: dict, peak: float) -> dict:
     """HBM fractions of the batched sweep: its packed working set (4.8 M cells) is far larger
     than L2. The face pass's algorithmic bytes per launch over its in-graph launch time, and
@@ -472,7 +489,7 @@ def c3_low_mach(args, aero_gb300, capi, peak):
         nbytes = algorithmic_bytes("face", mesh.num_cells, info["slots_per_cell"], prec[:4], int(info["faces"]))
         res[prec] = dict(mcell=mesh.num_cells * args.steps / (ms / 1e3) / 1e6, cl=float(rec["cl"][-1]),
                          cd=float(rec["cd"][-1]), pw=p[mesh.owner[wall]], face_ms=avg, face_gbs=nbytes / (avg / 1e3) / 1e9,
-                         kernels=kernel_times(prof))
+                         kernels=kernel_times(prof), fractions=kernel_fractions(prof, info, prec[:4], peak))
     q = 0.5 * 1.4 * 101325.0 * mach * mach
     m01 = {}
     for prec, code, pfp in legs:
@@ -511,7 +528,8 @@ def c3_low_mach(args, aero_gb300, capi, peak):
                                         "frac": res["fp32"]["face_gbs"] / peak, "avg_launch_ms": res["fp32"]["face_ms"]},
             "roofline_face_pass_fp64": {"achieved": res["fp64"]["face_gbs"], "frac": res["fp64"]["face_gbs"] / peak,
                                         "avg_launch_ms": res["fp64"]["face_ms"]},
-            "in_graph_kernel_us_per_launch_fp32": res["fp32"]["kernels"]}
+            "in_graph_kernel_us_per_launch_fp32": res["fp32"]["kernels"],
+            "hbm_fraction_per_kernel_fp32": res["fp32"]["fractions"]}
 
 
 def c3_case(capi, precision, mach=0.05):
@@ -831,6 +849,7 @@ def run_gpu_arm(args):
         bytes_face = algorithmic_bytes("face", n, info["slots_per_cell"], prec, int(info["faces"]))
         main_ms = sum(v[0] for k, v in graph_prof.items() if k != "control")
         in_graph = {"us_per_launch": kernel_times(graph_prof),
+                    "hbm_fraction_per_kernel": kernel_fractions(graph_prof, info, prec, peak),
                     "launches_per_iteration": {k: v[1] / nprof for k, v in graph_prof.items()},
                     "us_per_iteration": {k: v[0] / nprof * 1e3 for k, v in graph_prof.items()},
                     "kernels_on_main_stream_us_per_iteration": main_ms / nprof * 1e3,
@@ -883,6 +902,7 @@ def run_gpu_arm(args):
               "fp32_batched_mcell_iter_s": world * c4_cells * args.steps / (c4_ms / 1e3) / 1e6,
               "launches_per_step": c4_launch,
               "in_graph_kernel_us_per_launch": kernel_times(c4_prof),
+              "hbm_fraction_per_kernel": kernel_fractions(c4_prof, c4_info, "fp32", peak),
               "roofline": batch_roofline(c4_ms / args.steps, c4_prof, c4_info, peak),
               "autotuned": {"ordering": {1: "morton", 2: "rcm"}.get(c4_tuned[0], c4_tuned[0]),
                             "block_size": c4_tuned[1], "cells_per_thread": c4_tuned[2]},

@@ -916,29 +916,25 @@ template <class T, int CPT = 1>
 __global__ void __launch_bounds__(256) k_gradient(DevMesh<T> m, const typename Vec<T>::v4* __restrict__ W,
                                                   typename Vec<T>::v4* __restrict__ gx,
                                                   typename Vec<T>::v4* __restrict__ gy, Cases<T> cs, int nblk = 0) {
-  // the block's own cells' W staged in shared memory: with the cells in Morton / RCM order
-  // most neighbours fall inside the block, and their loads no longer go to L2
-  __shared__ typename Vec<T>::v4 sW[256 * CPT];
   if constexpr (CPT == 1) {
     pdl_trigger();
     pdl_wait();
     const int base = blockIdx.x * blockDim.x;
     const int c = base + threadIdx.x;
-    // the cell's own state before the case lookup, so that its latency overlaps it (every
-    // block lies inside the block-padded arrays). Its slots are loaded after: held across the
-    // barrier they cost 9 registers per thread and a slower pass.
-    const auto w_own = W[c];
+    // No shared-memory staging of the block's own cells: their neighbour loads hit L1 and L2
+    // as well, and the staging's store and barrier cost more than they saved (131k cells:
+    // 4.64 -> 4.39 us per launch without them; 524k: 14.96 -> 13.0 us).
     const int2 bd = cs.blk[blockIdx.x];
     if (cs.ctrl[bd.x].done) return;  // uniform over the block (one case per block)
-    const int nsw = min(static_cast<int>(blockDim.x), bd.y - base);
-    if (threadIdx.x < nsw) sW[threadIdx.x] = w_own;
-    __syncthreads();
     if (c >= bd.y) return;
     typename Vec<T>::v4 ox, oy;
-    cell_gradient<T>(m, W, c, &ox, &oy, sW, base, nsw);
+    cell_gradient<T>(m, W, c, &ox, &oy);
     gx[c] = ox;
     gy[c] = oy;
   } else {
+    // the covered blocks' own cells' W staged in shared memory: with the cells in Morton /
+    // RCM order most neighbours fall inside them
+    __shared__ typename Vec<T>::v4 sW[256 * CPT];
     pdl_trigger();
     pdl_wait();
     const int B = blockDim.x, lb0 = blockIdx.x * CPT;

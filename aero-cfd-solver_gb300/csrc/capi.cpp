@@ -217,12 +217,8 @@ int create_ctx(int n, const aero_mesh_desc* meshes, const aero_case_desc* cfgs, 
   try {
     std::unique_ptr<aero_ctx> ctx(new aero_ctx());
     ctx->cfg = cfgs[0];
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || !device_ok(dev)) {
-      cudaGetLastError();
-      return fail(nullptr, AERO_ERR_CUDA, "no usable CUDA device of compute capability 10.3");
-    }
-    ctx->device = dev;
+    // the meshes are checked and prepared on the host first, so that an invalid mesh is
+    // reported as such on any machine
     std::vector<aero::HostSlots> hv(static_cast<size_t>(n));
     std::vector<aero_case_desc> cv(cfgs, cfgs + n);
     std::vector<aero::Resolved> rv;
@@ -233,6 +229,12 @@ int create_ctx(int n, const aero_mesh_desc* meshes, const aero_case_desc* cfgs, 
       }
       rv.push_back(resolve(cfgs[k]));
     }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || !device_ok(dev)) {
+      cudaGetLastError();
+      return fail(nullptr, AERO_ERR_CUDA, "no usable CUDA device of compute capability 10.3");
+    }
+    ctx->device = dev;
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
       cudaGetLastError();
       return fail(nullptr, AERO_ERR_CUDA, "cudaStreamCreate failed");

@@ -74,6 +74,63 @@ def test_invalid_arguments_are_rejected(lib):
     assert exc.value.code == capi.AERO_ERR_INVALID
 
 
+def _corrupted(mesh, what):
+    """A copy of `mesh` with one defect."""
+    m = capi.Mesh(mesh.owner.copy(), mesh.neighbor.copy(), mesh.bc.copy(), mesh.normal.copy(), mesh.center.copy(),
+                  mesh.area.copy(), mesh.volume.copy(), mesh.cell_center.copy(), mesh.wall_faces.copy())
+    interior = int(np.flatnonzero(m.neighbor >= 0)[0])
+    boundary = int(np.flatnonzero(m.neighbor < 0)[0])
+    if what == "owner out of range":
+        m.owner[interior] = m.num_cells
+    elif what == "neighbour equals owner":
+        m.neighbor[interior] = m.owner[interior]
+    elif what == "neighbour below -1":
+        m.neighbor[boundary] = -2
+    elif what == "boundary face without a type":
+        m.bc[boundary] = capi.BC_INTERIOR
+    elif what == "non-finite normal":
+        m.normal[3 * interior] = np.nan
+    elif what == "non-finite length":
+        m.area[interior] = np.inf
+    elif what == "non-finite volume":
+        m.volume[0] = np.nan
+    elif what == "interior face in the wall list":
+        m.wall_faces[0] = interior
+    elif what == "wall face out of range":
+        m.wall_faces[0] = m.num_faces
+    return m
+
+
+@pytest.mark.parametrize("what, message", [
+    ("owner out of range", "invalid owner/neighbour"),
+    ("neighbour equals owner", "invalid owner/neighbour"),
+    ("neighbour below -1", "invalid owner/neighbour"),
+    ("boundary face without a type", "no far-field/wall type"),
+    ("non-finite normal", "non-finite geometry"),
+    ("non-finite length", "non-finite geometry"),
+    ("non-finite volume", "non-finite volume"),
+    ("interior face in the wall list", "wall face list"),
+    ("wall face out of range", "wall face list"),
+])
+def test_invalid_meshes_are_refused(lib, what, message):
+    """aero_create checks the mesh on the host before it looks for a device: each defect is
+    refused with AERO_ERR_INVALID and a message naming it, on any machine."""
+    mesh = aero_gb300.ogrid_reference(n_circ=32, n_radial=4, farfield_radius=10.0, radial_stretch=1.25)
+    with pytest.raises(aero_gb300.AeroError) as exc:
+        aero_gb300.Solver(_corrupted(mesh, what), capi.make_case())
+    assert exc.value.code == capi.AERO_ERR_INVALID
+    assert message in str(exc.value)
+
+
+def test_empty_mesh_is_refused(lib):
+    mesh = aero_gb300.ogrid_reference(n_circ=32, n_radial=4, farfield_radius=10.0, radial_stretch=1.25)
+    empty = capi.Mesh(np.zeros(0, np.int32), np.zeros(0, np.int32), np.zeros(0, np.int32), np.zeros(0), np.zeros(0),
+                      np.zeros(0), mesh.volume, mesh.cell_center, np.zeros(0, np.int32))
+    with pytest.raises(aero_gb300.AeroError) as exc:
+        aero_gb300.Solver(empty, capi.make_case())
+    assert exc.value.code == capi.AERO_ERR_INVALID and "cells and faces" in str(exc.value)
+
+
 def test_record_struct_size_matches_header():
     # aero_iter_record: 4 ints + 42 doubles + 2 ints + 1 double
     assert C.sizeof(capi.IterRecord) == 4 * 4 + 42 * 8 + 2 * 4 + 8

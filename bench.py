@@ -636,7 +636,7 @@ C1_MESH = dict(n_circ=128, n_radial=32, cell_type=4, permute=False, jitter=0.0, 
 C1_CASE = dict(mach=0.5, aoa_deg=2.0, flux=0, limiter=0, cfl_start=0.8, cfl_max=0.8, startup_first_order_iters=10 ** 9,
                iterations=2000, min_iterations=2000, residual_reduction_target=0.0)
 C1_ITERS = 2000
-C2_ORACLE_ITERS = 30  # 25 first-order start-up iterations and 5 second-order ones
+C2_ORACLE_ITERS = 100  # 25 first-order start-up iterations and 75 second-order ones
 
 
 def _oracle_history(tag, mesh_kw, case_kw, iters, out_q):
@@ -655,7 +655,7 @@ def _oracle_history(tag, mesh_kw, case_kw, iters, out_q):
 
 def start_oracle_checks(enabled: bool):
     """Spawned before the first GPU call: the C1 case (plain FP64 quads, 2,000 iterations) and
-    the first 30 iterations of the workload case, both in the FP64 oracle."""
+    the first 100 iterations of the workload case, both in the FP64 oracle."""
     if not enabled:
         return None
     import multiprocessing as mp

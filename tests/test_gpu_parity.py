@@ -153,6 +153,30 @@ def test_freestream_preservation_jittered(precision):
 
 
 @pytest.mark.parametrize("precision", [capi.PRECISION_FP64, capi.PRECISION_FP32])
+def test_reference_uniform_invariance_on_the_demo_mesh(precision, golden_meshes):
+    """The reference's uniform-flow invariance test (tests/cpp/test_euler_uniform_invariance.cpp:
+    13-75) on the device: the reference's 2x2 demo mesh (all boundary faces far field), the
+    uniform state rho = 1.05, (u, v) = (0.32, -0.08), p = 0.9 with the far field equal to it,
+    HLLC + venkat, second order, preconditioning on (Mach reference 0.15, minimum 1e-3, beta in
+    [0.2, 1]): max |R| <= 1e-6 (:68). The reference's state also carries w = 0.03, the
+    out-of-plane velocity, which this 2D path holds at zero."""
+    mesh = golden_mesh(golden_meshes, "demo_2x2")
+    assert mesh.num_cells == 8 and np.all(mesh.bc[mesh.neighbor < 0] == capi.BC_FARFIELD)
+    gamma, rho, u, v, p = 1.4, 1.05, 0.32, -0.08, 0.9
+    mach = np.hypot(u, v) / np.sqrt(gamma * p / rho)
+    case = capi.make_case(mach=mach, aoa_deg=np.degrees(np.arctan2(v, u)), rho_inf=rho, p_inf=p, gas_constant=1.0,
+                          t_inf=p / rho, flux=capi.FLUX_HLLC, limiter=capi.LIMITER_VENKAT, precond_on=1,
+                          precond_mach_ref=0.15, precond_mach_min=1e-3, precond_beta_min=0.2, precond_beta_max=1.0,
+                          precision=precision)
+    with aero_gb300.Solver(mesh, case) as s:
+        uf = s.get_state()  # the free stream: uniform, and the far-field state itself
+        assert abs(uf[0, 0] - rho) < 1e-6 and abs(uf[0, 1] / uf[0, 0] - u) < 1e-6 and abs(uf[0, 2] / uf[0, 0] - v) < 1e-6
+        r, sr, _ = s.residual(uf, 1, 0.0, 0, 0.05, 1.0)
+    assert np.all(np.isfinite(r)) and np.all(sr > 0)
+    assert np.max(np.abs(r)) <= 1e-6
+
+
+@pytest.mark.parametrize("precision", [capi.PRECISION_FP64, capi.PRECISION_FP32])
 def test_ordering_and_block_size_do_not_change_results(precision):
     """Each cell sums its faces in the original face order whatever the renumbering, so the
     residual is bit-identical across orderings and block sizes."""

@@ -1633,15 +1633,9 @@ static __global__ void __launch_bounds__(kCtlThreads) k_control(const CtrlConfig
   __shared__ double s_sum[kWarps][3 + 4];   // l1, l2 sum, density l2 sum, pressure-jump sums
   __shared__ long long s_max[kWarps][1 + kMon];  // linf, monitors (bit patterns)
   __shared__ double s_wall[kWarps][kWall];
-  if (ctrl->done) return;
-  if (ctrl->wait_stop) {  // the iteration was not applied: stop without a record
-    if (threadIdx.x == 0) {
-      fb[0] = 0;  // its face passes' fallback counts are dropped with it
-      fb[1] = 0;
-      ctrl->done = 1;
-    }
-    return;
-  }
+  // The controller state is copied to shared memory and the block partials are read before
+  // the done / wait-stop checks, which then come from the shared copy: the loads do not wait
+  // for a round trip on the flags, and nothing is written before the checks.
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   constexpr int kWords = int(sizeof(Ctrl) / 16);
   {
@@ -1751,6 +1745,15 @@ static __global__ void __launch_bounds__(kCtlThreads) k_control(const CtrlConfig
     for (int k = 0; k < 1 + kMon; ++k) s_max[wid][k] = mx[k];
   }
   __syncthreads();
+  if (sc.done) return;  // uniform over the block
+  if (sc.wait_stop) {   // the iteration was not applied: stop without a record
+    if (tid == 0) {
+      fb[0] = 0;  // its face passes' fallback counts are dropped with it
+      fb[1] = 0;
+      ctrl->done = 1;
+    }
+    return;
+  }
   __shared__ CtlIn s_in;
   __shared__ Record srec;
   __shared__ SchedBase snext;

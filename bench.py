@@ -118,7 +118,15 @@ def measured_peak():
 
 
 class ClockSampler:
-    """nvidia-smi samples every 200 ms while the timed region runs."""
+    """nvidia-smi samples every 200 ms over a window in which the GPU runs the timed workload.
+
+    The timed steps of the workload last a few milliseconds, less than one sampling period, so
+    the caller keeps the GPU on the same iterations (untimed, L2 flushed as in the timed run)
+    for LOAD_BEFORE_S before and LOAD_AFTER_S after them: every sample then sees the workload's
+    own load and clocks."""
+
+    LOAD_BEFORE_S = 0.8
+    LOAD_AFTER_S = 0.4
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -135,14 +143,12 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                                           "-lms", "200", "-i", str(self.device)], stdout=self.fh,
                                          stderr=subprocess.DEVNULL)
-            time.sleep(0.3)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
 
     def __exit__(self, *exc):
         if self.proc is not None:
-            time.sleep(0.25)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -165,7 +171,17 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows),
+                "window": f"{self.LOAD_BEFORE_S:g} s of untimed iterations of the workload, the timed steps, "
+                          f"{self.LOAD_AFTER_S:g} s of untimed iterations"}
+
+
+def keep_busy(solver, seconds: float) -> None:
+    """Untimed iterations of the solver (graphs, L2 flushed before each, as in the timed run)
+    for about `seconds` of wall time."""
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        solver.time_iterations(200, use_graph=True, flush_l2=True)
 
 
 def dist_setup(args):
@@ -836,8 +852,10 @@ def run_gpu_arm(args):
             sampler = ClockSampler(local) if prec == "fp32" and not args.no_clocks else None
             if sampler:
                 sampler.__enter__()
+                keep_busy(s, ClockSampler.LOAD_BEFORE_S)
             ms = s.time_iterations(args.steps, use_graph=True, flush_l2=not args.no_flush)
             if sampler:
+                keep_busy(s, ClockSampler.LOAD_AFTER_S)
                 sampler.__exit__(None, None, None)
             barrier(dist)
             ms_max = reduce_max(dist, ms)

@@ -852,7 +852,9 @@ def run_gpu_arm(args):
             sampler = ClockSampler(local) if prec == "fp32" and not args.no_clocks else None
             if sampler:
                 sampler.__enter__()
+                u_start = s.get_state()
                 keep_busy(s, ClockSampler.LOAD_BEFORE_S)
+                s.set_state(u_start)  # the timed steps start from the warmed-up flow, as without the load
             ms = s.time_iterations(args.steps, use_graph=True, flush_l2=not args.no_flush)
             if sampler:
                 keep_busy(s, ClockSampler.LOAD_AFTER_S)

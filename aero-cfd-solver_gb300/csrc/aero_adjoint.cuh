@@ -49,6 +49,7 @@ __device__ __forceinline__ FaceParams<ad::Dual<N>> dual_params(const FaceParams<
   d.as_cutoff = D(f.as_cutoff);
   d.as_fmin = D(f.as_fmin);
   d.as_ramp = D(f.as_ramp);
+  d.inv_gm1 = D(f.inv_gm1);
   return d;
 }
 

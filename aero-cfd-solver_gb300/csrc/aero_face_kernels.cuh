@@ -44,10 +44,10 @@ __device__ __forceinline__ void eval_face(const FaceParams<T>& fp, int b, const 
   }
   // owner side: the reconstructed state (interior) or the cell state (boundary); the other
   // side: the neighbour's, the free stream (far field) or the owner's own (slip wall)
-  const Cons<T> cl = prim_to_cons(L, fp.gamma);
+  const Cons<T> cl = prim_to_cons_face(L, fp);
   Cons<T> cr = cl;
   if (b >= 0) {
-    cr = prim_to_cons(Rt, fp.gamma);
+    cr = prim_to_cons_face(Rt, fp);
   } else if (b != -2) {
     cr = fp.farfield;
   }
@@ -63,9 +63,9 @@ __device__ __forceinline__ void eval_face(const FaceParams<T>& fp, int b, const 
   } else {
     if (b < 0 && fp.precond_farfield_bc) {  // the characteristic state replaces the free stream
       cr = precond_farfield_state(cl, nx, ny, fp, as);
-      sd.pr = cons_to_prim(cr, fp.gamma);
+      sd.pr = cons_to_prim(cr, fp.gamma, &sd.ir);
       sd.unr = sd.pr.u * nx + sd.pr.v * ny;
-      sd.ar = sound_speed(sd.pr, fp.gamma);
+      sd.ar = sound_speed_inv(sd.pr, sd.ir, fp.gamma);
       if (LM) sm = side_mach(sd);
     }
     *f = face_flux<T, FLUX, LM>(cl, cr, sd, sm, nx, ny, fp, as, mws, df);

@@ -178,6 +178,7 @@ struct PrecondD {
   int fp64;  // FP32 contexts: energy row 0 float, 1 IEEE double (beta too), 2 double-float
   double gamma, mach_ref, mach_min, beta_min, beta_max;
   float gamma_f, gm1_f;  // float(gamma), float(gamma - 1)
+  double pfe;            // p_floor / (gamma - 1) in double: the energy floor of enforce_physical
   float mach_ref_f, mach_min_f, beta_min_f, beta_max_f;  // float copies (FP32 update)
 };
 
@@ -1243,14 +1244,17 @@ __global__ void __launch_bounds__(256) k_update(int stage, Cases<T> cs, typename
         s.rv = a * un.z + b * s.rv;
         s.rE = a * un.w + b * s.rE;
       }
-      enforce_physical(&s, pc.gamma);
+      // the case's energy floor and the floored rho's reciprocal reused by the primitive
+      // refresh: the same quotients as enforce_physical and cons_to_prim form, two FP64
+      // divisions fewer per cell
+      const double inv = enforce_physical_pf(&s, pc.gamma, pc.pfe);
       const d4 o{s.r, s.ru, s.rv, s.rE};
       if (LAST) {
         U.un[c] = o;
       } else {
         Us[c] = o;
       }
-      w = cons_to_prim(Cons<T>{T(s.r), T(s.ru), T(s.rv), T(s.rE)}, T(pc.gamma));
+      w = cons_to_prim_from(Cons<T>{T(s.r), T(s.ru), T(s.rv), T(s.rE)}, T(pc.gamma), T(s.r), T(inv));
       if (LAST) bad = !finite4(s.r, s.ru, s.rv, s.rE) || !finite4(w.r, w.u, w.v, w.p);
     }
     typename Vec<T>::v4 wo;
@@ -1845,19 +1849,22 @@ static __global__ void k_split_state(int n, const d4* __restrict__ Un, float4* _
 // State exchange with a caller's host array, read and written by the GPU in place where the
 // device shares the host's page tables (Grace: NVLink-C2C with address translation): u is
 // AoS [N][5] in the original cell order, perm maps device cell -> original cell.
-static __global__ void k_state_from_host(int n, const double* __restrict__ u, const int* __restrict__ perm,
+// The host array is walked in its own (the reference's) cell order, so that a warp's accesses
+// over the host link cover one contiguous range; iperm maps an original cell to its device
+// cell, and the device side takes the scattered accesses.
+static __global__ void k_state_from_host(int n, const double* __restrict__ u, const int* __restrict__ iperm,
                                          d4* __restrict__ Un) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n) return;
-  const double* s = u + 5 * static_cast<size_t>(perm[c]);
-  Un[c] = d4{s[0], s[1], s[2], s[4]};
+  const int co = blockIdx.x * blockDim.x + threadIdx.x;
+  if (co >= n) return;
+  const double* s = u + 5 * static_cast<size_t>(co);
+  Un[iperm[co]] = d4{s[0], s[1], s[2], s[4]};
 }
-static __global__ void k_state_to_host(int n, const d4* __restrict__ Un, const int* __restrict__ perm,
+static __global__ void k_state_to_host(int n, const d4* __restrict__ Un, const int* __restrict__ iperm,
                                        double* __restrict__ u) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n) return;
-  const d4 v = Un[c];
-  double* s = u + 5 * static_cast<size_t>(perm[c]);
+  const int co = blockIdx.x * blockDim.x + threadIdx.x;
+  if (co >= n) return;
+  const d4 v = Un[iperm[co]];
+  double* s = u + 5 * static_cast<size_t>(co);
   s[0] = v.x;
   s[1] = v.y;
   s[2] = v.z;

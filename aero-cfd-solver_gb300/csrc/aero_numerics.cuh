@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <type_traits>
+
 namespace aero {
 
 template <class T>
@@ -136,36 +138,68 @@ __device__ __forceinline__ Cons<T> prim_to_cons(const Prim<T>& w, T gamma) {
   return c;
 }
 
-// euler_flux.cpp:115-127
+// euler_flux.cpp:115-127 from the floored density r and its reciprocal inv
 template <class T>
-__device__ __forceinline__ Prim<T> cons_to_prim(const Cons<T>& c, T gamma) {
+__device__ __forceinline__ Prim<T> cons_to_prim_from(const Cons<T>& c, T gamma, T r, T inv) {
   Prim<T> w;
-  w.r = smax(c.r, Kn<T>::rho_floor);
-  const T inv = sdiv(T(1), w.r);
+  w.r = r;
   w.u = c.ru * inv;
   w.v = c.rv * inv;
   const T ke = T(0.5) * w.r * (w.u * w.u + w.v * w.v);
   w.p = smax((gamma - T(1)) * (c.rE - ke), Kn<T>::p_floor);
   return w;
 }
-
-// euler_flux.cpp:129-144
+// euler_flux.cpp:115-127. *inv_out, when given, receives the 1/rho the velocities use.
 template <class T>
-__device__ __forceinline__ void enforce_physical(Cons<T>* s, T gamma) {
+__device__ __forceinline__ Prim<T> cons_to_prim(const Cons<T>& c, T gamma, T* inv_out = nullptr) {
+  const T r = smax(c.r, Kn<T>::rho_floor);
+  const T inv = sdiv(T(1), r);
+  if (inv_out) *inv_out = inv;
+  return cons_to_prim_from(c, gamma, r, inv);
+}
+
+// euler_flux.cpp:129-144 with the energy floor pf = p_floor / (gamma - 1) given; returns the
+// 1/rho of the result (rho is floored and not changed after it), which is the reciprocal
+// cons_to_prim of the result forms
+template <class T>
+__device__ __forceinline__ T enforce_physical_pf(Cons<T>* s, T gamma, T pf) {
   s->r = smax(s->r, Kn<T>::rho_floor);
   const T inv = sdiv(T(1), s->r);
   const T u = s->ru * inv, v = s->rv * inv;
   const T ke = T(0.5) * s->r * (u * u + v * v);
-  const T pf = sdiv(Kn<T>::p_floor, gamma - T(1));
   s->rE = smax(s->rE, ke + pf);
   const T p = (gamma - T(1)) * (s->rE - ke);
   if (p < Kn<T>::p_floor) s->rE = ke + pf;
+  return inv;
+}
+// euler_flux.cpp:129-144
+template <class T>
+__device__ __forceinline__ void enforce_physical(Cons<T>* s, T gamma) {
+  enforce_physical_pf(s, gamma, sdiv(Kn<T>::p_floor, gamma - T(1)));
 }
 
 // euler_flux.cpp:150-152
 template <class T>
 __device__ __forceinline__ T sound_speed(const Prim<T>& w, T gamma) {
   return ssqrt(smax(sdiv(gamma * w.p, smax(w.r, Kn<T>::rho_floor)), T(0)));
+}
+
+// Double precision spends a division on the FP64 pipe, which GB300 runs at a small fraction
+// of the float rate. Where a state's 1/rho is already formed, the FP64 face pass multiplies
+// by it instead of dividing by rho again. The product is within an ulp of the quotient,
+// far inside the FP64 path's 1e-12 agreement with the FP64 oracle. Float and dual numbers
+// keep the quotient.
+template <class T>
+constexpr bool kReuseInverse = std::is_same<T, double>::value;
+
+// sound_speed of a state from cons_to_prim (w.r floored), given its 1/rho
+template <class T>
+__device__ __forceinline__ T sound_speed_inv(const Prim<T>& w, T inv, T gamma) {
+  if constexpr (kReuseInverse<T>) {
+    return ssqrt(smax(gamma * w.p * inv, T(0)));
+  } else {
+    return sound_speed(w, gamma);
+  }
 }
 
 template <class T>
@@ -256,7 +290,26 @@ struct alignas(16) FaceParams {
   T pc_mach_ref, pc_mach_min, pc_beta_min, pc_beta_max;
   T stab_floor;
   T as_cutoff, as_fmin, as_ramp;
+  T inv_gm1;  // 1 / (gamma - 1), formed once per case (used by the FP64 face pass)
 };
+
+// prim_to_cons (euler_flux.cpp:101-113) in the face pass: in FP64 the energy's pressure term
+// is p * (1 / (gamma - 1)) with the case's reciprocal (kReuseInverse)
+template <class T>
+__device__ __forceinline__ Cons<T> prim_to_cons_face(const Prim<T>& w, const FaceParams<T>& fp) {
+  if constexpr (kReuseInverse<T>) {
+    Cons<T> c;
+    c.r = smax(w.r, Kn<T>::rho_floor);
+    c.ru = c.r * w.u;
+    c.rv = c.r * w.v;
+    const T ke = T(0.5) * c.r * (w.u * w.u + w.v * w.v);
+    const T p = smax(w.p, Kn<T>::p_floor);
+    c.rE = p * fp.inv_gm1 + ke;
+    return c;
+  } else {
+    return prim_to_cons(w, fp.gamma);
+  }
+}
 
 // The two sides of a face in primitive form with the quantities the acoustic scale, the
 // all-speed pressure scale and the flux all use, formed once per face: the reference's helpers
@@ -267,16 +320,17 @@ struct FaceSides {
   Prim<T> pl, pr;
   T unl, unr;  // normal velocities
   T al, ar;    // sound speeds
+  T il, ir;    // 1/rho of each side
 };
 template <class T>
 __device__ __forceinline__ FaceSides<T> face_sides(const Cons<T>& l, const Cons<T>& r, T nx, T ny, T gamma) {
   FaceSides<T> f;
-  f.pl = cons_to_prim(l, gamma);
-  f.pr = cons_to_prim(r, gamma);
+  f.pl = cons_to_prim(l, gamma, &f.il);
+  f.pr = cons_to_prim(r, gamma, &f.ir);
   f.unl = f.pl.u * nx + f.pl.v * ny;
   f.unr = f.pr.u * nx + f.pr.v * ny;
-  f.al = sound_speed(f.pl, gamma);
-  f.ar = sound_speed(f.pr, gamma);
+  f.al = sound_speed_inv(f.pl, f.il, gamma);
+  f.ar = sound_speed_inv(f.pr, f.ir, gamma);
   return f;
 }
 // local Mach numbers |u| / max(a, floor) of both sides (preconditioning.cpp:17-22, the
@@ -395,7 +449,8 @@ __device__ __forceinline__ Flux<T> hllc(const Cons<T>& ul, const Cons<T>& ur, co
           stl.r = rs;
           stl.ru = rs * (pl.u + sh * nx);
           stl.rv = rs * (pl.v + sh * ny);
-          const T et = sdiv(ul.rE, rl);
+          // rl is pl.r (cons_to_prim floors it), whose reciprocal the face sides hold
+          const T et = kReuseInverse<T> ? ul.rE * f.il : sdiv(ul.rE, rl);
           const T pt = sdiv(plc, with_sign_floor(rl * skun));
           stl.rE = rs * (et + sh * (s_m + pt));
         }
@@ -408,7 +463,7 @@ __device__ __forceinline__ Flux<T> hllc(const Cons<T>& ul, const Cons<T>& ur, co
           str.r = rs;
           str.ru = rs * (pr.u + sh * nx);
           str.rv = rs * (pr.v + sh * ny);
-          const T et = sdiv(ur.rE, rr);
+          const T et = kReuseInverse<T> ? ur.rE * f.ir : sdiv(ur.rE, rr);
           const T pt = sdiv(prc, with_sign_floor(rr * skun));
           str.rE = rs * (et + sh * (s_m + pt));
         }
@@ -505,7 +560,7 @@ __device__ __forceinline__ Cons<T> precond_farfield_state(const Cons<T>& in, T n
   b.u = unb * nx + tu;
   b.v = unb * ny + tv;
   b.p = pb;
-  return prim_to_cons(b, gamma);
+  return prim_to_cons_face(b, fp);
 }
 
 // euler_flux.cpp:366-395

@@ -272,11 +272,12 @@ class EngineT final : public Engine {
     std::vector<int> perm0(hs_[0].perm);
     perm_dev_ = upload(perm0);
     {
-      std::vector<int> perm_all(static_cast<size_t>(ntot_), 0);
+      std::vector<int> iperm_all(static_cast<size_t>(ntot_), 0);  // original -> device cell within the case
       for (int k = 0; k < K_; ++k) {
-        std::copy(hs_[k].perm.begin(), hs_[k].perm.end(), perm_all.begin() + pk_[k].c0);
+        const std::vector<int>& pm = hs_[k].perm;
+        for (int cn = 0; cn < static_cast<int>(pm.size()); ++cn) iperm_all[pk_[k].c0 + pm[cn]] = cn;
       }
-      perm_all_dev_ = upload(perm_all);
+      iperm_all_dev_ = upload(iperm_all);
     }
     // direct state exchange with host arrays where the GPU walks the host's page tables
     {
@@ -534,7 +535,7 @@ class EngineT final : public Engine {
   void set_state(int k, const double* u) override {
     const Pack& p = pk_[k];
     if (host_direct_) {
-      k_state_from_host<<<(p.n + 255) / 256, 256, 0, st_>>>(p.n, u, perm_all_dev_ + p.c0, Un_ + p.c0);
+      k_state_from_host<<<(p.n + 255) / 256, 256, 0, st_>>>(p.n, u, iperm_all_dev_ + p.c0, Un_ + p.c0);
       AERO_CK(cudaGetLastError());
       state_from_staging(p.c0, p.n);
       AERO_CK(cudaStreamSynchronize(st_));
@@ -559,7 +560,7 @@ class EngineT final : public Engine {
     const Pack& p = pk_[k];
     if (host_direct_) {
       state_to_staging(p.c0, p.n);
-      k_state_to_host<<<(p.n + 255) / 256, 256, 0, st_>>>(p.n, Un_ + p.c0, perm_all_dev_ + p.c0, u);
+      k_state_to_host<<<(p.n + 255) / 256, 256, 0, st_>>>(p.n, Un_ + p.c0, iperm_all_dev_ + p.c0, u);
       AERO_CK(cudaGetLastError());
       AERO_CK(cudaStreamSynchronize(st_));
       return;
@@ -1265,6 +1266,7 @@ class EngineT final : public Engine {
     const Pack& p = pk_[k];
     FaceParams<T>& fp = fps_[k];
     fp.gamma = T(rs.gamma);
+    fp.inv_gm1 = T(1.0 / (rs.gamma - 1.0));
     fp.farfield = Cons<T>{T(rs.cons_inf[0]), T(rs.cons_inf[1]), T(rs.cons_inf[2]), T(rs.cons_inf[3])};
     fp.limiter = cfg.limiter;
     fp.precond = cfg.precond_on;
@@ -1294,6 +1296,7 @@ class EngineT final : public Engine {
     pc.beta_max = double(fp.pc_beta_max);
     pc.gamma_f = float(rs.gamma);
     pc.gm1_f = float(rs.gamma - 1.0);
+    pc.pfe = Kn<double>::p_floor / (rs.gamma - 1.0);
     pc.mach_ref_f = float(pc.mach_ref);
     pc.mach_min_f = float(pc.mach_min);
     pc.beta_min_f = float(pc.beta_min);
@@ -1987,7 +1990,7 @@ class EngineT final : public Engine {
   T* inv_vol_ = nullptr;
   unsigned char* flags_ = nullptr;
   int* perm_dev_ = nullptr;  // case 0: new -> original cell
-  int* perm_all_dev_ = nullptr;  // every case's new -> original cell, at the case's cell offset
+  int* iperm_all_dev_ = nullptr;  // every case's original -> new cell, at the case's cell offset
   bool host_direct_ = false;     // the GPU reads and writes host state arrays in place
   bool grad_tma_ = false;        // gradient pass through bulk copies into shared memory
   bool pdl_ = false;             // programmatic dependent launch of the iteration's kernels

@@ -99,14 +99,17 @@ def algorithmic_bytes(kernel: str, n: int, slots: int, precision: str, faces: in
     raise KeyError(kernel)
 
 
-def workload_config(args, cells: int, faces: int) -> dict:
-    """The workload keys both arms report under `config`."""
+def workload_config(args, cells: int, faces: int, world: int) -> dict:
+    """`config` of both arms' lines, identical in both: the workload, how the GPU arm's timed
+    iterations treat L2, and the replication over ranks. Measured figures go elsewhere."""
     if args.mesh:
         name = f"NACA0012 {args.mesh[0]}x{args.mesh[1]} O-grid (small profiling case)"
     else:
         name = ("NACA0012 512x128 O-grid, 131072 triangles, jitter 10%, permuted; M=0.8, alpha=1.25, "
                 "HLLC+MUSCL venkat, RK3 local dt, CFL 0.8")
-    return {"workload": name, "cells": cells, "faces": faces}
+    return {"workload": name, "cells": cells, "faces": faces,
+            "l2": "flushed before every timed iteration (256 MiB write)" if not args.no_flush else "not flushed",
+            "parallelism": f"replicas x{world}"}
 
 
 def measured_peak():
@@ -367,7 +370,7 @@ def run_reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mcell-iter/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(args, n, faces),
+        "config": workload_config(args, n, faces, world),
         "cpu_baseline": {"value": value, "unit": "Mcell-iter/s", "cores": procs_n, "kind": "port",
                          "sample": f"{args.steps} second-order iterations per process after {args.warmup} "
                                    f"warm-up, {procs_n} independent single-thread replicas (one per host core) "
@@ -969,11 +972,10 @@ def run_gpu_arm(args):
     r32 = results.get("fp32")
     r64 = results.get("fp64")
     traffic, traffic_note = measured_traffic("face_pass", precisions[0], n)
-    config = workload_config(args, n, int(head["info"]["faces"]))
-    config.update({
+    config = workload_config(args, n, int(head["info"]["faces"]), world)
+    measurements = {
         "precision_headline": precisions[0],
-        "l2": "flushed before every timed iteration (256 MiB write)" if not args.no_flush else "not flushed",
-        "parallelism": f"replicas x{world}", "timing": "CUDA events on the library stream, CUDA graph per iteration",
+        "timing": "CUDA events on the library stream, CUDA graph per iteration",
         "fp32_mcell_iter_s": r32["value"] if r32 else None,
         "fp64_mcell_iter_s": r64["value"] if r64 else None,
         "fp32_over_fp64": (r32["value"] / r64["value"]) if (r32 and r64) else None,
@@ -987,7 +989,7 @@ def run_gpu_arm(args):
         "c3_low_mach": c3,
         "c5_adjoint": c5,
         "state_finite": head["finite"],
-    })
+    }
     line = {
         "metric": METRIC, "value": head["value"], "unit": "Mcell-iter/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms"] / args.steps,
@@ -1004,6 +1006,7 @@ def run_gpu_arm(args):
         "e2e": e2e,
         "gpu_launches": int(head["info"]["launches_per_iteration"]) * args.steps,
         "clocks": head["clocks"],
+        "measurements": measurements,
     }
     if r64 and precisions[0] == "fp32":
         line["roofline_fp64"] = {"achieved": r64["achieved"], "frac": r64["achieved"] / peak,

@@ -1,6 +1,7 @@
 """bench.py's contract on the CPU: the reference arm's JSON line (the oracle float port timed
 on host cores), the algorithmic-byte model the roofline divides by, and the warm-up rule."""
 
+import argparse
 import json
 import subprocess
 import sys
@@ -38,7 +39,9 @@ def test_reference_arm_prints_the_contract_line():
         assert key in line, key
     assert line["metric"] == bench.METRIC and line["unit"] == "Mcell-iter/s" and line["higher_is_better"] is True
     assert line["value"] > 0 and line["steps"] == 1 and line["warmup"] == 3 and line["vs_baseline"] is None
-    assert "workload" in line["config"]
+    # the same config object as the GPU arm's line: the workload, L2 treatment and replication
+    assert line["config"] == bench.workload_config(argparse.Namespace(mesh=None, no_flush=False), 2 * 512 * 128,
+                                                   512 * (3 * 128 + 1), 1)
     cb = line["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] == 2 and cb["value"] == line["value"] and cb["sample"]
     e2e = line["e2e"]
@@ -75,7 +78,9 @@ def test_reference_arm_worker_neither_imports_nor_maps_the_product():
 def test_reference_arm_reports_the_gpu_arm_workload():
     class A:
         mesh = None
+        no_flush = False
 
-    cfg = bench.workload_config(A(), 131072, 197120)
-    assert cfg == {"workload": cfg["workload"], "cells": 131072, "faces": 197120}
+    cfg = bench.workload_config(A(), 131072, 197120, 1)
+    assert cfg == {"workload": cfg["workload"], "cells": 131072, "faces": 197120,
+                   "l2": "flushed before every timed iteration (256 MiB write)", "parallelism": "replicas x1"}
     assert "512x128" in cfg["workload"] and "HLLC+MUSCL venkat" in cfg["workload"]

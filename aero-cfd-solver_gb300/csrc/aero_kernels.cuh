@@ -1848,28 +1848,45 @@ static __global__ void k_split_state(int n, const d4* __restrict__ Un, float4* _
 }
 // State exchange with a caller's host array, read and written by the GPU in place where the
 // device shares the host's page tables (Grace: NVLink-C2C with address translation): u is
-// AoS [N][5] in the original cell order, perm maps device cell -> original cell.
-// The host array is walked in its own (the reference's) cell order, so that a warp's accesses
-// over the host link cover one contiguous range; iperm maps an original cell to its device
-// cell, and the device side takes the scattered accesses.
-static __global__ void k_state_from_host(int n, const double* __restrict__ u, const int* __restrict__ iperm,
-                                         d4* __restrict__ Un) {
-  const int co = blockIdx.x * blockDim.x + threadIdx.x;
-  if (co >= n) return;
-  const double* s = u + 5 * static_cast<size_t>(co);
-  Un[iperm[co]] = d4{s[0], s[1], s[2], s[4]};
+// AoS [N][5] in the original cell order, and iperm maps an original cell to its device cell.
+// A block moves kXferCells consecutive original cells. Their 5 * kXferCells doubles cross the
+// host link as consecutive words, 256 contiguous bytes per warp and instruction, and are
+// regrouped per cell in shared memory. The device side takes the scattered accesses.
+constexpr int kXferCells = 256;
+static __global__ void __launch_bounds__(kXferCells) k_state_from_host(int n, const double* __restrict__ u,
+                                                                       const int* __restrict__ iperm,
+                                                                       d4* __restrict__ Un) {
+  __shared__ double buf[5 * kXferCells];
+  const int c0 = blockIdx.x * kXferCells;
+  const int cnt = min(kXferCells, n - c0);
+  const double* src = u + 5 * static_cast<size_t>(c0);
+  for (int i = threadIdx.x; i < 5 * cnt; i += kXferCells) buf[i] = src[i];
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t < cnt) {
+    const double* s = buf + 5 * t;
+    Un[iperm[c0 + t]] = d4{s[0], s[1], s[2], s[4]};
+  }
 }
-static __global__ void k_state_to_host(int n, const d4* __restrict__ Un, const int* __restrict__ iperm,
-                                       double* __restrict__ u) {
-  const int co = blockIdx.x * blockDim.x + threadIdx.x;
-  if (co >= n) return;
-  const d4 v = Un[iperm[co]];
-  double* s = u + 5 * static_cast<size_t>(co);
-  s[0] = v.x;
-  s[1] = v.y;
-  s[2] = v.z;
-  s[3] = 0.0;
-  s[4] = v.w;
+static __global__ void __launch_bounds__(kXferCells) k_state_to_host(int n, const d4* __restrict__ Un,
+                                                                     const int* __restrict__ iperm,
+                                                                     double* __restrict__ u) {
+  __shared__ double buf[5 * kXferCells];
+  const int c0 = blockIdx.x * kXferCells;
+  const int cnt = min(kXferCells, n - c0);
+  const int t = threadIdx.x;
+  if (t < cnt) {
+    const d4 v = Un[iperm[c0 + t]];
+    double* s = buf + 5 * t;
+    s[0] = v.x;
+    s[1] = v.y;
+    s[2] = v.z;
+    s[3] = 0.0;
+    s[4] = v.w;
+  }
+  __syncthreads();
+  double* dst = u + 5 * static_cast<size_t>(c0);
+  for (int i = t; i < 5 * cnt; i += kXferCells) dst[i] = buf[i];
 }
 
 static __global__ void k_combine_state(int n, const float4* __restrict__ hi, const float4* __restrict__ lo,

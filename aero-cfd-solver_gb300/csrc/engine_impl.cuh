@@ -535,7 +535,8 @@ class EngineT final : public Engine {
   void set_state(int k, const double* u) override {
     const Pack& p = pk_[k];
     if (host_direct_) {
-      k_state_from_host<<<(p.n + 255) / 256, 256, 0, st_>>>(p.n, u, iperm_all_dev_ + p.c0, Un_ + p.c0);
+      k_state_from_host<<<(p.n + kXferCells - 1) / kXferCells, kXferCells, 0, st_>>>(p.n, u, iperm_all_dev_ + p.c0,
+                                                                                         Un_ + p.c0);
       AERO_CK(cudaGetLastError());
       state_from_staging(p.c0, p.n);
       AERO_CK(cudaStreamSynchronize(st_));
@@ -560,7 +561,8 @@ class EngineT final : public Engine {
     const Pack& p = pk_[k];
     if (host_direct_) {
       state_to_staging(p.c0, p.n);
-      k_state_to_host<<<(p.n + 255) / 256, 256, 0, st_>>>(p.n, Un_ + p.c0, iperm_all_dev_ + p.c0, u);
+      k_state_to_host<<<(p.n + kXferCells - 1) / kXferCells, kXferCells, 0, st_>>>(p.n, Un_ + p.c0,
+                                                                                       iperm_all_dev_ + p.c0, u);
       AERO_CK(cudaGetLastError());
       AERO_CK(cudaStreamSynchronize(st_));
       return;

@@ -565,7 +565,8 @@ def c3_case(capi, precision, mach=0.05):
 def profile_run(args):
     """One of the measured cases with direct (non-graph) launches, for kernel profilers: 30
     iterations (25 first-order start-up, 5 second-order), then 5 timed second-order iterations.
-    workload: the 512x128 single-case workload (FP32); c3: the 1024x256 low-Mach case (FP32)."""
+    workload: the 512x128 single-case workload (FP32); workload_fp64: the same in FP64; c3: the
+    1024x256 low-Mach case (FP32)."""
     import aero_gb300
     from aero_gb300 import capi
 
@@ -575,7 +576,8 @@ def profile_run(args):
         case = c3_case(capi, capi.PRECISION_FP32)
     else:
         mesh = make_mesh(args)
-        case = capi.make_case(**CASE, precision=capi.PRECISION_FP32)
+        prec = capi.PRECISION_FP64 if args.profile_run == "workload_fp64" else capi.PRECISION_FP32
+        case = capi.make_case(**CASE, precision=prec)
     with aero_gb300.Solver(mesh, case) as s:
         s.time_iterations(30, use_graph=False, flush_l2=False)
         ms = s.time_iterations(5, use_graph=False, flush_l2=True)
@@ -1034,7 +1036,7 @@ def main():
     ap.add_argument("--no-c4", action="store_true", help="skip the 96-case batched sweep measurement")
     ap.add_argument("--cpu-procs", type=int, default=0, help="processes of the reference arm (0: all cores)")
     ap.add_argument("--no-c3", action="store_true", help="skip the 524k-cell low-Mach measurement")
-    ap.add_argument("--profile-run", choices=["workload", "c3"], default=None,
+    ap.add_argument("--profile-run", choices=["workload", "workload_fp64", "c3"], default=None,
                     help="only run one case with direct launches (for kernel profilers)")
     ap.add_argument("--no-c5", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--c5", action="store_true",

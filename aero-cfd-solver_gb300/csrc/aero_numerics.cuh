@@ -27,6 +27,34 @@ struct Kn {
   static constexpr T vol_floor = T(1.0e-12);
 };
 
+// Double compares on the device run on the integer pipe. GB300 executes double-precision
+// compares (and max / min) on the same narrow FP64 pipe as its double arithmetic, and the
+// FP64 face pass keeps that pipe busy. A double's bit pattern with the magnitude bits of a
+// negative value inverted (its orderable key) orders like the value, so the integer pipe can
+// compare instead. dlt equals a < b for every pair of non-NaN doubles, the two zeros
+// included; a NaN operand, which only a non-finite state produces, orders above every
+// positive number.
+__device__ __forceinline__ long long dkey(double x) {
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool dlt(double a, double b) {
+  const long long both = __double_as_longlong(a) | __double_as_longlong(b);
+  return dkey(a) < dkey(b) && (both & 0x7fffffffffffffffLL) != 0;  // -0 < +0 is false
+}
+// a < b in the numerics' kernels: dlt for two doubles on the device, the operator otherwise
+template <class A, class B>
+__host__ __device__ __forceinline__ bool slt(A a, B b) {
+  return a < b;
+}
+__host__ __device__ __forceinline__ bool slt(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return dlt(a, b);
+#else
+  return a < b;
+#endif
+}
+
 // std::max / std::min / std::clamp semantics (NaN handling included).
 template <class T>
 __host__ __device__ __forceinline__ T smax(T a, T b) {
@@ -69,6 +97,19 @@ template <>
 __host__ __device__ __forceinline__ float sclamp<float>(float v, float lo, float hi) {
   return smin<float>(smax<float>(v, lo), hi);
 }
+// Double on the device: the same selections with the compares on the integer pipe (slt).
+template <>
+__host__ __device__ __forceinline__ double smax<double>(double a, double b) {
+  return slt(a, b) ? b : a;
+}
+template <>
+__host__ __device__ __forceinline__ double smin<double>(double a, double b) {
+  return slt(b, a) ? b : a;
+}
+template <>
+__host__ __device__ __forceinline__ double sclamp<double>(double v, double lo, double hi) {
+  return slt(v, lo) ? lo : (slt(hi, v) ? hi : v);
+}
 // Quotient a / b. Float on the device: the approximate divide (__fdividef, 2 ulp for divisors
 // of magnitude 2^-126 to 2^126, the range of every divisor here: floored densities, pressures,
 // sound speeds and wave-speed differences). The float division as this library compiles it
@@ -94,6 +135,15 @@ template <>
 __host__ __device__ __forceinline__ float sabs<float>(float x) {
   return fabsf(x);
 }
+// double on the device: the sign bit cleared on the integer pipe (fabs, bit for bit)
+template <>
+__host__ __device__ __forceinline__ double sabs<double>(double x) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(__double_as_longlong(x) & 0x7fffffffffffffffLL);
+#else
+  return fabs(x);
+#endif
+}
 template <class T>
 __host__ __device__ __forceinline__ T ssqrt(T x) {
   return sqrt(x);
@@ -110,6 +160,15 @@ __host__ __device__ __forceinline__ bool sfinite(T x) {
 template <>
 __host__ __device__ __forceinline__ bool sfinite<float>(float x) {
   return fabsf(x) < INFINITY;
+}
+// double on the device: the exponent field is all ones exactly for the infinities and NaN
+template <>
+__host__ __device__ __forceinline__ bool sfinite<double>(double x) {
+#ifdef __CUDA_ARCH__
+  return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+#else
+  return isfinite(x);
+#endif
 }
 
 template <class T>
@@ -169,7 +228,7 @@ __device__ __forceinline__ T enforce_physical_pf(Cons<T>* s, T gamma, T pf) {
   const T ke = T(0.5) * s->r * (u * u + v * v);
   s->rE = smax(s->rE, ke + pf);
   const T p = (gamma - T(1)) * (s->rE - ke);
-  if (p < Kn<T>::p_floor) s->rE = ke + pf;
+  if (slt(p, Kn<T>::p_floor)) s->rE = ke + pf;
   return inv;
 }
 // euler_flux.cpp:129-144
@@ -223,8 +282,8 @@ __device__ __forceinline__ Flux<T> physical_flux(const Cons<T>& c, const Prim<T>
 // euler_flux.cpp:45-51
 template <class T>
 __device__ __forceinline__ T with_sign_floor(T x) {
-  if (sabs(x) >= Kn<T>::wave_floor) return x;
-  return (x >= T(0)) ? Kn<T>::wave_floor : -Kn<T>::wave_floor;
+  if (!slt(sabs(x), Kn<T>::wave_floor)) return x;
+  return !slt(x, T(0)) ? Kn<T>::wave_floor : -Kn<T>::wave_floor;
 }
 
 template <class T>
@@ -425,17 +484,17 @@ __device__ __forceinline__ Flux<T> hllc(const Cons<T>& ul, const Cons<T>& ur, co
   *mws = smax(smax(sabs(slp), sabs(srp)), Kn<T>::wave_floor);
   *fallback = false;
 
-  bool diffusive = sabs(s_r - s_l) < Kn<T>::wave_floor;
+  bool diffusive = slt(sabs(s_r - s_l), Kn<T>::wave_floor);
   Flux<T> fx;
   if (!diffusive) {
     const Flux<T> fl = physical_flux(ul, pl, nx, ny);
     const Flux<T> fr = physical_flux(ur, pr, nx, ny);
-    if (s_l >= T(0)) return fl;
-    if (s_r <= T(0)) return fr;
+    if (!slt(s_l, T(0))) return fl;
+    if (!slt(T(0), s_r)) return fr;
     const T rl = smax(pl.r, Kn<T>::rho_floor);
     const T rr = smax(pr.r, Kn<T>::rho_floor);
     const T denom = rl * (s_l - unl) - rr * (s_r - unr);
-    diffusive = sabs(denom) < Kn<T>::wave_floor;
+    diffusive = slt(sabs(denom), Kn<T>::wave_floor);
     if (!diffusive) {
       const T s_m = sdiv(prc - plc + rl * unl * (s_l - unl) - rr * unr * (s_r - unr), denom);
       // star states (euler_flux.cpp:313-334) on the side the contact selects; the other
@@ -443,7 +502,7 @@ __device__ __forceinline__ Flux<T> hllc(const Cons<T>& ul, const Cons<T>& ur, co
       Cons<T> stl = ul, str = ur;
       {
         const T skun = s_l - unl, sksm = s_l - s_m;
-        if (!(sabs(skun) < Kn<T>::wave_floor || sabs(sksm) < Kn<T>::wave_floor)) {
+        if (!(slt(sabs(skun), Kn<T>::wave_floor) || slt(sabs(sksm), Kn<T>::wave_floor))) {
           const T rs = sdiv(rl * skun, sksm);
           const T sh = s_m - unl;
           stl.r = rs;
@@ -457,7 +516,7 @@ __device__ __forceinline__ Flux<T> hllc(const Cons<T>& ul, const Cons<T>& ur, co
       }
       {
         const T skun = s_r - unr, sksm = s_r - s_m;
-        if (!(sabs(skun) < Kn<T>::wave_floor || sabs(sksm) < Kn<T>::wave_floor)) {
+        if (!(slt(sabs(skun), Kn<T>::wave_floor) || slt(sabs(sksm), Kn<T>::wave_floor))) {
           const T rs = sdiv(rr * skun, sksm);
           const T sh = s_m - unr;
           str.r = rs;
@@ -470,9 +529,9 @@ __device__ __forceinline__ Flux<T> hllc(const Cons<T>& ul, const Cons<T>& ur, co
       }
       // the w component of both star states is rho_star*(0 + shift*0), always finite
       diffusive = !finite4(stl.r, stl.ru, stl.rv, stl.rE) || !finite4(str.r, str.ru, str.rv, str.rE) ||
-                  stl.r <= T(0) || str.r <= T(0);
+                  !slt(T(0), stl.r) || !slt(T(0), str.r);
       if (!diffusive) {
-        if (s_m >= T(0)) {
+        if (!slt(s_m, T(0))) {
           fx = {fl.m + s_l * (stl.r - ul.r), fl.fx + s_l * (stl.ru - ul.ru), fl.fy + s_l * (stl.rv - ul.rv),
                fl.e + s_l * (stl.rE - ul.rE)};
         } else {
@@ -576,25 +635,25 @@ __device__ __forceinline__ Flux<T> face_flux(const Cons<T>& l, const Cons<T>& r,
 // reconstruction.cpp:121-146
 template <class T>
 __device__ __forceinline__ T limit(int lim, T a, T b) {
-  if (a * b <= T(0)) return T(0);
+  if (!slt(T(0), a * b)) return T(0);  // a * b <= 0 (compares through slt)
   if (lim == 1) {
     const T eps2 = T(1.0e-12) * (T(1) + a * a + b * b);
     const T num = (b * b + T(2) * a * b + eps2) * a;
     const T den = a * a + T(2) * b * b + a * b + eps2;
-    if (sabs(den) <= T(1.0e-20)) return T(0);
+    if (!slt(T(1.0e-20), sabs(den))) return T(0);
     const T x = sdiv(num, den);
     if (!sfinite(x)) return T(0);
-    if (a > T(0)) return sclamp(x, T(0), a);
+    if (slt(T(0), a)) return sclamp(x, T(0), a);
     return sclamp(x, a, T(0));
   }
-  return (sabs(a) < sabs(b)) ? a : b;
+  return slt(sabs(a), sabs(b)) ? a : b;
 }
 
 // residual_assembly.cpp:53-58 (w is 0, always finite)
 template <class T>
 __device__ __forceinline__ bool valid_prim(const Prim<T>& w) {
-  return sfinite(w.r) && sfinite(w.u) && sfinite(w.v) && sfinite(w.p) && w.r > Kn<T>::rho_floor &&
-         w.p > Kn<T>::p_floor;
+  return sfinite(w.r) && sfinite(w.u) && sfinite(w.v) && sfinite(w.p) && slt(Kn<T>::rho_floor, w.r) &&
+         slt(Kn<T>::p_floor, w.p);
 }
 
 }  // namespace aero

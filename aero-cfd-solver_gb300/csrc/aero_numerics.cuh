@@ -32,8 +32,8 @@ struct Kn {
 // FP64 face pass keeps that pipe busy. A double's bit pattern with the magnitude bits of a
 // negative value inverted (its orderable key) orders like the value, so the integer pipe can
 // compare instead. dlt equals a < b for every pair of non-NaN doubles, the two zeros
-// included; a NaN operand, which only a non-finite state produces, orders above every
-// positive number.
+// included. A NaN operand, which only a non-finite state produces, orders by its bit pattern:
+// above +inf with the sign bit clear, below -inf with it set.
 __device__ __forceinline__ long long dkey(double x) {
   const long long b = __double_as_longlong(x);
   return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
@@ -97,7 +97,8 @@ template <>
 __host__ __device__ __forceinline__ float sclamp<float>(float v, float lo, float hi) {
   return smin<float>(smax<float>(v, lo), hi);
 }
-// Double on the device: the same selections with the compares on the integer pipe (slt).
+// Double on the device: the same selections with the compares on the integer pipe (slt);
+// equal to the forms above for every pair of non-NaN values, a NaN operand ordering as in dlt.
 template <>
 __host__ __device__ __forceinline__ double smax<double>(double a, double b) {
   return slt(a, b) ? b : a;

@@ -296,6 +296,10 @@ struct DevMesh {
   const typename Vec<T>::v2* nrm;
   const T* area;
   const T* inv_vol;
+  // per gradient slot, the face vector n * A formed in T as nrm * area, halved for a slot with
+  // a neighbour: the Green-Gauss sums multiply the two cells' sum by it, which is exactly the
+  // product of their average and n * A (halving is exact)
+  const typename Vec<T>::v2* gvec;
 };
 
 // Faces sorted by the new index of their owner. cells = (owner, neighbour) new indices, the
@@ -729,29 +733,54 @@ __device__ __forceinline__ double block_max(double v, double* shm) {
 // Green-Gauss gradient of cell c (reconstruction.cpp:73-119): the face averages of the
 // primitive state times the outward face vectors, over 1/V. sW (may be null) holds W of the
 // cells [base, base + nsw): neighbours in that range are read from shared memory.
-// One batch of a cell's gradient slots: links, normals and lengths of slots k0 .. k0 + 3.
-// The slot geometry does not depend on the links (padding slots hold zeros), so its loads go
-// out with the links' and only the neighbour states wait for them.
+// One batch of a cell's gradient slots: links and face vectors (DevMesh::gvec) of slots
+// k0 .. k0 + 3. The slot geometry does not depend on the links (padding slots hold zeros), so
+// its loads go out with the links' and only the neighbour states wait for them.
 constexpr int kGradBatch = 4;
 template <class T>
 struct GradSlots {
   int lk[kGradBatch];
-  typename Vec<T>::v2 nd[kGradBatch];
-  T ar[kGradBatch];
+  typename Vec<T>::v2 gv[kGradBatch];
 };
 template <class T>
 __device__ __forceinline__ void grad_slots(const DevMesh<T>& m, int c, int k0, GradSlots<T>* sb) {
 #pragma unroll
   for (int u = 0; u < kGradBatch; ++u) {
     sb->lk[u] = kPad;
-    sb->nd[u] = typename Vec<T>::v2{};
-    sb->ar[u] = T(0);
+    sb->gv[u] = typename Vec<T>::v2{};
     if (k0 + u < m.d) {
       const int s = (k0 + u) * m.n + c;
       sb->lk[u] = m.link[s];
-      sb->nd[u] = m.nrm[s];
-      sb->ar[u] = m.area[s];
+      sb->gv[u] = m.gvec[s];
     }
+  }
+}
+// One slot's terms of the Green-Gauss sums: q is the cell's state, plus the neighbour's for a
+// slot with one (g is then half the face vector), times the face vector; subtracted when the
+// cell is the face's neighbour.
+template <class T>
+__device__ __forceinline__ void grad_slot_terms(int link, const typename Vec<T>::v4& wc, const typename Vec<T>::v4& wo,
+                                                const typename Vec<T>::v2& g, T (&ax)[4], T (&ay)[4]) {
+  const T gx = g.x, gy = g.y;
+  T q0 = wc.x, q1 = wc.y, q2 = wc.z, q3 = wc.w;
+  bool minus = false;
+  if (link >= 0) {
+    q0 = q0 + wo.x;
+    q1 = q1 + wo.y;
+    q2 = q2 + wo.z;
+    q3 = q3 + wo.w;
+    minus = (link & 1) != 0;
+  }
+  if (minus) {
+    ax[0] -= q0 * gx; ay[0] -= q0 * gy;
+    ax[1] -= q1 * gx; ay[1] -= q1 * gy;
+    ax[2] -= q2 * gx; ay[2] -= q2 * gy;
+    ax[3] -= q3 * gx; ay[3] -= q3 * gy;
+  } else {
+    ax[0] += q0 * gx; ay[0] += q0 * gy;
+    ax[1] += q1 * gx; ay[1] += q1 * gy;
+    ax[2] += q2 * gx; ay[2] += q2 * gy;
+    ax[3] += q3 * gx; ay[3] += q3 * gy;
   }
 }
 
@@ -760,7 +789,7 @@ __device__ __forceinline__ void cell_gradient(const DevMesh<T>& m, const typenam
                                               typename Vec<T>::v4* gxo, typename Vec<T>::v4* gyo,
                                               const typename Vec<T>::v4* sW = nullptr, int base = 0, int nsw = 0) {
   const auto wc = sW ? sW[c - base] : W[c];
-  T ax0 = 0, ax1 = 0, ax2 = 0, ax3 = 0, ay0 = 0, ay1 = 0, ay2 = 0, ay3 = 0;
+  T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0};
   // slots in batches of kU: the links first, then every load of the batch, then the sums in
   // slot order, so the neighbour loads of one cell are in flight together
   constexpr int kU = kGradBatch;
@@ -768,8 +797,6 @@ __device__ __forceinline__ void cell_gradient(const DevMesh<T>& m, const typenam
     GradSlots<T> sb;
     grad_slots(m, c, k0, &sb);
     const int(&lk)[kU] = sb.lk;
-    const typename Vec<T>::v2(&nd)[kU] = sb.nd;
-    const T(&ar)[kU] = sb.ar;
     typename Vec<T>::v4 wo[kU];
 #pragma unroll
     for (int u = 0; u < kU; ++u) {
@@ -783,37 +810,16 @@ __device__ __forceinline__ void cell_gradient(const DevMesh<T>& m, const typenam
     }
 #pragma unroll
     for (int u = 0; u < kU; ++u) {
-      const int link = lk[u];
-      if (link == kPad) break;
-      const T nax = nd[u].x * ar[u], nay = nd[u].y * ar[u];
-      T q0 = wc.x, q1 = wc.y, q2 = wc.z, q3 = wc.w;
-      bool minus = false;
-      if (link >= 0) {
-        q0 = T(0.5) * (q0 + wo[u].x);
-        q1 = T(0.5) * (q1 + wo[u].y);
-        q2 = T(0.5) * (q2 + wo[u].z);
-        q3 = T(0.5) * (q3 + wo[u].w);
-        minus = (link & 1) != 0;
-      }
-      if (minus) {
-        ax0 -= q0 * nax; ay0 -= q0 * nay;
-        ax1 -= q1 * nax; ay1 -= q1 * nay;
-        ax2 -= q2 * nax; ay2 -= q2 * nay;
-        ax3 -= q3 * nax; ay3 -= q3 * nay;
-      } else {
-        ax0 += q0 * nax; ay0 += q0 * nay;
-        ax1 += q1 * nax; ay1 += q1 * nay;
-        ax2 += q2 * nax; ay2 += q2 * nay;
-        ax3 += q3 * nax; ay3 += q3 * nay;
-      }
+      if (lk[u] == kPad) break;
+      grad_slot_terms<T>(lk[u], wc, wo[u], sb.gv[u], ax, ay);
     }
     if (lk[kU - 1] == kPad) break;
   }
   const T inv = m.inv_vol[c];
   typename Vec<T>::v4& ox = *gxo;
   typename Vec<T>::v4& oy = *gyo;
-  ox.x = ax0 * inv; ox.y = ax1 * inv; ox.z = ax2 * inv; ox.w = ax3 * inv;
-  oy.x = ay0 * inv; oy.y = ay1 * inv; oy.z = ay2 * inv; oy.w = ay3 * inv;
+  ox.x = ax[0] * inv; ox.y = ax[1] * inv; ox.z = ax[2] * inv; ox.w = ax[3] * inv;
+  oy.x = ay[0] * inv; oy.y = ay[1] * inv; oy.z = ay[2] * inv; oy.w = ay[3] * inv;
 }
 
 // The Green-Gauss gradients of CPT cells per thread (cell_gradient's arithmetic, same order
@@ -838,8 +844,7 @@ __device__ __forceinline__ void cell_gradients(const DevMesh<T>& m, const typena
   constexpr int kU = 4;
   for (int k0 = 0; k0 < m.d; k0 += kU) {
     int lk[CPT][kU];
-    V2 nd[CPT][kU];
-    T ar[CPT][kU];
+    V2 gv[CPT][kU];
     V4 wo[CPT][kU];
 #pragma unroll
     for (int j = 0; j < CPT; ++j)
@@ -851,8 +856,7 @@ __device__ __forceinline__ void cell_gradients(const DevMesh<T>& m, const typena
       for (int u = 0; u < kU; ++u) {
         if (live[j] && k0 + u < m.d) {
           const int s = (k0 + u) * m.n + c[j];
-          nd[j][u] = m.nrm[s];
-          ar[j][u] = m.area[s];
+          gv[j][u] = m.gvec[s];
         }
       }
 #pragma unroll
@@ -873,27 +877,7 @@ __device__ __forceinline__ void cell_gradients(const DevMesh<T>& m, const typena
       for (int u = 0; u < kU; ++u) {
         const int link = lk[j][u];
         if (link == kPad) break;
-        const T nax = nd[j][u].x * ar[j][u], nay = nd[j][u].y * ar[j][u];
-        T q0 = wc[j].x, q1 = wc[j].y, q2 = wc[j].z, q3 = wc[j].w;
-        bool minus = false;
-        if (link >= 0) {
-          q0 = T(0.5) * (q0 + wo[j][u].x);
-          q1 = T(0.5) * (q1 + wo[j][u].y);
-          q2 = T(0.5) * (q2 + wo[j][u].z);
-          q3 = T(0.5) * (q3 + wo[j][u].w);
-          minus = (link & 1) != 0;
-        }
-        if (minus) {
-          ax[j][0] -= q0 * nax; ay[j][0] -= q0 * nay;
-          ax[j][1] -= q1 * nax; ay[j][1] -= q1 * nay;
-          ax[j][2] -= q2 * nax; ay[j][2] -= q2 * nay;
-          ax[j][3] -= q3 * nax; ay[j][3] -= q3 * nay;
-        } else {
-          ax[j][0] += q0 * nax; ay[j][0] += q0 * nay;
-          ax[j][1] += q1 * nax; ay[j][1] += q1 * nay;
-          ax[j][2] += q2 * nax; ay[j][2] += q2 * nay;
-          ax[j][3] += q3 * nax; ay[j][3] += q3 * nay;
-        }
+        grad_slot_terms<T>(link, wc[j], wo[j][u], gv[j][u], ax[j], ay[j]);
       }
       if (lk[j][kU - 1] == kPad) live[j] = false;
     }

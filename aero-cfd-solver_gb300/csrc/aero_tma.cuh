@@ -63,7 +63,7 @@ constexpr int kTmaPolls = 1 << 20;  // ~1 s of polling before a wait is given up
 
 // Shared-memory layout of one tile buffer for B cells and D slots.
 struct GradTile {
-  uint32_t link, nrm, area, w, inv, bytes;  // byte offsets; bytes: size of one buffer
+  uint32_t link, gvec, w, inv, bytes;  // byte offsets; bytes: size of one buffer
   uint32_t tx;                              // bytes the copies of one tile deliver
 };
 template <class T>
@@ -78,13 +78,11 @@ __host__ __device__ inline GradTile grad_tile(int B, int D) {
     return o;
   };
   g.link = take(uint32_t(D) * B * 4u);
-  g.nrm = take(uint32_t(D) * B * uint32_t(sizeof(V2)));
-  g.area = take(uint32_t(D) * B * uint32_t(sizeof(T)));
+  g.gvec = take(uint32_t(D) * B * uint32_t(sizeof(V2)));
   g.w = take(uint32_t(B) * uint32_t(sizeof(V4)));
   g.inv = take(uint32_t(B) * uint32_t(sizeof(T)));
   g.bytes = off;
-  g.tx = uint32_t(D) * B * (4u + uint32_t(sizeof(V2)) + uint32_t(sizeof(T))) +
-         uint32_t(B) * uint32_t(sizeof(V4) + sizeof(T));
+  g.tx = uint32_t(D) * B * (4u + uint32_t(sizeof(V2))) + uint32_t(B) * uint32_t(sizeof(V4) + sizeof(T));
   return g;
 }
 // dynamic shared memory of the kernel: two buffers and two mbarriers
@@ -130,8 +128,7 @@ __global__ void __launch_bounds__(256) k_gradient_tma(DevMesh<T> m, const typena
     for (int k = 0; k < D; ++k) {
       const size_t s0 = size_t(k) * m.n + c0;
       bulk_copy_g2s(base + L.link + size_t(k) * B * 4, m.link + s0, uint32_t(B) * 4u, &bar[buf]);
-      bulk_copy_g2s(base + L.nrm + size_t(k) * B * sizeof(V2), m.nrm + s0, uint32_t(B * sizeof(V2)), &bar[buf]);
-      bulk_copy_g2s(base + L.area + size_t(k) * B * sizeof(T), m.area + s0, uint32_t(B * sizeof(T)), &bar[buf]);
+      bulk_copy_g2s(base + L.gvec + size_t(k) * B * sizeof(V2), m.gvec + s0, uint32_t(B * sizeof(V2)), &bar[buf]);
     }
     bulk_copy_g2s(base + L.w, W + c0, uint32_t(B * sizeof(V4)), &bar[buf]);
     bulk_copy_g2s(base + L.inv, m.inv_vol + c0, uint32_t(B * sizeof(T)), &bar[buf]);
@@ -168,8 +165,7 @@ __global__ void __launch_bounds__(256) k_gradient_tma(DevMesh<T> m, const typena
     }
     const unsigned char* base = smem + size_t(buf) * L.bytes;
     const int* sl = reinterpret_cast<const int*>(base + L.link);
-    const V2* sn = reinterpret_cast<const V2*>(base + L.nrm);
-    const T* sa = reinterpret_cast<const T*>(base + L.area);
+    const V2* sg = reinterpret_cast<const V2*>(base + L.gvec);
     const V4* sw = reinterpret_cast<const V4*>(base + L.w);
     const T* si = reinterpret_cast<const T*>(base + L.inv);
     const int2 bd = cs.blk[tile];
@@ -177,44 +173,23 @@ __global__ void __launch_bounds__(256) k_gradient_tma(DevMesh<T> m, const typena
     if (c < bd.y && !cs.ctrl[bd.x].done) {
       const int j = threadIdx.x;
       const V4 wc = sw[j];
-      T ax0 = 0, ax1 = 0, ax2 = 0, ax3 = 0, ay0 = 0, ay1 = 0, ay2 = 0, ay3 = 0;
+      T ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0};
       for (int k = 0; k < D; ++k) {
         const int link = sl[k * B + j];
         if (link == kPad) break;
-        const V2 nd = sn[k * B + j];
-        const T ar = sa[k * B + j];
+        const V2 g = sg[k * B + j];
         V4 wo = wc;
         if (link >= 0) {
           const int o = link >> 1;
           const unsigned off = static_cast<unsigned>(o - c0);
           wo = off < static_cast<unsigned>(B) ? sw[off] : W[o];
         }
-        const T nax = nd.x * ar, nay = nd.y * ar;
-        T q0 = wc.x, q1 = wc.y, q2 = wc.z, q3 = wc.w;
-        bool minus = false;
-        if (link >= 0) {
-          q0 = T(0.5) * (q0 + wo.x);
-          q1 = T(0.5) * (q1 + wo.y);
-          q2 = T(0.5) * (q2 + wo.z);
-          q3 = T(0.5) * (q3 + wo.w);
-          minus = (link & 1) != 0;
-        }
-        if (minus) {
-          ax0 -= q0 * nax; ay0 -= q0 * nay;
-          ax1 -= q1 * nax; ay1 -= q1 * nay;
-          ax2 -= q2 * nax; ay2 -= q2 * nay;
-          ax3 -= q3 * nax; ay3 -= q3 * nay;
-        } else {
-          ax0 += q0 * nax; ay0 += q0 * nay;
-          ax1 += q1 * nax; ay1 += q1 * nay;
-          ax2 += q2 * nax; ay2 += q2 * nay;
-          ax3 += q3 * nax; ay3 += q3 * nay;
-        }
+        grad_slot_terms<T>(link, wc, wo, g, ax, ay);
       }
       const T inv = si[j];
       V4 ox, oy;
-      ox.x = ax0 * inv; ox.y = ax1 * inv; ox.z = ax2 * inv; ox.w = ax3 * inv;
-      oy.x = ay0 * inv; oy.y = ay1 * inv; oy.z = ay2 * inv; oy.w = ay3 * inv;
+      ox.x = ax[0] * inv; ox.y = ax[1] * inv; ox.z = ax[2] * inv; ox.w = ax[3] * inv;
+      oy.x = ay[0] * inv; oy.y = ay[1] * inv; oy.z = ay[2] * inv; oy.w = ay[3] * inv;
       gx[c] = ox;
       gy[c] = oy;
     }

@@ -151,12 +151,13 @@ class EngineT final : public Engine {
     {
       const size_t ns = static_cast<size_t>(ntot_) * d_;
       std::vector<int> link(ns, kPad), gslot(ns, kPad);
-      std::vector<V2> nrm(ns);
+      std::vector<V2> nrm(ns), gvec(ns);
       std::vector<T> area(ns, T(0));
       std::vector<T> inv_vol(static_cast<size_t>(ntot_), T(1));
       std::vector<unsigned char> flags(static_cast<size_t>(ntot_), 0);
       std::vector<int> wall_first(static_cast<size_t>(ntot_), 0);
       for (auto& v : nrm) v.x = v.y = T(0);
+      for (auto& v : gvec) v.x = v.y = T(0);
       for (int k = 0; k < K_; ++k) {
         const HostSlots& h = hs_[k];
         const Pack& p = pk_[k];
@@ -171,6 +172,11 @@ class EngineT final : public Engine {
             nrm[dst].x = T(h.nx[src]);
             nrm[dst].y = T(h.ny[src]);
             area[dst] = T(h.area[src]);
+            if (l != kPad) {  // the face vector in T as the gradient formed it, halved with a neighbour
+              const T h2 = l >= 0 ? T(0.5) : T(1);
+              gvec[dst].x = h2 * (nrm[dst].x * area[dst]);
+              gvec[dst].y = h2 * (nrm[dst].y * area[dst]);
+            }
           }
         }
         for (int c = 0; c < h.n; ++c) {
@@ -182,6 +188,7 @@ class EngineT final : public Engine {
       link_ = upload(link);
       nrm_ = upload(nrm);
       area_ = upload(area);
+      gvec_ = upload(gvec);
       inv_vol_ = upload(inv_vol);
       flags_ = upload(flags);
       dg_.slot = upload(gslot);
@@ -349,6 +356,7 @@ class EngineT final : public Engine {
     dm_.link = link_;
     dm_.nrm = nrm_;
     dm_.area = area_;
+    dm_.gvec = gvec_;
     dm_.inv_vol = inv_vol_;
     dg_.n = ntot_;
     dg_.d = d_;
@@ -1985,6 +1993,7 @@ class EngineT final : public Engine {
   int* link_ = nullptr;
   V2* nrm_ = nullptr;
   T* area_ = nullptr;
+  V2* gvec_ = nullptr;
   DevFaces<T> df_{};
   DevGather<T> dg_{};
   V4* F_ = nullptr;   // per face: F*A

@@ -82,7 +82,7 @@ def algorithmic_bytes(kernel: str, n: int, slots: int, precision: str, faces: in
     """Compulsory bytes of one launch: every array element the kernel reads or writes,
     once (neighbour re-reads excluded). s = bulk real size; `slots` per cell."""
     s = 4 if precision == "fp32" else 8
-    slot_geo = 4 + 2 * s + s  # link, normal, area
+    slot_geo = 4 + 2 * s  # link, face vector
     if kernel == "face":
         # face pass: W and gradients of every cell once; per face its two cell ids, normal,
         # length and MUSCL offsets, and the F*A (4 reals) and wave-speed term it writes

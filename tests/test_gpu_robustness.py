@@ -6,8 +6,9 @@
   in flight and returns). The run must report AERO_ERR_TIMEOUT, leave the conserved state of
   the failed iteration untouched and write no record for it; after the limit is restored the
   same context continues, and its records and state agree with a run that never timed out.
-* Meshes with many faces per cell: the bulk-copy pass's two tile buffers outgrow a CTA's
-  shared memory at FP64 and block size 256 for cells of 16 faces. Such a context must still
+* Meshes with many faces per cell: the bulk-copy pass's two tile buffers (per slot a link
+  and a face vector) outgrow a CTA's shared memory at FP64 and block size 256 for cells of
+  24 faces. Such a context must still
   be created (the plain gather gradient runs) and match the FP64 oracle; forcing the
   bulk-copy pass there is refused with a clear error.
 """
@@ -106,7 +107,7 @@ def flower_mesh(petals: int = 16):
 
 
 def test_cells_with_many_faces_at_block_256(monkeypatch):
-    mesh = flower_mesh(16)
+    mesh = flower_mesh(24)
     case64 = capi.make_case(mach=0.5, aoa_deg=2.0, flux=capi.FLUX_HLLC, limiter=capi.LIMITER_VENKAT,
                             precision=capi.PRECISION_FP64, block_size=256)
     o = op.OracleSolver(op.MODE_DOUBLE, mesh, case64)
@@ -116,7 +117,7 @@ def test_cells_with_many_faces_at_block_256(monkeypatch):
         u[:, k] *= 1.0 + 0.02 * rng.standard_normal(len(u))
     with aero_gb300.Solver(mesh, case64) as s:
         info = s.info()
-        assert info["slots_per_cell"] >= 16 and info["bulk_copy_gradient"] == 0
+        assert info["slots_per_cell"] >= 24 and info["bulk_copy_gradient"] == 0
         for second in (0, 1):
             r, sr, _ = s.residual(u, second, 0.0, 0, 0.05, 1.0)
             ro, sro, _, _, fs = o.residual(u, second, 0.0, 0, 0.05, 1.0, with_scale=True)
@@ -129,7 +130,7 @@ def test_cells_with_many_faces_at_block_256(monkeypatch):
         aero_gb300.Solver(mesh, case64)
     case32 = capi.make_case(mach=0.5, aoa_deg=2.0, flux=capi.FLUX_HLLC, limiter=capi.LIMITER_VENKAT,
                             precision=capi.PRECISION_FP32, block_size=256)
-    with aero_gb300.Solver(mesh, case32) as s:  # two float tile buffers of 16 slots fit
+    with aero_gb300.Solver(mesh, case32) as s:  # two float tile buffers of 24 slots fit
         assert s.info()["bulk_copy_gradient"] == 1
         _, rec = s.run(5)
         assert np.all(np.isfinite(rec["residual_l2"]))
